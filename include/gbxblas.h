@@ -1,0 +1,138 @@
+/*
+ * gbxblas.h — C ABI of the GB300 BLAS offload library (libgbxblas.so).
+ *
+ * Two layers are exported:
+ *
+ *  1. The drop-in layer: the Fortran-ABI BLAS symbols (dgemm_, dtrsm_, …) and
+ *     the CBLAS symbols (cblas_dgemm, …) that the reference intercepts.  They
+ *     take HOST (or managed / device) pointers, validate arguments with the
+ *     netlib INFO numbering, stage operands, run on the GPU and return only
+ *     after the result is visible to the caller.  See gbxblas_f77.h.
+ *
+ *  2. The device layer declared here: gbx_* functions over DEVICE pointers,
+ *     asynchronous on the context's CUDA stream, returning a status code.
+ *     This is the "thin C ABI" the host code calls; it never reads host
+ *     operand memory and never synchronises unless the function says so.
+ *
+ * Everything is column-major FP64 (complex: interleaved re/im pairs, leading
+ * dimensions counted in complex elements).  Integer arguments are 32-bit, as
+ * in the LP64 Fortran ABI.
+ */
+#ifndef GBXBLAS_H
+#define GBXBLAS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBX_OK = 0,
+    GBX_ERR_ARG = 1,         /* invalid argument (info holds the netlib position) */
+    GBX_ERR_CUDA = 2,        /* a CUDA runtime call failed                        */
+    GBX_ERR_ALLOC = 3,       /* device or pinned allocation failed               */
+    GBX_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up               */
+    GBX_ERR_UNSUPPORTED = 5, /* combination not implemented                      */
+    GBX_ERR_ADMISSION = 6    /* serving: request rejected by the memory budget   */
+} gbx_status;
+
+typedef struct gbx_ctx gbx_ctx;
+
+/* ---- contexts ------------------------------------------------------------
+ * A context owns one non-blocking CUDA stream and a growable device
+ * workspace.  gbx_thread_ctx() returns the calling thread's context, created
+ * on first use (the Fortran layer uses it; every host thread gets its own
+ * stream).  Replaces the single global cuBLAS handle of the reference
+ * (runtime-blas.c:14-23).                                                      */
+gbx_status gbx_ctx_create(gbx_ctx **ctx, int device);
+gbx_status gbx_ctx_destroy(gbx_ctx *ctx);
+gbx_ctx   *gbx_thread_ctx(void);
+/* Use a caller-provided stream (cudaStream_t passed as void*); NULL restores
+ * the context's own stream. */
+gbx_status gbx_ctx_set_stream(gbx_ctx *ctx, void *stream);
+void      *gbx_ctx_get_stream(gbx_ctx *ctx);
+gbx_status gbx_ctx_sync(gbx_ctx *ctx);
+/* Pre-size the workspace so later calls do not allocate (bytes). */
+gbx_status gbx_ctx_reserve(gbx_ctx *ctx, size_t bytes);
+/* Number of kernels this library launched on the context since creation. */
+uint64_t   gbx_ctx_launches(const gbx_ctx *ctx);
+/* Last status / CUDA error text recorded on the context. */
+const char *gbx_ctx_last_error(const gbx_ctx *ctx);
+const char *gbx_status_string(gbx_status s);
+
+/* ---- Level 1 (device pointers) --------------------------------------------
+ * Results of reductions are written to DEVICE memory (res) so the call stays
+ * asynchronous and capturable.  Negative increments follow netlib (the
+ * vector is walked from its far end).                                        */
+/* y := alpha*x + y                   replaces cublasDaxpy, blas_level1/axpy.cc:49 */
+gbx_status gbx_daxpy(gbx_ctx *ctx, int n, double alpha, const double *x, int incx,
+                     double *y, int incy);
+/* res := x^T y (deterministic)       replaces cublasDdot,  blas_level1/dot.cc:46  */
+gbx_status gbx_ddot(gbx_ctx *ctx, int n, const double *x, int incx,
+                    const double *y, int incy, double *res);
+/* res := ||x||_2 (overflow-safe)     replaces cublasDnrm2, blas_level1/nrm2.cc:39 */
+gbx_status gbx_dnrm2(gbx_ctx *ctx, int n, const double *x, int incx, double *res);
+/* res := first 1-based i maximising |x_i|; 0 if n<1 or incx<=0
+ *                                     replaces cublasIdamax, blas_level1/amax.cc:40 */
+gbx_status gbx_idamax(gbx_ctx *ctx, int n, const double *x, int incx, int *res);
+/* res := first 1-based i minimising |x_i|; 0 if n<1 or incx<=0
+ *                                     replaces cublasIdamin, blas_level1/amin.cc:40 */
+gbx_status gbx_idamin(gbx_ctx *ctx, int n, const double *x, int incx, int *res);
+/* x := alpha*x (helper used by the Level-3 paths) */
+gbx_status gbx_dscal(gbx_ctx *ctx, int n, double alpha, double *x, int incx);
+
+/* ---- Level 2 ---------------------------------------------------------------
+ * y := alpha*op(A)*x + beta*y         replaces cublasDgemv, blas_level2/gemv.cc:97 */
+gbx_status gbx_dgemv(gbx_ctx *ctx, char trans, int m, int n, double alpha,
+                     const double *A, int lda, const double *x, int incx,
+                     double beta, double *y, int incy);
+
+/* ---- Level 3 ---------------------------------------------------------------
+ * C := alpha*op(A)*op(B) + beta*C     replaces cublasDgemm, blas_level3/gemm.cc:62-82,174
+ * beta == 0 sets C (NaN/Inf in C are not propagated), as netlib does.          */
+gbx_status gbx_dgemm(gbx_ctx *ctx, char transa, char transb, int m, int n, int k,
+                     double alpha, const double *A, int lda, const double *B, int ldb,
+                     double beta, double *C, int ldc);
+/* complex: alpha/beta point to HOST (re, im) pairs
+ *                                     replaces cublasZgemm, blas_level3/gemm.cc:200-216 */
+gbx_status gbx_zgemm(gbx_ctx *ctx, char transa, char transb, int m, int n, int k,
+                     const double *alpha, const double *A, int lda, const double *B, int ldb,
+                     const double *beta, double *C, int ldc);
+/* C := alpha*A*A^T + beta*C (or A^T*A), one triangle
+ *                                     replaces cublasDsyrk, blas_level3/syrk.cc:43-76,175 */
+gbx_status gbx_dsyrk(gbx_ctx *ctx, char uplo, char trans, int n, int k, double alpha,
+                     const double *A, int lda, double beta, double *C, int ldc);
+/* B := alpha*op(A)^-1*B or alpha*B*op(A)^-1
+ *                                     replaces cublasDtrsm, blas_level3/trsm.cc:40-73,167 */
+gbx_status gbx_dtrsm(gbx_ctx *ctx, char side, char uplo, char transa, char diag,
+                     int m, int n, double alpha, const double *A, int lda,
+                     double *B, int ldb);
+/* B := alpha*op(A)*B or alpha*B*op(A)
+ *                                     replaces cublasDtrmm, blas_level3/trmm.cc:41-80,170 */
+gbx_status gbx_dtrmm(gbx_ctx *ctx, char side, char uplo, char transa, char diag,
+                     int m, int n, double alpha, const double *A, int lda,
+                     double *B, int ldb);
+
+/* ---- Ozaki split-precision products (opt-in; no reference counterpart) ----
+ * FP64 results from exact low-precision tensor-core products of integer
+ * slices, recombined in FP64.  tol is the target relative Frobenius error
+ * (<= 0 picks 1e-14); the slice count is chosen per call from the operands'
+ * exponent range (slices > 0 forces a count).  *slices_used may be NULL.     */
+gbx_status gbx_dgemm_ozaki(gbx_ctx *ctx, char transa, char transb, int m, int n, int k,
+                           double alpha, const double *A, int lda, const double *B, int ldb,
+                           double beta, double *C, int ldc, double tol, int slices,
+                           int *slices_used);
+gbx_status gbx_zgemm_ozaki(gbx_ctx *ctx, char transa, char transb, int m, int n, int k,
+                           const double *alpha, const double *A, int lda,
+                           const double *B, int ldb, const double *beta, double *C, int ldc,
+                           double tol, int slices, int *slices_used);
+gbx_status gbx_dsyrk_ozaki(gbx_ctx *ctx, char uplo, char trans, int n, int k, double alpha,
+                           const double *A, int lda, double beta, double *C, int ldc,
+                           double tol, int slices, int *slices_used);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

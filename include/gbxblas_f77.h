@@ -1,0 +1,102 @@
+/*
+ * gbxblas_f77.h — the drop-in symbols exported by libgbxblas.so.
+ *
+ * Fortran ABI (LP64): every argument by reference, option characters as
+ * const char*, 32-bit integers.  Trailing hidden character-length arguments
+ * that gfortran passes are accepted and ignored (they are not read).
+ * Column-major storage.  Every call is synchronous: the result is in the
+ * caller's memory when the function returns.  Invalid arguments call
+ * xerbla_("NAME  ", &info) with the netlib parameter position and return.
+ *
+ * Each declaration names the reference interface it replaces.
+ */
+#ifndef GBXBLAS_F77_H
+#define GBXBLAS_F77_H
+
+#include "gbxblas.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* F77_gemm(d, double)  blas.h:202-215, body blas_level3/gemm.cc:162-179 */
+void dgemm_(const char *transa, const char *transb, const int *m, const int *n, const int *k,
+            const double *alpha, const double *a, const int *lda, const double *b, const int *ldb,
+            const double *beta, double *c, const int *ldc);
+/* F77_gemm(z, double _Complex)  blas.h:202-215, body blas_level3/gemm.cc:200-216 */
+void zgemm_(const char *transa, const char *transb, const int *m, const int *n, const int *k,
+            const double *alpha, const double *a, const int *lda, const double *b, const int *ldb,
+            const double *beta, double *c, const int *ldc);
+/* F77_syrk(d, double)  blas.h:268-274, body blas_level3/syrk.cc:165-180 */
+void dsyrk_(const char *uplo, const char *trans, const int *n, const int *k, const double *alpha,
+            const double *a, const int *lda, const double *beta, double *c, const int *ldc);
+/* F77_trsm(d, double)  blas.h:303-314, body blas_level3/trsm.cc:154-172 */
+void dtrsm_(const char *side, const char *uplo, const char *transa, const char *diag,
+            const int *m, const int *n, const double *alpha, const double *a, const int *lda,
+            double *b, const int *ldb);
+/* F77_trmm(d, double)  blas.h:290-301, body blas_level3/trmm.cc:158-175 (disabled there) */
+void dtrmm_(const char *side, const char *uplo, const char *transa, const char *diag,
+            const int *m, const int *n, const double *alpha, const double *a, const int *lda,
+            double *b, const int *ldb);
+/* F77_gemv(d, double)  blas.h:85-92 (no body in the reference) */
+void dgemv_(const char *trans, const int *m, const int *n, const double *alpha, const double *a,
+            const int *lda, const double *x, const int *incx, const double *beta, double *y,
+            const int *incy);
+/* F77_axpy(d, double)  blas.h:20-31 */
+void daxpy_(const int *n, const double *alpha, const double *x, const int *incx, double *y,
+            const int *incy);
+/* F77_dot(d, double)  blas.h:45-51 (declared void there; returns double here) */
+double ddot_(const int *n, const double *x, const int *incx, const double *y, const int *incy);
+/* F77_nrm2(d, double)  blas.h:33-36 (declared void there; returns double here) */
+double dnrm2_(const int *n, const double *x, const int *incx);
+/* i?amax / i?amin: 1-based index, 0 when n < 1 or incx <= 0.
+ * CBLAS bodies blas_level1/amax.cc:32-43, amin.cc:32-43 */
+int idamax_(const int *n, const double *x, const int *incx);
+int idamin_(const int *n, const double *x, const int *incx);
+
+/* Error handler (weak; an application or tester may supply its own).
+ * The reference forwards to the CPU BLAS's xerbla_ (runtime-blas.c:34-37). */
+void xerbla_(const char *srname, const int *info, size_t len);
+/* Case-insensitive character compare (weak), runtime-blas.c:55-58. */
+int lsame_(const char *ca, const char *cb);
+
+/* ---- CBLAS (enum values of cblas.h:21-25) ---------------------------------- */
+enum GBX_CBLAS_LAYOUT { GbxRowMajor = 101, GbxColMajor = 102 };
+enum GBX_CBLAS_TRANSPOSE { GbxNoTrans = 111, GbxTrans = 112, GbxConjTrans = 113 };
+enum GBX_CBLAS_UPLO { GbxUpper = 121, GbxLower = 122 };
+enum GBX_CBLAS_DIAG { GbxNonUnit = 131, GbxUnit = 132 };
+enum GBX_CBLAS_SIDE { GbxLeft = 141, GbxRight = 142 };
+
+/* cblas.h:751-765 */
+void cblas_dgemm(int layout, int transa, int transb, int m, int n, int k, double alpha,
+                 const double *a, int lda, const double *b, int ldb, double beta, double *c,
+                 int ldc);
+void cblas_zgemm(int layout, int transa, int transb, int m, int n, int k, const void *alpha,
+                 const void *a, int lda, const void *b, int ldb, const void *beta, void *c,
+                 int ldc);
+/* cblas.h:807-822 */
+void cblas_dsyrk(int layout, int uplo, int trans, int n, int k, double alpha, const double *a,
+                 int lda, double beta, double *c, int ldc);
+void cblas_dtrsm(int layout, int side, int uplo, int transa, int diag, int m, int n, double alpha,
+                 const double *a, int lda, double *b, int ldb);
+void cblas_dtrmm(int layout, int side, int uplo, int transa, int diag, int m, int n, double alpha,
+                 const double *a, int lda, double *b, int ldb);
+/* cblas.h:283-297 */
+void cblas_dgemv(int layout, int trans, int m, int n, double alpha, const double *a, int lda,
+                 const double *x, int incx, double beta, double *y, int incy);
+void cblas_daxpy(int n, double alpha, const double *x, int incx, double *y, int incy);
+double cblas_ddot(int n, const double *x, int incx, const double *y, int incy);
+double cblas_dnrm2(int n, const double *x, int incx);
+/* 0-based index (CBLAS_INDEX, cblas.h:18) */
+int cblas_idamax(int n, const double *x, int incx);
+int cblas_idamin(int n, const double *x, int incx);
+
+/* ---- library statistics (the reference writes statistics.csv at exit,
+ *      blas2cuda.c:266-273) -------------------------------------------------- */
+void gbx_stats(uint64_t *calls, uint64_t *hits, uint64_t *misses, uint64_t *bytes_h2d,
+               uint64_t *bytes_d2h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,9 @@
+"""libgpublas_gb300 -- GB300-native BLAS offload library (libgbxblas.so).
+
+The product is the C shared library ``libgbxblas.so`` built from ``csrc/``:
+Fortran-ABI and CBLAS drop-in symbols over hand-written sm_103a kernels, plus
+the gbx_* device-pointer C ABI declared in ``include/gbxblas.h``.  This
+Python package only builds it (``build.build_library``) and binds it with
+ctypes (``_lib``) for tests and benchmarks.
+"""
+from ._lib import F77, Device, GbxError, LIB_PATH, declared_symbols, load, stats  # noqa: F401

@@ -1,0 +1,321 @@
+"""ctypes binding of libgbxblas.so.
+
+Two views of the same library:
+
+* ``F77``    -- the drop-in Fortran-ABI symbols (dgemm_, dtrsm_, ...) called
+  exactly as a Fortran program calls them (every argument by reference), on
+  host numpy arrays in Fortran order.
+* ``Device`` -- the gbx_* C ABI over device pointers (torch CUDA tensors or
+  raw integers), asynchronous on a context's stream.
+
+There is no fallback: if the shared library is missing or fails to load, the
+import error propagates.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbxblas.so")
+HEADERS = [os.path.join(os.path.dirname(HERE), "include", h)
+           for h in ("gbxblas.h", "gbxblas_f77.h")]
+
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+_CH = C.c_char
+
+_lib = None
+
+
+def load(path=None):
+    """Load libgbxblas.so (once).  Raises OSError if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise OSError(f"{path} is missing: build it with __graft_entry__.build() "
+                      "(libgpublas_gb300.build.build_library())")
+    lib = C.CDLL(path, mode=C.RTLD_GLOBAL)
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def declared_symbols():
+    """Function names declared in the public headers."""
+    names = []
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", text, flags=re.M):
+            name = m.group(1)
+            if name in ("if", "defined", "sizeof"):
+                continue
+            names.append(name)
+    return sorted(set(names))
+
+
+def _declare(L):
+    pp = C.POINTER(_P)
+    L.gbx_ctx_create.argtypes = [pp, _I]
+    L.gbx_ctx_create.restype = _I
+    L.gbx_ctx_destroy.argtypes = [_P]
+    L.gbx_thread_ctx.restype = _P
+    L.gbx_ctx_set_stream.argtypes = [_P, _P]
+    L.gbx_ctx_get_stream.argtypes = [_P]
+    L.gbx_ctx_get_stream.restype = _P
+    L.gbx_ctx_sync.argtypes = [_P]
+    L.gbx_ctx_reserve.argtypes = [_P, C.c_size_t]
+    L.gbx_ctx_launches.argtypes = [_P]
+    L.gbx_ctx_launches.restype = C.c_uint64
+    L.gbx_ctx_last_error.argtypes = [_P]
+    L.gbx_ctx_last_error.restype = C.c_char_p
+    L.gbx_status_string.argtypes = [_I]
+    L.gbx_status_string.restype = C.c_char_p
+    L.gbx_daxpy.argtypes = [_P, _I, _D, _P, _I, _P, _I]
+    L.gbx_dscal.argtypes = [_P, _I, _D, _P, _I]
+    L.gbx_ddot.argtypes = [_P, _I, _P, _I, _P, _I, _P]
+    L.gbx_dnrm2.argtypes = [_P, _I, _P, _I, _P]
+    L.gbx_idamax.argtypes = [_P, _I, _P, _I, _P]
+    L.gbx_idamin.argtypes = [_P, _I, _P, _I, _P]
+    L.gbx_dgemv.argtypes = [_P, _CH, _I, _I, _D, _P, _I, _P, _I, _D, _P, _I]
+    L.gbx_dgemm.argtypes = [_P, _CH, _CH, _I, _I, _I, _D, _P, _I, _P, _I, _D, _P, _I]
+    L.gbx_zgemm.argtypes = [_P, _CH, _CH, _I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _I]
+    L.gbx_dsyrk.argtypes = [_P, _CH, _CH, _I, _I, _D, _P, _I, _D, _P, _I]
+    L.gbx_dtrsm.argtypes = [_P, _CH, _CH, _CH, _CH, _I, _I, _D, _P, _I, _P, _I]
+    L.gbx_dtrmm.argtypes = [_P, _CH, _CH, _CH, _CH, _I, _I, _D, _P, _I, _P, _I]
+    L.gbx_dgemm_ozaki.argtypes = [_P, _CH, _CH, _I, _I, _I, _D, _P, _I, _P, _I, _D, _P, _I,
+                                  _D, _I, C.POINTER(_I)]
+    L.gbx_zgemm_ozaki.argtypes = [_P, _CH, _CH, _I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _I,
+                                  _D, _I, C.POINTER(_I)]
+    L.gbx_dsyrk_ozaki.argtypes = [_P, _CH, _CH, _I, _I, _D, _P, _I, _D, _P, _I, _D, _I,
+                                  C.POINTER(_I)]
+    L.ddot_.restype = _D
+    L.dnrm2_.restype = _D
+    L.idamax_.restype = _I
+    L.idamin_.restype = _I
+    L.cblas_ddot.restype = _D
+    L.cblas_ddot.argtypes = [_I, _P, _I, _P, _I]
+    L.cblas_dnrm2.restype = _D
+    L.cblas_dnrm2.argtypes = [_I, _P, _I]
+    L.cblas_idamax.argtypes = [_I, _P, _I]
+    L.cblas_idamin.argtypes = [_I, _P, _I]
+    L.cblas_dgemm.argtypes = [_I, _I, _I, _I, _I, _I, _D, _P, _I, _P, _I, _D, _P, _I]
+    L.gbx_stats.argtypes = [C.POINTER(C.c_uint64)] * 5
+
+
+def stats():
+    L = load()
+    v = [C.c_uint64() for _ in range(5)]
+    L.gbx_stats(*[C.byref(x) for x in v])
+    return dict(zip(("calls", "hits", "misses", "bytes_h2d", "bytes_d2h"), [x.value for x in v]))
+
+
+class GbxError(RuntimeError):
+    pass
+
+
+def _ch(c):
+    return c.encode() if isinstance(c, str) else c
+
+
+def _byref_i(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _byref_d(v):
+    return C.byref(C.c_double(float(v)))
+
+
+def _hp(a):
+    """Pointer to a host numpy array, or a raw integer address."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return C.c_void_p(a)
+    return a.ctypes.data_as(_P)
+
+
+class F77:
+    """The Fortran-ABI entry points, called by reference as Fortran does."""
+
+    def __init__(self):
+        self.L = load()
+
+    def dgemm(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+        self.L.dgemm_(C.c_char_p(_ch(ta)), C.c_char_p(_ch(tb)), _byref_i(m), _byref_i(n),
+                      _byref_i(k), _byref_d(alpha), _hp(a), _byref_i(lda), _hp(b), _byref_i(ldb),
+                      _byref_d(beta), _hp(c), _byref_i(ldc))
+
+    def zgemm(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+        al = np.array([complex(alpha)], dtype=np.complex128)
+        be = np.array([complex(beta)], dtype=np.complex128)
+        self.L.zgemm_(C.c_char_p(_ch(ta)), C.c_char_p(_ch(tb)), _byref_i(m), _byref_i(n),
+                      _byref_i(k), _hp(al), _hp(a), _byref_i(lda), _hp(b), _byref_i(ldb), _hp(be),
+                      _hp(c), _byref_i(ldc))
+
+    def dsyrk(self, uplo, trans, n, k, alpha, a, lda, beta, c, ldc):
+        self.L.dsyrk_(C.c_char_p(_ch(uplo)), C.c_char_p(_ch(trans)), _byref_i(n), _byref_i(k),
+                      _byref_d(alpha), _hp(a), _byref_i(lda), _byref_d(beta), _hp(c), _byref_i(ldc))
+
+    def dtrsm(self, side, uplo, ta, diag, m, n, alpha, a, lda, b, ldb):
+        self.L.dtrsm_(C.c_char_p(_ch(side)), C.c_char_p(_ch(uplo)), C.c_char_p(_ch(ta)),
+                      C.c_char_p(_ch(diag)), _byref_i(m), _byref_i(n), _byref_d(alpha), _hp(a),
+                      _byref_i(lda), _hp(b), _byref_i(ldb))
+
+    def dtrmm(self, side, uplo, ta, diag, m, n, alpha, a, lda, b, ldb):
+        self.L.dtrmm_(C.c_char_p(_ch(side)), C.c_char_p(_ch(uplo)), C.c_char_p(_ch(ta)),
+                      C.c_char_p(_ch(diag)), _byref_i(m), _byref_i(n), _byref_d(alpha), _hp(a),
+                      _byref_i(lda), _hp(b), _byref_i(ldb))
+
+    def dgemv(self, trans, m, n, alpha, a, lda, x, incx, beta, y, incy):
+        self.L.dgemv_(C.c_char_p(_ch(trans)), _byref_i(m), _byref_i(n), _byref_d(alpha), _hp(a),
+                      _byref_i(lda), _hp(x), _byref_i(incx), _byref_d(beta), _hp(y), _byref_i(incy))
+
+    def daxpy(self, n, alpha, x, incx, y, incy):
+        self.L.daxpy_(_byref_i(n), _byref_d(alpha), _hp(x), _byref_i(incx), _hp(y), _byref_i(incy))
+
+    def ddot(self, n, x, incx, y, incy):
+        return self.L.ddot_(_byref_i(n), _hp(x), _byref_i(incx), _hp(y), _byref_i(incy))
+
+    def dnrm2(self, n, x, incx):
+        return self.L.dnrm2_(_byref_i(n), _hp(x), _byref_i(incx))
+
+    def idamax(self, n, x, incx):
+        return self.L.idamax_(_byref_i(n), _hp(x), _byref_i(incx))
+
+    def idamin(self, n, x, incx):
+        return self.L.idamin_(_byref_i(n), _hp(x), _byref_i(incx))
+
+
+def _dp(t):
+    """Device pointer of a torch tensor (or an int address)."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return C.c_void_p(t)
+    return C.c_void_p(t.data_ptr())
+
+
+class Device:
+    """A gbx context and the device-pointer C ABI."""
+
+    def __init__(self, device=0, stream=None):
+        self.L = load()
+        h = _P()
+        st = self.L.gbx_ctx_create(C.byref(h), device)
+        if st != 0:
+            raise GbxError(f"gbx_ctx_create failed with status {st}")
+        self.ctx = h
+        if stream is not None:
+            self.L.gbx_ctx_set_stream(self.ctx, C.c_void_p(stream))
+
+    def close(self):
+        if self.ctx:
+            self.L.gbx_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, st, what):
+        if st != 0:
+            msg = self.L.gbx_ctx_last_error(self.ctx).decode(errors="replace")
+            raise GbxError(f"{what}: {self.L.gbx_status_string(st).decode()} ({msg})")
+
+    def status(self, st):
+        return st
+
+    def sync(self):
+        self._ok(self.L.gbx_ctx_sync(self.ctx), "sync")
+
+    def launches(self):
+        return self.L.gbx_ctx_launches(self.ctx)
+
+    def stream(self):
+        return self.L.gbx_ctx_get_stream(self.ctx)
+
+    def set_stream(self, s):
+        self.L.gbx_ctx_set_stream(self.ctx, C.c_void_p(s) if s else None)
+
+    def last_error(self):
+        return self.L.gbx_ctx_last_error(self.ctx).decode(errors="replace")
+
+    # Level 1
+    def daxpy(self, n, alpha, x, incx, y, incy):
+        self._ok(self.L.gbx_daxpy(self.ctx, n, alpha, _dp(x), incx, _dp(y), incy), "daxpy")
+
+    def dscal(self, n, alpha, x, incx):
+        self._ok(self.L.gbx_dscal(self.ctx, n, alpha, _dp(x), incx), "dscal")
+
+    def ddot(self, n, x, incx, y, incy, res):
+        self._ok(self.L.gbx_ddot(self.ctx, n, _dp(x), incx, _dp(y), incy, _dp(res)), "ddot")
+
+    def dnrm2(self, n, x, incx, res):
+        self._ok(self.L.gbx_dnrm2(self.ctx, n, _dp(x), incx, _dp(res)), "dnrm2")
+
+    def idamax(self, n, x, incx, res):
+        self._ok(self.L.gbx_idamax(self.ctx, n, _dp(x), incx, _dp(res)), "idamax")
+
+    def idamin(self, n, x, incx, res):
+        self._ok(self.L.gbx_idamin(self.ctx, n, _dp(x), incx, _dp(res)), "idamin")
+
+    # Level 2 / 3
+    def dgemv(self, trans, m, n, alpha, a, lda, x, incx, beta, y, incy):
+        self._ok(self.L.gbx_dgemv(self.ctx, _ch(trans), m, n, alpha, _dp(a), lda, _dp(x), incx,
+                                  beta, _dp(y), incy), "dgemv")
+
+    def dgemm(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+        return self.L.gbx_dgemm(self.ctx, _ch(ta), _ch(tb), m, n, k, alpha, _dp(a), lda, _dp(b),
+                                ldb, beta, _dp(c), ldc)
+
+    def dgemm_checked(self, *args):
+        self._ok(self.dgemm(*args), "dgemm")
+
+    def zgemm(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+        al = (C.c_double * 2)(complex(alpha).real, complex(alpha).imag)
+        be = (C.c_double * 2)(complex(beta).real, complex(beta).imag)
+        self._ok(self.L.gbx_zgemm(self.ctx, _ch(ta), _ch(tb), m, n, k, al, _dp(a), lda, _dp(b),
+                                  ldb, be, _dp(c), ldc), "zgemm")
+
+    def dsyrk(self, uplo, trans, n, k, alpha, a, lda, beta, c, ldc):
+        self._ok(self.L.gbx_dsyrk(self.ctx, _ch(uplo), _ch(trans), n, k, alpha, _dp(a), lda, beta,
+                                  _dp(c), ldc), "dsyrk")
+
+    def dtrsm(self, side, uplo, ta, diag, m, n, alpha, a, lda, b, ldb):
+        self._ok(self.L.gbx_dtrsm(self.ctx, _ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n, alpha,
+                                  _dp(a), lda, _dp(b), ldb), "dtrsm")
+
+    def dtrmm(self, side, uplo, ta, diag, m, n, alpha, a, lda, b, ldb):
+        self._ok(self.L.gbx_dtrmm(self.ctx, _ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n, alpha,
+                                  _dp(a), lda, _dp(b), ldb), "dtrmm")
+
+    def dgemm_ozaki(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, tol=0.0, slices=0):
+        used = C.c_int(0)
+        self._ok(self.L.gbx_dgemm_ozaki(self.ctx, _ch(ta), _ch(tb), m, n, k, alpha, _dp(a), lda,
+                                        _dp(b), ldb, beta, _dp(c), ldc, tol, slices,
+                                        C.byref(used)), "dgemm_ozaki")
+        return used.value
+
+    def zgemm_ozaki(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, tol=0.0, slices=0):
+        al = (C.c_double * 2)(complex(alpha).real, complex(alpha).imag)
+        be = (C.c_double * 2)(complex(beta).real, complex(beta).imag)
+        used = C.c_int(0)
+        self._ok(self.L.gbx_zgemm_ozaki(self.ctx, _ch(ta), _ch(tb), m, n, k, al, _dp(a), lda,
+                                        _dp(b), ldb, be, _dp(c), ldc, tol, slices,
+                                        C.byref(used)), "zgemm_ozaki")
+        return used.value
+
+    def dsyrk_ozaki(self, uplo, trans, n, k, alpha, a, lda, beta, c, ldc, tol=0.0, slices=0):
+        used = C.c_int(0)
+        self._ok(self.L.gbx_dsyrk_ozaki(self.ctx, _ch(uplo), _ch(trans), n, k, alpha, _dp(a), lda,
+                                        beta, _dp(c), ldc, tol, slices, C.byref(used)),
+                 "dsyrk_ozaki")
+        return used.value

@@ -1,0 +1,97 @@
+"""Build recipe for libgbxblas.so (sm_103a only).
+
+Compiles every CUDA translation unit with nvcc and every C file with gcc,
+in parallel, and links one shared library in-tree:
+
+    libgpublas_gb300/libgbxblas.so
+
+The build is skipped when a stamp of all sources, headers and flags matches
+the last successful build.  No cmake, no torch extension machinery: the
+library is a plain C ABI that Fortran programs load with LD_PRELOAD.
+"""
+import concurrent.futures as cf
+import glob
+import hashlib
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libgbxblas.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+                     "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
+CC_FLAGS = ["-O2", "-fPIC", "-std=gnu11", "-Wall", "-I" + os.path.join(ROOT, "include")]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libgbxblas")
+
+
+def _sources():
+    cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    c = sorted(glob.glob(os.path.join(CSRC, "*.c")))
+    hdr = sorted(glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+                 glob.glob(os.path.join(ROOT, "include", "*.h")))
+    return cu, c, hdr
+
+
+def _stamp(files, extra):
+    h = hashlib.sha256()
+    for f in files:
+        h.update(f.encode())
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    h.update(" ".join(extra).encode())
+    return h.hexdigest()
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+    return r.stdout
+
+
+def build_library(force: bool = False, verbose: bool = False) -> str:
+    cu, c, hdr = _sources()
+    nvcc = _nvcc()
+    stamp = _stamp(cu + c + hdr, NVCC_FLAGS + CC_FLAGS + [nvcc])
+    stamp_file = os.path.join(BUILD, "stamp")
+    if (not force and os.path.exists(LIB) and os.path.exists(stamp_file)
+            and open(stamp_file).read() == stamp):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    jobs = []
+    for src in cu:
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        jobs.append(([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj], obj))
+    for src in c:
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        jobs.append((["gcc"] + CC_FLAGS + ["-c", src, "-o", obj], obj))
+    workers = max(1, min(len(jobs), os.cpu_count() or 4))
+    with cf.ThreadPoolExecutor(workers) as ex:
+        outs = list(ex.map(lambda j: _run(j[0]), jobs))
+    if verbose:
+        for o in outs:
+            if o.strip():
+                print(o)
+    objs = [j[1] for j in jobs]
+    tmp = LIB + ".tmp%d" % os.getpid()
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"])
+    os.replace(tmp, LIB)
+    with open(stamp_file, "w") as fh:
+        fh.write(stamp)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build_library(force="--force" in sys.argv, verbose=True))

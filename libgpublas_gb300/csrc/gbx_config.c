@@ -1,0 +1,93 @@
+/*
+ * gbx_config.c — BLAS2CUDA_OPTIONS parsing.
+ *
+ * Same variable and syntax as the reference (blas2cuda.c:46-124): options
+ * chained with ';'.  Kept: help, debug_execfail, debug_exec, trace_copy,
+ * heuristic=random|true|false|oracle:<file> (the allocation placement policy;
+ * read by the allocation interposer).  Added:
+ *   precision=fp64|ozaki[:<tol>]  route dgemm_/zgemm_/dsyrk_ to the Ozaki
+ *                                 split-precision path (default fp64)
+ *   prefetch=on|off               prefetch managed operands (default on)
+ *   errors=abort|return           on a CUDA failure inside a Fortran call,
+ *                                 abort (the reference's behaviour) or print
+ *                                 and return (default abort)
+ * Unlike the reference, the environment string is copied before tokenising.
+ */
+#include "gbx_internal.h"
+
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+static gbx_config g_cfg = {0, 1e-14, 1, 1, 0, 0};
+static pthread_once_t g_once = PTHREAD_ONCE_INIT;
+
+static void print_help(void)
+{
+    fputs("gbxblas options (set BLAS2CUDA_OPTIONS, chain with ';'):\n"
+          "   help                      -- print help\n"
+          "   debug_execfail            -- accepted for compatibility\n"
+          "   debug_exec                -- accepted for compatibility\n"
+          "   trace_copy                -- accepted for compatibility\n"
+          "   heuristic=<val>           -- one of: 'random', 'true', 'false', or\n"
+          "                                'oracle:<filename>' (allocation placement)\n"
+          "   precision=fp64|ozaki[:t]  -- FP64 or Ozaki split products (target error t)\n"
+          "   prefetch=on|off           -- prefetch managed operands to the GPU\n"
+          "   errors=abort|return       -- behaviour on a device failure\n",
+          stderr);
+}
+
+static void parse(void)
+{
+    const char *env = getenv("BLAS2CUDA_OPTIONS");
+    if (!env || !*env) return;
+    char *copy = strdup(env);
+    if (!copy) return;
+    char *save = NULL;
+    int helped = 0;
+    for (char *opt = strtok_r(copy, ";", &save); opt; opt = strtok_r(NULL, ";", &save)) {
+        if (strcmp(opt, "help") == 0) {
+            if (!helped) print_help();
+            helped = 1;
+        } else if (strcmp(opt, "debug_execfail") == 0 || strcmp(opt, "debug_exec") == 0 ||
+                   strcmp(opt, "trace_copy") == 0) {
+            /* parsed but unused in the reference as well */
+        } else if (strncmp(opt, "heuristic=", 10) == 0) {
+            const char *h = opt + 10;
+            if (strncmp(h, "random", 6) == 0) g_cfg.heuristic = 2;
+            else if (strncmp(h, "true", 4) == 0) g_cfg.heuristic = 1;
+            else if (strncmp(h, "false", 5) == 0) g_cfg.heuristic = 0;
+            else if (strncmp(h, "oracle:", 7) == 0) g_cfg.heuristic = 3;
+            else fprintf(stderr, "gbxblas: unsupported heuristic '%s'\n", h);
+        } else if (strncmp(opt, "precision=", 10) == 0) {
+            const char *p = opt + 10;
+            if (strncmp(p, "ozaki", 5) == 0) {
+                g_cfg.precision_ozaki = 1;
+                if (p[5] == ':') {
+                    double t = atof(p + 6);
+                    if (t > 0.0) g_cfg.ozaki_tol = t;
+                }
+            } else if (strcmp(p, "fp64") == 0) {
+                g_cfg.precision_ozaki = 0;
+            } else {
+                fprintf(stderr, "gbxblas: unknown precision '%s'\n", p);
+            }
+        } else if (strncmp(opt, "prefetch=", 9) == 0) {
+            g_cfg.prefetch = strcmp(opt + 9, "off") != 0;
+        } else if (strncmp(opt, "errors=", 7) == 0) {
+            g_cfg.abort_on_error = strcmp(opt + 7, "return") != 0;
+        } else if (strncmp(opt, "trace=", 6) == 0) {
+            g_cfg.trace = 1;
+        } else {
+            fprintf(stderr, "gbxblas: unknown option '%s'. Set BLAS2CUDA_OPTIONS=help.\n", opt);
+        }
+    }
+    free(copy);
+}
+
+const gbx_config *gbx_get_config(void)
+{
+    pthread_once(&g_once, parse);
+    return &g_cfg;
+}

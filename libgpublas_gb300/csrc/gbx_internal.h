@@ -1,0 +1,88 @@
+/*
+ * gbx_internal.h — shared between the CUDA translation units and the C host
+ * layer of libgbxblas.  Not installed.
+ */
+#ifndef GBX_INTERNAL_H
+#define GBX_INTERNAL_H
+
+#include "../../include/gbxblas.h"
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- host-side helpers implemented in gbx_runtime.cu ---------------------- */
+int  gbx_lsame(char a, char b);
+/* Record an error string on the context (printf-style) and return status. */
+gbx_status gbx_fail(gbx_ctx *ctx, gbx_status st, const char *fmt, ...);
+/* Device workspace owned by the context: returns a pointer to >= bytes,
+ * 256-byte aligned.  Slot s (0..GBX_WS_SLOTS-1) is an independent buffer;
+ * growing a slot synchronises the context's stream first. */
+#define GBX_WS_SLOTS 16
+/* slot assignment */
+#define GBX_WS_TMP0     0   /* routine temporaries (dtrmm copy, ...)        */
+#define GBX_WS_TMP1     1
+#define GBX_WS_TMP2     2
+#define GBX_WS_STAGE_A  3   /* staging of caller operands (Fortran layer)   */
+#define GBX_WS_STAGE_B  4
+#define GBX_WS_STAGE_C  5
+#define GBX_WS_OZ0      6   /* Ozaki slices and scales                      */
+#define GBX_WS_OZ1      7
+#define GBX_WS_OZ2      8
+#define GBX_WS_OZ3      9
+#define GBX_WS_BATCH    10  /* grouped/batched descriptors                  */
+#define GBX_WS_STAGE_D  11
+#define GBX_WS_GEMV     14  /* gemv partial sums                            */
+#define GBX_WS_RED      15  /* reduction partials                           */
+gbx_status gbx_ws(gbx_ctx *ctx, int slot, size_t bytes, void **ptr);
+/* Pinned host scratch owned by the context (for small results). */
+gbx_status gbx_pinned(gbx_ctx *ctx, size_t bytes, void **ptr);
+void gbx_count_launch(gbx_ctx *ctx, int n);
+/* Check cudaGetLastError after a launch, record and map it. */
+gbx_status gbx_check_launch(gbx_ctx *ctx, const char *what);
+int gbx_ctx_device(const gbx_ctx *ctx);
+/* SM count of the context's device (cached). */
+int gbx_ctx_sms(const gbx_ctx *ctx);
+
+/* ---- placement of host operands (gbx_placement.cu) ------------------------
+ * Classifies a caller pointer: device-resident and managed memory are used in
+ * place (a "hit"), anything else is staged through a workspace slot (a
+ * "miss").  Counters mirror the reference's b2c_hits / b2c_misses
+ * (runtime-mem.hpp:9,83,112), made atomic. */
+typedef struct {
+    const void *host;    /* caller's pointer                                */
+    void       *dev;     /* pointer the kernel uses                         */
+    int         ld;      /* leading dimension of dev (elements)             */
+    int         host_ld; /* leading dimension of host (elements)            */
+    int         staged;  /* 1 if dev is a staging copy                      */
+} gbx_operand;
+/* rows×cols block with leading dimension ld (elements of elem bytes). */
+gbx_status gbx_place_in(gbx_ctx *ctx, int slot, const void *host, int rows, int cols,
+                        int ld, size_t elem, int copy_in, gbx_operand *op);
+/* Copy a staged operand back into the caller's memory (no-op for hits). */
+gbx_status gbx_place_out(gbx_ctx *ctx, const gbx_operand *op, int rows, int cols, size_t elem);
+/* Vector operand of n elements with increment inc (any sign). Staged as a
+ * compact copy covering 1+(n-1)*|inc| elements. */
+gbx_status gbx_place_vec(gbx_ctx *ctx, int slot, const void *host, int n, int inc,
+                         size_t elem, int copy_in, gbx_operand *op);
+gbx_status gbx_place_vec_out(gbx_ctx *ctx, const gbx_operand *op, int n, int inc, size_t elem);
+void gbx_placement_counters(uint64_t *hits, uint64_t *misses, uint64_t *bytes_h2d,
+                            uint64_t *bytes_d2h);
+
+/* ---- library configuration (gbx_config.c) ---------------------------------- */
+typedef struct {
+    int    precision_ozaki;  /* precision=ozaki                                */
+    double ozaki_tol;        /* precision=ozaki:<tol>                           */
+    int    prefetch;         /* prefetch=on: managed operands prefetched        */
+    int    abort_on_error;   /* errors=abort                                     */
+    int    trace;            /* trace=<file> set                                 */
+    int    heuristic;        /* 0 false, 1 true, 2 random, 3 oracle             */
+} gbx_config;
+const gbx_config *gbx_get_config(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

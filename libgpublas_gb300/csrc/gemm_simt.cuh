@@ -1,0 +1,231 @@
+// gemm_simt.cuh — FP64 / complex-FP64 GEMM core on the FP64 FMA pipe.
+//
+// Measured on GB300: SIMT DFMA sustains about 1.2 TFLOP/s per GPU, the legacy
+// FP64 tensor path (mma.sync.m8n8k4.f64) about 1.05 TFLOP/s, so the plain
+// FP64 GEMM-class routines run on DFMA.  At 2 DFMA lanes per clock per SM the
+// kernel is compute-bound at any sane tile size: a 128x128 block tile with
+// 8x8 register tiles moves 16 KB of operands per 131k FMAs, so operand
+// staging through shared memory with register prefetch is all the memory
+// pipeline needs.
+//
+// One kernel template serves DGEMM, ZGEMM, DSYRK (triangular tile grid),
+// DTRMM (triangular operand masking) and the DTRSM updates.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbx_gemm {
+
+struct dcplx { double x, y; };
+
+template <typename T> struct Ops;
+template <> struct Ops<double> {
+    static __device__ __forceinline__ double zero() { return 0.0; }
+    static __device__ __forceinline__ double one() { return 1.0; }
+    static __device__ __forceinline__ void fma_acc(double &acc, double a, double b) { acc = fma(a, b, acc); }
+    static __device__ __forceinline__ double conj(double a) { return a; }
+    static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+    static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+    static __device__ __forceinline__ bool is_zero(double a) { return a == 0.0; }
+};
+template <> struct Ops<dcplx> {
+    static __device__ __forceinline__ dcplx zero() { return {0.0, 0.0}; }
+    static __device__ __forceinline__ dcplx one() { return {1.0, 0.0}; }
+    static __device__ __forceinline__ void fma_acc(dcplx &acc, dcplx a, dcplx b)
+    {
+        acc.x = fma(a.x, b.x, acc.x);
+        acc.x = fma(-a.y, b.y, acc.x);
+        acc.y = fma(a.x, b.y, acc.y);
+        acc.y = fma(a.y, b.x, acc.y);
+    }
+    static __device__ __forceinline__ dcplx conj(dcplx a) { return {a.x, -a.y}; }
+    static __device__ __forceinline__ dcplx mul(dcplx a, dcplx b)
+    {
+        return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+    }
+    static __device__ __forceinline__ dcplx add(dcplx a, dcplx b) { return {a.x + b.x, a.y + b.y}; }
+    static __device__ __forceinline__ bool is_zero(dcplx a) { return a.x == 0.0 && a.y == 0.0; }
+};
+
+// Triangular description of an operand (op() already applied):
+//   TRI_NONE, or TRI_LOWER / TRI_UPPER optionally | TRI_UNIT.
+enum { TRI_NONE = 0, TRI_LOWER = 1, TRI_UPPER = 2, TRI_UNIT = 4 };
+// Which part of C is written.
+enum { C_FULL = 0, C_LOWER = 1, C_UPPER = 2 };
+
+template <typename T>
+struct GemmArgs {
+    int m, n, k;
+    const T *A; long long lda; int ta; int conja;   // ta: op(A) = A^T (A stored k x m)
+    const T *B; long long ldb; int tb; int conjb;   // tb: op(B) = B^T (B stored n x k)
+    T alpha, beta;
+    T *C; long long ldc;
+    int tri_a, tri_b;   // triangular masks of op(A) (m x m) / op(B) (n x n)
+    int c_part;         // C_FULL / C_LOWER / C_UPPER (symmetric rank-k update)
+    int tiles_m, tiles_n;
+};
+
+constexpr int GEMM_THREADS = 256;
+
+// Load the (MN x BK) panel of op(X) starting at (mn0, k0) into registers.
+// contig_mn: X is stored with the MN index contiguous (i.e. op(X) = X for A,
+// op(X) = X^T for B); otherwise the k index is contiguous.
+template <typename T, int MN, int BK>
+struct PanelLoader {
+    static constexpr int PER = MN * BK / GEMM_THREADS;
+    T r[PER];
+
+    __device__ __forceinline__ void load(const T *__restrict__ X, long long ld, bool contig_mn,
+                                         int mn0, int mn_lim, int k0, int k_lim, int conj, int tri,
+                                         bool is_a)
+    {
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const int idx = threadIdx.x + q * GEMM_THREADS;
+            int mn, kk;
+            if (contig_mn) { mn = idx % MN; kk = idx / MN; }
+            else           { kk = idx % BK; mn = idx / BK; }
+            const int gm = mn0 + mn, gk = k0 + kk;
+            T v = Ops<T>::zero();
+            if (gm < mn_lim && gk < k_lim) {
+                bool keep = true, unit_diag = false;
+                if (tri) {
+                    // element of op(X) at (row, col): for A rows are mn, for B rows are k
+                    const int row = is_a ? gm : gk, col = is_a ? gk : gm;
+                    keep = (tri & TRI_LOWER) ? (col <= row) : (col >= row);
+                    unit_diag = (tri & TRI_UNIT) && row == col;
+                }
+                if (unit_diag) v = Ops<T>::one();
+                else if (keep) {
+                    v = contig_mn ? X[(long long)gk * ld + gm] : X[(long long)gm * ld + gk];
+                    if (conj) v = Ops<T>::conj(v);
+                }
+            }
+            r[q] = v;
+        }
+    }
+    __device__ __forceinline__ void store(T (*S)[MN], bool contig_mn)
+    {
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const int idx = threadIdx.x + q * GEMM_THREADS;
+            int mn, kk;
+            if (contig_mn) { mn = idx % MN; kk = idx / MN; }
+            else           { kk = idx % BK; mn = idx / BK; }
+            S[kk][mn] = r[q];
+        }
+    }
+};
+
+// Triangular-tile decode for C_LOWER/C_UPPER grids: t -> (bi, bj), bi >= bj.
+__device__ __forceinline__ void tri_decode(int t, int &bi, int &bj)
+{
+    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((long long)(i + 1) * (i + 2) / 2 <= t) i++;
+    while ((long long)i * (i + 1) / 2 > t) i--;
+    bi = i;
+    bj = t - i * (i + 1) / 2;
+}
+
+template <typename T, int TM, int TN, int BK>
+__global__ void __launch_bounds__(GEMM_THREADS)
+gemm_simt_kernel(GemmArgs<T> p)
+{
+    constexpr int BM = 16 * TM, BN = 16 * TN;
+    __shared__ __align__(16) T As[2][BK][BM];
+    __shared__ __align__(16) T Bs[2][BK][BN];
+
+    int bi, bj;
+    if (p.c_part == C_FULL) {
+        bi = blockIdx.x % p.tiles_m;
+        bj = blockIdx.x / p.tiles_m;
+    } else {
+        int r, c;
+        tri_decode(blockIdx.x, r, c);
+        if (p.c_part == C_LOWER) { bi = r; bj = c; } else { bi = c; bj = r; }
+    }
+    const int m0 = bi * BM, n0 = bj * BN;
+
+    // K range that can contribute given triangular operands
+    int kbeg = 0, kend = p.k;
+    if (p.tri_a & TRI_LOWER) kend = min(kend, m0 + BM);
+    if (p.tri_a & TRI_UPPER) kbeg = max(kbeg, m0);
+    if (p.tri_b & TRI_LOWER) kbeg = max(kbeg, n0);
+    if (p.tri_b & TRI_UPPER) kend = min(kend, n0 + BN);
+    kbeg = (kbeg / BK) * BK;
+
+    const bool a_contig_mn = !p.ta;   // A (m x k) column-major: m contiguous
+    const bool b_contig_mn = p.tb;    // B^T stored n x k: n contiguous
+
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; i++)
+#pragma unroll
+        for (int j = 0; j < TN; j++) acc[i][j] = Ops<T>::zero();
+
+    PanelLoader<T, BM, BK> la;
+    PanelLoader<T, BN, BK> lb;
+    int cur = 0;
+    if (kbeg < kend) {
+        la.load(p.A, p.lda, a_contig_mn, m0, p.m, kbeg, p.k, p.conja, p.tri_a, true);
+        lb.load(p.B, p.ldb, b_contig_mn, n0, p.n, kbeg, p.k, p.conjb, p.tri_b, false);
+        la.store(As[0], a_contig_mn);
+        lb.store(Bs[0], b_contig_mn);
+    }
+    __syncthreads();
+
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+        const bool more = k0 + BK < kend;
+        if (more) {
+            la.load(p.A, p.lda, a_contig_mn, m0, p.m, k0 + BK, p.k, p.conja, p.tri_a, true);
+            lb.load(p.B, p.ldb, b_contig_mn, n0, p.n, k0 + BK, p.k, p.conjb, p.tri_b, false);
+        }
+#pragma unroll
+        for (int kk = 0; kk < BK; kk++) {
+            T a[TM], b[TN];
+#pragma unroll
+            for (int i = 0; i < TM / 2; i++) {
+                a[i] = As[cur][kk][ty * (TM / 2) + i];
+                a[i + TM / 2] = As[cur][kk][BM / 2 + ty * (TM / 2) + i];
+            }
+#pragma unroll
+            for (int j = 0; j < TN / 2; j++) {
+                b[j] = Bs[cur][kk][tx * (TN / 2) + j];
+                b[j + TN / 2] = Bs[cur][kk][BN / 2 + tx * (TN / 2) + j];
+            }
+#pragma unroll
+            for (int i = 0; i < TM; i++)
+#pragma unroll
+                for (int j = 0; j < TN; j++) Ops<T>::fma_acc(acc[i][j], a[i], b[j]);
+        }
+        if (more) {
+            la.store(As[cur ^ 1], a_contig_mn);
+            lb.store(Bs[cur ^ 1], b_contig_mn);
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+
+    // epilogue: C = alpha*acc + beta*C ; beta == 0 overwrites C
+    const bool beta0 = Ops<T>::is_zero(p.beta);
+#pragma unroll
+    for (int j = 0; j < TN; j++) {
+        const int col = n0 + (j < TN / 2 ? tx * (TN / 2) + j : BN / 2 + tx * (TN / 2) + (j - TN / 2));
+        if (col >= p.n) continue;
+#pragma unroll
+        for (int i = 0; i < TM; i++) {
+            const int row = m0 + (i < TM / 2 ? ty * (TM / 2) + i : BM / 2 + ty * (TM / 2) + (i - TM / 2));
+            if (row >= p.m) continue;
+            if (p.c_part == C_LOWER && row < col) continue;
+            if (p.c_part == C_UPPER && row > col) continue;
+            T *cp = p.C + (long long)col * p.ldc + row;
+            T v = Ops<T>::mul(p.alpha, acc[i][j]);
+            if (!beta0) v = Ops<T>::add(v, Ops<T>::mul(p.beta, *cp));
+            *cp = v;
+        }
+    }
+}
+
+}  // namespace gbx_gemm

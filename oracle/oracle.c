@@ -1,0 +1,595 @@
+/*
+ * oracle.c — CPU restatement of the netlib BLAS semantics on the intercepted
+ * path, plus double-double accuracy checkers.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker).  The shipped library never links or
+ * calls this file.  Build with -ffp-contract=off so that x86 and Arm hosts
+ * round every operation the same way and the error-free transformations stay
+ * exact.
+ *
+ * Reference anchors (paths inside the reference project):
+ *   DGEMM  argument checks and quick returns  blas_level3/gemm.cc:87-127
+ *   DTRSM  argument checks, alpha==0 zeroing  blas_level3/trsm.cc:76-132
+ *   DSYRK  argument checks, alpha==0 scaling  blas_level3/syrk.cc:78-146
+ *   DTRMM  argument checks                    blas_level3/trmm.cc:82-137
+ *   DGEMV  CBLAS wrapper (dead code)          blas_level2/gemv.cc:11-98
+ *   DAXPY/DDOT/DNRM2/IDAMAX/IDAMIN wrappers   blas_level1/axpy.cc:10-50,
+ *          dot.cc:9-48, nrm2.cc:9-41, amax.cc:32-43, amin.cc:32-43
+ *   CPU BLAS fallback that actually runs      runtime-blas.c:60-69,
+ *                                             gemm.cc:129-141
+ * The arithmetic the reference finally executes is the CPU BLAS's; the loop
+ * orders below are the netlib reference-BLAS ones for that arithmetic.
+ */
+#include "oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+static int up(char c) { return (c >= 'a' && c <= 'z') ? c - 32 : c; }
+static int same(char a, char b) { return up(a) == up(b); }
+static int imax(int a, int b) { return a > b ? a : b; }
+
+/* ------------------------------------------------------------------------ */
+/* SplitMix64 (Steele, Lea, Flood 2014)                                      */
+/* ------------------------------------------------------------------------ */
+uint64_t orc_splitmix64_next(uint64_t *state)
+{
+    uint64_t z = (*state += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static double u01(uint64_t *s) { return (double)(orc_splitmix64_next(s) >> 11) * 0x1.0p-53; }
+static double um11(uint64_t *s) { return 2.0 * u01(s) - 1.0; }
+
+uint64_t orc_fill_uniform(uint64_t state, double *out, size_t n)
+{
+    for (size_t i = 0; i < n; i++) out[i] = um11(&state);
+    return state;
+}
+
+uint64_t orc_fill_matrix(uint64_t state, double *a, int m, int n, int ld)
+{
+    for (int j = 0; j < n; j++) {
+        for (int i = 0; i < m; i++) a[(size_t)j * ld + i] = um11(&state);
+        for (int i = m; i < ld; i++) a[(size_t)j * ld + i] = 0.0;
+    }
+    return state;
+}
+
+uint64_t orc_fill_trsm_matrix(uint64_t state, double *a, int n, int ld)
+{
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < ld; i++) {
+            if (i >= n) { a[(size_t)j * ld + i] = 0.0; continue; }
+            double v = um11(&state);
+            a[(size_t)j * ld + i] = (i == j) ? 1.5 + 0.5 * v : v / (double)n;
+        }
+    return state;
+}
+
+uint64_t orc_fill_spread(uint64_t state, double *a, size_t n, int s)
+{
+    for (size_t i = 0; i < n; i++) {
+        double u = um11(&state);
+        int e = 0;
+        if (s > 0) {
+            uint64_t r = orc_splitmix64_next(&state);
+            e = (int)(r % (uint64_t)(2 * s + 1)) - s;
+        }
+        a[i] = ldexp(u, e);
+    }
+    return state;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Level 1                                                                   */
+/* ------------------------------------------------------------------------ */
+/* element i (0-based) of a strided vector, netlib convention for inc < 0 */
+static size_t vidx(int i, int n, int inc)
+{
+    return inc >= 0 ? (size_t)i * inc : (size_t)(n - 1 - i) * (size_t)(-inc);
+}
+
+void orc_daxpy(int n, double alpha, const double *x, int incx, double *y, int incy)
+{
+    if (n <= 0 || alpha == 0.0) return;
+    for (int i = 0; i < n; i++) y[vidx(i, n, incy)] += alpha * x[vidx(i, n, incx)];
+}
+
+double orc_ddot(int n, const double *x, int incx, const double *y, int incy)
+{
+    double s = 0.0;
+    if (n <= 0) return 0.0;
+    for (int i = 0; i < n; i++) s += x[vidx(i, n, incx)] * y[vidx(i, n, incy)];
+    return s;
+}
+
+/* ---- double-double helpers (Knuth TwoSum, FMA TwoProduct; Ogita, Rump and
+ *      Oishi, "Accurate sum and dot product", SISC 2005) ------------------ */
+typedef struct { double hi, lo; } dd;
+static inline void two_sum(double a, double b, double *s, double *e)
+{
+    double x = a + b, bb = x - a;
+    *s = x; *e = (a - (x - bb)) + (b - bb);
+}
+static inline void two_prod(double a, double b, double *p, double *e)
+{
+    *p = a * b; *e = fma(a, b, -*p);
+}
+static inline dd dd_add_d(dd a, double b)
+{
+    double s, e; two_sum(a.hi, b, &s, &e);
+    e += a.lo;
+    dd r; two_sum(s, e, &r.hi, &r.lo); return r;
+}
+static inline dd dd_add(dd a, dd b)
+{
+    double s, e; two_sum(a.hi, b.hi, &s, &e);
+    e += a.lo + b.lo;
+    dd r; two_sum(s, e, &r.hi, &r.lo); return r;
+}
+static inline dd dd_fma(dd acc, double a, double b) /* acc + a*b */
+{
+    double p, pe; two_prod(a, b, &p, &pe);
+    double s, e; two_sum(acc.hi, p, &s, &e);
+    e += acc.lo + pe;
+    dd r; two_sum(s, e, &r.hi, &r.lo); return r;
+}
+static inline dd dd_mul_d(dd a, double b)
+{
+    double p, pe; two_prod(a.hi, b, &p, &pe);
+    pe += a.lo * b;
+    dd r; two_sum(p, pe, &r.hi, &r.lo); return r;
+}
+static inline double dd_to_d(dd a) { return a.hi + a.lo; }
+
+double orc_dnrm2(int n, const double *x, int incx)
+{
+    /* Two-pass scaling: find max |x|, scale by the power of two nearest to it
+     * (exact), accumulate the squares in double-double, unscale. */
+    if (n < 1 || incx < 1) return 0.0;
+    double amax = 0.0;
+    for (int i = 0; i < n; i++) {
+        double v = fabs(x[(size_t)i * incx]);
+        if (isnan(v)) return v;
+        if (v > amax) amax = v;
+    }
+    if (amax == 0.0 || isinf(amax)) return amax;
+    int e; frexp(amax, &e);
+    dd s = {0.0, 0.0};
+    for (int i = 0; i < n; i++) {
+        double v = ldexp(x[(size_t)i * incx], -e);
+        s = dd_fma(s, v, v);
+    }
+    /* sqrt of a double-double: one Newton step from sqrt(hi) */
+    double r = sqrt(s.hi);
+    if (r > 0.0) {
+        double p, pe; two_prod(r, r, &p, &pe);
+        double corr = ((s.hi - p) - pe + s.lo) / (2.0 * r);
+        r = r + corr;
+    }
+    return ldexp(r, e);
+}
+
+int orc_idamax(int n, const double *x, int incx)
+{
+    if (n < 1 || incx <= 0) return 0;
+    int best = 1;
+    double m = fabs(x[0]);
+    for (int i = 1; i < n; i++) {
+        double v = fabs(x[(size_t)i * incx]);
+        if (v > m) { m = v; best = i + 1; }
+    }
+    return best;
+}
+
+int orc_idamin(int n, const double *x, int incx)
+{
+    if (n < 1 || incx <= 0) return 0;
+    int best = 1;
+    double m = fabs(x[0]);
+    for (int i = 1; i < n; i++) {
+        double v = fabs(x[(size_t)i * incx]);
+        if (v < m) { m = v; best = i + 1; }
+    }
+    return best;
+}
+
+double orc_ddot_dd(int n, const double *x, int incx, const double *y, int incy)
+{
+    dd s = {0.0, 0.0};
+    if (n <= 0) return 0.0;
+    for (int i = 0; i < n; i++) s = dd_fma(s, x[vidx(i, n, incx)], y[vidx(i, n, incy)]);
+    return dd_to_d(s);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Level 2                                                                   */
+/* ------------------------------------------------------------------------ */
+int orc_check_dgemv(char trans, int m, int n, int lda, int incx, int incy)
+{
+    if (!same(trans, 'N') && !same(trans, 'T') && !same(trans, 'C')) return 1;
+    if (m < 0) return 2;
+    if (n < 0) return 3;
+    if (lda < imax(1, m)) return 6;
+    if (incx == 0) return 8;
+    if (incy == 0) return 11;
+    return 0;
+}
+
+void orc_dgemv(char trans, int m, int n, double alpha, const double *a, int lda,
+               const double *x, int incx, double beta, double *y, int incy)
+{
+    if (orc_check_dgemv(trans, m, n, lda, incx, incy)) return;
+    if (m == 0 || n == 0 || (alpha == 0.0 && beta == 1.0)) return;
+    int notr = same(trans, 'N');
+    int lenx = notr ? n : m, leny = notr ? m : n;
+    if (beta != 1.0)
+        for (int i = 0; i < leny; i++) {
+            size_t iy = vidx(i, leny, incy);
+            y[iy] = (beta == 0.0) ? 0.0 : beta * y[iy];
+        }
+    if (alpha == 0.0) return;
+    if (notr) {
+        for (int j = 0; j < n; j++) {
+            double t = alpha * x[vidx(j, lenx, incx)];
+            for (int i = 0; i < m; i++) y[vidx(i, leny, incy)] += t * a[(size_t)j * lda + i];
+        }
+    } else {
+        for (int j = 0; j < n; j++) {
+            double t = 0.0;
+            for (int i = 0; i < m; i++) t += a[(size_t)j * lda + i] * x[vidx(i, lenx, incx)];
+            y[vidx(j, leny, incy)] += alpha * t;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Level 3                                                                   */
+/* ------------------------------------------------------------------------ */
+#define A_(i, j) a[(size_t)(j) * lda + (i)]
+#define B_(i, j) b[(size_t)(j) * ldb + (i)]
+#define C_(i, j) c[(size_t)(j) * ldc + (i)]
+
+int orc_check_dgemm(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc)
+{
+    int nota = same(ta, 'N'), notb = same(tb, 'N');
+    int nrowa = nota ? m : k, nrowb = notb ? k : n;
+    if (!nota && !same(ta, 'C') && !same(ta, 'T')) return 1;
+    if (!notb && !same(tb, 'C') && !same(tb, 'T')) return 2;
+    if (m < 0) return 3;
+    if (n < 0) return 4;
+    if (k < 0) return 5;
+    if (lda < imax(1, nrowa)) return 8;
+    if (ldb < imax(1, nrowb)) return 10;
+    if (ldc < imax(1, m)) return 13;
+    return 0;
+}
+
+void orc_dgemm(char ta, char tb, int m, int n, int k, double alpha,
+               const double *a, int lda, const double *b, int ldb,
+               double beta, double *c, int ldc)
+{
+    if (orc_check_dgemm(ta, tb, m, n, k, lda, ldb, ldc)) return;
+    if (m == 0 || n == 0 || ((alpha == 0.0 || k == 0) && beta == 1.0)) return;
+    int nota = same(ta, 'N'), notb = same(tb, 'N');
+    if (alpha == 0.0) {
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < m; i++) C_(i, j) = (beta == 0.0) ? 0.0 : beta * C_(i, j);
+        return;
+    }
+    if (nota) {
+        /* C(:,j) = beta*C(:,j) + sum_l (alpha*opB(l,j)) * A(:,l) */
+        for (int j = 0; j < n; j++) {
+            if (beta == 0.0) for (int i = 0; i < m; i++) C_(i, j) = 0.0;
+            else if (beta != 1.0) for (int i = 0; i < m; i++) C_(i, j) *= beta;
+            for (int l = 0; l < k; l++) {
+                double t = alpha * (notb ? B_(l, j) : B_(j, l));
+                for (int i = 0; i < m; i++) C_(i, j) += t * A_(i, l);
+            }
+        }
+    } else {
+        /* C(i,j) = alpha * sum_l A(l,i)*opB(l,j) + beta*C(i,j) */
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < m; i++) {
+                double t = 0.0;
+                for (int l = 0; l < k; l++) t += A_(l, i) * (notb ? B_(l, j) : B_(j, l));
+                C_(i, j) = (beta == 0.0) ? alpha * t : alpha * t + beta * C_(i, j);
+            }
+    }
+}
+
+/* complex helpers on interleaved pairs */
+typedef struct { double re, im; } zc;
+static inline zc zld(const double *p) { zc r = {p[0], p[1]}; return r; }
+static inline zc zmul(zc a, zc b) { zc r = {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; return r; }
+static inline zc zadd(zc a, zc b) { zc r = {a.re + b.re, a.im + b.im}; return r; }
+static inline zc zconj(zc a) { zc r = {a.re, -a.im}; return r; }
+
+static zc zop(const double *m, int ld, int i, int j, char t)
+{
+    /* element (i,j) of op(M) */
+    if (same(t, 'N')) return zld(m + 2 * ((size_t)j * ld + i));
+    zc v = zld(m + 2 * ((size_t)i * ld + j));
+    return same(t, 'C') ? zconj(v) : v;
+}
+
+void orc_zgemm(char ta, char tb, int m, int n, int k, const double *alpha,
+               const double *a, int lda, const double *b, int ldb,
+               const double *beta, double *c, int ldc)
+{
+    if (orc_check_dgemm(ta, tb, m, n, k, lda, ldb, ldc)) return;
+    zc al = {alpha[0], alpha[1]}, be = {beta[0], beta[1]};
+    int alpha0 = al.re == 0.0 && al.im == 0.0, beta0 = be.re == 0.0 && be.im == 0.0;
+    int beta1 = be.re == 1.0 && be.im == 0.0;
+    if (m == 0 || n == 0 || ((alpha0 || k == 0) && beta1)) return;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            double *cp = c + 2 * ((size_t)j * ldc + i);
+            zc t = {0.0, 0.0};
+            if (!alpha0)
+                for (int l = 0; l < k; l++) t = zadd(t, zmul(zop(a, lda, i, l, ta), zop(b, ldb, l, j, tb)));
+            zc r = zmul(al, t);
+            if (!beta0) r = zadd(r, zmul(be, zld(cp)));
+            cp[0] = r.re; cp[1] = r.im;
+        }
+}
+
+int orc_check_dsyrk(char uplo, char trans, int n, int k, int lda, int ldc)
+{
+    int nrowa = same(trans, 'N') ? n : k;
+    if (!same(uplo, 'U') && !same(uplo, 'L')) return 1;
+    if (!same(trans, 'N') && !same(trans, 'T') && !same(trans, 'C')) return 2;
+    if (n < 0) return 3;
+    if (k < 0) return 4;
+    if (lda < imax(1, nrowa)) return 7;
+    if (ldc < imax(1, n)) return 10;
+    return 0;
+}
+
+void orc_dsyrk(char uplo, char trans, int n, int k, double alpha,
+               const double *a, int lda, double beta, double *c, int ldc)
+{
+    if (orc_check_dsyrk(uplo, trans, n, k, lda, ldc)) return;
+    if (n == 0 || ((alpha == 0.0 || k == 0) && beta == 1.0)) return;
+    int upper = same(uplo, 'U'), notr = same(trans, 'N');
+    for (int j = 0; j < n; j++) {
+        int i0 = upper ? 0 : j, i1 = upper ? j + 1 : n;
+        if (alpha == 0.0) {
+            for (int i = i0; i < i1; i++) C_(i, j) = (beta == 0.0) ? 0.0 : beta * C_(i, j);
+            continue;
+        }
+        if (notr) {
+            if (beta == 0.0) for (int i = i0; i < i1; i++) C_(i, j) = 0.0;
+            else if (beta != 1.0) for (int i = i0; i < i1; i++) C_(i, j) *= beta;
+            for (int l = 0; l < k; l++) {
+                double t = alpha * A_(j, l);
+                for (int i = i0; i < i1; i++) C_(i, j) += t * A_(i, l);
+            }
+        } else {
+            for (int i = i0; i < i1; i++) {
+                double t = 0.0;
+                for (int l = 0; l < k; l++) t += A_(l, i) * A_(l, j);
+                C_(i, j) = (beta == 0.0) ? alpha * t : alpha * t + beta * C_(i, j);
+            }
+        }
+    }
+}
+
+int orc_check_dtrsm(char side, char uplo, char ta, char diag, int m, int n, int lda, int ldb)
+{
+    int lside = same(side, 'L');
+    int nrowa = lside ? m : n;
+    if (!lside && !same(side, 'R')) return 1;
+    if (!same(uplo, 'U') && !same(uplo, 'L')) return 2;
+    if (!same(ta, 'N') && !same(ta, 'T') && !same(ta, 'C')) return 3;
+    if (!same(diag, 'U') && !same(diag, 'N')) return 4;
+    if (m < 0) return 5;
+    if (n < 0) return 6;
+    if (lda < imax(1, nrowa)) return 9;
+    if (ldb < imax(1, m)) return 11;
+    return 0;
+}
+
+/* Explicit op(A) as a dense na×na matrix, zero outside the effective triangle,
+ * unit diagonal when diag == 'U'.  Returns 1 if op(A) is lower triangular. */
+static int explicit_tri(char uplo, char ta, char diag, int na, const double *a, int lda, double *t)
+{
+    int upper = same(uplo, 'U'), notr = same(ta, 'N'), unit = same(diag, 'U');
+    for (int j = 0; j < na; j++)
+        for (int i = 0; i < na; i++) {
+            int ai = notr ? i : j, aj = notr ? j : i;     /* A element backing op(A)(i,j) */
+            int in_tri = upper ? (ai <= aj) : (ai >= aj);
+            double v = in_tri ? A_(ai, aj) : 0.0;
+            if (i == j && unit) v = 1.0;
+            t[(size_t)j * na + i] = v;
+        }
+    return upper ? !notr : notr;
+}
+
+void orc_dtrsm(char side, char uplo, char ta, char diag, int m, int n,
+               double alpha, const double *a, int lda, double *b, int ldb)
+{
+    if (orc_check_dtrsm(side, uplo, ta, diag, m, n, lda, ldb)) return;
+    if (m == 0 || n == 0) return;
+    if (alpha == 0.0) {
+        for (int j = 0; j < n; j++) for (int i = 0; i < m; i++) B_(i, j) = 0.0;
+        return;
+    }
+    int lside = same(side, 'L'), unit = same(diag, 'U');
+    int na = lside ? m : n;
+    double *t = (double *)malloc(sizeof(double) * (size_t)na * na);
+    int lower = explicit_tri(uplo, ta, diag, na, a, lda, t);
+#define T_(i, j) t[(size_t)(j) * na + (i)]
+    for (int j = 0; j < n; j++) for (int i = 0; i < m; i++) B_(i, j) *= alpha;
+    if (lside) {
+        for (int j = 0; j < n; j++) {
+            if (lower) {
+                for (int kk = 0; kk < m; kk++) {
+                    if (!unit) B_(kk, j) /= T_(kk, kk);
+                    for (int i = kk + 1; i < m; i++) B_(i, j) -= B_(kk, j) * T_(i, kk);
+                }
+            } else {
+                for (int kk = m - 1; kk >= 0; kk--) {
+                    if (!unit) B_(kk, j) /= T_(kk, kk);
+                    for (int i = 0; i < kk; i++) B_(i, j) -= B_(kk, j) * T_(i, kk);
+                }
+            }
+        }
+    } else {
+        /* X * T = alpha*B, column by column */
+        if (!lower) {
+            for (int j = 0; j < n; j++) {
+                for (int kk = 0; kk < j; kk++)
+                    for (int i = 0; i < m; i++) B_(i, j) -= T_(kk, j) * B_(i, kk);
+                if (!unit) for (int i = 0; i < m; i++) B_(i, j) /= T_(j, j);
+            }
+        } else {
+            for (int j = n - 1; j >= 0; j--) {
+                for (int kk = j + 1; kk < n; kk++)
+                    for (int i = 0; i < m; i++) B_(i, j) -= T_(kk, j) * B_(i, kk);
+                if (!unit) for (int i = 0; i < m; i++) B_(i, j) /= T_(j, j);
+            }
+        }
+    }
+#undef T_
+    free(t);
+}
+
+void orc_dtrmm(char side, char uplo, char ta, char diag, int m, int n,
+               double alpha, const double *a, int lda, double *b, int ldb)
+{
+    if (orc_check_dtrsm(side, uplo, ta, diag, m, n, lda, ldb)) return;
+    if (m == 0 || n == 0) return;
+    if (alpha == 0.0) {
+        for (int j = 0; j < n; j++) for (int i = 0; i < m; i++) B_(i, j) = 0.0;
+        return;
+    }
+    int lside = same(side, 'L');
+    int na = lside ? m : n;
+    double *t = (double *)malloc(sizeof(double) * (size_t)na * na);
+    double *r = (double *)malloc(sizeof(double) * (size_t)m * n);
+    explicit_tri(uplo, ta, diag, na, a, lda, t);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            double s = 0.0;
+            if (lside) for (int l = 0; l < m; l++) s += t[(size_t)l * na + i] * B_(l, j);
+            else       for (int l = 0; l < n; l++) s += B_(i, l) * t[(size_t)j * na + l];
+            r[(size_t)j * m + i] = alpha * s;
+        }
+    for (int j = 0; j < n; j++) for (int i = 0; i < m; i++) B_(i, j) = r[(size_t)j * m + i];
+    free(r); free(t);
+}
+
+/* ------------------------------------------------------------------------ */
+/* double-double checkers                                                    */
+/* ------------------------------------------------------------------------ */
+static double opd(const double *m, int ld, int i, int j, char t)
+{
+    return same(t, 'N') ? m[(size_t)j * ld + i] : m[(size_t)i * ld + j];
+}
+
+static double dgemm_dd_one(char ta, char tb, int k, double alpha, const double *a, int lda,
+                           const double *b, int ldb, double beta, double cij, int i, int j)
+{
+    dd s = {0.0, 0.0};
+    for (int l = 0; l < k; l++) s = dd_fma(s, opd(a, lda, i, l, ta), opd(b, ldb, l, j, tb));
+    dd r = dd_mul_d(s, alpha);
+    if (beta != 0.0) {
+        double p, pe; two_prod(beta, cij, &p, &pe);
+        dd t = {p, pe};
+        r = dd_add(r, t);
+    }
+    return dd_to_d(r);
+}
+
+void orc_dgemm_dd(char ta, char tb, int m, int n, int k, double alpha,
+                  const double *a, int lda, const double *b, int ldb,
+                  double beta, const double *c, int ldc, double *out, int ldo)
+{
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++)
+            out[(size_t)j * ldo + i] = dgemm_dd_one(ta, tb, k, alpha, a, lda, b, ldb, beta,
+                                                    beta != 0.0 ? C_(i, j) : 0.0, i, j);
+}
+
+void orc_dgemm_dd_sample(char ta, char tb, int k, double alpha,
+                         const double *a, int lda, const double *b, int ldb,
+                         double beta, const double *c, int ldc,
+                         int nsample, const int *rows, const int *cols, double *out)
+{
+    for (int s = 0; s < nsample; s++) {
+        int i = rows[s], j = cols[s];
+        out[s] = dgemm_dd_one(ta, tb, k, alpha, a, lda, b, ldb, beta,
+                              beta != 0.0 ? C_(i, j) : 0.0, i, j);
+    }
+}
+
+void orc_zgemm_dd_sample(char ta, char tb, int k, const double *alpha,
+                         const double *a, int lda, const double *b, int ldb,
+                         const double *beta, const double *c, int ldc,
+                         int nsample, const int *rows, const int *cols, double *out)
+{
+    for (int s = 0; s < nsample; s++) {
+        int i = rows[s], j = cols[s];
+        dd re = {0.0, 0.0}, im = {0.0, 0.0};
+        for (int l = 0; l < k; l++) {
+            zc x = zop(a, lda, i, l, ta), y = zop(b, ldb, l, j, tb);
+            re = dd_fma(re, x.re, y.re); re = dd_fma(re, -x.im, y.im);
+            im = dd_fma(im, x.re, y.im); im = dd_fma(im, x.im, y.re);
+        }
+        /* alpha * t */
+        dd rr = dd_add(dd_mul_d(re, alpha[0]), dd_mul_d(im, -alpha[1]));
+        dd ri = dd_add(dd_mul_d(im, alpha[0]), dd_mul_d(re, alpha[1]));
+        if (beta[0] != 0.0 || beta[1] != 0.0) {
+            zc cv = zld(c + 2 * ((size_t)j * ldc + i));
+            rr = dd_fma(rr, beta[0], cv.re); rr = dd_fma(rr, -beta[1], cv.im);
+            ri = dd_fma(ri, beta[0], cv.im); ri = dd_fma(ri, beta[1], cv.re);
+        }
+        out[2 * s] = dd_to_d(rr);
+        out[2 * s + 1] = dd_to_d(ri);
+    }
+}
+
+double orc_dtrsm_residual(char side, char uplo, char ta, char diag, int m, int n,
+                          double alpha, const double *a, int lda,
+                          const double *b0, int ldb0, const double *x, int ldx)
+{
+    int lside = same(side, 'L');
+    int na = lside ? m : n;
+    double *t = (double *)malloc(sizeof(double) * (size_t)na * na);
+    explicit_tri(uplo, ta, diag, na, a, lda, t);
+    dd rn = {0.0, 0.0}, tn = {0.0, 0.0}, xn = {0.0, 0.0}, bn = {0.0, 0.0};
+    for (size_t q = 0; q < (size_t)na * na; q++) tn = dd_fma(tn, t[q], t[q]);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            double xv = x[(size_t)j * ldx + i], bv = b0[(size_t)j * ldb0 + i];
+            xn = dd_fma(xn, xv, xv);
+            bn = dd_fma(bn, bv, bv);
+            dd s = {0.0, 0.0};
+            if (lside) for (int l = 0; l < m; l++) s = dd_fma(s, t[(size_t)l * na + i], x[(size_t)j * ldx + l]);
+            else       for (int l = 0; l < n; l++) s = dd_fma(s, x[(size_t)l * ldx + i], t[(size_t)j * na + l]);
+            double p, pe; two_prod(-alpha, bv, &p, &pe);
+            dd q = {p, pe};
+            double r = dd_to_d(dd_add(s, q));
+            rn = dd_fma(rn, r, r);
+        }
+    free(t);
+    double den = sqrt(dd_to_d(tn)) * sqrt(dd_to_d(xn)) + fabs(alpha) * sqrt(dd_to_d(bn));
+    return den > 0.0 ? sqrt(dd_to_d(rn)) / den : sqrt(dd_to_d(rn));
+}
+
+double orc_rel_fro(int m, int n, const double *x, int ldx, const double *ref, int ldr)
+{
+    dd num = {0.0, 0.0}, den = {0.0, 0.0};
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            double r = ref[(size_t)j * ldr + i], d = x[(size_t)j * ldx + i] - r;
+            num = dd_fma(num, d, d);
+            den = dd_fma(den, r, r);
+        }
+    double dn = dd_to_d(den);
+    return dn > 0.0 ? sqrt(dd_to_d(num) / dn) : sqrt(dd_to_d(num));
+}
