@@ -58,6 +58,25 @@ gbx_status gbx_ctx_sync(gbx_ctx *ctx);
 gbx_status gbx_ctx_reserve(gbx_ctx *ctx, size_t bytes);
 /* Number of kernels this library launched on the context since creation. */
 uint64_t   gbx_ctx_launches(const gbx_ctx *ctx);
+/* Device-time accounting: with timing on, the main kernel of each routine is
+ * bracketed by CUDA events on the context's stream (up to 256 most recent
+ * launches are kept).  gbx_ctx_kernel_time synchronises the stream and
+ * returns the summed milliseconds and launch count for one tag.  The
+ * reference has no equivalent (its statistics are hit/miss counts only,
+ * blas2cuda.c:266-273). */
+enum {
+    GBX_TIMER_GEMM_FP64 = 1,   /* DFMA GEMM core (dgemm/zgemm/dsyrk/dtrmm/dtrsm) */
+    GBX_TIMER_OZAKI_MMA = 2,   /* tensor-core slice products                     */
+    GBX_TIMER_OZAKI_SPLIT = 3, /* slicing of the FP64 operands                   */
+    GBX_TIMER_LEVEL1 = 4,      /* Level-1 streaming kernels                      */
+    GBX_TIMER_GEMV = 5,        /* DGEMV streaming kernel                         */
+    GBX_TIMER_BATCH = 6        /* grouped / batched kernels                      */
+};
+gbx_status gbx_ctx_enable_timing(gbx_ctx *ctx, int on);
+gbx_status gbx_ctx_kernel_time(gbx_ctx *ctx, int tag, double *ms, uint64_t *count);
+/* Measured FP64 FMA throughput of the device (TFLOP/s) from a ~50 ms DFMA
+ * loop on the context's stream; the denominator of the FP64 roofline. */
+gbx_status gbx_diag_fp64_peak(gbx_ctx *ctx, double *tflops);
 /* Last status / CUDA error text recorded on the context. */
 const char *gbx_ctx_last_error(const gbx_ctx *ctx);
 const char *gbx_status_string(gbx_status s);

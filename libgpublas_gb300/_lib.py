@@ -106,6 +106,9 @@ def _declare(L):
     L.cblas_idamin.argtypes = [_I, _P, _I]
     L.cblas_dgemm.argtypes = [_I, _I, _I, _I, _I, _I, _D, _P, _I, _P, _I, _D, _P, _I]
     L.gbx_stats.argtypes = [C.POINTER(C.c_uint64)] * 5
+    L.gbx_ctx_enable_timing.argtypes = [_P, _I]
+    L.gbx_ctx_kernel_time.argtypes = [_P, _I, C.POINTER(_D), C.POINTER(C.c_uint64)]
+    L.gbx_diag_fp64_peak.argtypes = [_P, C.POINTER(_D)]
 
 
 def stats():
@@ -247,6 +250,23 @@ class Device:
 
     def last_error(self):
         return self.L.gbx_ctx_last_error(self.ctx).decode(errors="replace")
+
+    TIMER_GEMM_FP64, TIMER_OZAKI_MMA, TIMER_OZAKI_SPLIT = 1, 2, 3
+    TIMER_LEVEL1, TIMER_GEMV, TIMER_BATCH = 4, 5, 6
+
+    def enable_timing(self, on=True):
+        self._ok(self.L.gbx_ctx_enable_timing(self.ctx, 1 if on else 0), "enable_timing")
+
+    def kernel_time(self, tag):
+        """(total milliseconds, launches) recorded for one timer tag."""
+        ms, n = C.c_double(0.0), C.c_uint64(0)
+        self._ok(self.L.gbx_ctx_kernel_time(self.ctx, tag, C.byref(ms), C.byref(n)), "kernel_time")
+        return ms.value, n.value
+
+    def fp64_peak(self):
+        t = C.c_double(0.0)
+        self._ok(self.L.gbx_diag_fp64_peak(self.ctx, C.byref(t)), "fp64_peak")
+        return t.value
 
     # Level 1
     def daxpy(self, n, alpha, x, incx, y, incy):

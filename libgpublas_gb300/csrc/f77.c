@@ -88,7 +88,8 @@ void dgemm_(const char *transa, const char *transb, const int *m, const int *n, 
     gbx_status st;
     const int nota = gbx_lsame(*transa, 'N'), notb = gbx_lsame(*transb, 'N');
     const int work = !(*alpha == 0.0 || *k == 0);
-    gbx_operand oa = {0}, ob = {0}, oc = {0};
+    /* operands left unplaced on quick paths keep the caller's (valid) ld */
+    gbx_operand oa = {.ld = *lda}, ob = {.ld = *ldb}, oc = {0};
     if (work) {
         TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, nota ? *m : *k, nota ? *k : *m, *lda, 8, 1, &oa));
         TRY(gbx_place_in(ctx, GBX_WS_STAGE_B, b, notb ? *k : *n, notb ? *n : *k, *ldb, 8, 1, &ob));
@@ -124,7 +125,8 @@ void zgemm_(const char *transa, const char *transb, const int *m, const int *n, 
     gbx_status st;
     const int nota = gbx_lsame(*transa, 'N'), notb = gbx_lsame(*transb, 'N');
     const int work = !(alpha0 || *k == 0);
-    gbx_operand oa = {0}, ob = {0}, oc = {0};
+    /* operands left unplaced on quick paths keep the caller's (valid) ld */
+    gbx_operand oa = {.ld = *lda}, ob = {.ld = *ldb}, oc = {0};
     if (work) {
         TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, nota ? *m : *k, nota ? *k : *m, *lda, 16, 1, &oa));
         TRY(gbx_place_in(ctx, GBX_WS_STAGE_B, b, notb ? *k : *n, notb ? *n : *k, *ldb, 16, 1, &ob));
@@ -156,7 +158,7 @@ void dsyrk_(const char *uplo, const char *trans, const int *n, const int *k, con
     gbx_status st;
     const int notr = gbx_lsame(*trans, 'N');
     const int work = !(*alpha == 0.0 || *k == 0);
-    gbx_operand oa = {0}, oc = {0};
+    gbx_operand oa = {.ld = *lda}, oc = {0};
     if (work)
         TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, notr ? *n : *k, notr ? *k : *n, *lda, 8, 1, &oa));
     /* the other triangle of C must survive the round trip: always copy in */
@@ -189,7 +191,7 @@ static void trxm(const char *name, trxm_fn fn, const char *side, const char *upl
     if (!ctx) return;
     gbx_status st;
     const int na = gbx_lsame(*side, 'L') ? *m : *n;
-    gbx_operand oa = {0}, ob = {0};
+    gbx_operand oa = {.ld = *lda}, ob = {0};
     if (*alpha != 0.0) TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, na, na, *lda, 8, 1, &oa));
     TRY(gbx_place_in(ctx, GBX_WS_STAGE_B, b, *m, *n, *ldb, 8, *alpha != 0.0, &ob));
     TRY(fn(ctx, *side, *uplo, *transa, *diag, *m, *n, *alpha, oa.dev, oa.ld, ob.dev, ob.ld));
@@ -227,7 +229,7 @@ void dgemv_(const char *trans, const int *m, const int *n, const double *alpha, 
     gbx_status st;
     const int notr = gbx_lsame(*trans, 'N');
     const int lenx = notr ? *n : *m, leny = notr ? *m : *n;
-    gbx_operand oa = {0}, ox = {0}, oy = {0};
+    gbx_operand oa = {.ld = *lda}, ox = {0}, oy = {0};
     if (*alpha != 0.0) {
         TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, *m, *n, *lda, 8, 1, &oa));
         TRY(gbx_place_vec(ctx, GBX_WS_STAGE_B, x, lenx, *incx, 8, 1, &ox));

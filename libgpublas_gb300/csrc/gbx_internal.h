@@ -40,6 +40,12 @@ gbx_status gbx_ws(gbx_ctx *ctx, int slot, size_t bytes, void **ptr);
 /* Pinned host scratch owned by the context (for small results). */
 gbx_status gbx_pinned(gbx_ctx *ctx, size_t bytes, void **ptr);
 void gbx_count_launch(gbx_ctx *ctx, int n);
+/* Event bracket around one launch (no-op unless timing is enabled). */
+void gbx_timer_begin(gbx_ctx *ctx, int tag);
+void gbx_timer_end(gbx_ctx *ctx);
+/* Queue a copy of a device status word (nonzero = a bounded wait gave up);
+ * gbx_ctx_sync reports it as GBX_ERR_TIMEOUT. */
+void gbx_watch_status(gbx_ctx *ctx, const int *dev_status);
 /* Check cudaGetLastError after a launch, record and map it. */
 gbx_status gbx_check_launch(gbx_ctx *ctx, const char *what);
 int gbx_ctx_device(const gbx_ctx *ctx);

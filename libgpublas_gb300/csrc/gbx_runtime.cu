@@ -20,6 +20,16 @@
 #include <cstring>
 #include <mutex>
 
+// Kernel timing: when enabled, the main kernel of each routine is bracketed by
+// a pair of CUDA events on the context's stream; gbx_ctx_kernel_time() sums
+// the elapsed times per tag after a synchronisation.
+#define GBX_TIMER_PAIRS 256
+struct gbx_timer_rec {
+    cudaEvent_t start, stop;
+    int tag;
+    int used;
+};
+
 struct gbx_ctx {
     int device;
     int sms;
@@ -30,8 +40,68 @@ struct gbx_ctx {
     void  *pinned;
     size_t pinned_bytes;
     uint64_t launches;
+    int *watch_host;     // pinned copies of device status words (bounded waits)
+    int watch_pending;
+    int timing;
+    int timer_next;
+    int timer_open;
+    gbx_timer_rec timers[GBX_TIMER_PAIRS];
     char err[512];
 };
+
+extern "C" gbx_status gbx_ctx_enable_timing(gbx_ctx *c, int on)
+{
+    if (!c) return GBX_ERR_ARG;
+    if (on && !c->timers[0].start) {
+        for (int i = 0; i < GBX_TIMER_PAIRS; i++) {
+            if (cudaEventCreate(&c->timers[i].start) != cudaSuccess ||
+                cudaEventCreate(&c->timers[i].stop) != cudaSuccess)
+                return gbx_fail(c, GBX_ERR_CUDA, "timer events");
+        }
+    }
+    c->timing = on;
+    c->timer_next = 0;
+    for (int i = 0; i < GBX_TIMER_PAIRS; i++) c->timers[i].used = 0;
+    return GBX_OK;
+}
+
+extern "C" void gbx_timer_begin(gbx_ctx *c, int tag)
+{
+    if (!c || !c->timing) return;
+    gbx_timer_rec *r = &c->timers[c->timer_next % GBX_TIMER_PAIRS];
+    r->tag = tag;
+    r->used = 1;
+    c->timer_open = c->timer_next % GBX_TIMER_PAIRS;
+    cudaEventRecord(r->start, c->stream);
+}
+
+extern "C" void gbx_timer_end(gbx_ctx *c)
+{
+    if (!c || !c->timing) return;
+    cudaEventRecord(c->timers[c->timer_open].stop, c->stream);
+    c->timer_next++;
+}
+
+extern "C" gbx_status gbx_ctx_kernel_time(gbx_ctx *c, int tag, double *ms, uint64_t *count)
+{
+    if (!c || !ms) return GBX_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return gbx_fail(c, GBX_ERR_CUDA, "timer sync: %s", cudaGetErrorString(e));
+    double total = 0.0;
+    uint64_t n = 0;
+    for (int i = 0; i < GBX_TIMER_PAIRS; i++) {
+        gbx_timer_rec *r = &c->timers[i];
+        if (!r->used || r->tag != tag) continue;
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, r->start, r->stop) == cudaSuccess) {
+            total += t;
+            n++;
+        }
+    }
+    *ms = total;
+    if (count) *count = n;
+    return GBX_OK;
+}
 
 extern "C" int gbx_lsame(char a, char b)
 {
@@ -92,6 +162,11 @@ extern "C" gbx_status gbx_ctx_destroy(gbx_ctx *c)
     for (int i = 0; i < GBX_WS_SLOTS; i++)
         if (c->ws[i]) cudaFree(c->ws[i]);
     if (c->pinned) cudaFreeHost(c->pinned);
+    if (c->watch_host) cudaFreeHost(c->watch_host);
+    for (int i = 0; i < GBX_TIMER_PAIRS; i++) {
+        if (c->timers[i].start) cudaEventDestroy(c->timers[i].start);
+        if (c->timers[i].stop) cudaEventDestroy(c->timers[i].stop);
+    }
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     free(c);
     return GBX_OK;
@@ -130,11 +205,41 @@ extern "C" gbx_status gbx_ctx_set_stream(gbx_ctx *c, void *stream)
 
 extern "C" void *gbx_ctx_get_stream(gbx_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
+#define GBX_WATCH_SLOTS 64
+
+// Kernels with bounded device-side waits write a status word; the word is
+// copied to pinned memory behind the kernel and checked at the next sync.
+extern "C" void gbx_watch_status(gbx_ctx *c, const int *dev_status)
+{
+    if (!c) return;
+    if (!c->watch_host) {
+        if (cudaMallocHost((void **)&c->watch_host, sizeof(int) * GBX_WATCH_SLOTS) != cudaSuccess) {
+            cudaGetLastError();
+            c->watch_host = nullptr;
+            return;
+        }
+        memset(c->watch_host, 0, sizeof(int) * GBX_WATCH_SLOTS);
+    }
+    if (c->watch_pending >= GBX_WATCH_SLOTS) {
+        // all slots in use: settle them before reusing
+        gbx_ctx_sync(c);
+    }
+    cudaMemcpyAsync(&c->watch_host[c->watch_pending++], dev_status, sizeof(int), cudaMemcpyDeviceToHost,
+                    c->stream);
+}
+
 extern "C" gbx_status gbx_ctx_sync(gbx_ctx *c)
 {
     if (!c) return GBX_ERR_ARG;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return gbx_fail(c, GBX_ERR_CUDA, "stream sync: %s", cudaGetErrorString(e));
+    int bad = 0;
+    for (int i = 0; i < c->watch_pending; i++) {
+        if (c->watch_host[i] != 0 && !bad) bad = c->watch_host[i];
+        c->watch_host[i] = 0;
+    }
+    c->watch_pending = 0;
+    if (bad) return gbx_fail(c, GBX_ERR_TIMEOUT, "a bounded device wait gave up (code %d)", bad);
     return GBX_OK;
 }
 

@@ -66,7 +66,9 @@ gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
         blocks = (long long)p.tiles_m * (p.tiles_m + 1) / 2;
     }
     if (blocks > 0x7fffffffLL) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "%s: grid too large", what);
+    gbx_timer_begin(ctx, GBX_TIMER_GEMM_FP64);
     gemm_simt_kernel<T, TM, TN, BK><<<(unsigned)blocks, GEMM_THREADS, 0, S(ctx)>>>(p);
+    gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);
     return gbx_check_launch(ctx, what);
 }

@@ -7,6 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# A device failure inside a Fortran-ABI call prints and returns instead of
+# aborting the whole test process, so the failing test is reported.
+os.environ.setdefault("BLAS2CUDA_OPTIONS", "errors=return")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")

@@ -107,7 +107,7 @@ def test_device_failure_is_reported_not_silent(lib):
         import numpy as np, libgpublas_gb300 as g
         f = g.F77(); a = np.ones((8, 8), order='F')
         f.dgemm('N', 'N', 8, 8, 8, 1.0, a, 8, a, 8, 0.0, a, 8)
-    """)
+    """, env={"BLAS2CUDA_OPTIONS": ""})
     assert r2.returncode != 0 and "gbxblas: DGEMM failed" in r2.stderr
 
 
