@@ -415,7 +415,9 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 const double rs = ldexp(rsc, -5 * q);
                 for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
                     const bool last = (q == 0) && (g0 + gp.items_per_group >= nitems);
-                    if (!mbar_wait(&tfull[buf], tphase, status, TC_TIMEOUT_TMEM_FULL)) { ok = false; break; }
+                    // warp-uniform outcome: tcgen05.ld below is .sync.aligned
+                    ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tphase, status, TC_TIMEOUT_TMEM_FULL));
+                    if (!ok) break;
                     tc_fence_after();
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * OZ_BN);
                     for (int c = 0; c < OZ_BN / 32; c++) {
