@@ -99,6 +99,20 @@ gbx_status gbx_idamax(gbx_ctx *ctx, int n, const double *x, int incx, int *res);
 /* res := first 1-based i minimising |x_i|; 0 if n<1 or incx<=0
  *                                     replaces cublasIdamin, blas_level1/amin.cc:40 */
 gbx_status gbx_idamin(gbx_ctx *ctx, int n, const double *x, int incx, int *res);
+/* res := x^T y without allocating anything (no reference counterpart: it is
+ * an addition of this library).  For callers that cannot allocate device
+ * memory when they need the reduction: code running inside a malloc/free
+ * interposer (which must not re-enter the CUDA allocator), code recording a
+ * CUDA graph (cudaMalloc is not allowed during stream capture), or code under
+ * a fixed memory budget.  It needs no context: it runs on 'stream'
+ * (cudaStream_t as void*, NULL = default stream), and its partial sums live
+ * in one 32 KiB device array shared by all calls; n is limited to 2^28
+ * (4096 partials of 65536 elements) and larger n returns GBX_ERR_ARG.
+ * Calls that overlap on the GPU race on that array.  The first call on a
+ * device looks up the array's address; make it before any stream capture.
+ * Results agree with gbx_ddot within rounding (different partition). */
+gbx_status gbx_ddot_noalloc(void *stream, int n, const double *x, int incx,
+                            const double *y, int incy, double *res);
 /* x := alpha*x (helper used by the Level-3 paths) */
 gbx_status gbx_dscal(gbx_ctx *ctx, int n, double alpha, double *x, int incx);
 

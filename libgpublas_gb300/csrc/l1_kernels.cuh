@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// The kernels are static: this header is included by more than one
+// translation unit.
 namespace gbx_l1 {
 
 constexpr int L1_THREADS = 256;
@@ -36,14 +38,14 @@ __device__ __forceinline__ double block_sum(double v)
 
 __device__ __forceinline__ double2 ldg2(const double2 *p) { return __ldg(p); }
 
-__global__ void zero_result(double *res) { *res = 0.0; }
-__global__ void zero_index(int *res) { *res = 0; }
+static __global__ void zero_result(double *res) { *res = 0.0; }
+static __global__ void zero_index(int *res) { *res = 0; }
 
 // ---------------------------------------------------------------- daxpy ---
 // Unit stride.  When x and y have the same 16-byte phase the body runs on
 // double2 (128-bit) accesses after peeling one leading element; otherwise it
 // falls back to 64-bit accesses.
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 axpy_unit(int n, double a, const double *__restrict__ x, double *__restrict__ y)
 {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -75,7 +77,7 @@ axpy_unit(int n, double a, const double *__restrict__ x, double *__restrict__ y)
 }
 
 // Any increments; x and y point at element 0 of the logical vectors.
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 axpy_strided(int n, double a, const double *__restrict__ x, int incx, double *__restrict__ y, int incy)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -85,7 +87,7 @@ axpy_strided(int n, double a, const double *__restrict__ x, int incx, double *__
     }
 }
 
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 scal_kernel(int n, double a, double *__restrict__ x, int incx)
 {
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -94,7 +96,7 @@ scal_kernel(int n, double a, double *__restrict__ x, int incx)
 }
 
 // ----------------------------------------------------------------- ddot ---
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 dot_partial(int n, const double *__restrict__ x, int incx, const double *__restrict__ y, int incy,
             double *__restrict__ part)
 {
@@ -126,7 +128,7 @@ dot_partial(int n, const double *__restrict__ x, int incx, const double *__restr
     if (threadIdx.x == 0) part[blockIdx.x] = b;
 }
 
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 sum_partials(const double *__restrict__ part, int g, double *__restrict__ res)
 {
     double s = 0.0;
@@ -155,7 +157,7 @@ __device__ __forceinline__ void blue_acc(double v, double &asml, double &amed, d
     else amed = fma(ax, ax, amed);   // also takes NaN, which then propagates
 }
 
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 nrm2_partial(int n, const double *__restrict__ x, int incx, double *__restrict__ part)
 {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -213,7 +215,7 @@ __device__ __forceinline__ double blue_finish(double asml, double amed, double a
     return scl * sqrt(sumsq);
 }
 
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 nrm2_finish(const double *__restrict__ part, int g, double *__restrict__ res)
 {
     double s = 0.0, m = 0.0, b = 0.0;
@@ -273,7 +275,7 @@ __device__ __forceinline__ void block_best(unsigned long long &k, long long &i)
 }
 
 template <bool IS_MIN>
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 iamax_partial(int n, const double *__restrict__ x, int incx, unsigned long long *__restrict__ keys,
               long long *__restrict__ idx)
 {
@@ -305,7 +307,7 @@ iamax_partial(int n, const double *__restrict__ x, int incx, unsigned long long 
 }
 
 template <bool IS_MIN>
-__global__ void __launch_bounds__(L1_THREADS)
+static __global__ void __launch_bounds__(L1_THREADS)
 iamax_finish(const double *__restrict__ x, const unsigned long long *__restrict__ keys,
              const long long *__restrict__ idx, int g, int *__restrict__ res)
 {
