@@ -239,6 +239,7 @@ extern "C" gbx_status gbx_ctx_sync(gbx_ctx *c)
         c->watch_host[i] = 0;
     }
     c->watch_pending = 0;
+    if (bad == 5) return gbx_fail(c, GBX_ERR_ARG, "non-finite operand: the Ozaki path needs finite inputs");
     if (bad) return gbx_fail(c, GBX_ERR_TIMEOUT, "a bounded device wait gave up (code %d)", bad);
     return GBX_OK;
 }

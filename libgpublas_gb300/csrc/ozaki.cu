@@ -81,58 +81,127 @@ __device__ __forceinline__ double src_get(const SrcView &v, int r, int k)
     return part == 0 ? re : (part == 1 ? im : -im);
 }
 
-// Per-row max |x| -> exponent e (max < 2^e), and sum of (x 2^-e)^2.
-// One warp per row for row_k sources, a 32-row x 8-lane block for col_k.
-__global__ void __launch_bounds__(256)
-oz_row_stats(SrcView v, int rows, int K, int *__restrict__ expo, double *__restrict__ ss)
+// ---- operand statistics on the binary64 bit patterns --------------------
+// GB300 runs FP64 at ~1.2 TFLOP/s, so the statistics and the slicing work on
+// the integer pipe: row maxima are integer maxima of |x| bit patterns, and
+// the sum of squares (used only to choose the slice count) is an FP32
+// estimate built from the exponent and top mantissa bits.
+constexpr int OZ_NONFINITE = 5;   // status word: an operand holds Inf/NaN
+
+__device__ __forceinline__ unsigned long long abs_bits(double x)
 {
-    __shared__ double s_max[8][32];
-    __shared__ double s_ss[8][32];
-    if (v.row_k && !v.cplx) {
-        const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-        if (warp >= rows) return;
-        double m = 0.0;
-        for (int k = lane; k < K; k += 32) m = fmax(m, fabs(src_get(v, warp, k)));
-        for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        int e = 0;
-        if (m > 0.0) frexp(m, &e);
-        double s = 0.0;
-        for (int k = lane; k < K; k += 32) {
-            const double y = ldexp(src_get(v, warp, k), -e);
-            s = fma(y, y, s);
-        }
-        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) { expo[warp] = e; ss[warp] = s; }
-        return;
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// frexp exponent e (|x| < 2^e, |x| >= 2^(e-1)) of a finite |x| bit pattern.
+__device__ __forceinline__ int expo_of_bits(unsigned long long b)
+{
+    if (b == 0) return 0;
+    const int E = (int)(b >> 52);
+    if (E == 0) return (64 - __clzll((long long)b)) - 1074;   // subnormal
+    return E - 1022;
+}
+
+// Running max and scaled sum of squares: ss = sum (|x| / 2^(mref-1023))^2
+// over the elements seen, mref the largest biased exponent seen.
+struct SsAcc {
+    unsigned long long maxb;
+    int mref;
+    float ss;
+    __device__ __forceinline__ void init() { maxb = 0ull; mref = 0; ss = 0.f; }
+    // v * 2^(2*d) for d <= 0 (exact power-of-two factor; tiny -> 0)
+    static __device__ __forceinline__ float scale(float v, int d)
+    {
+        return d < -60 ? 0.f : v * __int_as_float((127 + 2 * d) << 23);
     }
-    // 32 rows per block, 8 k-lanes per row
+    __device__ __forceinline__ void add(unsigned long long b)
+    {
+        maxb = b > maxb ? b : maxb;
+        const int E = (int)(b >> 52);
+        if (E == 0) return;   // zeros and subnormals do not move the estimate
+        if (E > mref) { ss = scale(ss, mref - E); mref = E; }
+        const int d = mref - E;
+        if (d > 60) return;
+        const float y = __int_as_float(((127 - d) << 23) | (int)((b >> 29) & 0x7FFFFFull));
+        ss = fmaf(y, y, ss);
+    }
+    __device__ __forceinline__ void merge(const SsAcc &o)
+    {
+        maxb = o.maxb > maxb ? o.maxb : maxb;
+        if (o.mref > mref) { ss = scale(ss, mref - o.mref) + o.ss; mref = o.mref; }
+        else ss += scale(o.ss, o.mref - mref);
+    }
+    // expo = e of the row max; ss of x * 2^-e (a factor 1/4 from the
+    // definition of mref for normal maxima)
+    __device__ __forceinline__ void finish(int &e, double &s) const
+    {
+        e = expo_of_bits(maxb);
+        s = (maxb >> 52) ? 0.25 * (double)ss : 0.0;
+    }
+};
+
+__device__ __forceinline__ void flag_nonfinite(unsigned long long b, int *status)
+{
+    if ((b >> 52) == 0x7FFull) atomicCAS(status, 0, OZ_NONFINITE);
+}
+
+// row_k sources (K contiguous per row): one warp per row.
+__global__ void __launch_bounds__(256)
+oz_stats_rowk(SrcView v, int rows, int K, int *__restrict__ expo, double *__restrict__ ss, int *status)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= rows) return;
+    SsAcc a;
+    a.init();
+    for (int k = lane; k < K; k += 32) {
+        const unsigned long long b = abs_bits(src_get(v, warp, k));
+        flag_nonfinite(b, status);
+        a.add(b);
+    }
+    for (int o = 16; o; o >>= 1) {
+        SsAcc t;
+        t.maxb = __shfl_xor_sync(0xffffffffu, a.maxb, o);
+        t.mref = __shfl_xor_sync(0xffffffffu, a.mref, o);
+        t.ss = __shfl_xor_sync(0xffffffffu, a.ss, o);
+        a.merge(t);
+    }
+    if (lane == 0) a.finish(expo[warp], ss[warp]);
+}
+
+// col_k sources (rows contiguous): 32 rows x 8 k-lanes per block, one block
+// column per chunk of OZ_STATS_KCH k; partials merged by oz_stats_combine.
+constexpr int OZ_STATS_KCH = 1024;
+
+__global__ void __launch_bounds__(256)
+oz_stats_colk(SrcView v, int rows, int K, SsAcc *__restrict__ part, int *status)
+{
+    __shared__ SsAcc s_acc[8][32];
     const int rr = threadIdx.x & 31, kl = threadIdx.x >> 5;
     const int r = blockIdx.x * 32 + rr;
-    double m = 0.0;
+    const int k0 = blockIdx.y * OZ_STATS_KCH, k1 = min(K, k0 + OZ_STATS_KCH);
+    SsAcc a;
+    a.init();
     if (r < rows)
-        for (int k = kl; k < K; k += 8) m = fmax(m, fabs(src_get(v, r, k)));
-    s_max[kl][rr] = m;
-    __syncthreads();
-    if (kl == 0) {
-        for (int q = 1; q < 8; q++) m = fmax(m, s_max[q][rr]);
-        s_max[0][rr] = m;
-    }
-    __syncthreads();
-    m = s_max[0][rr];
-    int e = 0;
-    if (m > 0.0) frexp(m, &e);
-    double s = 0.0;
-    if (r < rows)
-        for (int k = kl; k < K; k += 8) {
-            const double y = ldexp(src_get(v, r, k), -e);
-            s = fma(y, y, s);
+        for (int k = k0 + kl; k < k1; k += 8) {
+            const unsigned long long b = abs_bits(src_get(v, r, k));
+            flag_nonfinite(b, status);
+            a.add(b);
         }
-    s_ss[kl][rr] = s;
+    s_acc[kl][rr] = a;
     __syncthreads();
     if (kl == 0 && r < rows) {
-        for (int q = 1; q < 8; q++) s += s_ss[q][rr];
-        expo[r] = e;
-        ss[r] = s;
+        for (int q = 1; q < 8; q++) a.merge(s_acc[q][rr]);
+        part[(size_t)blockIdx.y * rows + r] = a;
+    }
+}
+
+__global__ void oz_stats_combine(const SsAcc *__restrict__ part, int rows, int nkb, int *__restrict__ expo,
+                                 double *__restrict__ ss)
+{
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        SsAcc a = part[r];
+        for (int q = 1; q < nkb; q++) a.merge(part[(size_t)q * rows + r]);
+        a.finish(expo[r], ss[r]);
     }
 }
 
@@ -169,27 +238,68 @@ oz_split(SrcView v, int rows, int K, int Rp, int Kp, const int *__restrict__ exp
     const int r = r0 + rr;
     if (r >= Rp) return;
     const int e = r < rows ? expo[r] : 0;
-    double y[16];
+    // N_j = round(|x_j| * 2^(4 - e + 5(S-1))) as a 128-bit integer hi:lo.
+    // |x| < 2^e bounds N_j by 16 * 32^(S-1) <= 2^69.  Integer pipe only.
+    const int top = 4 - e + 5 * (S - 1);
+    unsigned long long lo[16], hi[16];
+    unsigned neg = 0u;
 #pragma unroll
-    for (int j = 0; j < 16; j++) y[j] = ldexp(tile[rr][kq + j], -e) * 16.0;   // |y| < 16
-    for (int s = 0; s < S; s++) {
+    for (int j = 0; j < 16; j++) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(tile[rr][kq + j]);
+        neg |= (unsigned)(b >> 63) << j;
+        const int E = (int)((b >> 52) & 0x7FF);
+        const unsigned long long M = (b & 0xFFFFFFFFFFFFFull) | (E ? (1ull << 52) : 0ull);
+        const int sh = (E ? E : 1) - 1075 + top;
+        if (M == 0ull || sh <= -54) { lo[j] = 0ull; hi[j] = 0ull; }
+        else if (sh < 0) { lo[j] = (M + (1ull << (-sh - 1))) >> (-sh); hi[j] = 0ull; }
+        else if (sh == 0) { lo[j] = M; hi[j] = 0ull; }
+        else if (sh < 64) { lo[j] = M << sh; hi[j] = M >> (64 - sh); }
+        else { lo[j] = 0ull; hi[j] = M << (sh - 64); }
+    }
+    // balanced base-32 digits, least significant first: d in [-15, 16]
+    for (int s = S - 1; s >= 0; s--) {
         uint32_t w[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-            const double d = rint(y[j]);
-            y[j] = (y[j] - d) * 32.0;   // exact: |y - d| <= 1/2
-            w[j >> 2] |= e4m3_of_digit((int)d) << (8 * (j & 3));
+            int d = (int)(lo[j] & 31ull);
+            if (d > 16) {
+                d -= 32;
+                const unsigned long long nl = lo[j] + (unsigned long long)(-d);
+                hi[j] += (nl < lo[j]) ? 1ull : 0ull;
+                lo[j] = nl;
+            } else {
+                lo[j] -= (unsigned long long)d;   // clears the low 5 bits, no borrow
+            }
+            lo[j] = (lo[j] >> 5) | (hi[j] << 59);
+            hi[j] >>= 5;
+            const int sd = ((neg >> j) & 1u) ? -d : d;
+            w[j >> 2] |= e4m3_of_digit(sd) << (8 * (j & 3));
         }
         uint4 *dst = (uint4 *)(X8 + ((size_t)s * Rp + r) * Kp + k0 + kq);
         *dst = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
 
-// Scale vectors 2^(e-4) (row r, padded rows 0).
-__global__ void oz_scales(const int *__restrict__ expo, int rows, int Rp, double *__restrict__ scale)
+// Scale exponents e-4 of the slices' power-of-two scale 2^(e-4) (padded
+// rows: 0; their digits are zero).
+__global__ void oz_scales(const int *__restrict__ expo, int rows, int Rp, int *__restrict__ scale)
 {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < Rp; r += gridDim.x * blockDim.x)
-        scale[r] = r < rows ? ldexp(1.0, expo[r] - 4) : 0.0;
+        scale[r] = r < rows ? expo[r] - 4 : 0;
+}
+
+// acc * 2^shift as a double, built from the FP32 accumulator's bit pattern
+// with integer operations (acc is an integer-valued float, |acc| <= 2^24).
+// Results below the binary64 normal range flush to zero, above it give Inf.
+__device__ __forceinline__ double scaled_acc(uint32_t fb, int shift)
+{
+    if ((fb & 0x7FFFFFFFu) == 0u) return 0.0;
+    const int ex = (int)((fb >> 23) & 0xFFu) - 127 + 1023 + shift;
+    const unsigned long long sign = (unsigned long long)(fb >> 31) << 63;
+    if (ex <= 0) return __longlong_as_double((long long)sign);
+    if (ex >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+    return __longlong_as_double(
+        (long long)(sign | ((unsigned long long)ex << 52) | ((unsigned long long)(fb & 0x7FFFFFu) << 29)));
 }
 
 // Slice count: relative Frobenius error ~ c * 2^(-5S) * gamma_A * gamma_B with
@@ -237,10 +347,10 @@ oz_choose_slices(const int *ea, const double *ssa, int M, const int *eb, const d
         int S;
         if (forced > 0) S = forced;
         else {
-            // c = 2^3 covers the truncated cross terms and the rounding of
-            // the FP64 recombination with margin (calibrated against the
-            // double-double oracle on uniform and exponent-spread inputs).
-            const double bits = -log2(tol) + ga + gb + 3.0;
+            // error ~ c * 2^(-5S) * gamma_A * gamma_B; c = 2^1.5 covers the
+            // truncated cross terms and the FP64 recombination (measured
+            // c ~ 1.4 against the double-double oracle on uniform inputs).
+            const double bits = -log2(tol) + ga + gb + 1.5;
             S = (int)ceil(bits / 5.0);
         }
         S_dev[0] = max(1, min(OZ_SMAX, S));
@@ -254,8 +364,8 @@ struct OzParams {
     int M, N, Mp, Np, Kp;
     int tiles_m, tiles_n;
     const int *S;
-    const double *row_scale;   // Mp
-    const double *col_scale;   // Np
+    const int *row_exp;        // Mp: e_i - 4
+    const int *col_exp;        // Np: f_j - 4
     double *W;                 // Mp x Np, column-major
     double *C;
     long long ldc;
@@ -280,10 +390,10 @@ struct GroupPlan {
     }
 };
 
-__device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn)
+__device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, int bm = OZ_BM)
 {
     if (p.c_part == 0) return true;
-    const int r0 = tm * OZ_BM, r1 = r0 + OZ_BM - 1, c0 = tn * OZ_BN, c1 = c0 + OZ_BN - 1;
+    const int r0 = tm * bm, r1 = r0 + bm - 1, c0 = tn * OZ_BN, c1 = c0 + OZ_BN - 1;
     return p.c_part == 1 ? (r1 >= c0) : (r0 <= c1);
 }
 
@@ -407,12 +517,12 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             const int tm = t % p.tiles_m, tn = t / p.tiles_m;
             if (!tile_needed(p, tm, tn)) continue;
             const int grow = tm * OZ_BM + row;
-            const double rsc = p.row_scale[grow];
+            const int rexp = p.row_exp[grow];
             bool first = true;
             for (int q = gp.S - 1; q >= 0 && ok; q--) {
                 const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                 const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
-                const double rs = ldexp(rsc, -5 * q);
+                const int rs = rexp - 5 * q;   // weight 2^(e_i - 4 - 5q)
                 for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
                     const bool last = (q == 0) && (g0 + gp.items_per_group >= nitems);
                     // warp-uniform outcome: tcgen05.ld below is .sync.aligned
@@ -427,7 +537,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 #pragma unroll
                         for (int j = 0; j < 32; j++) {
                             const int gcol = tn * OZ_BN + c * 32 + j;
-                            const double v = (double)__uint_as_float(r[j]) * (rs * p.col_scale[gcol]);
+                            const double v = scaled_acc(r[j], rs + p.col_exp[gcol]);
                             double *w = p.W + (size_t)gcol * p.Mp + grow;
                             if (!last) {
                                 *w = first ? v : *w + v;
@@ -455,6 +565,205 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem_base, 512);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// CTA-pair variant (tcgen05 cta_group::2): a cluster of two CTAs on two SMs
+// computes a 256x256 tile with M=256 MMAs issued by the even CTA.  Each CTA
+// loads its own 128 rows of the A slice and its own 128 rows of the B slice
+// (half of N), so every SM moves 32 KB per k-block instead of 48 KB for the
+// same tensor work, and six stages fit in shared memory.  Each CTA's TMEM
+// holds its 128 rows x 256 columns of the accumulator; both CTAs drain their
+// own half in the epilogue.
+//   full[s]   (even CTA): both producers arrive + expect 32 KB each; both
+//             CTAs' TMA loads complete on it (cta_group::2 TMA)
+//   empty[s]  (each CTA): arrived by the MMA commit, multicast to both CTAs
+//   tfull[b]  (each CTA): arrived by the MMA commit, multicast to both CTAs
+//   tempty[b] (even CTA): 256 epilogue threads of both CTAs arrive
+// ---------------------------------------------------------------------------
+constexpr int OZ2_BM = 256, OZ2_STAGES = 6;
+constexpr int OZ2_HALF = 128 * OZ_BK;                // 16 KB: 128 rows x 128 bytes
+constexpr int OZ2_STAGE_BYTES = 2 * OZ2_HALF;        // A half + B half
+constexpr size_t OZ2_SMEM = (size_t)OZ2_STAGES * OZ2_STAGE_BYTES + 1024 + 256;
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(OZ_THREADS, 1)
+oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + OZ2_STAGES * OZ2_STAGE_BYTES);
+    uint64_t *full = bars, *empty = bars + OZ2_STAGES;
+    uint64_t *tfull = bars + 2 * OZ2_STAGES, *tempty = tfull + 2;
+    uint32_t *tmem_slot = (uint32_t *)(tempty + 2);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_ctarank();
+    const bool leader = (rank & 1u) == 0u;
+    volatile int *status = p.status;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < OZ2_STAGES; i++) { mbar_init(&full[i], 2); mbar_init(&empty[i], 1); }
+        for (int i = 0; i < 2; i++) { mbar_init(&tfull[i], 1); mbar_init(&tempty[i], 256); }
+        fence_barrier_init();
+        prefetch_tmap(&tmA);
+        prefetch_tmap(&tmB);
+    }
+    if (warp == 1) {
+        tmem_alloc_pair(tmem_slot, 512);
+        tmem_relinquish_pair();
+    }
+    tc_fence_before();
+    __syncthreads();
+    cluster_sync();   // peers' barriers are initialised before any remote arrive
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+    const uint32_t leader_rank = rank & ~1u;
+
+    GroupPlan gp;
+    gp.init(*p.S, p.Kp);
+    const int ntiles = p.tiles_m * p.tiles_n;
+    const int pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
+
+    if (warp == 0) {
+        // ---------------- TMA producer (both CTAs) ----------------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            for (int t = pair; t < ntiles && ok; t += npairs) {
+                const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+                if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
+                for (int q = gp.S - 1; q >= 0 && ok; q--) {
+                    const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
+                    const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
+                    for (int it = 0; it < nitems && ok; it++) {
+                        const int s = s_lo + it / gp.nchunks, t2 = q - s, ch = it % gp.nchunks;
+                        const int kb0 = ch * gp.kch_blocks, kb1 = min(gp.nkb, kb0 + gp.kch_blocks);
+                        for (int kb = kb0; kb < kb1; kb++) {
+                            if (!mbar_wait_cl(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
+                            uint8_t *sa = smem + stage * OZ2_STAGE_BYTES;
+                            const uint32_t fbar = mapa_cluster(smem_u32(&full[stage]), leader_rank);
+                            mbar_arrive_expect_tx_cluster(fbar, OZ2_STAGE_BYTES);
+                            tma_load_2d_pair(sa, &tmA, fbar, kb * OZ_BK,
+                                             s * p.Mp + tm * OZ2_BM + (int)(rank & 1u) * 128);
+                            tma_load_2d_pair(sa + OZ2_HALF, &tmB, fbar, kb * OZ_BK,
+                                             t2 * p.Np + tn * OZ_BN + (int)(rank & 1u) * 128);
+                            if (++stage == OZ2_STAGES) { stage = 0; phase ^= 1u; }
+                        }
+                    }
+                }
+            }
+            for (int i = 0; i < OZ2_STAGES; i++) {
+                mbar_wait_cl(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY);
+                if (++stage == OZ2_STAGES) { stage = 0; phase ^= 1u; }
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer (even CTA only) ----------------
+        if (leader && lane == 0) {
+            constexpr uint32_t idesc = idesc_e4m3_f32(OZ2_BM, OZ_BN);
+            int stage = 0, buf = 0;
+            uint32_t phase = 0, tphase = 0;
+            bool ok = true;
+            const uint32_t smem_base = smem_u32(smem);
+            for (int t = pair; t < ntiles && ok; t += npairs) {
+                const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+                if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
+                for (int q = gp.S - 1; q >= 0 && ok; q--) {
+                    const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
+                    const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
+                    for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
+                        const int g1 = min(nitems, g0 + gp.items_per_group);
+                        if (!mbar_wait_cl(&tempty[buf], tphase ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
+                        tc_fence_after();
+                        const uint32_t d_tmem = tmem_base + (uint32_t)(buf * OZ_BN);
+                        uint32_t acc = 0;
+                        for (int it = g0; it < g1 && ok; it++) {
+                            const int ch = it % gp.nchunks;
+                            const int kb0 = ch * gp.kch_blocks, kb1 = min(gp.nkb, kb0 + gp.kch_blocks);
+                            for (int kb = kb0; kb < kb1; kb++) {
+                                if (!mbar_wait_cl(&full[stage], phase, status, TC_TIMEOUT_FULL)) { ok = false; break; }
+                                tc_fence_after();
+                                const uint32_t a_addr = smem_base + stage * OZ2_STAGE_BYTES;
+                                const uint32_t b_addr = a_addr + OZ2_HALF;
+#pragma unroll
+                                for (int kk = 0; kk < OZ_BK / 32; kk++) {
+                                    mma_f8f6f4_pair(d_tmem, smem_desc_k128(a_addr + kk * 32),
+                                                    smem_desc_k128(b_addr + kk * 32), idesc, acc);
+                                    acc = 1;
+                                }
+                                mma_commit_pair_mc(&empty[stage], (uint16_t)(3u << leader_rank));
+                                if (++stage == OZ2_STAGES) { stage = 0; phase ^= 1u; }
+                            }
+                        }
+                        mma_commit_pair_mc(&tfull[buf], (uint16_t)(3u << leader_rank));
+                        if (++buf == 2) { buf = 0; tphase ^= 1u; }
+                    }
+                }
+            }
+        }
+    } else {
+        // ---------------- epilogue (warps 2..5, both CTAs) ----------------
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        int buf = 0;
+        uint32_t tphase = 0;
+        bool ok = true;
+        const uint32_t tempty_cl0 = mapa_cluster(smem_u32(&tempty[0]), leader_rank);
+        const uint32_t tempty_cl1 = mapa_cluster(smem_u32(&tempty[1]), leader_rank);
+        for (int t = pair; t < ntiles && ok; t += npairs) {
+            const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+            if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
+            const int grow = tm * OZ2_BM + (int)(rank & 1u) * 128 + row;
+            const int rexp = p.row_exp[grow];
+            bool first = true;
+            for (int q = gp.S - 1; q >= 0 && ok; q--) {
+                const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
+                const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
+                const int rs = rexp - 5 * q;
+                for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
+                    const bool last = (q == 0) && (g0 + gp.items_per_group >= nitems);
+                    ok = __all_sync(0xffffffffu, mbar_wait_cl(&tfull[buf], tphase, status, TC_TIMEOUT_TMEM_FULL));
+                    if (!ok) break;
+                    tc_fence_after();
+                    const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * OZ_BN);
+                    for (int c = 0; c < OZ_BN / 32; c++) {
+                        uint32_t r[32];
+                        tmem_ld_32x32b_x32(taddr + c * 32, r);
+                        tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 32; j++) {
+                            const int gcol = tn * OZ_BN + c * 32 + j;
+                            const double v = scaled_acc(r[j], rs + p.col_exp[gcol]);
+                            double *w = p.W + (size_t)gcol * p.Mp + grow;
+                            if (!last) {
+                                *w = first ? v : *w + v;
+                            } else {
+                                const double tot = first ? v : *w + v;
+                                if (grow < p.M && gcol < p.N &&
+                                    (p.c_part == 0 || (p.c_part == 1 ? grow >= gcol : grow <= gcol))) {
+                                    double *cp = p.C + (size_t)gcol * p.ldc + grow;
+                                    *cp = (p.beta == 0.0) ? p.alpha * tot : fma(p.alpha, tot, p.beta * *cp);
+                                }
+                            }
+                        }
+                    }
+                    tc_fence_before();
+                    mbar_arrive_cluster(buf ? tempty_cl1 : tempty_cl0);
+                    first = false;
+                    if (++buf == 2) { buf = 0; tphase ^= 1u; }
+                }
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    cluster_sync();   // no CTA leaves while its peer may still signal its barriers
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc_pair(tmem_base, 512);
     }
 }
 
@@ -515,11 +824,25 @@ bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int bo
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The CTA-pair kernel is selected with GBX_OZAKI_PAIR=1 for problems with
+// more than one 128-row tile of op(A).  It is correct but measured slower
+// than the one-CTA kernel at n = 8192 (43 ms vs 30 ms of MMA time), so the
+// one-CTA kernel is the default; the tests cover both.
+bool oz_use_pair(int M)
+{
+    static int env = [] {
+        const char *s = getenv("GBX_OZAKI_PAIR");
+        return s ? atoi(s) : 0;
+    }();
+    return env != 0 && M > OZ_BM;
+}
+
 // Workspace layout for one Ozaki product.
 struct OzBuffers {
     uint8_t *A8, *B8;
     int *ea, *eb, *S;
-    double *ssa, *ssb, *rsa, *csb, *W;
+    int *rsa, *csb;   // scale exponents e-4 (rows of op(A), columns of op(B))
+    double *ssa, *ssb, *W;
     int *status;
 };
 
@@ -540,24 +863,34 @@ gbx_status oz_buffers(gbx_ctx *ctx, int Mp, int Np, int Kp, int nW, OzBuffers &b
     b.S = (int *)q; q += 64;
     b.ssa = (double *)q; q += sizeof(double) * Mp;
     b.ssb = (double *)q; q += sizeof(double) * Np;
-    b.rsa = (double *)q; q += sizeof(double) * Mp;
-    b.csb = (double *)q; q += sizeof(double) * Np;
+    b.rsa = (int *)q; q += sizeof(double) * Mp;
+    b.csb = (int *)q; q += sizeof(double) * Np;
     b.ea = (int *)q; q += sizeof(int) * Mp;
     b.eb = (int *)q;
     return GBX_OK;
 }
 
 gbx_status split_operand(gbx_ctx *ctx, const SrcView &v, int rows, int K, int Rp, int Kp, int *expo, double *ss,
-                         const int *S_dev, uint8_t *X8, double *scale, bool stats_only)
+                         const int *S_dev, uint8_t *X8, int *scale, bool stats_only, int *status)
 {
     cudaStream_t s = S_(ctx);
     if (stats_only) {
-        if (v.row_k && !v.cplx)
-            oz_row_stats<<<(rows * 32 + 255) / 256, 256, 0, s>>>(v, rows, K, expo, ss);
-        else
-            oz_row_stats<<<(rows + 31) / 32, 256, 0, s>>>(v, rows, K, expo, ss);
+        if (v.row_k) {
+            oz_stats_rowk<<<(rows * 32 + 255) / 256, 256, 0, s>>>(v, rows, K, expo, ss, status);
+            gbx_count_launch(ctx, 1);
+        } else {
+            const int nkb = (K + OZ_STATS_KCH - 1) / OZ_STATS_KCH;
+            void *p;
+            gbx_status st = gbx_ws(ctx, GBX_WS_TMP2, sizeof(SsAcc) * (size_t)nkb * rows, &p);
+            if (st != GBX_OK) return st;
+            dim3 g((rows + 31) / 32, nkb);
+            oz_stats_colk<<<g, 256, 0, s>>>(v, rows, K, (SsAcc *)p, status);
+            oz_stats_combine<<<std::min(1024, (rows + 255) / 256), 256, 0, s>>>((const SsAcc *)p, rows, nkb,
+                                                                                expo, ss);
+            gbx_count_launch(ctx, 2);
+        }
         oz_scales<<<std::min(1024, (Rp + 255) / 256), 256, 0, s>>>(expo, rows, Rp, scale);
-        gbx_count_launch(ctx, 2);
+        gbx_count_launch(ctx, 1);
         return gbx_check_launch(ctx, "ozaki stats");
     }
     dim3 g(Kp / 128, Rp / 32);
@@ -580,7 +913,9 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
                      OzBuffers *keep = nullptr, int nW = 1, int w_index = 0)
 {
     if (pr.K > 0x3fffffff) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: K too large");
-    const int Mp = (int)rup(pr.M, OZ_BM), Np = (int)rup(pr.N, OZ_BN), Kp = (int)rup(std::max(pr.K, 1), OZ_BK);
+    const bool pair = oz_use_pair(pr.M);
+    const int Mp = (int)rup(pr.M, pair ? OZ2_BM : OZ_BM), Np = (int)rup(pr.N, OZ_BN);
+    const int Kp = (int)rup(std::max(pr.K, 1), OZ_BK);
     OzBuffers b;
     gbx_status st;
     if (keep) b = *keep;
@@ -590,63 +925,86 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     cudaMemsetAsync(b.status, 0, 64, s);
 
     gbx_timer_begin(ctx, GBX_TIMER_OZAKI_SPLIT);
-    if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Mp, Kp, b.ea, b.ssa, b.S, b.A8, b.rsa, true)) != GBX_OK) return st;
-    if (!pr.same_ab &&
-        (st = split_operand(ctx, pr.b, pr.N, pr.K, Np, Kp, b.eb, b.ssb, b.S, b.B8, b.csb, true)) != GBX_OK)
+    if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Mp, Kp, b.ea, b.ssa, b.S, b.A8, b.rsa, true, b.status)) !=
+        GBX_OK)
+        return st;
+    if (!pr.same_ab && (st = split_operand(ctx, pr.b, pr.N, pr.K, Np, Kp, b.eb, b.ssb, b.S, b.B8, b.csb, true,
+                                           b.status)) != GBX_OK)
         return st;
     const int *eb = pr.same_ab ? b.ea : b.eb;
     const double *ssb = pr.same_ab ? b.ssa : b.ssb;
     oz_choose_slices<<<1, 256, 0, s>>>(b.ea, b.ssa, pr.M, eb, ssb, pr.N, pr.K, tol, forced, b.S);
     gbx_count_launch(ctx, 1);
-    if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Mp, Kp, b.ea, b.ssa, b.S, b.A8, b.rsa, false)) != GBX_OK) return st;
+    if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Mp, Kp, b.ea, b.ssa, b.S, b.A8, b.rsa, false, b.status)) !=
+        GBX_OK)
+        return st;
     uint8_t *B8 = b.B8;
-    const double *csb = b.csb;
+    const int *csb = b.csb;
     if (pr.same_ab) {
         // B slices are the A slices; rows padded to Np (Np >= Mp here since M == N)
         B8 = b.A8;
         csb = b.rsa;
         if (Np != Mp) {
             // re-split into the Np-row layout the B tiles expect
-            if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Np, Kp, b.ea, b.ssa, b.S, b.B8, b.csb, false)) != GBX_OK)
+            if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Np, Kp, b.ea, b.ssa, b.S, b.B8, b.csb, false,
+                                    b.status)) != GBX_OK)
                 return st;
             oz_scales<<<std::min(1024, (Np + 255) / 256), 256, 0, s>>>(b.ea, pr.M, Np, b.csb);
             gbx_count_launch(ctx, 1);
             B8 = b.B8;
             csb = b.csb;
         }
-    } else if ((st = split_operand(ctx, pr.b, pr.N, pr.K, Np, Kp, b.eb, b.ssb, b.S, b.B8, b.csb, false)) != GBX_OK) {
+    } else if ((st = split_operand(ctx, pr.b, pr.N, pr.K, Np, Kp, b.eb, b.ssb, b.S, b.B8, b.csb, false,
+                                   b.status)) != GBX_OK) {
         return st;
     }
     gbx_timer_end(ctx);
 
     CUtensorMap tmA, tmB;
     if (!make_map(&tmA, b.A8, (long long)OZ_SMAX * Mp, Kp, OZ_BM) ||
-        !make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, OZ_BN))
+        !make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : OZ_BN))
         return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
 
     OzParams p{};
     p.M = pr.M; p.N = pr.N; p.Mp = Mp; p.Np = Np; p.Kp = Kp;
-    p.tiles_m = Mp / OZ_BM; p.tiles_n = Np / OZ_BN;
+    p.tiles_m = Mp / (pair ? OZ2_BM : OZ_BM); p.tiles_n = Np / OZ_BN;
     p.S = b.S;
-    p.row_scale = b.rsa;
-    p.col_scale = csb;
+    p.row_exp = b.rsa;
+    p.col_exp = csb;
     p.W = b.W + (size_t)w_index * Mp * Np;
     p.C = pr.C; p.ldc = pr.ldc;
     p.alpha = pr.alpha; p.beta = pr.beta;
     p.c_part = pr.c_part;
     p.status = b.status;
 
-    static bool attr = false;
-    if (!attr) {
+    static int max_pairs = -1;
+    if (max_pairs < 0) {
         if (cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM) !=
-            cudaSuccess)
+                cudaSuccess ||
+            cudaFuncSetAttribute(oz_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ2_SMEM) !=
+                cudaSuccess)
             return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: shared memory attribute");
-        attr = true;
+        // how many CTA pairs can be resident at once (clusters must fit in a GPC)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2 * (unsigned)std::max(1, gbx_ctx_sms(ctx) / 2));
+        cfg.blockDim = dim3(OZ_THREADS);
+        cfg.dynamicSmemBytes = OZ2_SMEM;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, oz_gemm2_kernel, &cfg) != cudaSuccess || nc < 1) {
+            cudaGetLastError();
+            nc = gbx_ctx_sms(ctx) / 2;
+        }
+        max_pairs = nc;
     }
     const int ntiles = p.tiles_m * p.tiles_n;
-    const int grid = std::min(ntiles, gbx_ctx_sms(ctx));
     gbx_timer_begin(ctx, GBX_TIMER_OZAKI_MMA);
-    oz_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(tmA, tmB, p);
+    if (pair) {
+        const int npairs = std::max(1, std::min(ntiles, max_pairs));
+        oz_gemm2_kernel<<<2 * npairs, OZ_THREADS, OZ2_SMEM, s>>>(tmA, tmB, p);
+    } else {
+        const int grid = std::min(ntiles, gbx_ctx_sms(ctx));
+        oz_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(tmA, tmB, p);
+    }
     gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);
     if ((st = gbx_check_launch(ctx, "ozaki gemm")) != GBX_OK) return st;
@@ -733,7 +1091,7 @@ extern "C" gbx_status gbx_zgemm_ozaki(gbx_ctx *ctx, char ta, char tb, int m, int
     }
     if (2LL * k > 0x3fffffffLL) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: K too large");
     const int K2 = 2 * k;
-    const int Mp = (int)rup(m, OZ_BM), Np = (int)rup(n, OZ_BN);
+    const int Mp = (int)rup(m, oz_use_pair(m) ? OZ2_BM : OZ_BM), Np = (int)rup(n, OZ_BN);
     const int Kp = (int)rup(K2, OZ_BK);
     OzBuffers b;
     gbx_status st = oz_buffers(ctx, Mp, Np, Kp, 2, b);

@@ -161,6 +161,22 @@ def test_zgemm_ozaki(orc, dev, ta, tb):
     assert rel(got[rows, cols], ref) <= TOL
 
 
+@pytest.mark.skipif(__import__("os").environ.get("GBX_OZAKI_PAIR") == "1",
+                    reason="already running with the CTA-pair kernel")
+def test_cta_pair_kernel_variant():
+    # The one-CTA kernel is the default; rerun the kernel tests in a child
+    # process with the CTA-pair (tcgen05 cta_group::2) kernel selected.
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GBX_OZAKI_PAIR="1", PYTHONPATH=root)
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider",
+                        os.path.abspath(__file__), "-k", "exact or shapes or spread or syrk or zgemm"],
+                       capture_output=True, text=True, env=env, cwd=root, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
+
+
 def test_f77_precision_option_routes_to_ozaki(orc):
     # BLAS2CUDA_OPTIONS=precision=ozaki sends dgemm_ through the split path;
     # checked in a child process because options are read once per process.
