@@ -1,30 +1,36 @@
 #!/usr/bin/env python
-"""Headline benchmark: FP64 DGEMM throughput of libgbxblas on one GB300.
+"""Benchmarks of libgbxblas on one GB300 (one JSON line per run).
 
-Workload (default): DGEMM 'N','N', M = N = K = 8192, column-major, lda = ldb =
-ldc = 8192, alpha = 1, beta = 0.5, A, B, C uniform[-1,1] from SplitMix64 seed
-1 (the plain FP64 drop-in sweep's DGEMM at n = 8192).  One step = one DGEMM
-call.  Operands (3 x 512 MiB) are larger than the 129 MB L2, so no flush is
-needed between steps.
+Default workload (the headline): DGEMM 'N','N', M = N = K = 8192,
+column-major, lda = ldb = ldc = 8192, alpha = 1, beta = 0.5, A, B, C uniform
+[-1,1] from SplitMix64 seed 1 -- the plain FP64 drop-in sweep's DGEMM at
+n = 8192.  One step = one DGEMM call.  Operands (3 x 512 MiB) exceed the
+129 MB L2, so no flush is needed between steps.
 
-  value  -- TFLOP/s (2*n^3 per step) with operands resident in HBM, timed
-            with CUDA events on the library's stream (device C ABI, gbx_dgemm)
-  e2e    -- the same metric through the drop-in Fortran symbol dgemm_ on
-            pinned host buffers: every step copies A, B, C host->device and C
-            device->host inside the timed region
-  ozaki  -- the opt-in Ozaki split-precision DGEMM on the same operands
-            (TFLOP/s counted as 2*n^3, relative Frobenius error against the
-            double-double oracle on sampled entries, slices used)
-  roofline -- the dominant kernel (DFMA GEMM core) against the FP64 FMA rate
-            measured in the same run
-  cpu_baseline -- the CPU BLAS the reference falls back to (OpenBLAS through
-            its Fortran symbol) on this host's cores
+  value    TFLOP/s (2 n^3 per step), operands resident in HBM, CUDA events on
+           the library's stream, device C ABI (gbx_dgemm)
+  e2e      the same metric through the drop-in Fortran symbol dgemm_ on
+           pinned host buffers: A, B, C host->device and C device->host in
+           every step
+  ozaki    the opt-in Ozaki split-precision DGEMM on the same operands:
+           TFLOP/s counted as 2 n^3, relative Frobenius error against the
+           double-double oracle on sampled entries, slices used
+  roofline dominant kernel (DFMA GEMM core) against the FP64 FMA rate
+           measured in the same run
+  cpu_baseline  the CPU BLAS the reference falls back to, on this host
 
---impl reference times that CPU BLAS alone on the same workload (the
-reference's runnable path: dlsym(RTLD_NEXT) to the CPU BLAS).
+Other workloads (--workload), each from the plain FP64 sweep or the Ozaki
+configuration: ozaki (Ozaki DGEMM as the value, roofline against the FP8
+tensor peak), daxpy / ddot / dnrm2 / idamax (n = 2^28), dgemv (16384^2,
+'N' or 'T'), dtrsm (left/lower/N/non-unit 8192 with 1024 right-hand sides),
+dsyrk (lower, n = 8192, k = 2048).  Level-1/2 report GB/s of algorithmic
+traffic against the measured HBM copy bandwidth.
+
+--impl reference times the CPU BLAS alone on the same workload (the
+reference's runnable path ends there: dlsym(RTLD_NEXT) to the CPU BLAS).
 
 Multi-GPU: calls are independent, so N > 1 runs N replicas (one per rank,
-no collective on the data path); value = all ranks' flops / max time.
+no collective on the data path); value = all ranks' work / max time.
 """
 import argparse
 import json
@@ -43,6 +49,7 @@ import numpy as np  # noqa: E402
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+WORKLOADS = ("dgemm", "ozaki", "daxpy", "ddot", "dnrm2", "idamax", "dgemv", "dtrsm", "dsyrk")
 
 
 def parse_args():
@@ -51,12 +58,23 @@ def parse_args():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--n", type=int, default=8192)
+    p.add_argument("--workload", choices=WORKLOADS, default="dgemm")
+    p.add_argument("--n", type=int, default=0, help="problem size (0: the workload's default)")
+    p.add_argument("--trans", default="N", help="dgemv transposition")
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ozaki", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return d, "MEASURED_PEAKS.json"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback (6.8 TB/s, 1.9 PFLOP/s bf16)"
 
 
 class ClockSampler:
@@ -94,8 +112,7 @@ class ClockSampler:
 
     def summary(self):
         sm, smax, reasons = [], [], set()
-        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
-                 "sw_power_cap"]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
@@ -105,7 +122,7 @@ class ClockSampler:
                 smax.append(float(f[2]))
             except ValueError:
                 continue
-            for name, val in zip(names[1:], f[5:9]):
+            for name, val in zip(names, f[5:9]):
                 if val.lower() == "active":
                     reasons.add(name)
         if not sm:
@@ -120,8 +137,7 @@ def dist_setup(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
-        backend = "nccl" if args.impl == "ours" else "gloo"
-        dist.init_process_group(backend)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
     return ws, rank, local
 
 
@@ -141,34 +157,190 @@ def max_over_ranks(ws, v, device=None):
     return float(t.item())
 
 
-def make_inputs(n, seed):
-    import oracle
-    orc = oracle.get()
-    a, s = orc.matrix(n, n, seed)
-    b, s = orc.matrix(n, n, s)
-    c, s = orc.matrix(n, n, s)
-    return orc, a, b, c
+# --------------------------------------------------------------------------
+# workload definitions
+# --------------------------------------------------------------------------
+class Work:
+    """Inputs, a device step, a Fortran-ABI step and the CPU-BLAS step."""
+
+    def __init__(self, args):
+        import oracle
+        self.orc = oracle.get()
+        self.args = args
+        self.kind = args.workload
+        w = self.kind
+        seed = args.seed
+        o = self.orc
+        if w in ("dgemm", "ozaki"):
+            n = args.n or 8192
+            self.n = n
+            self.a, s = o.matrix(n, n, seed)
+            self.b, s = o.matrix(n, n, s)
+            self.c, s = o.matrix(n, n, s)
+            self.units, self.unit, self.metric = 2.0 * n ** 3 / 1e12, "TFLOP/s", f"{w}_tflops"
+            self.config = {"workload": f"{w}_NN_m{n}_n{n}_k{n}", "m": n, "n": n, "k": n, "lda": n,
+                           "alpha": 1.0, "beta": 0.5}
+        elif w in ("daxpy", "ddot", "dnrm2", "idamax"):
+            n = args.n or (1 << 28)
+            self.n = n
+            self.x, s = o.uniform(n, seed)
+            self.y, _ = o.uniform(n, s) if w in ("daxpy", "ddot") else (None, s)
+            nbytes = {"daxpy": 24, "ddot": 16, "dnrm2": 8, "idamax": 8}[w] * n
+            self.units, self.unit, self.metric = nbytes / 1e9, "GB/s", f"{w}_gbs"
+            self.config = {"workload": f"{w}_n{n}", "n": n, "incx": 1, "incy": 1,
+                           "bytes_per_step": nbytes}
+        elif w == "dgemv":
+            n = args.n or 16384
+            self.n = n
+            self.trans = args.trans.upper()
+            self.a, s = o.matrix(n, n, seed)
+            self.x, s = o.uniform(n, s)
+            self.y, _ = o.uniform(n, s)
+            nbytes = 8 * (n * n + n + 2 * n)
+            self.units, self.unit, self.metric = nbytes / 1e9, "GB/s", "dgemv_gbs"
+            self.config = {"workload": f"dgemv_{self.trans}_m{n}_n{n}", "m": n, "n": n,
+                           "alpha": 1.0, "beta": 0.5, "bytes_per_step": nbytes}
+        elif w == "dtrsm":
+            m = args.n or 8192
+            nrhs = 1024
+            self.m, self.nrhs = m, nrhs
+            self.a, s = o.trsm_matrix(m, seed)
+            self.b, _ = o.matrix(m, nrhs, s)
+            self.units, self.unit, self.metric = float(m) * m * nrhs / 1e12, "TFLOP/s", "dtrsm_tflops"
+            self.config = {"workload": f"dtrsm_LLNN_m{m}_n{nrhs}", "side": "L", "uplo": "L",
+                           "transa": "N", "diag": "N", "m": m, "n": nrhs, "alpha": 1.0}
+        elif w == "dsyrk":
+            n = args.n or 8192
+            k = 2048
+            self.n, self.k = n, k
+            self.a, s = o.matrix(n, k, seed)
+            self.c, _ = o.matrix(n, n, s)
+            self.units, self.unit, self.metric = float(n) * (n + 1) * k / 1e12, "TFLOP/s", "dsyrk_tflops"
+            self.config = {"workload": f"dsyrk_LN_n{n}_k{k}", "uplo": "L", "trans": "N", "n": n,
+                           "k": k, "alpha": 1.0, "beta": 0.5}
+        self.config["inputs"] = f"uniform[-1,1] SplitMix64 seed {seed}" + (
+            "; A diag uniform[1,2], off-diagonal uniform[-1,1]/m" if w == "dtrsm" else "")
+        self.config["l2"] = "operands larger than the 129 MB L2; no flush needed"
+
+    # ---- device-resident step (gbx_* C ABI) -----------------------------
+    def to_device(self):
+        import torch
+
+        def d(a):
+            return None if a is None else torch.from_numpy(np.asarray(a).ravel(order="F")).cuda()
+        self.d = {k: d(getattr(self, k, None)) for k in ("a", "b", "c", "x", "y")}
+        self.d["res"] = torch.zeros(2, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+
+    def timer_tag(self, dev):
+        return {"dgemm": dev.TIMER_GEMM_FP64, "ozaki": dev.TIMER_OZAKI_MMA,
+                "dtrsm": dev.TIMER_GEMM_FP64, "dsyrk": dev.TIMER_GEMM_FP64,
+                "dgemv": dev.TIMER_GEMV}.get(self.kind, dev.TIMER_LEVEL1)
+
+    def device_step(self, dev):
+        d, w = self.d, self.kind
+        if w == "dgemm":
+            n = self.n
+            dev.dgemm_checked("N", "N", n, n, n, 1.0, d["a"], n, d["b"], n, 0.5, d["c"], n)
+        elif w == "ozaki":
+            n = self.n
+            self.slices = dev.dgemm_ozaki("N", "N", n, n, n, 1.0, d["a"], n, d["b"], n, 0.5,
+                                          d["c"], n)
+        elif w == "daxpy":
+            dev.daxpy(self.n, 0.5, d["x"], 1, d["y"], 1)
+        elif w == "ddot":
+            dev.ddot(self.n, d["x"], 1, d["y"], 1, d["res"])
+        elif w == "dnrm2":
+            dev.dnrm2(self.n, d["x"], 1, d["res"])
+        elif w == "idamax":
+            dev.idamax(self.n, d["x"], 1, d["res"])
+        elif w == "dgemv":
+            n = self.n
+            dev.dgemv(self.trans, n, n, 1.0, d["a"], n, d["x"], 1, 0.5, d["y"], 1)
+        elif w == "dtrsm":
+            dev.dtrsm("L", "L", "N", "N", self.m, self.nrhs, 1.0, d["a"], self.m, d["b"], self.m)
+        elif w == "dsyrk":
+            dev.dsyrk("L", "N", self.n, self.k, 1.0, d["a"], self.n, 0.5, d["c"], self.n)
+
+    # ---- end to end through the Fortran symbols on pinned host memory ----
+    def to_pinned(self):
+        import torch
+
+        def pin(a):
+            return None if a is None else torch.from_numpy(np.asarray(a).ravel(order="F")).pin_memory()
+        self.h = {k: pin(getattr(self, k, None)) for k in ("a", "b", "c", "x", "y")}
+        self.hp = {k: (v.data_ptr() if v is not None else None) for k, v in self.h.items()}
+
+    def f77_step(self, f):
+        p, w = self.hp, self.kind
+        if w in ("dgemm", "ozaki"):
+            n = self.n
+            f.dgemm("N", "N", n, n, n, 1.0, p["a"], n, p["b"], n, 0.5, p["c"], n)
+        elif w == "daxpy":
+            f.daxpy(self.n, 0.5, p["x"], 1, p["y"], 1)
+        elif w == "ddot":
+            f.ddot(self.n, p["x"], 1, p["y"], 1)
+        elif w == "dnrm2":
+            f.dnrm2(self.n, p["x"], 1)
+        elif w == "idamax":
+            f.idamax(self.n, p["x"], 1)
+        elif w == "dgemv":
+            n = self.n
+            f.dgemv(self.trans, n, n, 1.0, p["a"], n, p["x"], 1, 0.5, p["y"], 1)
+        elif w == "dtrsm":
+            f.dtrsm("L", "L", "N", "N", self.m, self.nrhs, 1.0, p["a"], self.m, p["b"], self.m)
+        elif w == "dsyrk":
+            f.dsyrk("L", "N", self.n, self.k, 1.0, p["a"], self.n, 0.5, p["c"], self.n)
+
+    # ---- CPU BLAS step -----------------------------------------------------
+    def cpu_prepare(self):
+        self.cc = {k: (np.asarray(getattr(self, k)).copy(order="F") if getattr(self, k, None) is not None
+                       else None) for k in ("a", "b", "c", "x", "y")}
+
+    def cpu_step(self, cb):
+        c, w = self.cc, self.kind
+        if w in ("dgemm", "ozaki"):
+            n = self.n
+            cb.dgemm("N", "N", n, n, n, 1.0, c["a"], c["b"], 0.5, c["c"])
+        elif w == "daxpy":
+            cb.daxpy(self.n, 0.5, c["x"], 1, c["y"], 1)
+        elif w == "ddot":
+            cb.ddot(self.n, c["x"], 1, c["y"], 1)
+        elif w == "dnrm2":
+            cb.dnrm2(self.n, c["x"], 1)
+        elif w == "idamax":
+            cb.idamax(self.n, c["x"], 1)
+        elif w == "dgemv":
+            cb.dgemv(self.trans, self.n, self.n, 1.0, c["a"], c["x"], 1, 0.5, c["y"], 1)
+        elif w == "dtrsm":
+            cb.dtrsm("L", "L", "N", "N", self.m, self.nrhs, 1.0, c["a"], c["b"])
+        elif w == "dsyrk":
+            cb.dsyrk("L", "N", self.n, self.k, 1.0, c["a"], 0.5, c["c"])
 
 
-def cpu_dgemm_rate(cb, a, b, c, n, reps, threads):
-    """Median TFLOP/s of the CPU BLAS dgemm_ (1 warm-up + reps timed)."""
+def common_line(args, work, ws, value, ms_per_step):
+    return {"metric": work.metric, "value": value, "unit": work.unit, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": dict(work.config,
+                                                parallelism="replicas" if ws > 1 else "single-gpu")}
+
+
+def cpu_rate(work, cb, threads, target_s=12.0, max_reps=5):
+    """Median rate of the CPU BLAS on the workload: 1 warm-up, then up to
+    max_reps calls bounded by ~target_s seconds of CPU work."""
     cb.set_threads(threads)
-    cc = c.copy(order="F")
-    cb.dgemm("N", "N", n, n, n, 1.0, a, b, 0.5, cc)
+    work.cpu_prepare()
+    t0 = time.perf_counter()
+    work.cpu_step(cb)
+    first = time.perf_counter() - t0
+    reps = int(max(1, min(max_reps, target_s / max(first, 1e-6))))
     times = []
     for _ in range(reps):
-        cc = c.copy(order="F")
         t0 = time.perf_counter()
-        cb.dgemm("N", "N", n, n, n, 1.0, a, b, 0.5, cc)
+        work.cpu_step(cb)
         times.append(time.perf_counter() - t0)
-    return 2.0 * n ** 3 / statistics.median(times) / 1e12, times
-
-
-def config_block(n, ws):
-    return {"workload": f"dgemm_NN_m{n}_n{n}_k{n}_fp64", "m": n, "n": n, "k": n,
-            "lda": n, "alpha": 1.0, "beta": 0.5, "inputs": "uniform[-1,1] SplitMix64 seed 1",
-            "l2": "operands 3 x %d MiB > 129 MB L2; no flush needed" % (n * n * 8 >> 20),
-            "parallelism": "replicas" if ws > 1 else "single-gpu"}
+    return work.units / statistics.median(times), reps
 
 
 def run_reference(args):
@@ -179,39 +351,31 @@ def run_reference(args):
     from oracle import cpublas
     cb = cpublas.get()
     threads = os.cpu_count() or 1
-    n = args.n
-    _, a, b, c = make_inputs(n, args.seed)
+    work = Work(args)
     cb.set_threads(threads)
-    cc = c.copy(order="F")
+    work.cpu_prepare()
     for _ in range(args.warmup):
-        cb.dgemm("N", "N", n, n, n, 1.0, a, b, 0.5, cc)
+        work.cpu_step(cb)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cb.dgemm("N", "N", n, n, n, 1.0, a, b, 0.5, cc)
+        work.cpu_step(cb)
     dt = time.perf_counter() - t0
-    value = 2.0 * n ** 3 * args.steps / dt / 1e12
-    line = {
-        "impl": "reference", "metric": "dgemm_tflops", "value": value, "unit": "TFLOP/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_block(n, ws),
-        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "reference",
-                         "sample": f"CPU BLAS dgemm_ NN n={n}, {args.steps} timed calls after "
-                                   f"{args.warmup} warm-up ({cb.config})"},
-        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
-    }
+    value = work.units * args.steps / dt
+    line = common_line(args, work, ws, value, dt / args.steps * 1e3)
+    line["impl"] = "reference"
+    line["cpu_baseline"] = {"value": value, "unit": work.unit, "cores": threads, "kind": "reference",
+                            "sample": f"CPU BLAS ({cb.config}) on the full workload, {args.steps} "
+                                      f"timed calls after {args.warmup} warm-up"}
+    line["e2e"] = {"value": value, "unit": work.unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     print(json.dumps(line), flush=True)
     barrier(ws)
 
 
-def traffic_from_profiles(name):
+def traffic_from_profiles(key):
     """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
-        with open(path) as fh:
-            return json.load(fh).get(name)
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            return json.load(fh).get(key)
     except (OSError, ValueError):
         return None
 
@@ -223,21 +387,14 @@ def run_ours(args):
     import libgpublas_gb300 as g
     from libgpublas_gb300 import build
     build.build_library()
-    n = args.n
-    orc, a, b, c = make_inputs(n, args.seed)
-    flops = 2.0 * n ** 3
-
+    work = Work(args)
+    work.to_device()
     dev = g.Device(local)
     stream = torch.cuda.ExternalStream(dev.stream())
-    da = torch.from_numpy(a.ravel(order="F")).cuda()
-    db = torch.from_numpy(b.ravel(order="F")).cuda()
-    dc0 = torch.from_numpy(c.ravel(order="F")).cuda()
-    dc = dc0.clone()
-    torch.cuda.synchronize()
+    peaks, peak_src = measured_peaks()
 
-    # ---- device-resident timed region ------------------------------------
     for _ in range(args.warmup):
-        dev.dgemm_checked("N", "N", n, n, n, 1.0, da, n, db, n, 0.5, dc, n)
+        work.device_step(dev)
     dev.sync()
     dev.enable_timing(True)
     l0 = dev.launches()
@@ -247,108 +404,141 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         ev0.record(stream)
         for _ in range(args.steps):
-            dev.dgemm_checked("N", "N", n, n, n, 1.0, da, n, db, n, 0.5, dc, n)
+            work.device_step(dev)
         ev1.record(stream)
         ev1.synchronize()
-    torch.cuda.synchronize()
+    dev.sync()
     barrier(ws)
     launches = dev.launches() - l0
     t = ev0.elapsed_time(ev1) / 1e3
     t_max = max_over_ranks(ws, t, device="cuda")
-    value = flops * args.steps * ws / t_max / 1e12
-    k_ms, k_n = dev.kernel_time(dev.TIMER_GEMM_FP64)
+    value = work.units * args.steps * ws / t_max
+    k_ms, k_n = dev.kernel_time(work.timer_tag(dev))
     dev.enable_timing(False)
-    peak = dev.fp64_peak()
-    achieved = flops / (k_ms / max(k_n, 1) / 1e3) / 1e12
+    per_launch_s = (k_ms / max(k_n, 1)) / 1e3
+    line = common_line(args, work, ws, value, t_max / args.steps * 1e3)
+    line["gpu_launches"] = int(launches)
+    line["clocks"] = clk.summary()
 
-    line = {
-        "metric": "dgemm_tflops", "value": value, "unit": "TFLOP/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": config_block(n, ws), "gpu_launches": int(launches),
-        "roofline": {"bound": "fp64", "kernel": "gemm_simt_kernel<double,8,8,8>",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None,
-                     "peak_source": "measured in this run: DFMA throughput loop "
-                                    "(gbx_diag_fp64_peak); MEASURED_PEAKS.json has no FP64 figure",
-                     "traffic": traffic_from_profiles("gemm_simt_kernel_dgemm_nn_8192"),
-                     "algorithmic": "2*n^3 flop per launch"},
-        "clocks": clk.summary(),
-    }
+    w = work.kind
+    if w in ("dgemm", "dtrsm", "dsyrk"):
+        peak = dev.fp64_peak()
+        # DGEMM and DSYRK are one launch per call; DTRSM is many GEMM launches,
+        # so its achieved rate counts the whole call's flops over the summed
+        # GEMM-core time.
+        achieved = work.units * args.steps / (k_ms / 1e3) if k_ms > 0 else None
+        line["roofline"] = {"bound": "fp64", "kernel": "gemm_simt_kernel<double,8,8,8>",
+                            "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                            "frac": achieved / peak if (achieved and peak) else None,
+                            "peak_source": "measured in this run: DFMA throughput loop "
+                                           "(gbx_diag_fp64_peak); MEASURED_PEAKS.json has no "
+                                           "FP64 figure",
+                            "traffic": traffic_from_profiles(f"{w}_{work.config['workload']}"),
+                            "kernel_launches_timed": int(k_n)}
+    elif w == "ozaki":
+        s = getattr(work, "slices", 0)
+        raw = s * (s + 1) / 2 * work.units   # FP8 tensor TFLOP per step
+        peak = 2.0 * peaks.get("bf16_tflops", 1900.0)
+        achieved = raw / per_launch_s if per_launch_s > 0 else None
+        line["roofline"] = {"bound": "tensor", "kernel": "oz_gemm_kernel (tcgen05 kind::f8f6f4)",
+                            "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                            "frac": achieved / peak if achieved else None,
+                            "peak_source": f"2 x bf16_tflops of {peak_src} (FP8 dense = 2x bf16 "
+                                           "dense on this part)",
+                            "traffic": traffic_from_profiles(f"ozaki_{work.config['workload']}"),
+                            "algorithmic": "S(S+1)/2 * 2 n^3 FP8 flop per launch",
+                            "slices": s}
+    else:
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = work.units / per_launch_s if per_launch_s > 0 else None
+        line["roofline"] = {"bound": "hbm", "kernel": {"dgemv": "gemv_n_partial/gemv_t_warp"}.get(
+                                w, f"{w} streaming kernel"),
+                            "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak if achieved else None,
+                            "peak_source": f"hbm_gbs of {peak_src}",
+                            "traffic": traffic_from_profiles(f"{w}_{work.config['workload']}"),
+                            "algorithmic": f"{work.config.get('bytes_per_step')} bytes per launch"}
 
     # ---- end to end through the Fortran symbol on pinned host buffers ----
     if not args.no_e2e:
-        ha = torch.from_numpy(a.ravel(order="F")).pin_memory()
-        hb = torch.from_numpy(b.ravel(order="F")).pin_memory()
-        hc = torch.from_numpy(c.ravel(order="F")).pin_memory()
+        work.to_pinned()
         f = g.F77()
-        pa, pb, pc = ha.data_ptr(), hb.data_ptr(), hc.data_ptr()
-        f.dgemm("N", "N", n, n, n, 1.0, pa, n, pb, n, 0.5, pc, n)
-        s0 = g.stats()
-        barrier(ws)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            f.dgemm("N", "N", n, n, n, 1.0, pa, n, pb, n, 0.5, pc, n)
-        te = time.perf_counter() - t0
-        s1 = g.stats()
-        te = max_over_ranks(ws, te, device="cuda")
-        line["e2e"] = {"value": flops * args.steps * ws / te / 1e12, "unit": "TFLOP/s",
-                       "h2d_bytes_per_step": (s1["bytes_h2d"] - s0["bytes_h2d"]) // args.steps,
-                       "d2h_bytes_per_step": (s1["bytes_d2h"] - s0["bytes_d2h"]) // args.steps,
-                       "api": "dgemm_ (Fortran ABI), pinned host operands"}
+        if w == "ozaki":
+            line["e2e"] = {"unavailable": "the Fortran path selects Ozaki through "
+                                          "BLAS2CUDA_OPTIONS=precision=ozaki at load time"}
+        else:
+            work.f77_step(f)
+            s0 = g.stats()
+            barrier(ws)
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                work.f77_step(f)
+            te = max_over_ranks(ws, time.perf_counter() - t0, device="cuda")
+            s1 = g.stats()
+            line["e2e"] = {"value": work.units * args.steps * ws / te, "unit": work.unit,
+                           "h2d_bytes_per_step": (s1["bytes_h2d"] - s0["bytes_h2d"]) // args.steps,
+                           "d2h_bytes_per_step": (s1["bytes_d2h"] - s0["bytes_d2h"]) // args.steps,
+                           "api": "Fortran ABI symbol, pinned host operands"}
 
-    # ---- Ozaki split-precision on the same operands --------------------------
-    if not args.no_ozaki:
+    if w == "dgemm" and not args.no_ozaki:
         try:
-            line["ozaki"] = bench_ozaki(args, dev, orc, a, b, c, da, db, dc0, n, stream)
+            line["ozaki"] = bench_ozaki(args, dev, work, stream)
         except g.GbxError as e:
             line["ozaki"] = {"unavailable": str(e)}
+    if w == "ozaki":
+        line["ozaki_accuracy"] = ozaki_accuracy(dev, work)
 
-    # ---- CPU baseline: the CPU BLAS on this host --------------------------
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         from oracle import cpublas
         cb = cpublas.get()
         threads = os.cpu_count() or 1
-        rate, times = cpu_dgemm_rate(cb, a, b, c, n, 3, threads)
-        line["cpu_baseline"] = {"value": rate, "unit": "TFLOP/s", "cores": threads,
+        rate, reps = cpu_rate(work, cb, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": work.unit, "cores": threads,
                                 "kind": "reference",
-                                "sample": f"CPU BLAS dgemm_ NN n={n}: median of 3 calls after 1 "
-                                          f"warm-up ({cb.config})"}
+                                "sample": f"CPU BLAS ({cb.config}) on the full workload: median of "
+                                          f"{reps} calls after 1 warm-up"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     dev.close()
 
 
-def bench_ozaki(args, dev, orc, a, b, c, da, db, dc0, n, stream):
+def ozaki_accuracy(dev, work):
+    """Relative Frobenius error of one fresh Ozaki call against the
+    double-double oracle on 2048 sampled entries."""
     import torch
-    dc = dc0.clone()
-    used = dev.dgemm_ozaki("N", "N", n, n, n, 1.0, da, n, db, n, 0.5, dc, n)
-    for _ in range(max(0, args.warmup - 1)):
-        dev.dgemm_ozaki("N", "N", n, n, n, 1.0, da, n, db, n, 0.5, dc, n)
+    n = work.n
+    dc = torch.from_numpy(work.c.ravel(order="F")).cuda()
+    used = dev.dgemm_ozaki("N", "N", n, n, n, 1.0, work.d["a"], n, work.d["b"], n, 0.5, dc, n)
+    got = dc.cpu().numpy().reshape(n, n, order="F")
+    rng = np.random.default_rng(0)
+    rows = rng.integers(0, n, 2048)
+    cols = rng.integers(0, n, 2048)
+    ref = work.orc.dgemm_dd_sample("N", "N", n, 1.0, work.a, work.b, 0.5, work.c, rows, cols)
+    err = float(np.linalg.norm(got[rows, cols] - ref) / np.linalg.norm(ref))
+    return {"rel_err_fro_sampled": err, "slices": used, "samples": 2048, "tol": 1e-14}
+
+
+def bench_ozaki(args, dev, work, stream):
+    import torch
+    n = work.n
+    d = work.d
+    for _ in range(max(1, args.warmup - 1)):
+        dev.dgemm_ozaki("N", "N", n, n, n, 1.0, d["a"], n, d["b"], n, 0.5, d["c"], n)
     dev.sync()
     dev.enable_timing(True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for _ in range(args.steps):
-        dev.dgemm_ozaki("N", "N", n, n, n, 1.0, da, n, db, n, 0.5, dc, n)
+        dev.dgemm_ozaki("N", "N", n, n, n, 1.0, d["a"], n, d["b"], n, 0.5, d["c"], n)
     ev1.record(stream)
     ev1.synchronize()
     t = ev0.elapsed_time(ev1) / 1e3
     mma_ms, mma_n = dev.kernel_time(dev.TIMER_OZAKI_MMA)
     dev.enable_timing(False)
-    # accuracy on one fresh call, sampled against the double-double oracle
-    dc = dc0.clone()
-    dev.dgemm_ozaki("N", "N", n, n, n, 1.0, da, n, db, n, 0.5, dc, n)
-    dev.sync()
-    got = dc.cpu().numpy().reshape(n, n, order="F")
-    rng = np.random.default_rng(0)
-    rows = rng.integers(0, n, 2048)
-    cols = rng.integers(0, n, 2048)
-    ref = orc.dgemm_dd_sample("N", "N", n, 1.0, a, b, 0.5, c, rows, cols)
-    err = float(np.linalg.norm(got[rows, cols] - ref) / np.linalg.norm(ref))
-    flops = 2.0 * n ** 3
-    return {"value": flops * args.steps / t / 1e12, "unit": "TFLOP/s",
-            "ms_per_step": t / args.steps * 1e3, "slices": used, "rel_err_fro_sampled": err,
+    acc = ozaki_accuracy(dev, work)
+    return {"value": work.units * args.steps / t, "unit": "TFLOP/s",
+            "ms_per_step": t / args.steps * 1e3, "slices": acc["slices"],
+            "rel_err_fro_sampled": acc["rel_err_fro_sampled"],
             "mma_ms_per_call": mma_ms / max(mma_n, 1)}
 
 

@@ -21,6 +21,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbxblas.so")
+PRELOAD_LIB = os.path.join(HERE, "libgbxblas_preload.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
@@ -37,7 +38,7 @@ def _nvcc():
 
 def _sources():
     cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
-    c = sorted(glob.glob(os.path.join(CSRC, "*.c")))
+    c = sorted(glob.glob(os.path.join(CSRC, "*.c")))   # includes preload_*.c
     hdr = sorted(glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
                  glob.glob(os.path.join(ROOT, "include", "*.h")))
     return cu, c, hdr
@@ -84,9 +85,13 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
             if o.strip():
                 print(o)
     objs = [j[1] for j in jobs]
-    tmp = LIB + ".tmp%d" % os.getpid()
-    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"])
-    os.replace(tmp, LIB)
+    # libgbxblas.so: the BLAS library; libgbxblas_preload.so: the same plus
+    # the malloc/free interposer (preload_*.c), for LD_PRELOAD use.
+    core = [o for o in objs if not os.path.basename(o).startswith("preload_")]
+    for out, parts in ((LIB, core), (PRELOAD_LIB, objs)):
+        tmp = out + ".tmp%d" % os.getpid()
+        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + parts + ["-lpthread", "-ldl"])
+        os.replace(tmp, out)
     with open(stamp_file, "w") as fh:
         fh.write(stamp)
     return LIB

@@ -20,7 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-static gbx_config g_cfg = {0, 1e-14, 1, 1, 0, 0};
+static gbx_config g_cfg = {0, 1e-14, 1, 1, 0, 0, 0, {0}, {0}};
 static pthread_once_t g_once = PTHREAD_ONCE_INIT;
 
 static void print_help(void)
@@ -34,7 +34,9 @@ static void print_help(void)
           "                                'oracle:<filename>' (allocation placement)\n"
           "   precision=fp64|ozaki[:t]  -- FP64 or Ozaki split products (target error t)\n"
           "   prefetch=on|off           -- prefetch managed operands to the GPU\n"
-          "   errors=abort|return       -- behaviour on a device failure\n",
+          "   errors=abort|return       -- behaviour on a device failure\n"
+          "   managed_min=<bytes>       -- smaller allocations stay on the host\n"
+          "   statistics[=<file>]       -- write call/placement counters at exit\n",
           stderr);
 }
 
@@ -58,8 +60,16 @@ static void parse(void)
             if (strncmp(h, "random", 6) == 0) g_cfg.heuristic = 2;
             else if (strncmp(h, "true", 4) == 0) g_cfg.heuristic = 1;
             else if (strncmp(h, "false", 5) == 0) g_cfg.heuristic = 0;
-            else if (strncmp(h, "oracle:", 7) == 0) g_cfg.heuristic = 3;
-            else fprintf(stderr, "gbxblas: unsupported heuristic '%s'\n", h);
+            else if (strncmp(h, "oracle:", 7) == 0) {
+                g_cfg.heuristic = 3;
+                snprintf(g_cfg.oracle_file, sizeof g_cfg.oracle_file, "%s", h + 7);
+            } else fprintf(stderr, "gbxblas: unsupported heuristic '%s'\n", h);
+        } else if (strncmp(opt, "managed_min=", 12) == 0) {
+            g_cfg.managed_min = (size_t)strtoull(opt + 12, NULL, 10);
+        } else if (strcmp(opt, "statistics") == 0) {
+            snprintf(g_cfg.stats_file, sizeof g_cfg.stats_file, "statistics.csv");
+        } else if (strncmp(opt, "statistics=", 11) == 0) {
+            snprintf(g_cfg.stats_file, sizeof g_cfg.stats_file, "%s", opt + 11);
         } else if (strncmp(opt, "precision=", 10) == 0) {
             const char *p = opt + 10;
             if (strncmp(p, "ozaki", 5) == 0) {

@@ -85,6 +85,9 @@ typedef struct {
     int    abort_on_error;   /* errors=abort                                     */
     int    trace;            /* trace=<file> set                                 */
     int    heuristic;        /* 0 false, 1 true, 2 random, 3 oracle             */
+    size_t managed_min;      /* managed_min=<bytes>: smaller objects stay host  */
+    char   oracle_file[1024];/* heuristic=oracle:<file>                          */
+    char   stats_file[1024]; /* statistics[=<file>] written at exit              */
 } gbx_config;
 const gbx_config *gbx_get_config(void);
 

@@ -135,6 +135,10 @@ extern "C" gbx_status gbx_fail(gbx_ctx *ctx, gbx_status st, const char *fmt, ...
     return st;
 }
 
+// Defined only in libgbxblas_preload.so (the allocation interposer): rescans
+// the mapped CUDA libraries, which are loaded when the first context is made.
+extern "C" void gbx_tracker_refresh(void) __attribute__((weak));
+
 extern "C" gbx_status gbx_ctx_create(gbx_ctx **out, int device)
 {
     if (!out) return GBX_ERR_ARG;
@@ -151,6 +155,7 @@ extern "C" gbx_status gbx_ctx_create(gbx_ctx **out, int device)
     }
     c->stream = c->own_stream;
     *out = c;
+    if (gbx_tracker_refresh) gbx_tracker_refresh();
     return GBX_OK;
 }
 

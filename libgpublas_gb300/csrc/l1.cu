@@ -38,12 +38,14 @@ extern "C" gbx_status gbx_daxpy(gbx_ctx *ctx, int n, double alpha, const double 
     if (!ctx) return GBX_ERR_ARG;
     if (n <= 0 || alpha == 0.0) return GBX_OK;
     int g = grid_for(ctx, n, 4);
+    gbx_timer_begin(ctx, GBX_TIMER_LEVEL1);
     if (incx == 1 && incy == 1) {
         axpy_unit<<<g, L1_THREADS, 0, S(ctx)>>>(n, alpha, x, y);
     } else {
         axpy_strided<<<g, L1_THREADS, 0, S(ctx)>>>(n, alpha, x + base_off(n, incx), incx,
                                                     y + base_off(n, incy), incy);
     }
+    gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);
     return gbx_check_launch(ctx, "daxpy");
 }
@@ -71,8 +73,10 @@ extern "C" gbx_status gbx_ddot(gbx_ctx *ctx, int n, const double *x, int incx,
         gbx_count_launch(ctx, 1);
         return gbx_check_launch(ctx, "ddot");
     }
+    gbx_timer_begin(ctx, GBX_TIMER_LEVEL1);
     dot_partial<<<g, L1_THREADS, 0, S(ctx)>>>(n, x + base_off(n, incx), incx,
                                               y + base_off(n, incy), incy, part);
+    gbx_timer_end(ctx);
     sum_partials<<<1, L1_THREADS, 0, S(ctx)>>>(part, g, res);
     gbx_count_launch(ctx, 2);
     return gbx_check_launch(ctx, "ddot");
@@ -90,7 +94,9 @@ extern "C" gbx_status gbx_dnrm2(gbx_ctx *ctx, int n, const double *x, int incx, 
     double *part;
     gbx_status st = gbx_ws(ctx, GBX_WS_RED, 3 * sizeof(double) * (size_t)g, (void **)&part);
     if (st != GBX_OK) return st;
+    gbx_timer_begin(ctx, GBX_TIMER_LEVEL1);
     nrm2_partial<<<g, L1_THREADS, 0, S(ctx)>>>(n, x, incx, part);
+    gbx_timer_end(ctx);
     nrm2_finish<<<1, L1_THREADS, 0, S(ctx)>>>(part, g, res);
     gbx_count_launch(ctx, 2);
     return gbx_check_launch(ctx, "dnrm2");
@@ -110,13 +116,12 @@ static gbx_status iamax_common(gbx_ctx *ctx, int n, const double *x, int incx, i
                            (void **)&keys);
     if (st != GBX_OK) return st;
     long long *idx = (long long *)(keys + g);
-    if (is_min) {
-        iamax_partial<true><<<g, L1_THREADS, 0, S(ctx)>>>(n, x, incx, keys, idx);
-        iamax_finish<true><<<1, L1_THREADS, 0, S(ctx)>>>(x, keys, idx, g, res);
-    } else {
-        iamax_partial<false><<<g, L1_THREADS, 0, S(ctx)>>>(n, x, incx, keys, idx);
-        iamax_finish<false><<<1, L1_THREADS, 0, S(ctx)>>>(x, keys, idx, g, res);
-    }
+    gbx_timer_begin(ctx, GBX_TIMER_LEVEL1);
+    if (is_min) iamax_partial<true><<<g, L1_THREADS, 0, S(ctx)>>>(n, x, incx, keys, idx);
+    else iamax_partial<false><<<g, L1_THREADS, 0, S(ctx)>>>(n, x, incx, keys, idx);
+    gbx_timer_end(ctx);
+    if (is_min) iamax_finish<true><<<1, L1_THREADS, 0, S(ctx)>>>(x, keys, idx, g, res);
+    else iamax_finish<false><<<1, L1_THREADS, 0, S(ctx)>>>(x, keys, idx, g, res);
     gbx_count_launch(ctx, 2);
     return gbx_check_launch(ctx, is_min ? "idamin" : "idamax");
 }

@@ -189,13 +189,16 @@ extern "C" gbx_status gbx_dgemv(gbx_ctx *ctx, char trans, int m, int n, double a
         if (st != GBX_OK) return st;
         const int vec = ((((uintptr_t)A) & 15) == 0) && (lda % 2 == 0);
         dim3 g(rtiles, nchunks);
+        gbx_timer_begin(ctx, GBX_TIMER_GEMV);
         gemv_n_partial<<<g, GEMV_THREADS, 0, S(ctx)>>>(m, n, chunk, A, lda, xb, incx, part, vec);
+        gbx_timer_end(ctx);
         gemv_n_finish<<<std::min(sms * 4, (m + 255) / 256), 256, 0, S(ctx)>>>(m, nchunks, part, alpha,
                                                                                beta, yb, incy);
         gbx_count_launch(ctx, 2);
         return gbx_check_launch(ctx, "dgemv");
     }
     const int warps_per_block = GEMV_THREADS / 32;
+    gbx_timer_begin(ctx, GBX_TIMER_GEMV);
     if (n >= sms * 4 * warps_per_block / 2) {
         const int vec = incx == 1 && ((((uintptr_t)A) & 15) == 0) && (lda % 2 == 0) &&
                         ((((uintptr_t)xb) & 15) == 0);
@@ -204,6 +207,7 @@ extern "C" gbx_status gbx_dgemv(gbx_ctx *ctx, char trans, int m, int n, double a
     } else {
         gemv_t_block<<<n, GEMV_THREADS, 0, S(ctx)>>>(m, n, A, lda, xb, incx, alpha, beta, yb, incy);
     }
+    gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);
     return gbx_check_launch(ctx, "dgemv");
 }
