@@ -165,6 +165,34 @@ gbx_status gbx_dsyrk_ozaki(gbx_ctx *ctx, char uplo, char trans, int n, int k, do
                            const double *A, int lda, double beta, double *C, int ldc,
                            double tol, int slices, int *slices_used);
 
+/* ---- grouped execution of many small calls (no reference counterpart) ------
+ * A plan turns a list of independent DGEMM / DTRSM operations (device
+ * pointers) into one persistent grouped kernel: GEMMs are tiled (tile size
+ * per size bucket chosen by an autotuner that times both variants the first
+ * time a bucket is seen and caches the choice in GBX_AUTOTUNE_CACHE or
+ * $HOME/.cache/gbxblas/autotune.json), TRSMs of order <= 256 are solved one
+ * CTA per 16 right-hand sides, and all work items are scheduled dynamically.
+ * gbx_plan_launch enqueues a counter reset and the kernel (capturable);
+ * gbx_plan_graph_launch records that into a CUDA graph once and replays it.
+ * The operations must not overlap in their outputs. */
+enum { GBX_OP_GEMM = 1, GBX_OP_TRSM = 2 };
+typedef struct {
+    int kind;                 /* GBX_OP_GEMM or GBX_OP_TRSM                     */
+    char transa, transb;      /* GEMM: op(A), op(B); TRSM: transa = op(A)       */
+    char side, uplo, diag;    /* TRSM                                            */
+    int m, n, k;              /* GEMM: C is m x n, K = k; TRSM: B is m x n       */
+    double alpha, beta;       /* TRSM: alpha only                                */
+    const double *A; int lda;
+    const double *B; int ldb; /* GEMM: B (TRSM: unused)                          */
+    double *C; int ldc;       /* GEMM: C; TRSM: the right-hand sides B, in/out   */
+} gbx_op;
+typedef struct gbx_plan gbx_plan;
+gbx_status gbx_plan_create(gbx_ctx *ctx, const gbx_op *ops, int count, gbx_plan **plan);
+gbx_status gbx_plan_launch(gbx_ctx *ctx, gbx_plan *plan);
+gbx_status gbx_plan_graph_launch(gbx_ctx *ctx, gbx_plan *plan);
+gbx_status gbx_plan_destroy(gbx_plan *plan);
+gbx_status gbx_plan_info(const gbx_plan *plan, int *work_items, double *flops);
+
 #ifdef __cplusplus
 }
 #endif

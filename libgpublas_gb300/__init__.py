@@ -6,4 +6,5 @@ the gbx_* device-pointer C ABI declared in ``include/gbxblas.h``.  This
 Python package only builds it (``build.build_library``) and binds it with
 ctypes (``_lib``) for tests and benchmarks.
 """
-from ._lib import F77, Device, GbxError, LIB_PATH, declared_symbols, load, stats  # noqa: F401
+from ._lib import (F77, OP_GEMM, OP_TRSM, Device, GbxError, GbxOp, LIB_PATH, declared_symbols,  # noqa: F401
+                   load, stats)

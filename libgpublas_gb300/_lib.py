@@ -106,9 +106,27 @@ def _declare(L):
     L.cblas_idamin.argtypes = [_I, _P, _I]
     L.cblas_dgemm.argtypes = [_I, _I, _I, _I, _I, _I, _D, _P, _I, _P, _I, _D, _P, _I]
     L.gbx_stats.argtypes = [C.POINTER(C.c_uint64)] * 5
+    L.gbx_plan_create.argtypes = [_P, _P, _I, C.POINTER(_P)]
+    L.gbx_plan_launch.argtypes = [_P, _P]
+    L.gbx_plan_graph_launch.argtypes = [_P, _P]
+    L.gbx_plan_destroy.argtypes = [_P]
+    L.gbx_plan_info.argtypes = [_P, C.POINTER(_I), C.POINTER(_D)]
     L.gbx_ctx_enable_timing.argtypes = [_P, _I]
     L.gbx_ctx_kernel_time.argtypes = [_P, _I, C.POINTER(_D), C.POINTER(C.c_uint64)]
     L.gbx_diag_fp64_peak.argtypes = [_P, C.POINTER(_D)]
+
+
+class GbxOp(C.Structure):
+    """gbx_op of include/gbxblas.h (one operation of a grouped plan)."""
+    _fields_ = [("kind", C.c_int), ("transa", C.c_char), ("transb", C.c_char),
+                ("side", C.c_char), ("uplo", C.c_char), ("diag", C.c_char),
+                ("m", C.c_int), ("n", C.c_int), ("k", C.c_int),
+                ("alpha", C.c_double), ("beta", C.c_double),
+                ("A", C.c_void_p), ("lda", C.c_int), ("B", C.c_void_p), ("ldb", C.c_int),
+                ("C", C.c_void_p), ("ldc", C.c_int)]
+
+
+OP_GEMM, OP_TRSM = 1, 2
 
 
 def stats():
@@ -262,6 +280,25 @@ class Device:
         ms, n = C.c_double(0.0), C.c_uint64(0)
         self._ok(self.L.gbx_ctx_kernel_time(self.ctx, tag, C.byref(ms), C.byref(n)), "kernel_time")
         return ms.value, n.value
+
+    # grouped plans
+    def plan_create(self, ops):
+        arr = (GbxOp * len(ops))(*ops)
+        h = _P()
+        self._ok(self.L.gbx_plan_create(self.ctx, arr, len(ops), C.byref(h)), "plan_create")
+        return h
+
+    def plan_launch(self, plan, graph=False):
+        f = self.L.gbx_plan_graph_launch if graph else self.L.gbx_plan_launch
+        self._ok(f(self.ctx, plan), "plan_launch")
+
+    def plan_destroy(self, plan):
+        self.L.gbx_plan_destroy(plan)
+
+    def plan_info(self, plan):
+        n, fl = C.c_int(0), C.c_double(0.0)
+        self.L.gbx_plan_info(plan, C.byref(n), C.byref(fl))
+        return n.value, fl.value
 
     def fp64_peak(self):
         t = C.c_double(0.0)

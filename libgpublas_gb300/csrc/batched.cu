@@ -1,0 +1,507 @@
+// batched.cu — grouped execution of many small, uneven DGEMM / DTRSM calls in
+// one persistent kernel (no reference counterpart: the reference issues one
+// cuBLAS call at a time on one handle, runtime-blas.c:14-23).
+//
+// A plan is built once from a list of operations:
+//   * every DGEMM is cut into C tiles of 32x32 or 64x64 (the variant is chosen
+//     per size bucket by the autotuner below); every DTRSM (order <= 256) is
+//     one work item solved by one CTA;
+//   * work items are ordered by decreasing cost (longest first) and handed
+//     out dynamically: each CTA of a persistent grid (2 CTAs per SM) takes
+//     the next item with one atomicAdd on a counter that the launch resets;
+//   * the launch is a memset + one kernel, so it can be recorded in a CUDA
+//     graph; gbx_plan_graph_launch records it on first use and replays it.
+// Autotuner: for each bucket of GEMMs (by max(M,N)), both tile variants are
+// timed on the plan's own operands (results written to scratch, beta = 0)
+// the first time the bucket is seen; the choice is kept per device in
+// memory and in a JSON cache file (GBX_AUTOTUNE_CACHE, default
+// $HOME/.cache/gbxblas/autotune.json), so later plans skip the timing.
+#include "gbx_internal.h"
+#include "gemm_host.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+#include <algorithm>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+namespace {
+
+constexpr int BT_THREADS = 256;
+constexpr int BT_BK = 16;
+constexpr int TRSM_MAX_ORDER = 256;
+constexpr int TRSM_SYS = 16;      // right-hand sides solved together
+constexpr int NBUCKET = 6;        // max(M,N) <= 32, 64, 128, 256, 512, larger
+
+struct DevOp {
+    int kind;                     // GBX_OP_GEMM / GBX_OP_TRSM
+    int ta, tb;                   // GEMM transpositions; TRSM: ta = op(A) transposed
+    int lower, unit, left;        // TRSM: effective triangle of the solved matrix, diag, side
+    int m, n, k;
+    double alpha, beta;
+    const double *A;
+    long long lda;
+    const double *B;
+    long long ldb;
+    double *C;
+    long long ldc;
+};
+
+struct Item {
+    int op;
+    int variant;                  // GEMM: 0 = 32x32 tile, 1 = 64x64; TRSM: systems chunk
+    int tm, tn;
+};
+
+// ---------------------------------------------------------------- GEMM tile
+template <int TS>
+__device__ void gemm_tile(const DevOp &o, int tm, int tn, double *smem)
+{
+    constexpr int TPR = TS / 16;               // outputs per thread per dim (2 or 4)
+    double (*As)[TS] = (double (*)[TS])smem;             // [BT_BK][TS]
+    double (*Bs)[TS] = (double (*)[TS])(smem + BT_BK * TS);
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int m0 = tm * TS, n0 = tn * TS;
+    double acc[TPR][TPR];
+#pragma unroll
+    for (int i = 0; i < TPR; i++)
+#pragma unroll
+        for (int j = 0; j < TPR; j++) acc[i][j] = 0.0;
+    for (int k0 = 0; k0 < o.k; k0 += BT_BK) {
+        for (int t = threadIdx.x; t < TS * BT_BK; t += BT_THREADS) {
+            int mn, kk;
+            // A tile: op(A)(m0+mn, k0+kk)
+            if (!o.ta) { mn = t % TS; kk = t / TS; } else { kk = t % BT_BK; mn = t / BT_BK; }
+            int gm = m0 + mn, gk = k0 + kk;
+            As[kk][mn] = (gm < o.m && gk < o.k)
+                             ? (o.ta ? o.A[(long long)gm * o.lda + gk] : o.A[(long long)gk * o.lda + gm])
+                             : 0.0;
+            // B tile: op(B)(k0+kk, n0+mn)
+            if (o.tb) { mn = t % TS; kk = t / TS; } else { kk = t % BT_BK; mn = t / BT_BK; }
+            const int gn = n0 + mn;
+            gk = k0 + kk;
+            Bs[kk][mn] = (gn < o.n && gk < o.k)
+                             ? (o.tb ? o.B[(long long)gk * o.ldb + gn] : o.B[(long long)gn * o.ldb + gk])
+                             : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BT_BK; kk++) {
+            double a[TPR], b[TPR];
+#pragma unroll
+            for (int i = 0; i < TPR; i++) {
+                a[i] = As[kk][ty + 16 * i];
+                b[i] = Bs[kk][tx + 16 * i];
+            }
+#pragma unroll
+            for (int i = 0; i < TPR; i++)
+#pragma unroll
+                for (int j = 0; j < TPR; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < TPR; j++) {
+        const int col = n0 + tx + 16 * j;
+        if (col >= o.n) continue;
+#pragma unroll
+        for (int i = 0; i < TPR; i++) {
+            const int row = m0 + ty + 16 * i;
+            if (row >= o.m) continue;
+            double *cp = o.C + (long long)col * o.ldc + row;
+            *cp = (o.beta == 0.0) ? o.alpha * acc[i][j] : fma(o.alpha, acc[i][j], o.beta * *cp);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- TRSM item
+// Solves T y = alpha*b for up to TRSM_SYS systems of order n (<= 256), where
+// for side 'L' T = op(A) and the systems are columns of B (m x nrhs), and for
+// side 'R' T = op(A)^T and the systems are rows of B.  Substitution order is
+// chosen by the effective triangle of T.
+__device__ void trsm_item(const DevOp &o, int sys0, double *smem)
+{
+    const int n = o.left ? o.m : o.n;                 // order of T
+    const int nsys_total = o.left ? o.n : o.m;
+    const int nsys = min(TRSM_SYS, nsys_total - sys0);
+    double *X = smem;                                  // X[i * TRSM_SYS + s]
+    // element (i, s) of system vector s
+    auto bidx = [&](int i, int s) -> long long {
+        return o.left ? (long long)(sys0 + s) * o.ldc + i : (long long)i * o.ldc + (sys0 + s);
+    };
+    // T(i, j): side L: op(A)(i,j); side R: op(A)(j,i)
+    auto T = [&](int i, int j) -> double {
+        int r = i, c = j;
+        if (!o.left) { r = j; c = i; }
+        return o.ta ? o.A[(long long)r * o.lda + c] : o.A[(long long)c * o.lda + r];
+    };
+    for (int t = threadIdx.x; t < n * TRSM_SYS; t += BT_THREADS) {
+        const int i = t / TRSM_SYS, s = t % TRSM_SYS;
+        X[t] = s < nsys ? o.alpha * o.C[bidx(i, s)] : 0.0;
+    }
+    __syncthreads();
+    for (int step = 0; step < n; step++) {
+        const int kk = o.lower ? step : n - 1 - step;
+        if (!o.unit) {
+            const double d = T(kk, kk);
+            if (threadIdx.x < TRSM_SYS) X[kk * TRSM_SYS + threadIdx.x] /= d;
+            __syncthreads();
+        }
+        // update the rows still to be solved
+        const int r0 = o.lower ? kk + 1 : 0, r1 = o.lower ? n : kk;
+        for (int t = threadIdx.x; t < (r1 - r0) * TRSM_SYS; t += BT_THREADS) {
+            const int i = r0 + t / TRSM_SYS, s = t % TRSM_SYS;
+            X[i * TRSM_SYS + s] = fma(-T(i, kk), X[kk * TRSM_SYS + s], X[i * TRSM_SYS + s]);
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n * TRSM_SYS; t += BT_THREADS) {
+        const int i = t / TRSM_SYS, s = t % TRSM_SYS;
+        if (s < nsys) o.C[bidx(i, s)] = X[t];
+    }
+}
+
+__global__ void __launch_bounds__(BT_THREADS, 2)
+grouped_kernel(const DevOp *__restrict__ ops, const Item *__restrict__ items, int nitems, int *counter)
+{
+    __shared__ __align__(16) double smem[2 * BT_BK * 64 > TRSM_MAX_ORDER * TRSM_SYS ? 2 * BT_BK * 64
+                                                                                   : TRSM_MAX_ORDER * TRSM_SYS];
+    __shared__ int s_item;
+    while (true) {
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= nitems) break;
+        const Item w = items[it];
+        const DevOp o = ops[w.op];
+        if (o.kind == GBX_OP_TRSM) trsm_item(o, w.variant * TRSM_SYS, smem);
+        else if (w.variant == 0) gemm_tile<32>(o, w.tm, w.tn, smem);
+        else gemm_tile<64>(o, w.tm, w.tn, smem);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- autotune
+int bucket_of(int m, int n)
+{
+    const int s = std::max(m, n);
+    int b = 0;
+    for (int lim = 32; b < NBUCKET - 1 && s > lim; lim *= 2) b++;
+    return b;
+}
+
+std::mutex g_tune_mu;
+int g_tune[64][NBUCKET];          // per device: -1 unknown, else variant
+bool g_tune_loaded = false;
+
+std::string tune_path()
+{
+    const char *p = getenv("GBX_AUTOTUNE_CACHE");
+    if (p) return p;
+    const char *h = getenv("HOME");
+    return std::string(h ? h : "/tmp") + "/.cache/gbxblas/autotune.json";
+}
+
+// The cache file is a small JSON object {"<device name>": [v0, ..., v5]}; it
+// is written by this library only, so a fixed-format parser suffices.
+void tune_load_locked(int dev, const char *devname)
+{
+    for (int d = 0; d < 64; d++)
+        for (int b = 0; b < NBUCKET; b++) g_tune[d][b] = -1;
+    g_tune_loaded = true;
+    FILE *f = fopen(tune_path().c_str(), "r");
+    if (!f) return;
+    char buf[4096];
+    size_t len = fread(buf, 1, sizeof buf - 1, f);
+    fclose(f);
+    buf[len] = '\0';
+    std::string key = std::string("\"") + devname + "\": [";
+    const char *p = strstr(buf, key.c_str());
+    if (!p) return;
+    p += key.size();
+    for (int b = 0; b < NBUCKET; b++) {
+        int v = -1;
+        if (sscanf(p, "%d", &v) == 1 && (v == 0 || v == 1)) g_tune[dev][b] = v;
+        p = strchr(p, b + 1 < NBUCKET ? ',' : ']');
+        if (!p) break;
+        p++;
+    }
+}
+
+void tune_save_locked(int dev, const char *devname)
+{
+    std::string path = tune_path();
+    std::string dir = path.substr(0, path.find_last_of('/'));
+    if (!dir.empty()) {
+        // create the directory chain (best effort)
+        for (size_t i = 1; i <= dir.size(); i++)
+            if (i == dir.size() || dir[i] == '/') {
+                std::string sub = dir.substr(0, i);
+                if (!sub.empty()) (void)mkdir(sub.c_str(), 0755);
+            }
+    }
+    FILE *f = fopen(path.c_str(), "w");
+    if (!f) return;
+    fprintf(f, "{\"%s\": [", devname);
+    for (int b = 0; b < NBUCKET; b++) fprintf(f, "%d%s", g_tune[dev][b] < 0 ? 1 : g_tune[dev][b], b + 1 < NBUCKET ? ", " : "");
+    fprintf(f, "]}\n");
+    fclose(f);
+}
+
+}  // namespace
+
+struct gbx_plan {
+    int device;
+    DevOp *d_ops;
+    Item *d_items;
+    int *d_counter;
+    int nitems, nops;
+    double flops;
+    int grid;
+    cudaGraphExec_t gexec;
+};
+
+namespace {
+
+void tile_items(const DevOp &o, int opi, int variant, std::vector<Item> &items, std::vector<double> &cost)
+{
+    if (o.kind == GBX_OP_TRSM) {
+        const int nsys = o.left ? o.n : o.m;
+        const int order = o.left ? o.m : o.n;
+        for (int s = 0; s * TRSM_SYS < nsys; s++) {
+            items.push_back({opi, s, 0, 0});
+            cost.push_back((double)order * order * TRSM_SYS * 4.0);   // serial substitution
+        }
+        return;
+    }
+    const int ts = variant ? 64 : 32;
+    const int tmn = (o.m + ts - 1) / ts, tnn = (o.n + ts - 1) / ts;
+    for (int j = 0; j < tnn; j++)
+        for (int i = 0; i < tmn; i++) {
+            items.push_back({opi, variant, i, j});
+            cost.push_back((double)ts * ts * std::max(o.k, 1));
+        }
+}
+
+gbx_status upload(gbx_ctx *ctx, const std::vector<DevOp> &ops, const std::vector<int> &variant, gbx_plan *p)
+{
+    std::vector<Item> items;
+    std::vector<double> cost;
+    for (size_t i = 0; i < ops.size(); i++) tile_items(ops[i], (int)i, variant[i], items, cost);
+    std::vector<int> order(items.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::vector<Item> sorted(items.size());
+    for (size_t i = 0; i < order.size(); i++) sorted[i] = items[order[i]];
+    p->nitems = (int)sorted.size();
+    p->nops = (int)ops.size();
+    cudaError_t e = cudaMalloc(&p->d_ops, sizeof(DevOp) * std::max<size_t>(1, ops.size()));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_items, sizeof(Item) * std::max<size_t>(1, sorted.size()));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_counter, sizeof(int));
+    if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_ALLOC, "plan: %s", cudaGetErrorString(e));
+    cudaStream_t s = (cudaStream_t)gbx_ctx_get_stream(ctx);
+    if (!ops.empty()) cudaMemcpyAsync(p->d_ops, ops.data(), sizeof(DevOp) * ops.size(), cudaMemcpyHostToDevice, s);
+    if (!sorted.empty())
+        cudaMemcpyAsync(p->d_items, sorted.data(), sizeof(Item) * sorted.size(), cudaMemcpyHostToDevice, s);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "plan upload: %s", cudaGetErrorString(e));
+    p->grid = gbx_ctx_sms(ctx) * 2;
+    return GBX_OK;
+}
+
+gbx_status launch(gbx_ctx *ctx, gbx_plan *p)
+{
+    cudaStream_t s = (cudaStream_t)gbx_ctx_get_stream(ctx);
+    if (p->nitems == 0) return GBX_OK;
+    cudaError_t e = cudaMemsetAsync(p->d_counter, 0, sizeof(int), s);
+    if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "plan counter: %s", cudaGetErrorString(e));
+    gbx_timer_begin(ctx, GBX_TIMER_BATCH);
+    grouped_kernel<<<std::min(p->grid, p->nitems), BT_THREADS, 0, s>>>(p->d_ops, p->d_items, p->nitems,
+                                                                       p->d_counter);
+    gbx_timer_end(ctx);
+    gbx_count_launch(ctx, 1);
+    return gbx_check_launch(ctx, "grouped kernel");
+}
+
+void plan_free(gbx_plan *p)
+{
+    if (!p) return;
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->d_ops) cudaFree(p->d_ops);
+    if (p->d_items) cudaFree(p->d_items);
+    if (p->d_counter) cudaFree(p->d_counter);
+    free(p);
+}
+
+// time one plan variant (median of 3 launches), ms
+float time_variant(gbx_ctx *ctx, const std::vector<DevOp> &ops, int variant)
+{
+    gbx_plan *p = (gbx_plan *)calloc(1, sizeof(gbx_plan));
+    std::vector<int> v(ops.size(), variant);
+    float best = 1e30f;
+    if (p && upload(ctx, ops, v, p) == GBX_OK) {
+        cudaStream_t s = (cudaStream_t)gbx_ctx_get_stream(ctx);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        launch(ctx, p);
+        for (int r = 0; r < 3; r++) {
+            cudaEventRecord(e0, s);
+            launch(ctx, p);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best = std::min(best, ms);
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    plan_free(p);
+    return best;
+}
+
+}  // namespace
+
+extern "C" gbx_status gbx_plan_create(gbx_ctx *ctx, const gbx_op *ops, int count, gbx_plan **out)
+{
+    if (!ctx || !out || count < 0 || (count > 0 && !ops)) return GBX_ERR_ARG;
+    *out = nullptr;
+    std::vector<DevOp> dops;
+    dops.reserve(count);
+    double flops = 0.0;
+    for (int i = 0; i < count; i++) {
+        const gbx_op &o = ops[i];
+        DevOp d{};
+        d.kind = o.kind;
+        d.m = o.m; d.n = o.n; d.k = o.k;
+        d.alpha = o.alpha; d.beta = o.beta;
+        d.A = o.A; d.lda = o.lda; d.B = o.B; d.ldb = o.ldb; d.C = o.C; d.ldc = o.ldc;
+        if (o.kind == GBX_OP_GEMM) {
+            int info = gbx_check_gemm_args(o.transa, o.transb, o.m, o.n, o.k, o.lda, o.ldb, o.ldc);
+            if (info) return gbx_fail(ctx, GBX_ERR_ARG, "plan op %d: DGEMM parameter %d", i, info);
+            d.ta = !gbx_lsame(o.transa, 'N');
+            d.tb = !gbx_lsame(o.transb, 'N');
+            if (o.m == 0 || o.n == 0) continue;
+            if (o.k == 0 || o.alpha == 0.0) d.k = 0;   // tiles then scale C by beta
+            flops += 2.0 * o.m * o.n * o.k;
+        } else if (o.kind == GBX_OP_TRSM) {
+            int info = gbx_check_trxm_args(o.side, o.uplo, o.transa, o.diag, o.m, o.n, o.lda, o.ldc);
+            if (info) return gbx_fail(ctx, GBX_ERR_ARG, "plan op %d: DTRSM parameter %d", i, info);
+            d.left = gbx_lsame(o.side, 'L');
+            const int order = d.left ? o.m : o.n;
+            if (order > TRSM_MAX_ORDER)
+                return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "plan op %d: triangle order %d > %d", i, order,
+                                TRSM_MAX_ORDER);
+            d.ta = !gbx_lsame(o.transa, 'N');
+            // effective triangle of the matrix T solved against (op(A) for
+            // side L, op(A)^T for side R)
+            const int tri = gbx_op_tri(o.uplo, o.transa, o.diag);
+            const bool op_lower = (tri & 1) != 0;
+            d.lower = d.left ? op_lower : !op_lower;
+            d.unit = gbx_lsame(o.diag, 'U');
+            if (o.m == 0 || o.n == 0) continue;
+            flops += (double)order * order * (d.left ? o.n : o.m);
+        } else {
+            return gbx_fail(ctx, GBX_ERR_ARG, "plan op %d: unknown kind %d", i, o.kind);
+        }
+        dops.push_back(d);
+    }
+
+    // autotune the GEMM tile variant per bucket
+    int dev = gbx_ctx_device(ctx);
+    cudaDeviceProp prop;
+    char devname[256] = "gpu";
+    if (cudaGetDeviceProperties(&prop, dev) == cudaSuccess) snprintf(devname, sizeof devname, "%s", prop.name);
+    std::vector<int> variant(dops.size(), 1);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        if (!g_tune_loaded) tune_load_locked(dev, devname);
+        bool changed = false;
+        for (int b = 0; b < NBUCKET; b++) {
+            std::vector<DevOp> sub;
+            for (auto &d : dops)
+                if (d.kind == GBX_OP_GEMM && bucket_of(d.m, d.n) == b) sub.push_back(d);
+            if (sub.empty() || (dev < 64 && g_tune[dev][b] >= 0)) continue;
+            // time on scratch output: same shapes and operands, beta = 0
+            double *scratch = nullptr;
+            size_t need = 0;
+            for (auto &d : sub) need = std::max(need, (size_t)d.ldc * d.n);
+            if (cudaMalloc(&scratch, sizeof(double) * std::max<size_t>(need, 1)) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            for (auto &d : sub) { d.C = scratch; d.beta = 0.0; }
+            const float t32 = time_variant(ctx, sub, 0), t64 = time_variant(ctx, sub, 1);
+            cudaFree(scratch);
+            if (dev < 64) g_tune[dev][b] = t32 < t64 ? 0 : 1;
+            changed = true;
+        }
+        if (changed && dev < 64) tune_save_locked(dev, devname);
+        for (size_t i = 0; i < dops.size(); i++)
+            if (dops[i].kind == GBX_OP_GEMM && dev < 64) {
+                const int v = g_tune[dev][bucket_of(dops[i].m, dops[i].n)];
+                variant[i] = v < 0 ? 1 : v;
+            }
+    }
+
+    gbx_plan *p = (gbx_plan *)calloc(1, sizeof(gbx_plan));
+    if (!p) return GBX_ERR_ALLOC;
+    p->device = dev;
+    p->flops = flops;
+    gbx_status st = upload(ctx, dops, variant, p);
+    if (st != GBX_OK) {
+        plan_free(p);
+        return st;
+    }
+    *out = p;
+    return GBX_OK;
+}
+
+extern "C" gbx_status gbx_plan_launch(gbx_ctx *ctx, gbx_plan *p)
+{
+    if (!ctx || !p) return GBX_ERR_ARG;
+    return launch(ctx, p);
+}
+
+extern "C" gbx_status gbx_plan_graph_launch(gbx_ctx *ctx, gbx_plan *p)
+{
+    if (!ctx || !p) return GBX_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)gbx_ctx_get_stream(ctx);
+    if (!p->gexec) {
+        cudaGraph_t g;
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "capture: %s", cudaGetErrorString(e));
+        gbx_status st = launch(ctx, p);
+        e = cudaStreamEndCapture(s, &g);
+        if (st != GBX_OK) return st;
+        if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "capture end: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&p->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "instantiate: %s", cudaGetErrorString(e));
+    }
+    gbx_count_launch(ctx, 1);
+    cudaError_t e = cudaGraphLaunch(p->gexec, s);
+    return e == cudaSuccess ? GBX_OK : gbx_fail(ctx, GBX_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
+}
+
+extern "C" gbx_status gbx_plan_destroy(gbx_plan *p)
+{
+    plan_free(p);
+    return GBX_OK;
+}
+
+extern "C" gbx_status gbx_plan_info(const gbx_plan *p, int *items, double *flops)
+{
+    if (!p) return GBX_ERR_ARG;
+    if (items) *items = p->nitems;
+    if (flops) *flops = p->flops;
+    return GBX_OK;
+}
