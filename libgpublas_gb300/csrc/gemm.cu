@@ -50,13 +50,11 @@ gbx_status scale_matrix(gbx_ctx *ctx, int m, int n, T beta, T *C, long long ldc,
 template gbx_status scale_matrix<double>(gbx_ctx *, int, int, double, double *, long long, int);
 template gbx_status scale_matrix<dcplx>(gbx_ctx *, int, int, dcplx, dcplx *, long long, int);
 
-template <typename T>
-gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
+template <typename T, int TM>
+gbx_status launch_gemm_tile(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
 {
-    // double: 128x128 block tile, 8x8 per thread; complex: 64x64, 4x4.
-    constexpr int TM = sizeof(T) == 8 ? 8 : 4, TN = TM, BK = 8;
+    constexpr int TN = TM, BK = 8;
     constexpr int BM = 16 * TM, BN = 16 * TN;
-    if (p.m <= 0 || p.n <= 0) return GBX_OK;
     p.tiles_m = (p.m + BM - 1) / BM;
     p.tiles_n = (p.n + BN - 1) / BN;
     long long blocks;
@@ -71,6 +69,29 @@ gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
     gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);
     return gbx_check_launch(ctx, what);
+}
+
+// Tile choice: the largest block tile that still gives every SM two tiles;
+// 128x128 (8x8 per thread) for large problems, 64x64 and 32x32 for the
+// skinny and small products that DTRSM's recursion and small calls produce
+// (with few large tiles most SMs would idle).  Complex uses 64x64 / 32x32.
+template <typename T>
+gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
+{
+    if (p.m <= 0 || p.n <= 0) return GBX_OK;
+    const long long want = 2LL * gbx_ctx_sms(ctx);
+    auto tiles = [&](int bm) {
+        const long long tm = (p.m + bm - 1) / bm, tn = (p.n + bm - 1) / bm;
+        return p.c_part == C_FULL ? tm * tn : tm * (tm + 1) / 2;
+    };
+    if constexpr (sizeof(T) == 8) {
+        if (tiles(128) >= want) return launch_gemm_tile<T, 8>(ctx, p, what);
+        if (tiles(64) >= want) return launch_gemm_tile<T, 4>(ctx, p, what);
+        return launch_gemm_tile<T, 2>(ctx, p, what);
+    } else {
+        if (tiles(64) >= want) return launch_gemm_tile<T, 4>(ctx, p, what);
+        return launch_gemm_tile<T, 2>(ctx, p, what);
+    }
 }
 template gbx_status launch_gemm<double>(gbx_ctx *, GemmArgs<double>, const char *);
 template gbx_status launch_gemm<dcplx>(gbx_ctx *, GemmArgs<dcplx>, const char *);

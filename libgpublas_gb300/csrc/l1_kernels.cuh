@@ -149,12 +149,18 @@ struct Blue {
     static constexpr double ssml = 0x1p+537, sbig = 0x1p-538;
 };
 
+// The range test runs on the integer pipe (bit patterns of |v| compare like
+// the values); the common mid-range element costs one DFMA, which matters on
+// a part whose FP64 pipe is the bound for this 8-byte-per-FMA kernel.
 __device__ __forceinline__ void blue_acc(double v, double &asml, double &amed, double &abig)
 {
-    const double ax = fabs(v);
-    if (ax > Blue::tbig) { const double t = ax * Blue::sbig; abig = fma(t, t, abig); }
-    else if (ax < Blue::tsml) { const double t = ax * Blue::ssml; asml = fma(t, t, asml); }
-    else amed = fma(ax, ax, amed);   // also takes NaN, which then propagates
+    constexpr unsigned long long kBig = (unsigned long long)(486 + 1023) << 52;   // bits of tbig
+    constexpr unsigned long long kSml = (unsigned long long)(1023 - 511) << 52;   // bits of tsml
+    constexpr unsigned long long kInf = 0x7FF0000000000000ull;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    if (b > kBig && b <= kInf) { const double t = fabs(v) * Blue::sbig; abig = fma(t, t, abig); }
+    else if (b < kSml) { const double t = fabs(v) * Blue::ssml; asml = fma(t, t, asml); }
+    else amed = fma(v, v, amed);   // also takes NaN, which then propagates
 }
 
 static __global__ void __launch_bounds__(L1_THREADS)
@@ -238,8 +244,9 @@ nrm2_finish(const double *__restrict__ part, int g, double *__restrict__ res)
 template <bool IS_MIN>
 __device__ __forceinline__ unsigned long long amax_key(double v)
 {
-    if (isnan(v)) return 0ull;
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(fabs(v));
+    // integer pipe only: |v| is the bit pattern without the sign bit
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    if (bits > 0x7FF0000000000000ull) return 0ull;   // NaN
     return IS_MIN ? ~bits : bits;
 }
 
