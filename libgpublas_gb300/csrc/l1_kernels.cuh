@@ -173,11 +173,17 @@ nrm2_partial(int n, const double *__restrict__ x, int incx, double *__restrict__
         const long long n2 = (long long)n >> 1;
         const double2 *x2 = (const double2 *)x;
         long long i = tid;
+        // four independent accumulator chains per thread (the DFMA latency
+        // would otherwise serialise the loop)
+        double s1 = 0.0, m1 = 0.0, b1 = 0.0, s2 = 0.0, m2 = 0.0, b2 = 0.0, s3 = 0.0, m3 = 0.0, b3 = 0.0;
         for (; i + stride < n2; i += 2 * stride) {
             double2 a = ldg2(x2 + i), b = ldg2(x2 + i + stride);
-            blue_acc(a.x, asml, amed, abig); blue_acc(a.y, asml, amed, abig);
-            blue_acc(b.x, asml, amed, abig); blue_acc(b.y, asml, amed, abig);
+            blue_acc(a.x, asml, amed, abig); blue_acc(a.y, s1, m1, b1);
+            blue_acc(b.x, s2, m2, b2); blue_acc(b.y, s3, m3, b3);
         }
+        asml += (s1 + s2) + s3;
+        amed += (m1 + m2) + m3;
+        abig += (b1 + b2) + b3;
         for (; i < n2; i += stride) {
             double2 a = ldg2(x2 + i);
             blue_acc(a.x, asml, amed, abig); blue_acc(a.y, asml, amed, abig);
@@ -293,7 +299,22 @@ iamax_partial(int n, const double *__restrict__ x, int incx, unsigned long long 
     if (incx == 1 && (((uintptr_t)x & 15) == 0)) {
         const long long n2 = (long long)n >> 1;
         const double2 *x2 = (const double2 *)x;
-        for (long long i = tid; i < n2; i += stride) {
+        long long i = tid;
+        // four loads in flight per thread; elements are visited in increasing
+        // index order within the thread, so the first index keeps winning ties
+        for (; i + 3 * stride < n2; i += 4 * stride) {
+            double2 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = ldg2(x2 + i + u * stride);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const long long e = 2 * (i + u * stride);
+                const unsigned long long k0 = amax_key<IS_MIN>(v[u].x), k1 = amax_key<IS_MIN>(v[u].y);
+                if (better(k0, e, bk, bi)) { bk = k0; bi = e; }
+                if (better(k1, e + 1, bk, bi)) { bk = k1; bi = e + 1; }
+            }
+        }
+        for (; i < n2; i += stride) {
             double2 v = ldg2(x2 + i);
             unsigned long long k0 = amax_key<IS_MIN>(v.x), k1 = amax_key<IS_MIN>(v.y);
             if (better(k0, 2 * i, bk, bi)) { bk = k0; bi = 2 * i; }
