@@ -175,7 +175,14 @@ gbx_status gbx_dsyrk_ozaki(gbx_ctx *ctx, char uplo, char trans, int n, int k, do
  * gbx_plan_launch enqueues a counter reset and the kernel (capturable);
  * gbx_plan_graph_launch records that into a CUDA graph once and replays it.
  * The operations must not overlap in their outputs. */
-enum { GBX_OP_GEMM = 1, GBX_OP_TRSM = 2 };
+enum {
+    GBX_OP_GEMM = 1, /* grouped kernel and serving loop                        */
+    GBX_OP_TRSM = 2, /* grouped kernel and serving loop                        */
+    GBX_OP_SYRK = 3, /* serving loop: uplo, transa as trans, n, k, A, beta, C   */
+    GBX_OP_DOT = 4,  /* serving loop: n, x = A (incx = lda), y = B (incy = ldb),
+                        result in device memory at C                           */
+    GBX_OP_NRM2 = 5  /* serving loop: n, x = A (incx = lda), result at C        */
+};
 typedef struct {
     int kind;                 /* GBX_OP_GEMM or GBX_OP_TRSM                     */
     char transa, transb;      /* GEMM: op(A), op(B); TRSM: transa = op(A)       */
@@ -192,6 +199,30 @@ gbx_status gbx_plan_launch(gbx_ctx *ctx, gbx_plan *plan);
 gbx_status gbx_plan_graph_launch(gbx_ctx *ctx, gbx_plan *plan);
 gbx_status gbx_plan_destroy(gbx_plan *plan);
 gbx_status gbx_plan_info(const gbx_plan *plan, int *work_items, double *flops);
+
+/* ---- serving loop (no reference counterpart: the reference serves one call
+ * at a time on one cuBLAS handle, runtime-blas.c:14-23) -------------------
+ * Continuous batching of calls from many host threads on device-resident
+ * operands: a dispatcher thread takes everything queued, groups the small
+ * DGEMM (m, n <= 512, k <= 4096) and DTRSM (order <= 256) requests into one
+ * grouped kernel and runs the others with the regular routines, each batch
+ * on the stream of a free slot, so new requests overlap with work already on
+ * the GPU.  Routing depends only on the operation, so results are identical
+ * served alone or in a mix.  gbx_server_admit / gbx_server_release reserve
+ * staging memory against a budget (mem_budget, or 80% of the HBM free at
+ * creation when 0) and block while it is exhausted. */
+typedef struct gbx_server gbx_server;
+gbx_status gbx_server_create(int device, int slots, size_t mem_budget, gbx_server **srv);
+gbx_status gbx_server_submit(gbx_server *srv, const gbx_op *op, uint64_t *ticket);
+gbx_status gbx_server_wait(gbx_server *srv, uint64_t ticket, double *latency_us);
+gbx_status gbx_server_call(gbx_server *srv, const gbx_op *op, double *latency_us);
+gbx_status gbx_server_admit(gbx_server *srv, size_t bytes);
+gbx_status gbx_server_release(gbx_server *srv, size_t bytes);
+gbx_status gbx_server_stats(gbx_server *srv, uint64_t *completed, uint64_t *batches,
+                            uint64_t *grouped_calls, double *p50_us, double *p99_us,
+                            uint64_t *admission_waits);
+gbx_status gbx_server_reset_stats(gbx_server *srv);
+gbx_status gbx_server_destroy(gbx_server *srv);
 
 #ifdef __cplusplus
 }

@@ -6,5 +6,5 @@ the gbx_* device-pointer C ABI declared in ``include/gbxblas.h``.  This
 Python package only builds it (``build.build_library``) and binds it with
 ctypes (``_lib``) for tests and benchmarks.
 """
-from ._lib import (F77, OP_GEMM, OP_TRSM, Device, GbxError, GbxOp, LIB_PATH, declared_symbols,  # noqa: F401
-                   load, stats)
+from ._lib import (F77, OP_DOT, OP_GEMM, OP_NRM2, OP_SYRK, OP_TRSM, Device, GbxError, GbxOp,  # noqa: F401
+                   LIB_PATH, Server, declared_symbols, load, stats)

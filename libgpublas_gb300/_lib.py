@@ -111,6 +111,17 @@ def _declare(L):
     L.gbx_plan_graph_launch.argtypes = [_P, _P]
     L.gbx_plan_destroy.argtypes = [_P]
     L.gbx_plan_info.argtypes = [_P, C.POINTER(_I), C.POINTER(_D)]
+    L.gbx_server_create.argtypes = [_I, _I, C.c_size_t, C.POINTER(_P)]
+    L.gbx_server_submit.argtypes = [_P, _P, C.POINTER(C.c_uint64)]
+    L.gbx_server_wait.argtypes = [_P, C.c_uint64, C.POINTER(_D)]
+    L.gbx_server_call.argtypes = [_P, _P, C.POINTER(_D)]
+    L.gbx_server_admit.argtypes = [_P, C.c_size_t]
+    L.gbx_server_release.argtypes = [_P, C.c_size_t]
+    L.gbx_server_stats.argtypes = [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                   C.POINTER(C.c_uint64), C.POINTER(_D), C.POINTER(_D),
+                                   C.POINTER(C.c_uint64)]
+    L.gbx_server_reset_stats.argtypes = [_P]
+    L.gbx_server_destroy.argtypes = [_P]
     L.gbx_ctx_enable_timing.argtypes = [_P, _I]
     L.gbx_ctx_kernel_time.argtypes = [_P, _I, C.POINTER(_D), C.POINTER(C.c_uint64)]
     L.gbx_diag_fp64_peak.argtypes = [_P, C.POINTER(_D)]
@@ -126,7 +137,59 @@ class GbxOp(C.Structure):
                 ("C", C.c_void_p), ("ldc", C.c_int)]
 
 
-OP_GEMM, OP_TRSM = 1, 2
+OP_GEMM, OP_TRSM, OP_SYRK, OP_DOT, OP_NRM2 = 1, 2, 3, 4, 5
+
+
+class Server:
+    """The serving loop (gbx_server_*): calls from many threads on
+    device-resident operands, continuously batched."""
+
+    def __init__(self, device=0, slots=8, mem_budget=0):
+        self.L = load()
+        h = _P()
+        st = self.L.gbx_server_create(device, slots, mem_budget, C.byref(h))
+        if st != 0:
+            raise GbxError(f"gbx_server_create failed with status {st}")
+        self.h = h
+
+    def call(self, op):
+        lat = C.c_double(0.0)
+        st = self.L.gbx_server_call(self.h, C.byref(op), C.byref(lat))
+        return st, lat.value
+
+    def submit(self, op):
+        t = C.c_uint64(0)
+        st = self.L.gbx_server_submit(self.h, C.byref(op), C.byref(t))
+        if st != 0:
+            raise GbxError(f"submit failed with status {st}")
+        return t.value
+
+    def wait(self, ticket):
+        lat = C.c_double(0.0)
+        st = self.L.gbx_server_wait(self.h, ticket, C.byref(lat))
+        return st, lat.value
+
+    def admit(self, nbytes):
+        return self.L.gbx_server_admit(self.h, nbytes)
+
+    def release(self, nbytes):
+        return self.L.gbx_server_release(self.h, nbytes)
+
+    def stats(self):
+        c, b, g = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        p50, p99, w = C.c_double(), C.c_double(), C.c_uint64()
+        self.L.gbx_server_stats(self.h, C.byref(c), C.byref(b), C.byref(g), C.byref(p50),
+                                C.byref(p99), C.byref(w))
+        return dict(completed=c.value, batches=b.value, grouped_calls=g.value, p50_us=p50.value,
+                    p99_us=p99.value, admission_waits=w.value)
+
+    def reset_stats(self):
+        self.L.gbx_server_reset_stats(self.h)
+
+    def close(self):
+        if self.h:
+            self.L.gbx_server_destroy(self.h)
+            self.h = None
 
 
 def stats():

@@ -370,6 +370,108 @@ float time_variant(gbx_ctx *ctx, const std::vector<DevOp> &ops, int variant)
 
 }  // namespace
 
+// Validates one operation and converts it to its device form.  Returns 0 and
+// sets *skip for operations with no work.  The flops of the operation are
+// added to *flops.
+static gbx_status to_devop(gbx_ctx *ctx, const gbx_op &o, int i, DevOp &d, bool &skip, double &flops)
+{
+    d = DevOp{};
+    skip = false;
+    d.kind = o.kind;
+    d.m = o.m; d.n = o.n; d.k = o.k;
+    d.alpha = o.alpha; d.beta = o.beta;
+    d.A = o.A; d.lda = o.lda; d.B = o.B; d.ldb = o.ldb; d.C = o.C; d.ldc = o.ldc;
+    if (o.kind == GBX_OP_GEMM) {
+        int info = gbx_check_gemm_args(o.transa, o.transb, o.m, o.n, o.k, o.lda, o.ldb, o.ldc);
+        if (info) return gbx_fail(ctx, GBX_ERR_ARG, "op %d: DGEMM parameter %d", i, info);
+        d.ta = !gbx_lsame(o.transa, 'N');
+        d.tb = !gbx_lsame(o.transb, 'N');
+        if (o.m == 0 || o.n == 0) { skip = true; return GBX_OK; }
+        if (o.k == 0 || o.alpha == 0.0) d.k = 0;   // tiles then scale C by beta
+        flops += 2.0 * o.m * o.n * o.k;
+        return GBX_OK;
+    }
+    if (o.kind == GBX_OP_TRSM) {
+        int info = gbx_check_trxm_args(o.side, o.uplo, o.transa, o.diag, o.m, o.n, o.lda, o.ldc);
+        if (info) return gbx_fail(ctx, GBX_ERR_ARG, "op %d: DTRSM parameter %d", i, info);
+        d.left = gbx_lsame(o.side, 'L');
+        const int order = d.left ? o.m : o.n;
+        if (order > TRSM_MAX_ORDER)
+            return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "op %d: triangle order %d > %d", i, order, TRSM_MAX_ORDER);
+        d.ta = !gbx_lsame(o.transa, 'N');
+        // effective triangle of the matrix T solved against (op(A) for side
+        // L, op(A)^T for side R)
+        const bool op_lower = (gbx_op_tri(o.uplo, o.transa, o.diag) & 1) != 0;
+        d.lower = d.left ? op_lower : !op_lower;
+        d.unit = gbx_lsame(o.diag, 'U');
+        if (o.m == 0 || o.n == 0) { skip = true; return GBX_OK; }
+        flops += (double)order * order * (d.left ? o.n : o.m);
+        return GBX_OK;
+    }
+    return gbx_fail(ctx, GBX_ERR_ARG, "op %d: kind %d is not a grouped operation", i, o.kind);
+}
+
+// Grouped launch without a plan: descriptors are packed into the context's
+// pinned buffer and copied to its workspace on its stream, then the counter
+// is reset and the kernel launched; nothing synchronises.  Used by the
+// serving loop.  The pinned buffer is reused by the next call on the same
+// context, which must therefore come after this one completed (the serving
+// loop hands a context out again only after its work finished).
+extern "C" gbx_status gbx_grouped_launch_inline(gbx_ctx *ctx, const gbx_op *ops, int count)
+{
+    std::vector<DevOp> dops;
+    dops.reserve(count);
+    double flops = 0.0;
+    for (int i = 0; i < count; i++) {
+        DevOp d;
+        bool skip;
+        gbx_status st = to_devop(ctx, ops[i], i, d, skip, flops);
+        if (st != GBX_OK) return st;
+        if (!skip) dops.push_back(d);
+    }
+    if (dops.empty()) return GBX_OK;
+    const int dev = gbx_ctx_device(ctx);
+    std::vector<Item> items;
+    std::vector<double> cost;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        for (size_t i = 0; i < dops.size(); i++) {
+            int v = 1;
+            if (dops[i].kind == GBX_OP_GEMM && g_tune_loaded && dev < 64) {
+                const int t = g_tune[dev][bucket_of(dops[i].m, dops[i].n)];
+                v = t < 0 ? 1 : t;
+            }
+            tile_items(dops[i], (int)i, v, items, cost);
+        }
+    }
+    std::vector<int> order(items.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    const size_t ops_bytes = sizeof(DevOp) * dops.size();
+    const size_t items_off = (ops_bytes + 255) & ~(size_t)255;
+    const size_t items_bytes = sizeof(Item) * items.size();
+    const size_t ctr_off = (items_off + items_bytes + 255) & ~(size_t)255;
+    const size_t total = ctr_off + 256;
+    void *h, *d;
+    gbx_status st;
+    if ((st = gbx_pinned(ctx, total, &h)) != GBX_OK) return st;
+    if ((st = gbx_ws(ctx, GBX_WS_BATCH, total, &d)) != GBX_OK) return st;
+    memcpy(h, dops.data(), ops_bytes);
+    Item *hi = (Item *)((char *)h + items_off);
+    for (size_t i = 0; i < order.size(); i++) hi[i] = items[order[i]];
+    memset((char *)h + ctr_off, 0, 256);
+    cudaStream_t s = (cudaStream_t)gbx_ctx_get_stream(ctx);
+    cudaError_t e = cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "grouped upload: %s", cudaGetErrorString(e));
+    const int nitems = (int)items.size();
+    gbx_timer_begin(ctx, GBX_TIMER_BATCH);
+    grouped_kernel<<<std::min(gbx_ctx_sms(ctx) * 2, nitems), BT_THREADS, 0, s>>>(
+        (const DevOp *)d, (const Item *)((char *)d + items_off), nitems, (int *)((char *)d + ctr_off));
+    gbx_timer_end(ctx);
+    gbx_count_launch(ctx, 1);
+    return gbx_check_launch(ctx, "grouped kernel");
+}
+
 extern "C" gbx_status gbx_plan_create(gbx_ctx *ctx, const gbx_op *ops, int count, gbx_plan **out)
 {
     if (!ctx || !out || count < 0 || (count > 0 && !ops)) return GBX_ERR_ARG;
@@ -378,41 +480,11 @@ extern "C" gbx_status gbx_plan_create(gbx_ctx *ctx, const gbx_op *ops, int count
     dops.reserve(count);
     double flops = 0.0;
     for (int i = 0; i < count; i++) {
-        const gbx_op &o = ops[i];
-        DevOp d{};
-        d.kind = o.kind;
-        d.m = o.m; d.n = o.n; d.k = o.k;
-        d.alpha = o.alpha; d.beta = o.beta;
-        d.A = o.A; d.lda = o.lda; d.B = o.B; d.ldb = o.ldb; d.C = o.C; d.ldc = o.ldc;
-        if (o.kind == GBX_OP_GEMM) {
-            int info = gbx_check_gemm_args(o.transa, o.transb, o.m, o.n, o.k, o.lda, o.ldb, o.ldc);
-            if (info) return gbx_fail(ctx, GBX_ERR_ARG, "plan op %d: DGEMM parameter %d", i, info);
-            d.ta = !gbx_lsame(o.transa, 'N');
-            d.tb = !gbx_lsame(o.transb, 'N');
-            if (o.m == 0 || o.n == 0) continue;
-            if (o.k == 0 || o.alpha == 0.0) d.k = 0;   // tiles then scale C by beta
-            flops += 2.0 * o.m * o.n * o.k;
-        } else if (o.kind == GBX_OP_TRSM) {
-            int info = gbx_check_trxm_args(o.side, o.uplo, o.transa, o.diag, o.m, o.n, o.lda, o.ldc);
-            if (info) return gbx_fail(ctx, GBX_ERR_ARG, "plan op %d: DTRSM parameter %d", i, info);
-            d.left = gbx_lsame(o.side, 'L');
-            const int order = d.left ? o.m : o.n;
-            if (order > TRSM_MAX_ORDER)
-                return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "plan op %d: triangle order %d > %d", i, order,
-                                TRSM_MAX_ORDER);
-            d.ta = !gbx_lsame(o.transa, 'N');
-            // effective triangle of the matrix T solved against (op(A) for
-            // side L, op(A)^T for side R)
-            const int tri = gbx_op_tri(o.uplo, o.transa, o.diag);
-            const bool op_lower = (tri & 1) != 0;
-            d.lower = d.left ? op_lower : !op_lower;
-            d.unit = gbx_lsame(o.diag, 'U');
-            if (o.m == 0 || o.n == 0) continue;
-            flops += (double)order * order * (d.left ? o.n : o.m);
-        } else {
-            return gbx_fail(ctx, GBX_ERR_ARG, "plan op %d: unknown kind %d", i, o.kind);
-        }
-        dops.push_back(d);
+        DevOp d;
+        bool skip;
+        gbx_status st = to_devop(ctx, ops[i], i, d, skip, flops);
+        if (st != GBX_OK) return st;
+        if (!skip) dops.push_back(d);
     }
 
     // autotune the GEMM tile variant per bucket

@@ -1,0 +1,199 @@
+"""The serving loop: calls from 16 host threads, continuously batched.
+
+* Each result is bit-identical whether the call was served alone (one call
+  in flight) or in a mix with all the others submitted concurrently from 16
+  threads, and matches the oracle (relative error <= 1e-13; DTRSM residual
+  <= 1e-14; DDOT/DNRM2 within 2*n*u of the double-double value).
+* Small calls are grouped: fewer device batches than calls.
+* Admission by memory: a reservation larger than the budget is refused; two
+  reservations that do not fit together are serialised.
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def loguni(rng, lo, hi):
+    return int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+
+
+class Calls:
+    def __init__(self, orc, count, seed):
+        import torch
+        import libgpublas_gb300 as g
+        rng = np.random.default_rng(seed)
+        chunks, self.specs, off = [], [], 0
+
+        def place(a):
+            nonlocal off
+            a = np.asfortranarray(a)
+            chunks.append(a.ravel(order="F"))
+            pad = -a.size % 4
+            if pad:
+                chunks.append(np.zeros(pad))
+            start = off
+            off += a.size + pad
+            return start
+
+        s = seed
+        for i in range(count):
+            kind = [1, 1, 1, 2, 3, 4, 1, 2][i % 8]
+            if kind == 1:
+                big = i % 16 == 0
+                m, n, k = ((loguni(rng, 600, 1200),) * 3 if big else
+                           (loguni(rng, 8, 300), loguni(rng, 8, 300), loguni(rng, 8, 300)))
+                a, s = orc.matrix(m, k, s)
+                b, s = orc.matrix(k, n, s)
+                c, s = orc.matrix(m, n, s)
+                self.specs.append(dict(kind=1, m=m, n=n, k=k, a=a, b=b, c=c, oa=place(a), ob=place(b),
+                                       oc=place(c)))
+            elif kind == 2:
+                order = loguni(rng, 8, 256) if i % 3 else loguni(rng, 300, 600)
+                a, s = orc.trsm_matrix(order, s)
+                b, s = orc.matrix(order, 16, s)
+                self.specs.append(dict(kind=2, m=order, n=16, a=a, b=b, oa=place(a), ob=place(b)))
+            elif kind == 3:
+                n, k = loguni(rng, 64, 700), loguni(rng, 16, 300)
+                a, s = orc.matrix(n, k, s)
+                c, s = orc.matrix(n, n, s)
+                self.specs.append(dict(kind=3, n=n, k=k, a=a, c=c, oa=place(a), oc=place(c)))
+            else:
+                n = loguni(rng, 100, 200000)
+                x, s = orc.uniform(n, s)
+                y, s = orc.uniform(n, s)
+                self.specs.append(dict(kind=4, n=n, x=x, y=y, ox=place(x), oy=place(y),
+                                       ores=place(np.zeros(1))))
+        self.host = np.concatenate(chunks)
+        self.dev = torch.from_numpy(self.host).cuda()
+        base = self.dev.data_ptr()
+        self.ops = []
+        for sp in self.specs:
+            if sp["kind"] == 1:
+                op = g.GbxOp(kind=1, transa=b"N", transb=b"N", m=sp["m"], n=sp["n"], k=sp["k"],
+                             alpha=1.0, beta=0.5, A=base + 8 * sp["oa"], lda=sp["m"],
+                             B=base + 8 * sp["ob"], ldb=sp["k"], C=base + 8 * sp["oc"], ldc=sp["m"])
+            elif sp["kind"] == 2:
+                op = g.GbxOp(kind=2, transa=b"N", side=b"L", uplo=b"L", diag=b"N", m=sp["m"], n=16,
+                             alpha=1.0, A=base + 8 * sp["oa"], lda=sp["m"], C=base + 8 * sp["ob"],
+                             ldc=sp["m"])
+            elif sp["kind"] == 3:
+                op = g.GbxOp(kind=3, uplo=b"L", transa=b"N", n=sp["n"], k=sp["k"], alpha=-1.0,
+                             beta=1.0, A=base + 8 * sp["oa"], lda=sp["n"], C=base + 8 * sp["oc"],
+                             ldc=sp["n"])
+            else:
+                op = g.GbxOp(kind=4, n=sp["n"], A=base + 8 * sp["ox"], lda=1, B=base + 8 * sp["oy"],
+                             ldb=1, C=base + 8 * sp["ores"])
+            self.ops.append(op)
+
+    def reset(self):
+        import torch
+        self.dev.copy_(torch.from_numpy(self.host))
+        torch.cuda.synchronize()
+
+    def outputs(self):
+        h = self.dev.cpu().numpy()
+        out = []
+        for sp in self.specs:
+            key = {1: "oc", 2: "ob", 3: "oc", 4: "ores"}[sp["kind"]]
+            ref = {1: "c", 2: "b", 3: "c", 4: None}[sp["kind"]]
+            size = 1 if ref is None else sp[ref].size
+            shape = (1,) if ref is None else sp[ref].shape
+            out.append(h[sp[key]: sp[key] + size].reshape(shape, order="F").copy())
+        return out
+
+
+@pytest.fixture(scope="module")
+def server(lib):
+    import libgpublas_gb300 as g
+    s = g.Server(0, slots=8)
+    yield s
+    s.close()
+
+
+def test_alone_equals_in_mix_and_oracle(orc, server):
+    calls = Calls(orc, 96, seed=11)
+    calls.reset()
+    for op in calls.ops:
+        st, _ = server.call(op)
+        assert st == 0
+    alone = calls.outputs()
+
+    calls.reset()
+    server.reset_stats()
+    errors = []
+
+    def worker(idx):
+        for j in range(idx, len(calls.ops), 16):
+            st, _ = server.call(calls.ops[j])
+            if st != 0:
+                errors.append((j, st))
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(16)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
+    mixed = calls.outputs()
+    st = server.stats()
+    assert st["completed"] == len(calls.ops)
+    assert st["batches"] < st["completed"]          # small calls were grouped
+    assert 0 < st["p50_us"] <= st["p99_us"]
+    for sp, a, m in zip(calls.specs, alone, mixed):
+        assert np.array_equal(a, m), sp["kind"]
+
+    for sp, got in zip(calls.specs, mixed):
+        if sp["kind"] == 1:
+            want = sp["c"].copy(order="F")
+            orc.dgemm("N", "N", sp["m"], sp["n"], sp["k"], 1.0, sp["a"], sp["b"], 0.5, want)
+            assert np.linalg.norm(got - want) <= 1e-13 * np.linalg.norm(want)
+        elif sp["kind"] == 2:
+            r = orc.dtrsm_residual("L", "L", "N", "N", sp["m"], 16, 1.0, sp["a"], sp["b"],
+                                   np.asfortranarray(got))
+            assert r <= 1e-14
+        elif sp["kind"] == 3:
+            want = sp["c"].copy(order="F")
+            orc.dsyrk("L", "N", sp["n"], sp["k"], -1.0, sp["a"], 1.0, want)
+            assert np.linalg.norm(np.tril(got - want)) <= 1e-13 * np.linalg.norm(np.tril(want))
+        else:
+            ref = orc.ddot_dd(sp["n"], sp["x"], 1, sp["y"], 1)
+            bound = 2 * sp["n"] * 2.0 ** -53 * float(np.abs(sp["x"]) @ np.abs(sp["y"]))
+            assert abs(got[0] - ref) <= bound
+
+
+def test_submit_many_then_wait(orc, server):
+    calls = Calls(orc, 40, seed=12)
+    calls.reset()
+    tickets = [server.submit(op) for op in calls.ops]
+    for t in reversed(tickets):
+        st, lat = server.wait(t)
+        assert st == 0 and lat > 0
+
+
+def test_memory_admission(lib):
+    import libgpublas_gb300 as g
+    s = g.Server(0, slots=2, mem_budget=1 << 20)
+    try:
+        assert s.admit(2 << 20) == 6        # GBX_ERR_ADMISSION: can never fit
+        assert s.admit(600 << 10) == 0
+        order = []
+
+        def second():
+            assert s.admit(600 << 10) == 0  # waits until the first is released
+            order.append("second admitted")
+            s.release(600 << 10)
+
+        t = threading.Thread(target=second)
+        t.start()
+        time.sleep(0.2)
+        order.append("first released")
+        s.release(600 << 10)
+        t.join(timeout=10)
+        assert order == ["first released", "second admitted"]
+        assert s.stats()["admission_waits"] >= 1
+    finally:
+        s.close()
