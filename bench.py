@@ -49,7 +49,8 @@ import numpy as np  # noqa: E402
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-WORKLOADS = ("dgemm", "ozaki", "daxpy", "ddot", "dnrm2", "idamax", "dgemv", "dtrsm", "dsyrk")
+WORKLOADS = ("dgemm", "ozaki", "daxpy", "ddot", "dnrm2", "idamax", "dgemv", "dtrsm", "dsyrk",
+             "batched", "serving")
 
 
 def parse_args():
@@ -545,8 +546,293 @@ def bench_ozaki(args, dev, work, stream):
             "mma_ms_per_call": mma_ms / max(mma_n, 1)}
 
 
+# --------------------------------------------------------------------------
+# grouped execution: 20,000 DGEMM (M, N, K log-uniform in [8, 512], seed 3)
+# interleaved with 5,000 DTRSM (order log-uniform in [8, 256], diagonal
+# uniform[1,2], 16 right-hand sides); one persistent grouped kernel replayed
+# from a CUDA graph, against one launch per call
+# --------------------------------------------------------------------------
+def loguni(rng, lo, hi, size):
+    return np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), size))).astype(np.int64)
+
+
+def build_batched(ngemm, ntrsm, seed, device_buffer_factory):
+    import libgpublas_gb300 as g
+    rng = np.random.default_rng(seed)
+    mnk = loguni(rng, 8, 512, (ngemm, 3))
+    orders = loguni(rng, 8, 256, ntrsm)
+    sizes = [int(m * k + k * n + m * n) for m, n, k in mnk] + [int(o * o + 16 * o) for o in orders]
+    padded = [s + (-s % 4) for s in sizes]
+    total = int(sum(padded))
+    buf = device_buffer_factory(total)
+    base = buf.data_ptr()
+    ops, off, flops, gi, ti = [], 0, 0.0, 0, 0
+    # interleave: four GEMMs, then one TRSM
+    while gi < ngemm or ti < ntrsm:
+        for _ in range(4):
+            if gi < ngemm:
+                m, n, k = (int(v) for v in mnk[gi])
+                pa, pb, pc = base + 8 * off, base + 8 * (off + m * k), base + 8 * (off + m * k + k * n)
+                ops.append(g.GbxOp(kind=1, transa=b"N", transb=b"N", m=m, n=n, k=k, alpha=1.0, beta=0.5,
+                                   A=pa, lda=m, B=pb, ldb=k, C=pc, ldc=m))
+                flops += 2.0 * m * n * k
+                off += padded[gi]
+                gi += 1
+        if ti < ntrsm:
+            o = int(orders[ti])
+            ops.append(g.GbxOp(kind=2, transa=b"N", side=b"L", uplo=b"L", diag=b"N", m=o, n=16,
+                               alpha=1.0, A=base + 8 * off, lda=o, C=base + 8 * (off + o * o), ldc=o))
+            flops += float(o) * o * 16
+            off += padded[ngemm + ti]
+            ti += 1
+    return buf, ops, flops
+
+
+def fill_batched(buf, ops, seed):
+    """uniform[-1,1] everywhere, then triangles get diagonal uniform[1,2]."""
+    import torch
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    buf.uniform_(-1.0, 1.0, generator=gen)
+    base = buf.data_ptr()
+    for op in ops:
+        if op.kind == 2:
+            o = op.m
+            start = (op.A - base) // 8
+            tri = buf[start: start + o * o].view(o, o)
+            tri.diagonal().uniform_(1.0, 2.0, generator=gen)
+    torch.cuda.synchronize()
+
+
+def run_batched(args):
+    import torch
+    import libgpublas_gb300 as g
+    from libgpublas_gb300 import build
+    build.build_library()
+    ngemm = args.n or 20000
+    ntrsm = ngemm // 4
+    dev = g.Device(0)
+    buf, ops, flops = build_batched(ngemm, ntrsm, 3,
+                                    lambda n: torch.empty(n, dtype=torch.float64, device="cuda"))
+    fill_batched(buf, ops, 3)
+    arr = (g.GbxOp * len(ops))(*ops)
+    stream = torch.cuda.ExternalStream(dev.stream())
+    plan = dev.plan_create(ops)             # autotunes unseen size buckets once
+    items, _ = dev.plan_info(plan)
+
+    def timed(fn, steps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            fn()
+        ev1.record(stream)
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) / 1e3 / steps
+
+    for _ in range(args.warmup):
+        dev.plan_launch(plan, graph=True)
+    dev.sync()
+    l0 = dev.launches()
+    with ClockSampler(0) as clk:
+        t_group = timed(lambda: dev.plan_launch(plan, graph=True), args.steps)
+    launches = dev.launches() - l0
+    dev.sync()
+    dev.ops_run(arr, len(ops))              # warm the per-call path
+    dev.sync()
+    t_call = timed(lambda: dev.ops_run(arr, len(ops)), max(1, min(args.steps, 3)))
+    dev.plan_destroy(plan)
+    peak = dev.fp64_peak()
+    value = flops / t_group / 1e12
+    line = {"metric": "batched_tflops", "value": value, "unit": "TFLOP/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_group * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"grouped_{ngemm}dgemm_{ntrsm}dtrsm",
+                       "gemm": "M, N, K log-uniform [8, 512], NN, alpha 1, beta 0.5",
+                       "trsm": "LLNN, order log-uniform [8, 256], diag uniform[1,2], 16 rhs",
+                       "inputs": "uniform[-1,1] (torch device generator, seed 3)",
+                       "execution": "one persistent grouped kernel replayed from a CUDA graph",
+                       "work_items": items, "flops_per_step": flops},
+            "gpu_launches": int(launches), "clocks": clk.summary(),
+            "calls_per_s": len(ops) / t_group,
+            "per_call": {"value": flops / t_call / 1e12, "unit": "TFLOP/s",
+                         "calls_per_s": len(ops) / t_call, "ms_per_step": t_call * 1e3,
+                         "execution": "one launch per call through gbx_dgemm / gbx_dtrsm"},
+            "speedup_vs_per_call": t_call / t_group,
+            "roofline": {"bound": "fp64", "kernel": "grouped_kernel", "achieved": value,
+                         "peak": peak, "unit": "TFLOP/s", "frac": value / peak,
+                         "peak_source": "measured in this run (gbx_diag_fp64_peak)",
+                         "traffic": None},
+            "e2e": {"unavailable": "operands are device-resident by design of this workload"}}
+    print(json.dumps(line), flush=True)
+    dev.close()
+
+
+# --------------------------------------------------------------------------
+# serving trace: 16 host threads each factorise A = G G^T + n I (blocked
+# right-looking Cholesky, n log-uniform in [1024, 16384], nb in {128, 256});
+# the calls are dpotrf (diagonal block), dtrsm (panel), dsyrk (diagonal
+# block of the trailing update), dgemm (rest of the trailing update), then
+# ddot residual checks on sampled entries.  Plain per-call dispatch (every
+# thread calls the library on its own stream and waits) against the serving
+# loop (every thread submits to one server and waits).
+# --------------------------------------------------------------------------
+def cholesky_calls(n, nb, base, lda, info_ptr, ozaki=False):
+    import libgpublas_gb300 as g
+    calls = []
+    at = lambda i, j: base + 8 * (j * lda + i)   # noqa: E731
+    for k in range(0, n, nb):
+        kb = min(nb, n - k)
+        calls.append(g.GbxOp(kind=6, uplo=b"L", n=kb, C=at(k, k), ldc=lda, B=info_ptr))
+        rest = n - k - kb
+        if rest <= 0:
+            continue
+        # L21 = A21 L11^-T
+        calls.append(g.GbxOp(kind=2, side=b"R", uplo=b"L", transa=b"T", diag=b"N", m=rest, n=kb,
+                             alpha=1.0, A=at(k, k), lda=lda, C=at(k + kb, k), ldc=lda))
+        # trailing update, block column by block column
+        for j in range(k + kb, n, nb):
+            jb = min(nb, n - j)
+            calls.append(g.GbxOp(kind=8 if ozaki else 3, uplo=b"L", transa=b"N", n=jb, k=kb,
+                                 alpha=-1.0, beta=1.0, A=at(j, k), lda=lda, C=at(j, j), ldc=lda))
+            below = n - j - jb
+            if below > 0:
+                calls.append(g.GbxOp(kind=7 if ozaki else 1, transa=b"N", transb=b"T", m=below, n=jb,
+                                     k=kb, alpha=-1.0, beta=1.0, A=at(j + jb, k), lda=lda,
+                                     B=at(j, k), ldb=lda, C=at(j + jb, j), ldc=lda))
+    return calls
+
+
+def run_serving(args):
+    import threading
+    import torch
+    import libgpublas_gb300 as g
+    from libgpublas_gb300 import build
+    build.build_library()
+    nthreads = 16
+    rng = np.random.default_rng(5)
+    nmax = args.n or 16384
+    sizes = [int(v) for v in loguni(rng, 1024, nmax, nthreads)]
+    nbs = [int(v) for v in rng.choice([128, 256], nthreads)]
+    dev = g.Device(0)
+    mats, origs = [], []
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(5)
+    for n in sizes:
+        G = torch.empty(n * n, dtype=torch.float64, device="cuda").uniform_(-1.0, 1.0, generator=gen)
+        A = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        # A = G G^T + n I, both triangles (setup, on the Ozaki path)
+        dev.dgemm_ozaki("N", "T", n, n, n, 1.0, G, n, G, n, 0.0, A, n)
+        A.view(n, n).diagonal().add_(float(n))
+        dev.sync()
+        del G
+        origs.append(A)
+    info = torch.zeros(nthreads, dtype=torch.int32, device="cuda")
+    results = {}
+
+    def run_mode(mode):
+        server = g.Server(0, slots=8) if mode != "plain" else None
+        work = [o.clone() for o in origs]
+        torch.cuda.synchronize()
+        lat, ncalls, errs = [], [0], []
+        lock = threading.Lock()
+
+        def worker(t):
+            A = work[t]
+            calls = cholesky_calls(sizes[t], nbs[t], A.data_ptr(), sizes[t], info.data_ptr() + 4 * t,
+                                   ozaki=(mode == "ozaki"))
+            local = []
+            if server is None:
+                d = g.Device(0)
+                for op in calls:
+                    t0 = time.perf_counter()
+                    st = d.L.gbx_ops_run(d.ctx, ctypes_ref(op), 1)
+                    st2 = d.L.gbx_ctx_sync(d.ctx)
+                    local.append((time.perf_counter() - t0) * 1e6)
+                    if st or st2:
+                        errs.append((t, st, st2))
+                        break
+                d.close()
+            else:
+                for op in calls:
+                    st, us = server.call(op)
+                    local.append(us)
+                    if st:
+                        errs.append((t, st))
+                        break
+            with lock:
+                lat.extend(local)
+                ncalls[0] += len(local)
+
+        threads = [threading.Thread(target=worker, args=(t,)) for t in range(nthreads)]
+        t0 = time.perf_counter()
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        wall = time.perf_counter() - t0
+        srv_stats = server.stats() if server else None
+        if server:
+            server.close()
+        # residual on sampled entries: (L L^T)_ij through ddot on rows of L
+        res_num = res_den = 0.0
+        d = g.Device(0)
+        out = torch.zeros(1, dtype=torch.float64, device="cuda")
+        srng = np.random.default_rng(9)
+        for t in range(nthreads):
+            n = sizes[t]
+            L = work[t]
+            for _ in range(8):
+                i, j = sorted(int(v) for v in srng.integers(0, n, 2))[::-1]   # i >= j
+                d.ddot(j + 1, L.data_ptr() + 8 * i, n, L.data_ptr() + 8 * j, n, out)
+                d.sync()
+                aij = float(origs[t][j * n + i].item())
+                res_num += (out.item() - aij) ** 2
+                res_den += aij ** 2
+        d.close()
+        lat.sort()
+        flops = sum(float(n) ** 3 / 3 for n in sizes)
+        results[mode] = {"calls": ncalls[0], "wall_s": wall, "calls_per_s": ncalls[0] / wall,
+                         "p50_us": lat[len(lat) // 2] if lat else None,
+                         "p99_us": lat[int(0.99 * (len(lat) - 1))] if lat else None,
+                         "tflops": flops / wall / 1e12,
+                         "residual_sampled": (res_num / res_den) ** 0.5 if res_den else None,
+                         "info_nonzero": int((info != 0).sum().item()), "errors": errs[:4],
+                         "server": srv_stats}
+        del work
+        torch.cuda.synchronize()
+
+    for mode in ("plain", "served", "ozaki"):
+        info.zero_()
+        run_mode(mode)
+    line = {"metric": "serving_calls_per_s", "value": results["served"]["calls_per_s"],
+            "unit": "calls/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": results["served"]["wall_s"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "cholesky_trace_16threads", "n": sizes, "nb": nbs,
+                       "matrix": "A = G G^T + n I, G uniform[-1,1] (device generator, seed 5)",
+                       "calls": "dpotrf(diag) dtrsm dsyrk dgemm + ddot residual checks"},
+            "modes": results,
+            "speedup_vs_plain_dispatch": results["served"]["calls_per_s"] / results["plain"]["calls_per_s"],
+            "e2e": {"unavailable": "operands are device-resident by design of this workload"}}
+    print(json.dumps(line), flush=True)
+    dev.close()
+
+
+def ctypes_ref(op):
+    import ctypes
+    return ctypes.byref(op)
+
+
 def main():
     args = parse_args()
+    if args.workload == "batched":
+        return run_batched(args) if args.impl == "ours" else print(json.dumps(
+            {"impl": "reference", "unavailable": "the reference has no grouped execution; "
+                                                 "the CPU BLAS runs one call at a time"}))
+    if args.workload == "serving":
+        return run_serving(args) if args.impl == "ours" else print(json.dumps(
+            {"impl": "reference", "unavailable": "the reference has no serving loop"}))
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -148,6 +148,12 @@ gbx_status gbx_dtrmm(gbx_ctx *ctx, char side, char uplo, char transa, char diag,
                      int m, int n, double alpha, const double *A, int lda,
                      double *B, int ldb);
 
+/* Cholesky of one small diagonal block, lower, n <= 256, in place; *info (a
+ * device int) is 0 or the 1-based column of a non-positive pivot.  Not a
+ * BLAS routine (no reference counterpart): the diagonal step of the blocked
+ * Cholesky that drives the serving trace. */
+gbx_status gbx_dpotrf_small(gbx_ctx *ctx, char uplo, int n, double *A, int lda, int *info);
+
 /* ---- Ozaki split-precision products (opt-in; no reference counterpart) ----
  * FP64 results from exact low-precision tensor-core products of integer
  * slices, recombined in FP64.  tol is the target relative Frobenius error
@@ -181,7 +187,11 @@ enum {
     GBX_OP_SYRK = 3, /* serving loop: uplo, transa as trans, n, k, A, beta, C   */
     GBX_OP_DOT = 4,  /* serving loop: n, x = A (incx = lda), y = B (incy = ldb),
                         result in device memory at C                           */
-    GBX_OP_NRM2 = 5  /* serving loop: n, x = A (incx = lda), result at C        */
+    GBX_OP_NRM2 = 5, /* serving loop: n, x = A (incx = lda), result at C        */
+    GBX_OP_POTRF = 6,      /* serving loop: lower Cholesky of the n x n block at
+                              C (ldc), n <= 256; int info at (int *)B          */
+    GBX_OP_GEMM_OZAKI = 7, /* serving loop: DGEMM through the Ozaki path       */
+    GBX_OP_SYRK_OZAKI = 8  /* serving loop: DSYRK through the Ozaki path       */
 };
 typedef struct {
     int kind;                 /* GBX_OP_GEMM or GBX_OP_TRSM                     */
@@ -199,6 +209,10 @@ gbx_status gbx_plan_launch(gbx_ctx *ctx, gbx_plan *plan);
 gbx_status gbx_plan_graph_launch(gbx_ctx *ctx, gbx_plan *plan);
 gbx_status gbx_plan_destroy(gbx_plan *plan);
 gbx_status gbx_plan_info(const gbx_plan *plan, int *work_items, double *flops);
+/* The same operations issued one call each through the regular routines
+ * (gbx_dgemm, gbx_dtrsm, ...) on the context's stream: the per-call
+ * baseline the grouped kernel is measured against. */
+gbx_status gbx_ops_run(gbx_ctx *ctx, const gbx_op *ops, int count);
 
 /* ---- serving loop (no reference counterpart: the reference serves one call
  * at a time on one cuBLAS handle, runtime-blas.c:14-23) -------------------

@@ -111,6 +111,8 @@ def _declare(L):
     L.gbx_plan_graph_launch.argtypes = [_P, _P]
     L.gbx_plan_destroy.argtypes = [_P]
     L.gbx_plan_info.argtypes = [_P, C.POINTER(_I), C.POINTER(_D)]
+    L.gbx_ops_run.argtypes = [_P, _P, _I]
+    L.gbx_dpotrf_small.argtypes = [_P, _CH, _I, _P, _I, _P]
     L.gbx_server_create.argtypes = [_I, _I, C.c_size_t, C.POINTER(_P)]
     L.gbx_server_submit.argtypes = [_P, _P, C.POINTER(C.c_uint64)]
     L.gbx_server_wait.argtypes = [_P, C.c_uint64, C.POINTER(_D)]
@@ -354,6 +356,13 @@ class Device:
     def plan_launch(self, plan, graph=False):
         f = self.L.gbx_plan_graph_launch if graph else self.L.gbx_plan_launch
         self._ok(f(self.ctx, plan), "plan_launch")
+
+    def ops_run(self, ops_array, count):
+        """Issue each operation alone through the regular routines."""
+        self._ok(self.L.gbx_ops_run(self.ctx, ops_array, count), "ops_run")
+
+    def dpotrf_small(self, n, a, lda, info):
+        self._ok(self.L.gbx_dpotrf_small(self.ctx, b"L", n, _dp(a), lda, _dp(info)), "dpotrf_small")
 
     def plan_destroy(self, plan):
         self.L.gbx_plan_destroy(plan)

@@ -158,9 +158,17 @@ __device__ __forceinline__ void blue_acc(double v, double &asml, double &amed, d
     constexpr unsigned long long kSml = (unsigned long long)(1023 - 511) << 52;   // bits of tsml
     constexpr unsigned long long kInf = 0x7FF0000000000000ull;
     const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    if (b > kBig && b <= kInf) { const double t = fabs(v) * Blue::sbig; abig = fma(t, t, abig); }
-    else if (b < kSml) { const double t = fabs(v) * Blue::ssml; asml = fma(t, t, asml); }
-    else amed = fma(v, v, amed);   // also takes NaN, which then propagates
+    const bool big = b > kBig && b <= kInf, sml = b < kSml && b != 0ull;   // zeros add nothing
+    // Warp-uniform fast path: when no lane holds an out-of-range element the
+    // warp executes the single DFMA only (a predicated if-conversion of the
+    // three branches would issue all three FP64 sequences for every element).
+    if (!__any_sync(__activemask(), big || sml)) {
+        amed = fma(v, v, amed);   // also takes NaN, which then propagates
+        return;
+    }
+    if (big) { const double t = fabs(v) * Blue::sbig; abig = fma(t, t, abig); }
+    else if (sml) { const double t = fabs(v) * Blue::ssml; asml = fma(t, t, asml); }
+    else amed = fma(v, v, amed);
 }
 
 static __global__ void __launch_bounds__(L1_THREADS)
@@ -306,13 +314,24 @@ iamax_partial(int n, const double *__restrict__ x, int incx, unsigned long long 
             double2 v[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) v[u] = ldg2(x2 + i + u * stride);
+            // pairwise tree over the 8 elements (short dependency chains),
+            // then one merge into the running best; ties resolve to the
+            // smaller index at every level
+            unsigned long long k[8];
+            long long e[8];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const long long e = 2 * (i + u * stride);
-                const unsigned long long k0 = amax_key<IS_MIN>(v[u].x), k1 = amax_key<IS_MIN>(v[u].y);
-                if (better(k0, e, bk, bi)) { bk = k0; bi = e; }
-                if (better(k1, e + 1, bk, bi)) { bk = k1; bi = e + 1; }
+                k[2 * u] = amax_key<IS_MIN>(v[u].x);
+                k[2 * u + 1] = amax_key<IS_MIN>(v[u].y);
+                e[2 * u] = 2 * (i + u * stride);
+                e[2 * u + 1] = e[2 * u] + 1;
             }
+#pragma unroll
+            for (int w = 1; w < 8; w *= 2)
+#pragma unroll
+                for (int a = 0; a < 8; a += 2 * w)
+                    if (better(k[a + w], e[a + w], k[a], e[a])) { k[a] = k[a + w]; e[a] = e[a + w]; }
+            if (better(k[0], e[0], bk, bi)) { bk = k[0]; bi = e[0]; }
         }
         for (; i < n2; i += stride) {
             double2 v = ldg2(x2 + i);

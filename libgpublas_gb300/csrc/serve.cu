@@ -97,10 +97,32 @@ gbx_status run_request(gbx_ctx *ctx, const gbx_op &o)
         return gbx_ddot(ctx, o.n, o.A, o.lda, o.B, o.ldb, o.C);
     case GBX_OP_NRM2:
         return gbx_dnrm2(ctx, o.n, o.A, o.lda, o.C);
+    case GBX_OP_POTRF:
+        return gbx_dpotrf_small(ctx, o.uplo, o.n, o.C, o.ldc, (int *)o.B);
+    case GBX_OP_GEMM_OZAKI:
+        return gbx_dgemm_ozaki(ctx, o.transa, o.transb, o.m, o.n, o.k, o.alpha, o.A, o.lda, o.B, o.ldb,
+                               o.beta, o.C, o.ldc, 0.0, 0, nullptr);
+    case GBX_OP_SYRK_OZAKI:
+        return gbx_dsyrk_ozaki(ctx, o.uplo, o.transa, o.n, o.k, o.alpha, o.A, o.lda, o.beta, o.C, o.ldc, 0.0, 0,
+                               nullptr);
     default:
         return GBX_ERR_ARG;
     }
 }
+
+}  // namespace
+
+extern "C" gbx_status gbx_ops_run(gbx_ctx *ctx, const gbx_op *ops, int count)
+{
+    if (!ctx || count < 0 || (count > 0 && !ops)) return GBX_ERR_ARG;
+    for (int i = 0; i < count; i++) {
+        gbx_status st = run_request(ctx, ops[i]);
+        if (st != GBX_OK) return st;
+    }
+    return GBX_OK;
+}
+
+namespace {
 
 void dispatcher_loop(gbx_server *s)
 {
