@@ -20,6 +20,7 @@
 #include "gbx_internal.h"
 #include "../../include/gbxblas_f77.h"
 
+#include <pthread.h>
 #include <stdatomic.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -75,6 +76,37 @@ static gbx_ctx *ctx_or_report(const char *name)
         if (st != GBX_OK) goto fail;              \
     } while (0)
 
+/* ---- serve=on: Level-3 calls go through one process-wide serving loop ----
+ * Calls from many application threads are then batched together on the GPU
+ * (small ones into one grouped kernel).  Staging memory is reserved against
+ * the server's budget before operands are placed (admission by free HBM) and
+ * given back when the call returns. */
+static gbx_server *g_srv;
+static pthread_once_t g_srv_once = PTHREAD_ONCE_INIT;
+
+static void srv_init(void)
+{
+    int dev = 0;
+    const char *d = getenv("GBX_DEVICE");
+    if (d) dev = atoi(d);
+    if (gbx_server_create(dev, 8, 0, &g_srv) != GBX_OK) g_srv = NULL;
+}
+
+static gbx_server *server(void)
+{
+    if (!gbx_get_config()->serve) return NULL;
+    pthread_once(&g_srv_once, srv_init);
+    return g_srv;
+}
+
+/* The staged operands were copied on the calling thread's stream. */
+static gbx_status served(gbx_ctx *ctx, gbx_server *srv, const gbx_op *op)
+{
+    gbx_status st = gbx_ctx_sync(ctx);
+    if (st != GBX_OK) return st;
+    return gbx_server_call(srv, op, NULL);
+}
+
 /* ---------------------------------------------------------------- DGEMM */
 void dgemm_(const char *transa, const char *transb, const int *m, const int *n, const int *k,
             const double *alpha, const double *a, const int *lda, const double *b, const int *ldb,
@@ -88,6 +120,9 @@ void dgemm_(const char *transa, const char *transb, const int *m, const int *n, 
     gbx_status st;
     const int nota = gbx_lsame(*transa, 'N'), notb = gbx_lsame(*transb, 'N');
     const int work = !(*alpha == 0.0 || *k == 0);
+    gbx_server *srv = server();
+    const size_t bytes = 8 * ((size_t)*m * *k + (size_t)*k * *n + (size_t)*m * *n);
+    if (srv && (st = gbx_server_admit(srv, bytes)) != GBX_OK) { report("DGEMM", ctx, st); return; }
     /* operands left unplaced on quick paths keep the caller's (valid) ld */
     gbx_operand oa = {.ld = *lda}, ob = {.ld = *ldb}, oc = {0};
     if (work) {
@@ -96,16 +131,26 @@ void dgemm_(const char *transa, const char *transb, const int *m, const int *n, 
     }
     TRY(gbx_place_in(ctx, GBX_WS_STAGE_C, c, *m, *n, *ldc, 8, *beta != 0.0, &oc));
     const gbx_config *cfg = gbx_get_config();
-    if (work && cfg->precision_ozaki)
+    if (srv) {
+        gbx_op op = {0};
+        op.kind = (work && cfg->precision_ozaki) ? GBX_OP_GEMM_OZAKI : GBX_OP_GEMM;
+        op.transa = *transa; op.transb = *transb;
+        op.m = *m; op.n = *n; op.k = *k; op.alpha = *alpha; op.beta = *beta;
+        op.A = oa.dev; op.lda = oa.ld; op.B = ob.dev; op.ldb = ob.ld; op.C = oc.dev; op.ldc = oc.ld;
+        TRY(served(ctx, srv, &op));
+    } else if (work && cfg->precision_ozaki) {
         TRY(gbx_dgemm_ozaki(ctx, *transa, *transb, *m, *n, *k, *alpha, oa.dev, oa.ld, ob.dev, ob.ld,
                             *beta, oc.dev, oc.ld, cfg->ozaki_tol, 0, NULL));
-    else
+    } else {
         TRY(gbx_dgemm(ctx, *transa, *transb, *m, *n, *k, *alpha, oa.dev, oa.ld, ob.dev, ob.ld,
                       *beta, oc.dev, oc.ld));
+    }
     TRY(gbx_place_out(ctx, &oc, *m, *n, 8));
     TRY(gbx_ctx_sync(ctx));
+    if (srv) gbx_server_release(srv, bytes);
     return;
 fail:
+    if (srv) gbx_server_release(srv, bytes);
     report("DGEMM", ctx, st);
 }
 
@@ -158,21 +203,33 @@ void dsyrk_(const char *uplo, const char *trans, const int *n, const int *k, con
     gbx_status st;
     const int notr = gbx_lsame(*trans, 'N');
     const int work = !(*alpha == 0.0 || *k == 0);
+    gbx_server *srv = server();
+    const size_t bytes = 8 * ((size_t)*n * *k + (size_t)*n * *n);
+    if (srv && (st = gbx_server_admit(srv, bytes)) != GBX_OK) { report("DSYRK", ctx, st); return; }
     gbx_operand oa = {.ld = *lda}, oc = {0};
     if (work)
         TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, notr ? *n : *k, notr ? *k : *n, *lda, 8, 1, &oa));
     /* the other triangle of C must survive the round trip: always copy in */
     TRY(gbx_place_in(ctx, GBX_WS_STAGE_C, c, *n, *n, *ldc, 8, 1, &oc));
     const gbx_config *cfg = gbx_get_config();
-    if (work && cfg->precision_ozaki)
+    if (srv) {
+        gbx_op op = {0};
+        op.kind = (work && cfg->precision_ozaki) ? GBX_OP_SYRK_OZAKI : GBX_OP_SYRK;
+        op.uplo = *uplo; op.transa = *trans; op.n = *n; op.k = *k; op.alpha = *alpha; op.beta = *beta;
+        op.A = oa.dev; op.lda = oa.ld; op.C = oc.dev; op.ldc = oc.ld;
+        TRY(served(ctx, srv, &op));
+    } else if (work && cfg->precision_ozaki) {
         TRY(gbx_dsyrk_ozaki(ctx, *uplo, *trans, *n, *k, *alpha, oa.dev, oa.ld, *beta, oc.dev, oc.ld,
                             cfg->ozaki_tol, 0, NULL));
-    else
+    } else {
         TRY(gbx_dsyrk(ctx, *uplo, *trans, *n, *k, *alpha, oa.dev, oa.ld, *beta, oc.dev, oc.ld));
+    }
     TRY(gbx_place_out(ctx, &oc, *n, *n, 8));
     TRY(gbx_ctx_sync(ctx));
+    if (srv) gbx_server_release(srv, bytes);
     return;
 fail:
+    if (srv) gbx_server_release(srv, bytes);
     report("DSYRK", ctx, st);
 }
 
@@ -191,14 +248,28 @@ static void trxm(const char *name, trxm_fn fn, const char *side, const char *upl
     if (!ctx) return;
     gbx_status st;
     const int na = gbx_lsame(*side, 'L') ? *m : *n;
+    gbx_server *srv = fn == gbx_dtrsm ? server() : NULL;   /* DTRMM runs directly */
+    const size_t bytes = 8 * ((size_t)na * na + (size_t)*m * *n);
+    if (srv && (st = gbx_server_admit(srv, bytes)) != GBX_OK) { report(name, ctx, st); return; }
     gbx_operand oa = {.ld = *lda}, ob = {0};
     if (*alpha != 0.0) TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, na, na, *lda, 8, 1, &oa));
     TRY(gbx_place_in(ctx, GBX_WS_STAGE_B, b, *m, *n, *ldb, 8, *alpha != 0.0, &ob));
-    TRY(fn(ctx, *side, *uplo, *transa, *diag, *m, *n, *alpha, oa.dev, oa.ld, ob.dev, ob.ld));
+    if (srv) {
+        gbx_op op = {0};
+        op.kind = GBX_OP_TRSM;
+        op.side = *side; op.uplo = *uplo; op.transa = *transa; op.diag = *diag;
+        op.m = *m; op.n = *n; op.alpha = *alpha;
+        op.A = oa.dev; op.lda = oa.ld; op.C = ob.dev; op.ldc = ob.ld;
+        TRY(served(ctx, srv, &op));
+    } else {
+        TRY(fn(ctx, *side, *uplo, *transa, *diag, *m, *n, *alpha, oa.dev, oa.ld, ob.dev, ob.ld));
+    }
     TRY(gbx_place_out(ctx, &ob, *m, *n, 8));
     TRY(gbx_ctx_sync(ctx));
+    if (srv) gbx_server_release(srv, bytes);
     return;
 fail:
+    if (srv) gbx_server_release(srv, bytes);
     report(name, ctx, st);
 }
 

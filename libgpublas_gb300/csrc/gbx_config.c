@@ -20,7 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-static gbx_config g_cfg = {0, 1e-14, 1, 1, 0, 0, 0, {0}, {0}};
+static gbx_config g_cfg = {0, 1e-14, 1, 1, 0, 0, 0, {0}, {0}, 0};
 static pthread_once_t g_once = PTHREAD_ONCE_INIT;
 
 static void print_help(void)
@@ -35,6 +35,7 @@ static void print_help(void)
           "   precision=fp64|ozaki[:t]  -- FP64 or Ozaki split products (target error t)\n"
           "   prefetch=on|off           -- prefetch managed operands to the GPU\n"
           "   errors=abort|return       -- behaviour on a device failure\n"
+          "   serve=on|off              -- route Level-3 calls through the serving loop\n"
           "   managed_min=<bytes>       -- smaller allocations stay on the host\n"
           "   statistics[=<file>]       -- write call/placement counters at exit\n",
           stderr);
@@ -83,6 +84,8 @@ static void parse(void)
             } else {
                 fprintf(stderr, "gbxblas: unknown precision '%s'\n", p);
             }
+        } else if (strncmp(opt, "serve=", 6) == 0) {
+            g_cfg.serve = strcmp(opt + 6, "on") == 0;
         } else if (strncmp(opt, "prefetch=", 9) == 0) {
             g_cfg.prefetch = strcmp(opt + 9, "off") != 0;
         } else if (strncmp(opt, "errors=", 7) == 0) {

@@ -88,6 +88,7 @@ typedef struct {
     size_t managed_min;      /* managed_min=<bytes>: smaller objects stay host  */
     char   oracle_file[1024];/* heuristic=oracle:<file>                          */
     char   stats_file[1024]; /* statistics[=<file>] written at exit              */
+    int    serve;            /* serve=on: Fortran calls go through the server    */
 } gbx_config;
 const gbx_config *gbx_get_config(void);
 

@@ -197,3 +197,41 @@ def test_memory_admission(lib):
         assert s.stats()["admission_waits"] >= 1
     finally:
         s.close()
+
+
+def test_fortran_calls_through_the_serving_loop(orc):
+    # BLAS2CUDA_OPTIONS=serve=on: dgemm_/dtrsm_/dsyrk_ from 8 threads on host
+    # operands go through one serving loop; results match the oracle.
+    import os
+    import subprocess
+    import sys
+    import textwrap
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = textwrap.dedent("""
+        import threading, numpy as np, oracle, libgpublas_gb300 as g
+        orc = oracle.get(); f = g.F77(); errs = []
+        def work(t):
+            try:
+                m, n, k = 100 + 37 * t, 90 + 11 * t, 120
+                a, s = orc.matrix(m, k, t); b, s = orc.matrix(k, n, s); c, s = orc.matrix(m, n, s)
+                want = orc.dgemm_dd('N', 'N', m, n, k, 1.0, a, b, 0.5, c)
+                got = c.copy(order='F'); f.dgemm('N', 'N', m, n, k, 1.0, a, m, b, k, 0.5, got, m)
+                assert np.linalg.norm(got - want) <= 1e-13 * np.linalg.norm(want)
+                tri, s = orc.trsm_matrix(m, s + 1); rhs, s = orc.matrix(m, 16, s)
+                x = rhs.copy(order='F'); f.dtrsm('L', 'L', 'N', 'N', m, 16, 1.0, tri, m, x, m)
+                assert orc.dtrsm_residual('L', 'L', 'N', 'N', m, 16, 1.0, tri, rhs, x) <= 1e-14
+                cs, s = orc.matrix(m, m, s); want = cs.copy(order='F')
+                orc.dsyrk('L', 'N', m, k, -1.0, a, 1.0, want)
+                gs = cs.copy(order='F'); f.dsyrk('L', 'N', m, k, -1.0, a, m, 1.0, gs, m)
+                assert np.linalg.norm(np.tril(gs - want)) <= 1e-13 * np.linalg.norm(np.tril(want))
+            except Exception as e:
+                errs.append(repr(e))
+        th = [threading.Thread(target=work, args=(t,)) for t in range(8)]
+        [x.start() for x in th]; [x.join() for x in th]
+        print('ERRS', errs)
+    """)
+    env = dict(os.environ, PYTHONPATH=root, BLAS2CUDA_OPTIONS="serve=on;errors=return")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, cwd=root,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "ERRS []" in r.stdout, r.stdout + r.stderr[-2000:]
