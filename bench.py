@@ -50,7 +50,7 @@ CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.a
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 WORKLOADS = ("dgemm", "ozaki", "daxpy", "ddot", "dnrm2", "idamax", "dgemv", "dtrsm", "dsyrk",
-             "batched", "serving")
+             "batched", "serving", "ozaki_sweep")
 
 
 def parse_args():
@@ -819,6 +819,91 @@ def run_serving(args):
     dev.close()
 
 
+# --------------------------------------------------------------------------
+# Ozaki configuration: DGEMM and ZGEMM at n in {4096, 8192, 16384}, entries
+# u * 2^e (u uniform[-1,1], e uniform integer in [-s, s]) for s in {0, 8, 24};
+# ZGEMM real and imaginary parts drawn independently the same way.  Reports
+# TFLOP/s (2n^3 real, 8n^3 complex), the slice count chosen for 1e-14 and
+# the relative Frobenius error against the double-double oracle on sampled
+# entries.
+# --------------------------------------------------------------------------
+def run_ozaki_sweep(args):
+    import torch
+    import libgpublas_gb300 as g
+    import oracle
+    from libgpublas_gb300 import build
+    build.build_library()
+    orc = oracle.get()
+    dev = g.Device(0)
+    stream = torch.cuda.ExternalStream(dev.stream())
+    sizes = [args.n] if args.n else [4096, 8192, 16384]
+    rows_out = []
+    for n in sizes:
+        for s in (0, 8, 24):
+            st = 1000 + n + s
+            a, st = orc.spread((n, n), s, st)
+            b, st = orc.spread((n, n), s, st)
+            da = torch.from_numpy(a.ravel(order="F")).cuda()
+            db = torch.from_numpy(b.ravel(order="F")).cuda()
+            dc = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+            used = dev.dgemm_ozaki("N", "N", n, n, n, 1.0, da, n, db, n, 0.0, dc, n)
+            dev.sync()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            for _ in range(args.steps):
+                dev.dgemm_ozaki("N", "N", n, n, n, 1.0, da, n, db, n, 0.0, dc, n)
+            ev1.record(stream)
+            ev1.synchronize()
+            t = ev0.elapsed_time(ev1) / 1e3 / args.steps
+            got = dc.cpu().numpy().reshape(n, n, order="F")
+            rng = np.random.default_rng(n + s)
+            ri, ci = rng.integers(0, n, 1024), rng.integers(0, n, 1024)
+            ref = orc.dgemm_dd_sample("N", "N", n, 1.0, a, b, 0.0, np.zeros((1, 1), order="F"), ri, ci)
+            err = float(np.linalg.norm(got[ri, ci] - ref) / np.linalg.norm(ref))
+            rows_out.append({"routine": "dgemm", "n": n, "spread": s, "slices": used,
+                             "tflops": 2.0 * n ** 3 / t / 1e12, "ms": t * 1e3, "rel_err": err})
+            del da, db, dc
+            # ZGEMM: independent real and imaginary parts, same distribution
+            ai, st = orc.spread((n, n), s, st)
+            bi, st = orc.spread((n, n), s, st)
+            za = np.empty((n, n), dtype=np.complex128, order="F")
+            za.real, za.imag = a, ai
+            zb = np.empty((n, n), dtype=np.complex128, order="F")
+            zb.real, zb.imag = b, bi
+            del ai, bi
+            dza = torch.from_numpy(za.ravel(order="F").view(np.float64)).cuda()
+            dzb = torch.from_numpy(zb.ravel(order="F").view(np.float64)).cuda()
+            dzc = torch.zeros(2 * n * n, dtype=torch.float64, device="cuda")
+            used = dev.zgemm_ozaki("N", "N", n, n, n, 1.0, dza, n, dzb, n, 0.0, dzc, n)
+            dev.sync()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                dev.zgemm_ozaki("N", "N", n, n, n, 1.0, dza, n, dzb, n, 0.0, dzc, n)
+            ev1.record(stream)
+            ev1.synchronize()
+            t = ev0.elapsed_time(ev1) / 1e3 / args.steps
+            zgot = dzc.cpu().numpy().view(np.complex128).reshape(n, n, order="F")
+            zref = orc.zgemm_dd_sample("N", "N", n, 1.0, za, zb, 0.0,
+                                       np.zeros((1, 1), dtype=np.complex128, order="F"), ri, ci)
+            err = float(np.linalg.norm(zgot[ri, ci] - zref) / np.linalg.norm(zref))
+            rows_out.append({"routine": "zgemm", "n": n, "spread": s, "slices": used,
+                             "tflops": 8.0 * n ** 3 / t / 1e12, "ms": t * 1e3, "rel_err": err})
+            del dza, dzb, dzc, za, zb, a, b
+            torch.cuda.empty_cache()
+            print(json.dumps(rows_out[-2]), json.dumps(rows_out[-1]), file=sys.stderr, flush=True)
+    head = next(r for r in rows_out if r["routine"] == "dgemm" and r["n"] == max(sizes) and r["spread"] == 0)
+    line = {"metric": "ozaki_dgemm_tflops", "value": head["tflops"], "unit": "TFLOP/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": 1, "ms_per_step": head["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"ozaki_sweep_dgemm_zgemm_n{'_'.join(map(str, sizes))}",
+                       "inputs": "u * 2^e, u uniform[-1,1], e uniform in [-s, s], SplitMix64",
+                       "tol": 1e-14, "value_is": f"DGEMM n={max(sizes)} s=0"},
+            "sweep": rows_out,
+            "e2e": {"unavailable": "device-resident sweep; see the dgemm workload for e2e"}}
+    print(json.dumps(line), flush=True)
+    dev.close()
+
+
 def ctypes_ref(op):
     import ctypes
     return ctypes.byref(op)
@@ -833,6 +918,9 @@ def main():
     if args.workload == "serving":
         return run_serving(args) if args.impl == "ours" else print(json.dumps(
             {"impl": "reference", "unavailable": "the reference has no serving loop"}))
+    if args.workload == "ozaki_sweep":
+        return run_ozaki_sweep(args) if args.impl == "ours" else print(json.dumps(
+            {"impl": "reference", "unavailable": "the reference has no Ozaki path"}))
     if args.impl == "reference":
         run_reference(args)
     else:

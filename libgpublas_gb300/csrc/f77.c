@@ -62,6 +62,12 @@ static void report(const char *name, gbx_ctx *ctx, gbx_status st)
     if (gbx_get_config()->abort_on_error) abort();
 }
 
+/* trace=<file> (preload library): name every operand object of the call */
+#define NOTE(fun, p)                                 \
+    do {                                             \
+        if (gbx_tracker_note) gbx_tracker_note(fun, p); \
+    } while (0)
+
 static gbx_ctx *ctx_or_report(const char *name)
 {
     gbx_ctx *ctx = gbx_thread_ctx();
@@ -114,6 +120,7 @@ void dgemm_(const char *transa, const char *transb, const int *m, const int *n, 
 {
     int info = gbx_check_gemm_args(*transa, *transb, *m, *n, *k, *lda, *ldb, *ldc);
     if (info) { xerbla_("DGEMM ", &info, 6); return; }
+    NOTE("dgemm_", a); NOTE("dgemm_", b); NOTE("dgemm_", c);
     if (*m == 0 || *n == 0 || ((*alpha == 0.0 || *k == 0) && *beta == 1.0)) return;
     gbx_ctx *ctx = ctx_or_report("DGEMM");
     if (!ctx) return;
@@ -161,6 +168,7 @@ void zgemm_(const char *transa, const char *transb, const int *m, const int *n, 
 {
     int info = gbx_check_gemm_args(*transa, *transb, *m, *n, *k, *lda, *ldb, *ldc);
     if (info) { xerbla_("ZGEMM ", &info, 6); return; }
+    NOTE("zgemm_", a); NOTE("zgemm_", b); NOTE("zgemm_", c);
     const int alpha0 = alpha[0] == 0.0 && alpha[1] == 0.0;
     const int beta0 = beta[0] == 0.0 && beta[1] == 0.0;
     const int beta1 = beta[0] == 1.0 && beta[1] == 0.0;
@@ -197,6 +205,7 @@ void dsyrk_(const char *uplo, const char *trans, const int *n, const int *k, con
 {
     int info = gbx_check_syrk_args(*uplo, *trans, *n, *k, *lda, *ldc);
     if (info) { xerbla_("DSYRK ", &info, 6); return; }
+    NOTE("dsyrk_", a); NOTE("dsyrk_", c);
     if (*n == 0 || ((*alpha == 0.0 || *k == 0) && *beta == 1.0)) return;
     gbx_ctx *ctx = ctx_or_report("DSYRK");
     if (!ctx) return;
@@ -243,6 +252,8 @@ static void trxm(const char *name, trxm_fn fn, const char *side, const char *upl
 {
     int info = gbx_check_trxm_args(*side, *uplo, *transa, *diag, *m, *n, *lda, *ldb);
     if (info) { xerbla_(name, &info, 6); return; }
+    NOTE(fn == gbx_dtrsm ? "dtrsm_" : "dtrmm_", a);
+    NOTE(fn == gbx_dtrsm ? "dtrsm_" : "dtrmm_", b);
     if (*m == 0 || *n == 0) return;
     gbx_ctx *ctx = ctx_or_report(name);
     if (!ctx) return;
@@ -294,6 +305,7 @@ void dgemv_(const char *trans, const int *m, const int *n, const double *alpha, 
 {
     int info = gbx_check_gemv_args(*trans, *m, *n, *lda, *incx, *incy);
     if (info) { xerbla_("DGEMV ", &info, 6); return; }
+    NOTE("dgemv_", a); NOTE("dgemv_", x); NOTE("dgemv_", y);
     if (*m == 0 || *n == 0 || (*alpha == 0.0 && *beta == 1.0)) return;
     gbx_ctx *ctx = ctx_or_report("DGEMV");
     if (!ctx) return;
@@ -321,6 +333,7 @@ void daxpy_(const int *n, const double *alpha, const double *x, const int *incx,
             const int *incy)
 {
     if (*n <= 0 || *alpha == 0.0) return;
+    NOTE("daxpy_", x); NOTE("daxpy_", y);
     gbx_ctx *ctx = ctx_or_report("DAXPY");
     if (!ctx) return;
     gbx_status st;
@@ -338,6 +351,7 @@ fail:
 double ddot_(const int *n, const double *x, const int *incx, const double *y, const int *incy)
 {
     if (*n <= 0) return 0.0;
+    NOTE("ddot_", x); NOTE("ddot_", y);
     gbx_ctx *ctx = ctx_or_report("DDOT");
     if (!ctx) return 0.0;
     gbx_status st;
@@ -357,6 +371,7 @@ fail:
 double dnrm2_(const int *n, const double *x, const int *incx)
 {
     if (*n < 1 || *incx < 1) return 0.0;
+    NOTE("dnrm2_", x);
     gbx_ctx *ctx = ctx_or_report("DNRM2");
     if (!ctx) return 0.0;
     gbx_status st;
@@ -375,6 +390,7 @@ fail:
 static int iamx(const char *name, int is_min, const int *n, const double *x, const int *incx)
 {
     if (*n < 1 || *incx <= 0) return 0;
+    NOTE(is_min ? "idamin_" : "idamax_", x);
     if (*n == 1) return 1;
     gbx_ctx *ctx = ctx_or_report(name);
     if (!ctx) return 0;

@@ -20,7 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-static gbx_config g_cfg = {0, 1e-14, 1, 1, 0, 0, 0, {0}, {0}, 0};
+static gbx_config g_cfg = {0, 1e-14, 1, 1, 0, 0, 0, {0}, {0}, 0, {0}};
 static pthread_once_t g_once = PTHREAD_ONCE_INIT;
 
 static void print_help(void)
@@ -37,7 +37,8 @@ static void print_help(void)
           "   errors=abort|return       -- behaviour on a device failure\n"
           "   serve=on|off              -- route Level-3 calls through the serving loop\n"
           "   managed_min=<bytes>       -- smaller allocations stay on the host\n"
-          "   statistics[=<file>]       -- write call/placement counters at exit\n",
+          "   statistics[=<file>]       -- write call/placement counters at exit\n"
+          "   trace=<file>              -- (preload library) write the allocation/call trace\n",
           stderr);
 }
 
@@ -92,6 +93,7 @@ static void parse(void)
             g_cfg.abort_on_error = strcmp(opt + 7, "return") != 0;
         } else if (strncmp(opt, "trace=", 6) == 0) {
             g_cfg.trace = 1;
+            snprintf(g_cfg.trace_file, sizeof g_cfg.trace_file, "%s", opt + 6);
         } else {
             fprintf(stderr, "gbxblas: unknown option '%s'. Set BLAS2CUDA_OPTIONS=help.\n", opt);
         }

@@ -89,7 +89,12 @@ typedef struct {
     char   oracle_file[1024];/* heuristic=oracle:<file>                          */
     char   stats_file[1024]; /* statistics[=<file>] written at exit              */
     int    serve;            /* serve=on: Fortran calls go through the server    */
+    char   trace_file[1024]; /* trace=<file>: allocation/call trace (preload)    */
 } gbx_config;
+
+/* Trace hook (defined by libgbxblas_preload.so when trace=<file> is set):
+ * records one "C" line naming the tracked object that contains ptr. */
+void gbx_tracker_note(const char *fun, const void *ptr) __attribute__((weak));
 const gbx_config *gbx_get_config(void);
 
 #ifdef __cplusplus

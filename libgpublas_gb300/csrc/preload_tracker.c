@@ -389,6 +389,100 @@ static int managed_release(void *p)
     return e != NULL;
 }
 
+/* ---- trace mode (trace=<file>): the producer side of the allocation-file
+ * workflow.  Same line grammar as the reference's standalone tracker
+ * (obj_tracker.c:426-483, blas_tracker.c:24-31):
+ *   T #<nth> [<ptr>] fun=[malloc] reqsize=[<n>] tid=[<tid>] time=[<s>s+<ns>ns] uid=[<uid>]
+ *   U #<nth> [<ptr>] fun=[free] ...         (object freed)
+ *   C #<nth> [<ptr>] fun=[dgemm_] ...       (a BLAS call names the object)
+ * analyze_trace.py turns it into the H/D decision file of heuristic=oracle.
+ * Every counted allocation is kept in a search tree keyed by address range,
+ * so interior pointers passed to BLAS resolve to their object. */
+#include <search.h>
+#include <sys/syscall.h>
+#include <time.h>
+
+struct tobj {
+    uintptr_t base;
+    size_t size;
+    uint64_t nth, uid;
+    const char *fun;
+};
+static int g_trace_fd = -1;
+static void *g_troot;
+static atomic_ullong g_uid;
+static pthread_mutex_t g_tmu = PTHREAD_MUTEX_INITIALIZER;
+
+static int tcmp(const void *a, const void *b)
+{
+    const struct tobj *x = (const struct tobj *)a, *y = (const struct tobj *)b;
+    /* ranges that overlap compare equal: a 1-byte probe finds its container */
+    if (x->base + (x->size ? x->size : 1) <= y->base) return -1;
+    if (y->base + (y->size ? y->size : 1) <= x->base) return 1;
+    return 0;
+}
+
+static void trace_line(char c, const struct tobj *o, const char *fun)
+{
+    char buf[256];
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC_RAW, &ts);
+    const long tid = (long)syscall(SYS_gettid);
+    int n = snprintf(buf, sizeof buf, "%c #%llu [%p] fun=[%s] reqsize=[%zu] tid=[%ld] time=[%llds+%ldns] uid=[%llu]\n",
+                     c, (unsigned long long)o->nth, (void *)o->base, fun, o->size, tid, (long long)ts.tv_sec,
+                     ts.tv_nsec, (unsigned long long)o->uid);
+    if (n > 0 && write(g_trace_fd, buf, (size_t)(n < (int)sizeof buf ? n : (int)sizeof buf - 1)) < 0) { /* ignore */ }
+}
+
+/* caller has t_in set */
+static void trace_alloc(void *p, size_t n, uint64_t nth, const char *fun)
+{
+    if (g_trace_fd < 0 || !p) return;
+    struct tobj *o = (struct tobj *)r_malloc(sizeof *o);
+    if (!o) return;
+    o->base = (uintptr_t)p;
+    o->size = n;
+    o->nth = nth;
+    o->uid = atomic_fetch_add(&g_uid, 1);
+    o->fun = fun;
+    pthread_mutex_lock(&g_tmu);
+    void *r = tsearch(o, &g_troot, tcmp);
+    if (r && *(struct tobj **)r == o) trace_line('T', o, fun);
+    else r_free(o);   /* stale overlapping record: keep the tree consistent */
+    pthread_mutex_unlock(&g_tmu);
+}
+
+/* caller has t_in set */
+static void trace_free(void *p)
+{
+    if (g_trace_fd < 0 || !p) return;
+    struct tobj key = {(uintptr_t)p, 1, 0, 0, NULL};
+    pthread_mutex_lock(&g_tmu);
+    void *r = tfind(&key, &g_troot, tcmp);
+    if (r) {
+        struct tobj *o = *(struct tobj **)r;
+        if (o->base == (uintptr_t)p) {
+            trace_line('U', o, "free");
+            tdelete(o, &g_troot, tcmp);
+            r_free(o);
+        }
+    }
+    pthread_mutex_unlock(&g_tmu);
+}
+
+void gbx_tracker_note(const char *fun, const void *ptr)
+{
+    if (g_trace_fd < 0 || !ptr) return;
+    const int saved = t_in;
+    t_in = 1;
+    struct tobj key = {(uintptr_t)ptr, 1, 0, 0, NULL};
+    pthread_mutex_lock(&g_tmu);
+    void *r = tfind(&key, &g_troot, tcmp);
+    if (r) trace_line('C', *(struct tobj **)r, fun);
+    pthread_mutex_unlock(&g_tmu);
+    t_in = saved;
+}
+
 /* ---- the interposed entry points -------------------------------------------- */
 static inline int bypass(const void *ret)
 {
@@ -403,6 +497,7 @@ void *malloc(size_t n)
     t_in = 1;
     void *p = (n && decide(nth, n)) ? managed_alloc(n) : NULL;
     if (!p) p = r_malloc(n);
+    trace_alloc(p, n, nth, "malloc");
     t_in = 0;
     return p;
 }
@@ -426,6 +521,7 @@ void *calloc(size_t nm, size_t sz)
     void *p = (n && decide(nth, n)) ? managed_alloc(n) : NULL;
     if (p) memset(p, 0, n);
     else p = r_calloc(nm, sz);
+    trace_alloc(p, n, nth, "calloc");
     t_in = 0;
     return p;
 }
@@ -434,6 +530,11 @@ void free(void *p)
 {
     if (!p || in_boot(p)) return;
     if (!ready()) return;
+    if (g_trace_fd >= 0 && !t_in) {
+        t_in = 1;
+        trace_free(p);
+        t_in = 0;
+    }
     if (managed_release(p)) return;
     r_free(p);
 }
@@ -449,11 +550,22 @@ void *realloc(void *p, size_t n)
         return q;
     }
     const size_t old = managed_size(p);
+    const int counted = !bypass(__builtin_return_address(0));
+    const uint64_t nth = counted ? atomic_fetch_add(&g_nth, 1) : 0;
     if (!old) {
-        if (!bypass(__builtin_return_address(0))) atomic_fetch_add(&g_nth, 1);
-        return r_realloc(p, n);
+        if (!counted || g_trace_fd < 0) return r_realloc(p, n);
+        t_in = 1;
+        trace_free(p);
+        void *q = r_realloc(p, n);
+        trace_alloc(q, n, nth, "realloc");
+        t_in = 0;
+        return q;
     }
-    if (!bypass(__builtin_return_address(0))) atomic_fetch_add(&g_nth, 1);
+    if (counted && g_trace_fd >= 0) {
+        t_in = 1;
+        trace_free(p);
+        t_in = 0;
+    }
     if (n == 0) {
         managed_release(p);
         return NULL;
@@ -463,6 +575,7 @@ void *realloc(void *p, size_t n)
     t_in = 1;
     void *q = managed_alloc(n);
     if (!q) q = r_malloc(n);
+    if (q && counted) trace_alloc(q, n, nth, "realloc");
     t_in = saved;
     if (!q) return NULL;
     memcpy(q, p, old < n ? old : n);
@@ -529,6 +642,10 @@ __attribute__((constructor(101))) static void tracker_init(void)
         fprintf(stderr, "gbxblas: failed to load allocation oracle '%s': %s\n", cfg->oracle_file,
                 strerror(errno));
         abort();
+    }
+    if (cfg->trace_file[0]) {
+        g_trace_fd = open(cfg->trace_file, O_WRONLY | O_CREAT | O_TRUNC | O_APPEND | O_CLOEXEC, 0644);
+        if (g_trace_fd < 0) fprintf(stderr, "gbxblas: cannot open trace file '%s'\n", cfg->trace_file);
     }
     g_tracking = 1;
     t_in = 0;

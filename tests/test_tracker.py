@@ -119,6 +119,25 @@ def test_statistics_file(prog, tmp_path):
     assert row["managed_objects"] == 0 and row["counted_allocs"] >= 10
 
 
+def test_trace_to_decision_file_workflow(prog, tmp_path):
+    # producer: trace a run; analyze: objects named by BLAS calls become "D";
+    # consumer: rerun with the decision file, exactly those are managed.
+    import sys
+    trace = tmp_path / "run.trace"
+    dec = tmp_path / "decisions.txt"
+    lines = run(prog, ["blas_note"], f"heuristic=false;errors=return;trace={trace}")
+    assert [ln.split()[1] for ln in lines] == ["0"] * 6
+    text = trace.read_text()
+    assert text.count("fun=[dgemm_]") == 3 and text.count("\nU #") + text.startswith("U #") >= 6
+    r = subprocess.run([sys.executable, "-m", "libgpublas_gb300.analyze_trace", str(trace), str(dec)],
+                       capture_output=True, text=True, cwd=ROOT, timeout=60)
+    assert r.returncode == 0, r.stderr
+    d_lines = [ln for ln in dec.read_text().splitlines() if ln.startswith("D ")]
+    assert len(d_lines) == 3
+    lines = run(prog, ["blas_note"], f"heuristic=oracle:{dec};errors=return")
+    assert [int(ln.split()[1]) for ln in lines] == [0, 1, 0, 1, 1, 0]
+
+
 @pytest.mark.gpu
 def test_managed_operands_are_used_in_place(prog):
     # real managed memory: dgemm_ on operands the interposer placed there is a

@@ -175,6 +175,26 @@ static int blas(int n)
     return 0;
 }
 
+/* six 8x8 matrices; dgemm_ names objects 1, 3 (through an interior pointer)
+ * and 4; prints "<index> <managed>" for each object.  Without a GPU the
+ * call reports its device failure and returns (errors=return); the trace
+ * lines are written before that. */
+static int blas_note(void)
+{
+    dgemm_fn dgemm = (dgemm_fn)dlsym(RTLD_DEFAULT, "dgemm_");
+    double *p[6];
+    for (int i = 0; i < 6; i++) {
+        p[i] = (double *)malloc(sizeof(double) * 80);
+        for (int j = 0; j < 80; j++) p[i][j] = 1.0;
+    }
+    int n = 8, ld = 8;
+    const double one = 1.0, zero = 0.0;
+    dgemm("N", "N", &n, &n, &n, &one, p[1], &ld, p[3] + 8, &ld, &zero, p[4], &ld);
+    for (int i = 0; i < 6; i++) out("%llu %llu %llu\n", (unsigned long long)i, (unsigned long long)is_managed(p[i]), 0);
+    for (int i = 0; i < 6; i++) free(p[i]);
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     is_managed = (int (*)(const void *))dlsym(RTLD_DEFAULT, "gbx_tracker_is_managed");
@@ -189,6 +209,7 @@ int main(int argc, char **argv)
     if (!strcmp(argv[1], "realloc")) return realloc_case();
     if (!strcmp(argv[1], "threads")) return threads();
     if (!strcmp(argv[1], "many")) return many();
+    if (!strcmp(argv[1], "blas_note")) return blas_note();
     if (!strcmp(argv[1], "blas")) return blas(argc > 2 ? atoi(argv[2]) : 512);
     return 8;
 }
