@@ -79,12 +79,22 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """nvidia-smi clock/throttle samples during the timed region.
+
+    Sampling runs every 200 ms.  A timed region shorter than that (the
+    Level-1 kernels run for milliseconds) is bracketed instead: entering
+    waits for the first sample, leaving waits for one sample taken after the
+    region ended, so every line carries at least two samples."""
 
     def __init__(self, gpu):
         self.gpu = gpu
         self.proc = None
         self.lines = []
+
+    def _wait_lines(self, count, timeout):
+        t_end = time.time() + timeout
+        while len(self.lines) < count and time.time() < t_end and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def __enter__(self):
         try:
@@ -94,6 +104,7 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self._wait_lines(1, 5.0)
         except (OSError, ValueError):
             self.proc = None
         return self
@@ -104,6 +115,7 @@ class ClockSampler:
 
     def __exit__(self, *exc):
         if self.proc is not None:
+            self._wait_lines(len(self.lines) + 1, 1.0)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)

@@ -149,25 +149,49 @@ struct Blue {
     static constexpr double ssml = 0x1p+537, sbig = 0x1p-538;
 };
 
-// The range test runs on the integer pipe (bit patterns of |v| compare like
-// the values); the common mid-range element costs one DFMA, which matters on
-// a part whose FP64 pipe is the bound for this 8-byte-per-FMA kernel.
+// High word of the bit pattern of |v|, taken in PTX.  Integer compares on
+// the bits of a double written in C are folded back into FP64 compares by
+// the compiler, and on this part every FP64 instruction per element costs as
+// much as the element's load: the streaming kernels below keep their range
+// and NaN tests on the integer pipe through these two helpers.
+__device__ __forceinline__ unsigned abs_hi_word(double v)
+{
+    unsigned h;
+    asm("{\n\t.reg .b32 lo;\n\tmov.b64 {lo, %0}, %1;\n\tand.b32 %0, %0, 0x7FFFFFFF;\n\t}"
+        : "=r"(h) : "l"(__double_as_longlong(v)));
+    return h;
+}
+
+// Bit pattern of |v| (monotone in |v| for non-NaN values), taken in PTX.
+__device__ __forceinline__ unsigned long long abs_bits(double v)
+{
+    unsigned long long b;
+    asm("and.b64 %0, %1, 0x7FFFFFFFFFFFFFFF;" : "=l"(b) : "l"(__double_as_longlong(v)));
+    return b;
+}
+
+// Warp-uniform fast path: when the high word of |v| puts every lane's
+// element in 2^-511 <= |v| < 2^486·(1 + 2^-20) the warp executes the single
+// DFMA only (a predicated if-conversion of the three branches would issue
+// all three FP64 sequences for every element).  Against the exact thresholds
+// this keeps the elements in [2^486, 2^486·(1 + 2^-20)) in the unscaled
+// accumulator, where their squares (< 2^973) still cannot overflow a sum of
+// 2^31 terms; the result differs from the exact-threshold sum by rounding
+// only.  A warp holding any other element (zeros included) classifies each
+// lane with the exact thresholds; NaN fails both compares and lands in the
+// unscaled accumulator, from where it propagates (netlib's rule).
 __device__ __forceinline__ void blue_acc(double v, double &asml, double &amed, double &abig)
 {
-    constexpr unsigned long long kBig = (unsigned long long)(486 + 1023) << 52;   // bits of tbig
-    constexpr unsigned long long kSml = (unsigned long long)(1023 - 511) << 52;   // bits of tsml
-    constexpr unsigned long long kInf = 0x7FF0000000000000ull;
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    const bool big = b > kBig && b <= kInf, sml = b < kSml && b != 0ull;   // zeros add nothing
-    // Warp-uniform fast path: when no lane holds an out-of-range element the
-    // warp executes the single DFMA only (a predicated if-conversion of the
-    // three branches would issue all three FP64 sequences for every element).
-    if (!__any_sync(__activemask(), big || sml)) {
-        amed = fma(v, v, amed);   // also takes NaN, which then propagates
+    constexpr unsigned kBigHi = (unsigned)(486 + 1023) << 20;   // high word of tbig
+    constexpr unsigned kSmlHi = (unsigned)(1023 - 511) << 20;   // high word of tsml
+    const unsigned h = abs_hi_word(v);
+    if (!__any_sync(__activemask(), h - kSmlHi > kBigHi - kSmlHi)) {
+        amed = fma(v, v, amed);
         return;
     }
-    if (big) { const double t = fabs(v) * Blue::sbig; abig = fma(t, t, abig); }
-    else if (sml) { const double t = fabs(v) * Blue::ssml; asml = fma(t, t, asml); }
+    const double ax = fabs(v);
+    if (ax > Blue::tbig) { const double t = ax * Blue::sbig; abig = fma(t, t, abig); }
+    else if (ax < Blue::tsml) { const double t = ax * Blue::ssml; asml = fma(t, t, asml); }
     else amed = fma(v, v, amed);
 }
 
@@ -259,7 +283,7 @@ template <bool IS_MIN>
 __device__ __forceinline__ unsigned long long amax_key(double v)
 {
     // integer pipe only: |v| is the bit pattern without the sign bit
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    const unsigned long long bits = abs_bits(v);
     if (bits > 0x7FF0000000000000ull) return 0ull;   // NaN
     return IS_MIN ? ~bits : bits;
 }

@@ -977,24 +977,34 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     p.c_part = pr.c_part;
     p.status = b.status;
 
-    static int max_pairs = -1;
-    if (max_pairs < 0) {
-        if (cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(oz_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ2_SMEM) !=
-                cudaSuccess)
-            return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: shared memory attribute");
-        // how many CTA pairs can be resident at once (clusters must fit in a GPC)
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(2 * (unsigned)std::max(1, gbx_ctx_sms(ctx) / 2));
-        cfg.blockDim = dim3(OZ_THREADS);
-        cfg.dynamicSmemBytes = OZ2_SMEM;
-        int nc = 0;
-        if (cudaOccupancyMaxActiveClusters(&nc, oz_gemm2_kernel, &cfg) != cudaSuccess || nc < 1) {
-            cudaGetLastError();
-            nc = gbx_ctx_sms(ctx) / 2;
+    // kernel attributes (per device) and the resident CTA-pair count; calls
+    // arrive from many host threads
+    static std::mutex attr_mu;
+    static int max_pairs_of[64] = {0};
+    const int dev = gbx_ctx_device(ctx);
+    int max_pairs;
+    {
+        std::lock_guard<std::mutex> lk(attr_mu);
+        max_pairs = (dev >= 0 && dev < 64) ? max_pairs_of[dev] : 0;
+        if (max_pairs == 0) {
+            if (cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(oz_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)OZ2_SMEM) != cudaSuccess)
+                return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: shared memory attribute");
+            // how many CTA pairs can be resident at once (clusters must fit in a GPC)
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(2 * (unsigned)std::max(1, gbx_ctx_sms(ctx) / 2));
+            cfg.blockDim = dim3(OZ_THREADS);
+            cfg.dynamicSmemBytes = OZ2_SMEM;
+            int nc = 0;
+            if (cudaOccupancyMaxActiveClusters(&nc, oz_gemm2_kernel, &cfg) != cudaSuccess || nc < 1) {
+                cudaGetLastError();
+                nc = gbx_ctx_sms(ctx) / 2;
+            }
+            max_pairs = std::max(1, nc);
+            if (dev >= 0 && dev < 64) max_pairs_of[dev] = max_pairs;
         }
-        max_pairs = nc;
     }
     const int ntiles = p.tiles_m * p.tiles_n;
     gbx_timer_begin(ctx, GBX_TIMER_OZAKI_MMA);

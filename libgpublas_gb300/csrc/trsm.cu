@@ -190,11 +190,8 @@ extern "C" gbx_status gbx_dtrsm(gbx_ctx *ctx, char side, char uplo, char ta, cha
     t.T = tmp;
 
     const size_t smem = sizeof(double) * (NB * (NB + 1) + NB * NB);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(trinv_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
-    }
+    // a per-device function attribute; setting it is a cheap host call
+    cudaFuncSetAttribute(trinv_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     trinv_blocks<<<nblk, NB, smem, S(ctx)>>>(t.na, A, lda, t.tr, t.lower, (tri & TRI_UNIT) != 0, inv);
     gbx_count_launch(ctx, 1);
     if ((st = gbx_check_launch(ctx, "dtrsm inverse")) != GBX_OK) return st;

@@ -161,6 +161,21 @@ def test_dnrm2_edges(f77):
     assert abs(f77.dnrm2(4, mixed, 1) - np.sqrt(2) * 1e200) <= 1e-14 * np.sqrt(2) * 1e200
 
 
+@pytest.mark.parametrize("edge", [486, -511])
+def test_dnrm2_range_thresholds(orc, f77, edge):
+    # elements on both sides of the scaling thresholds 2^486 and 2^-511, with
+    # zeros and subnormals, spread over many warps
+    rng = np.random.default_rng(edge & 0xffff)
+    t = np.ldexp(1.0, edge)
+    pool = np.array([t, np.nextafter(t, 0), np.nextafter(t, np.inf), t * (1 + 2.0 ** -20),
+                     t * (1 + 2.0 ** -21), t * 0.75, 0.0, -t, 5e-324, 2.2e-308, 1.0])
+    for n in (37, 4096, 100003):
+        x = rng.choice(pool, n) * rng.uniform(0.5, 1.0, n) ** (rng.integers(0, 2, n))
+        ref = orc.dnrm2(n, x, 1)
+        got = f77.dnrm2(n, x, 1)
+        assert abs(got - ref) <= 1e-14 * ref, (n, got, ref)
+
+
 def test_device_abi_level1(orc, dev):
     import torch
     n = 3 * (1 << 20) + 1
