@@ -148,6 +148,84 @@ gbx_status gbx_dtrmm(gbx_ctx *ctx, char side, char uplo, char transa, char diag,
                      int m, int n, double alpha, const double *A, int lda,
                      double *B, int ldb);
 
+/* The other precisions and the remaining Level-3 routines, same conventions
+ * (device pointers, netlib semantics, beta == 0 sets C).  Complex scalars
+ * point to HOST (re, im) pairs; complex matrices are interleaved (re, im).
+ * Hermitian routines take real alpha/beta where netlib does and leave the
+ * diagonal of C real.  Each replaces the cuBLAS call named, reached from the
+ * reference's Fortran wrapper at the line given. */
+/* cublasSgemm gemm.cc:143-160; cublasCgemm gemm.cc:181-198 */
+gbx_status gbx_sgemm(gbx_ctx *ctx, char transa, char transb, int m, int n, int k,
+                     float alpha, const float *A, int lda, const float *B, int ldb,
+                     float beta, float *C, int ldc);
+gbx_status gbx_cgemm(gbx_ctx *ctx, char transa, char transb, int m, int n, int k,
+                     const float *alpha, const float *A, int lda, const float *B, int ldb,
+                     const float *beta, float *C, int ldc);
+/* C := alpha*A*B + beta*C (side L) or alpha*B*A + beta*C (side R), A symmetric
+ * with one stored triangle: cublas[SDCZ]symm symm.cc:124-200 */
+gbx_status gbx_ssymm(gbx_ctx *ctx, char side, char uplo, int m, int n, float alpha,
+                     const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc);
+gbx_status gbx_dsymm(gbx_ctx *ctx, char side, char uplo, int m, int n, double alpha,
+                     const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc);
+gbx_status gbx_csymm(gbx_ctx *ctx, char side, char uplo, int m, int n, const float *alpha,
+                     const float *A, int lda, const float *B, int ldb, const float *beta, float *C, int ldc);
+gbx_status gbx_zsymm(gbx_ctx *ctx, char side, char uplo, int m, int n, const double *alpha,
+                     const double *A, int lda, const double *B, int ldb, const double *beta, double *C,
+                     int ldc);
+/* A Hermitian (diagonal taken as real): cublas[CZ]hemm hemm.cc:120-154 */
+gbx_status gbx_chemm(gbx_ctx *ctx, char side, char uplo, int m, int n, const float *alpha,
+                     const float *A, int lda, const float *B, int ldb, const float *beta, float *C, int ldc);
+gbx_status gbx_zhemm(gbx_ctx *ctx, char side, char uplo, int m, int n, const double *alpha,
+                     const double *A, int lda, const double *B, int ldb, const double *beta, double *C,
+                     int ldc);
+/* C := alpha*op(A)*op(A)^T + beta*C, one triangle (complex: trans N or T):
+ * cublas[SCZ]syrk syrk.cc:148-216 */
+gbx_status gbx_ssyrk(gbx_ctx *ctx, char uplo, char trans, int n, int k, float alpha,
+                     const float *A, int lda, float beta, float *C, int ldc);
+gbx_status gbx_csyrk(gbx_ctx *ctx, char uplo, char trans, int n, int k, const float *alpha,
+                     const float *A, int lda, const float *beta, float *C, int ldc);
+gbx_status gbx_zsyrk(gbx_ctx *ctx, char uplo, char trans, int n, int k, const double *alpha,
+                     const double *A, int lda, const double *beta, double *C, int ldc);
+/* C := alpha*op(A)*op(A)^H + beta*C, alpha and beta real (trans N or C):
+ * cublas[CZ]herk herk.cc:131-163 */
+gbx_status gbx_cherk(gbx_ctx *ctx, char uplo, char trans, int n, int k, float alpha,
+                     const float *A, int lda, float beta, float *C, int ldc);
+gbx_status gbx_zherk(gbx_ctx *ctx, char uplo, char trans, int n, int k, double alpha,
+                     const double *A, int lda, double beta, double *C, int ldc);
+/* C := alpha*op(A)*op(B)^T + alpha*op(B)*op(A)^T + beta*C, one triangle:
+ * cublas[SDCZ]syr2k syr2k.cc:146-218 */
+gbx_status gbx_ssyr2k(gbx_ctx *ctx, char uplo, char trans, int n, int k, float alpha,
+                      const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc);
+gbx_status gbx_dsyr2k(gbx_ctx *ctx, char uplo, char trans, int n, int k, double alpha,
+                      const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc);
+gbx_status gbx_csyr2k(gbx_ctx *ctx, char uplo, char trans, int n, int k, const float *alpha,
+                      const float *A, int lda, const float *B, int ldb, const float *beta, float *C,
+                      int ldc);
+gbx_status gbx_zsyr2k(gbx_ctx *ctx, char uplo, char trans, int n, int k, const double *alpha,
+                      const double *A, int lda, const double *B, int ldb, const double *beta, double *C,
+                      int ldc);
+/* C := alpha*op(A)*op(B)^H + conj(alpha)*op(B)*op(A)^H + beta*C, beta real:
+ * cublas[CZ]her2k her2k.cc:141-183 */
+gbx_status gbx_cher2k(gbx_ctx *ctx, char uplo, char trans, int n, int k, const float *alpha,
+                      const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc);
+gbx_status gbx_zher2k(gbx_ctx *ctx, char uplo, char trans, int n, int k, const double *alpha,
+                      const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc);
+/* cublas[SCZ]trmm trmm.cc:139-215 (the reference disables trmm.cc in its
+ * build, meson.build:86-87) */
+gbx_status gbx_strmm(gbx_ctx *ctx, char side, char uplo, char transa, char diag, int m, int n,
+                     float alpha, const float *A, int lda, float *B, int ldb);
+gbx_status gbx_ctrmm(gbx_ctx *ctx, char side, char uplo, char transa, char diag, int m, int n,
+                     const float *alpha, const float *A, int lda, float *B, int ldb);
+gbx_status gbx_ztrmm(gbx_ctx *ctx, char side, char uplo, char transa, char diag, int m, int n,
+                     const double *alpha, const double *A, int lda, double *B, int ldb);
+/* cublas[SCZ]trsm trsm.cc:134-215 */
+gbx_status gbx_strsm(gbx_ctx *ctx, char side, char uplo, char transa, char diag, int m, int n,
+                     float alpha, const float *A, int lda, float *B, int ldb);
+gbx_status gbx_ctrsm(gbx_ctx *ctx, char side, char uplo, char transa, char diag, int m, int n,
+                     const float *alpha, const float *A, int lda, float *B, int ldb);
+gbx_status gbx_ztrsm(gbx_ctx *ctx, char side, char uplo, char transa, char diag, int m, int n,
+                     const double *alpha, const double *A, int lda, double *B, int ldb);
+
 /* Cholesky of one small diagonal block, lower, n <= 256, in place; *info (a
  * device int) is 0 or the 1-based column of a non-positive pivot.  Not a
  * BLAS routine (no reference counterpart): the diagonal step of the blocked

@@ -277,6 +277,50 @@ class F77:
     def idamin(self, n, x, incx):
         return self.L.idamin_(_byref_i(n), _hp(x), _byref_i(incx))
 
+    # ---- the Level-3 family in every precision: p is 's', 'd', 'c' or 'z';
+    # scalars are passed by reference in the routine's type (real for the
+    # Hermitian alpha/beta that netlib declares real)
+    @staticmethod
+    def _s(p, v, real=False):
+        if p in "sc":
+            dt = np.float32 if (p == "s" or real) else np.complex64
+        else:
+            dt = np.float64 if (p == "d" or real) else np.complex128
+        return np.array([v], dtype=dt)
+
+    def _fn(self, name):
+        return getattr(self.L, name + "_")
+
+    def gemm(self, p, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+        al, be = self._s(p, alpha), self._s(p, beta)
+        self._fn(p + "gemm")(C.c_char_p(_ch(ta)), C.c_char_p(_ch(tb)), _byref_i(m), _byref_i(n), _byref_i(k),
+                             _hp(al), _hp(a), _byref_i(lda), _hp(b), _byref_i(ldb), _hp(be), _hp(c),
+                             _byref_i(ldc))
+
+    def symm(self, p, side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc, herm=False):
+        al, be = self._s(p, alpha), self._s(p, beta)
+        self._fn(p + ("hemm" if herm else "symm"))(
+            C.c_char_p(_ch(side)), C.c_char_p(_ch(uplo)), _byref_i(m), _byref_i(n), _hp(al), _hp(a),
+            _byref_i(lda), _hp(b), _byref_i(ldb), _hp(be), _hp(c), _byref_i(ldc))
+
+    def syrk(self, p, uplo, trans, n, k, alpha, a, lda, beta, c, ldc, herm=False):
+        al, be = self._s(p, alpha, herm), self._s(p, beta, herm)
+        self._fn(p + ("herk" if herm else "syrk"))(
+            C.c_char_p(_ch(uplo)), C.c_char_p(_ch(trans)), _byref_i(n), _byref_i(k), _hp(al), _hp(a),
+            _byref_i(lda), _hp(be), _hp(c), _byref_i(ldc))
+
+    def syr2k(self, p, uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc, herm=False):
+        al, be = self._s(p, alpha), self._s(p, beta, herm)
+        self._fn(p + ("her2k" if herm else "syr2k"))(
+            C.c_char_p(_ch(uplo)), C.c_char_p(_ch(trans)), _byref_i(n), _byref_i(k), _hp(al), _hp(a),
+            _byref_i(lda), _hp(b), _byref_i(ldb), _hp(be), _hp(c), _byref_i(ldc))
+
+    def trxm(self, p, routine, side, uplo, ta, diag, m, n, alpha, a, lda, b, ldb):
+        al = self._s(p, alpha)
+        self._fn(p + routine)(C.c_char_p(_ch(side)), C.c_char_p(_ch(uplo)), C.c_char_p(_ch(ta)),
+                              C.c_char_p(_ch(diag)), _byref_i(m), _byref_i(n), _hp(al), _hp(a), _byref_i(lda),
+                              _hp(b), _byref_i(ldb))
+
 
 def _dp(t):
     """Device pointer of a torch tensor (or an int address)."""

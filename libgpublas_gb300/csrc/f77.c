@@ -76,6 +76,10 @@ static gbx_ctx *ctx_or_report(const char *name)
     return ctx;
 }
 
+/* shared with the other Fortran/CBLAS translation unit (f77_level3.c) */
+gbx_ctx *gbx_f77_ctx(const char *name) { return ctx_or_report(name); }
+void gbx_f77_report(const char *name, gbx_ctx *ctx, gbx_status st) { report(name, ctx, st); }
+
 #define TRY(expr)                                 \
     do {                                          \
         st = (expr);                              \

@@ -97,6 +97,23 @@ typedef struct {
 void gbx_tracker_note(const char *fun, const void *ptr) __attribute__((weak));
 const gbx_config *gbx_get_config(void);
 
+/* Fortran-layer helpers (f77.c): the calling thread's context (counting
+ * the call; reports when no context can be made) and the failure report
+ * (prints, and aborts under errors=abort). */
+gbx_ctx *gbx_f77_ctx(const char *name);
+void gbx_f77_report(const char *name, gbx_ctx *ctx, gbx_status st);
+
+/* netlib argument checks (INFO numbering); 0 when the call is valid */
+enum { GBX_TR_N = 1, GBX_TR_T = 2, GBX_TR_C = 4 };   /* transposition letters a routine takes */
+int gbx_check_gemm_args(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc);
+int gbx_check_syrk_args(char uplo, char trans, int n, int k, int lda, int ldc);
+int gbx_check_trxm_args(char side, char uplo, char ta, char diag, int m, int n, int lda, int ldb);
+int gbx_check_rank_k_args(char uplo, char trans, int allowed, int n, int k, int lda, int ldc);
+int gbx_check_rank_2k_args(char uplo, char trans, int allowed, int n, int k, int lda, int ldb, int ldc);
+int gbx_check_symm_args(char side, char uplo, int m, int n, int lda, int ldb, int ldc);
+int gbx_trans_ok(char trans, int allowed);
+int gbx_op_tri(char uplo, char transa, char diag);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,11 +1,11 @@
-// gemm.cu — plain FP64 Level-3 routines on the DFMA GEMM core:
-// gbx_dgemm, gbx_zgemm, gbx_dsyrk, gbx_dtrmm.
+// gemm.cu — the host side of the GEMM core shared by every Level-3 routine:
+// the beta-scaling kernel, the tile-size choice and launch, and the netlib
+// argument checks.  The BLAS entry points themselves are in level3.cu.
 //
 // Argument checks use the netlib INFO numbering that the reference's wrappers
 // replicate (blas_level3/gemm.cc:87-127, syrk.cc:78-146, trmm.cc:82-137); on
 // the device layer an invalid argument returns GBX_ERR_ARG and the position
-// is recorded in the context's error text.  Unlike gemm.cc:121-125, beta == 0
-// overwrites C, as the netlib specification requires.
+// is recorded in the context's error text.
 #include "gbx_internal.h"
 #include "gemm_simt.cuh"
 #include "gemm_host.h"
@@ -20,7 +20,7 @@ namespace {
 inline cudaStream_t S(gbx_ctx *ctx) { return (cudaStream_t)gbx_ctx_get_stream(ctx); }
 
 template <typename T>
-__global__ void scale_matrix_kernel(int m, int n, T beta, T *C, long long ldc, int part)
+__global__ void scale_matrix_kernel(int m, int n, T beta, T *C, long long ldc, int part, int herm)
 {
     const long long total = (long long)m * n;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
@@ -29,7 +29,9 @@ __global__ void scale_matrix_kernel(int m, int n, T beta, T *C, long long ldc, i
         if (part == C_LOWER && i < j) continue;
         if (part == C_UPPER && i > j) continue;
         T *cp = C + (long long)j * ldc + i;
-        *cp = Ops<T>::is_zero(beta) ? Ops<T>::zero() : Ops<T>::mul(beta, *cp);
+        T v = Ops<T>::is_zero(beta) ? Ops<T>::zero() : Ops<T>::mul(beta, *cp);
+        if (herm && i == j) v = Ops<T>::real_only(v);
+        *cp = v;
     }
 }
 
@@ -38,17 +40,19 @@ __global__ void scale_matrix_kernel(int m, int n, T beta, T *C, long long ldc, i
 namespace gbx_gemm {
 
 template <typename T>
-gbx_status scale_matrix(gbx_ctx *ctx, int m, int n, T beta, T *C, long long ldc, int part)
+gbx_status scale_matrix(gbx_ctx *ctx, int m, int n, T beta, T *C, long long ldc, int part, int herm)
 {
     if (m <= 0 || n <= 0) return GBX_OK;
     long long total = (long long)m * n;
     long long g = std::min<long long>((total + 255) / 256, (long long)gbx_ctx_sms(ctx) * 8);
-    scale_matrix_kernel<T><<<(int)g, 256, 0, S(ctx)>>>(m, n, beta, C, ldc, part);
+    scale_matrix_kernel<T><<<(int)g, 256, 0, S(ctx)>>>(m, n, beta, C, ldc, part, herm);
     gbx_count_launch(ctx, 1);
     return gbx_check_launch(ctx, "scale_matrix");
 }
-template gbx_status scale_matrix<double>(gbx_ctx *, int, int, double, double *, long long, int);
-template gbx_status scale_matrix<dcplx>(gbx_ctx *, int, int, dcplx, dcplx *, long long, int);
+template gbx_status scale_matrix<float>(gbx_ctx *, int, int, float, float *, long long, int, int);
+template gbx_status scale_matrix<double>(gbx_ctx *, int, int, double, double *, long long, int, int);
+template gbx_status scale_matrix<fcplx>(gbx_ctx *, int, int, fcplx, fcplx *, long long, int, int);
+template gbx_status scale_matrix<dcplx>(gbx_ctx *, int, int, dcplx, dcplx *, long long, int, int);
 
 template <typename T, int TM>
 gbx_status launch_gemm_tile(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
@@ -74,7 +78,8 @@ gbx_status launch_gemm_tile(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
 // Tile choice: the largest block tile that still gives every SM two tiles;
 // 128x128 (8x8 per thread) for large problems, 64x64 and 32x32 for the
 // skinny and small products that DTRSM's recursion and small calls produce
-// (with few large tiles most SMs would idle).  Complex uses 64x64 / 32x32.
+// (with few large tiles most SMs would idle).  Complex double uses 64x64 /
+// 32x32 (its 8x8 register tile would not fit).
 template <typename T>
 gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
 {
@@ -84,7 +89,7 @@ gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
         const long long tm = (p.m + bm - 1) / bm, tn = (p.n + bm - 1) / bm;
         return p.c_part == C_FULL ? tm * tn : tm * (tm + 1) / 2;
     };
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (sizeof(T) <= 8) {
         if (tiles(128) >= want) return launch_gemm_tile<T, 8>(ctx, p, what);
         if (tiles(64) >= want) return launch_gemm_tile<T, 4>(ctx, p, what);
         return launch_gemm_tile<T, 2>(ctx, p, what);
@@ -93,7 +98,9 @@ gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
         return launch_gemm_tile<T, 2>(ctx, p, what);
     }
 }
+template gbx_status launch_gemm<float>(gbx_ctx *, GemmArgs<float>, const char *);
 template gbx_status launch_gemm<double>(gbx_ctx *, GemmArgs<double>, const char *);
+template gbx_status launch_gemm<fcplx>(gbx_ctx *, GemmArgs<fcplx>, const char *);
 template gbx_status launch_gemm<dcplx>(gbx_ctx *, GemmArgs<dcplx>, const char *);
 
 }  // namespace gbx_gemm
@@ -142,68 +149,57 @@ extern "C" int gbx_check_trxm_args(char side, char uplo, char ta, char diag, int
     return 0;
 }
 
-// ------------------------------------------------------------------- DGEMM
-extern "C" gbx_status gbx_dgemm(gbx_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha,
-                                const double *A, int lda, const double *B, int ldb, double beta,
-                                double *C, int ldc)
+// Rank-k and rank-2k updates: which transposition letters a routine takes
+// (real: N, T, C; complex symmetric: N, T; Hermitian: N, C).
+extern "C" int gbx_trans_ok(char trans, int allowed)
 {
-    if (!ctx) return GBX_ERR_ARG;
-    int info = gbx_check_gemm_args(ta, tb, m, n, k, lda, ldb, ldc);
-    if (info) return gbx_fail(ctx, GBX_ERR_ARG, "DGEMM parameter %d", info);
-    if (m == 0 || n == 0 || ((alpha == 0.0 || k == 0) && beta == 1.0)) return GBX_OK;
-    if (alpha == 0.0 || k == 0) return scale_matrix<double>(ctx, m, n, beta, C, ldc, C_FULL);
-    GemmArgs<double> p{};
-    p.m = m; p.n = n; p.k = k;
-    p.A = A; p.lda = lda; p.ta = !gbx_lsame(ta, 'N');
-    p.B = B; p.ldb = ldb; p.tb = !gbx_lsame(tb, 'N');
-    p.alpha = alpha; p.beta = beta;
-    p.C = C; p.ldc = ldc;
-    return launch_gemm<double>(ctx, p, "dgemm");
+    return (gbx_lsame(trans, 'N') && (allowed & GBX_TR_N)) || (gbx_lsame(trans, 'T') && (allowed & GBX_TR_T)) ||
+           (gbx_lsame(trans, 'C') && (allowed & GBX_TR_C));
 }
 
-// ------------------------------------------------------------------- ZGEMM
-extern "C" gbx_status gbx_zgemm(gbx_ctx *ctx, char ta, char tb, int m, int n, int k,
-                                const double *alpha, const double *A, int lda, const double *B,
-                                int ldb, const double *beta, double *C, int ldc)
+// xSYRK / xHERK (netlib numbering: uplo 1, trans 2, n 3, k 4, lda 7, ldc 10)
+extern "C" int gbx_check_rank_k_args(char uplo, char trans, int allowed, int n, int k, int lda, int ldc)
 {
-    if (!ctx || !alpha || !beta) return GBX_ERR_ARG;
-    int info = gbx_check_gemm_args(ta, tb, m, n, k, lda, ldb, ldc);
-    if (info) return gbx_fail(ctx, GBX_ERR_ARG, "ZGEMM parameter %d", info);
-    const dcplx al{alpha[0], alpha[1]}, be{beta[0], beta[1]};
-    const bool alpha0 = al.x == 0.0 && al.y == 0.0, beta1 = be.x == 1.0 && be.y == 0.0;
-    if (m == 0 || n == 0 || ((alpha0 || k == 0) && beta1)) return GBX_OK;
-    if (alpha0 || k == 0) return scale_matrix<dcplx>(ctx, m, n, be, (dcplx *)C, ldc, C_FULL);
-    GemmArgs<dcplx> p{};
-    p.m = m; p.n = n; p.k = k;
-    p.A = (const dcplx *)A; p.lda = lda; p.ta = !gbx_lsame(ta, 'N'); p.conja = gbx_lsame(ta, 'C');
-    p.B = (const dcplx *)B; p.ldb = ldb; p.tb = !gbx_lsame(tb, 'N'); p.conjb = gbx_lsame(tb, 'C');
-    p.alpha = al; p.beta = be;
-    p.C = (dcplx *)C; p.ldc = ldc;
-    return launch_gemm<dcplx>(ctx, p, "zgemm");
+    const int nrowa = gbx_lsame(trans, 'N') ? n : k;
+    if (!gbx_lsame(uplo, 'U') && !gbx_lsame(uplo, 'L')) return 1;
+    if (!gbx_trans_ok(trans, allowed)) return 2;
+    if (n < 0) return 3;
+    if (k < 0) return 4;
+    if (lda < std::max(1, nrowa)) return 7;
+    if (ldc < std::max(1, n)) return 10;
+    return 0;
 }
 
-// ------------------------------------------------------------------- DSYRK
-extern "C" gbx_status gbx_dsyrk(gbx_ctx *ctx, char uplo, char trans, int n, int k, double alpha,
-                                const double *A, int lda, double beta, double *C, int ldc)
+// xSYR2K / xHER2K (uplo 1, trans 2, n 3, k 4, lda 7, ldb 9, ldc 12)
+extern "C" int gbx_check_rank_2k_args(char uplo, char trans, int allowed, int n, int k, int lda, int ldb,
+                                      int ldc)
 {
-    if (!ctx) return GBX_ERR_ARG;
-    int info = gbx_check_syrk_args(uplo, trans, n, k, lda, ldc);
-    if (info) return gbx_fail(ctx, GBX_ERR_ARG, "DSYRK parameter %d", info);
-    if (n == 0 || ((alpha == 0.0 || k == 0) && beta == 1.0)) return GBX_OK;
-    const int part = gbx_lsame(uplo, 'U') ? C_UPPER : C_LOWER;
-    if (alpha == 0.0 || k == 0) return scale_matrix<double>(ctx, n, n, beta, C, ldc, part);
-    const bool notr = gbx_lsame(trans, 'N');
-    GemmArgs<double> p{};
-    p.m = n; p.n = n; p.k = k;
-    p.A = A; p.lda = lda; p.ta = !notr;   // N: op(A) = A (n x k);  T: op(A) = A^T
-    p.B = A; p.ldb = lda; p.tb = notr;    // N: op(B) = A^T;        T: op(B) = A (k x n)
-    p.alpha = alpha; p.beta = beta;
-    p.C = C; p.ldc = ldc;
-    p.c_part = part;
-    return launch_gemm<double>(ctx, p, "dsyrk");
+    const int nrowa = gbx_lsame(trans, 'N') ? n : k;
+    if (!gbx_lsame(uplo, 'U') && !gbx_lsame(uplo, 'L')) return 1;
+    if (!gbx_trans_ok(trans, allowed)) return 2;
+    if (n < 0) return 3;
+    if (k < 0) return 4;
+    if (lda < std::max(1, nrowa)) return 7;
+    if (ldb < std::max(1, nrowa)) return 9;
+    if (ldc < std::max(1, n)) return 12;
+    return 0;
 }
 
-// ------------------------------------------------------------------- DTRMM
+// xSYMM / xHEMM (side 1, uplo 2, m 3, n 4, lda 7, ldb 9, ldc 12)
+extern "C" int gbx_check_symm_args(char side, char uplo, int m, int n, int lda, int ldb, int ldc)
+{
+    const int nrowa = gbx_lsame(side, 'L') ? m : n;
+    if (!gbx_lsame(side, 'L') && !gbx_lsame(side, 'R')) return 1;
+    if (!gbx_lsame(uplo, 'U') && !gbx_lsame(uplo, 'L')) return 2;
+    if (m < 0) return 3;
+    if (n < 0) return 4;
+    if (lda < std::max(1, nrowa)) return 7;
+    if (ldb < std::max(1, m)) return 9;
+    if (ldc < std::max(1, m)) return 12;
+    return 0;
+}
+
+// ------------------------------------------------------ triangular operands
 // Effective triangle of op(A): transposing swaps lower and upper.
 extern "C" int gbx_op_tri(char uplo, char transa, char diag)
 {
@@ -214,35 +210,3 @@ extern "C" int gbx_op_tri(char uplo, char transa, char diag)
     return t;
 }
 
-extern "C" gbx_status gbx_dtrmm(gbx_ctx *ctx, char side, char uplo, char ta, char diag, int m,
-                                int n, double alpha, const double *A, int lda, double *B, int ldb)
-{
-    if (!ctx) return GBX_ERR_ARG;
-    int info = gbx_check_trxm_args(side, uplo, ta, diag, m, n, lda, ldb);
-    if (info) return gbx_fail(ctx, GBX_ERR_ARG, "DTRMM parameter %d", info);
-    if (m == 0 || n == 0) return GBX_OK;
-    if (alpha == 0.0) return scale_matrix<double>(ctx, m, n, 0.0, B, ldb, C_FULL);
-    // The product is formed out of place: B is copied to workspace first.
-    double *Bc;
-    gbx_status st = gbx_ws(ctx, 0, sizeof(double) * (size_t)m * n, (void **)&Bc);
-    if (st != GBX_OK) return st;
-    cudaError_t e = cudaMemcpy2DAsync(Bc, sizeof(double) * (size_t)m, B, sizeof(double) * (size_t)ldb,
-                                      sizeof(double) * (size_t)m, n, cudaMemcpyDeviceToDevice, S(ctx));
-    if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "dtrmm copy: %s", cudaGetErrorString(e));
-    const int tri = gbx_op_tri(uplo, ta, diag);
-    const bool tr = !gbx_lsame(ta, 'N');
-    GemmArgs<double> p{};
-    p.m = m; p.n = n;
-    p.alpha = alpha; p.beta = 0.0;
-    p.C = B; p.ldc = ldb;
-    if (gbx_lsame(side, 'L')) {
-        p.k = m;
-        p.A = A; p.lda = lda; p.ta = tr; p.tri_a = tri;
-        p.B = Bc; p.ldb = m; p.tb = 0;
-    } else {
-        p.k = n;
-        p.A = Bc; p.lda = m; p.ta = 0;
-        p.B = A; p.ldb = lda; p.tb = tr; p.tri_b = tri;
-    }
-    return launch_gemm<double>(ctx, p, "dtrmm");
-}

@@ -8,13 +8,8 @@
 namespace gbx_gemm {
 template <typename T>
 gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what);
+// C = beta * C on the whole matrix or one triangle (beta == 0 sets zero);
+// herm: the diagonal's imaginary part is set to zero (Hermitian C).
 template <typename T>
-gbx_status scale_matrix(gbx_ctx *ctx, int m, int n, T beta, T *C, long long ldc, int part);
+gbx_status scale_matrix(gbx_ctx *ctx, int m, int n, T beta, T *C, long long ldc, int part, int herm = 0);
 }  // namespace gbx_gemm
-
-extern "C" {
-int gbx_check_gemm_args(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc);
-int gbx_check_syrk_args(char uplo, char trans, int n, int k, int lda, int ldc);
-int gbx_check_trxm_args(char side, char uplo, char ta, char diag, int m, int n, int lda, int ldb);
-int gbx_op_tri(char uplo, char transa, char diag);
-}

@@ -1,4 +1,5 @@
-// gemm_simt.cuh — FP64 / complex-FP64 GEMM core on the FP64 FMA pipe.
+// gemm_simt.cuh — GEMM core on the SIMT FMA pipes, for the four BLAS
+// element types (float, double, complex float, complex double).
 //
 // Measured on GB300: SIMT DFMA sustains about 1.2 TFLOP/s per GPU, the legacy
 // FP64 tensor path (mma.sync.m8n8k4.f64) about 1.05 TFLOP/s, so the plain
@@ -8,8 +9,9 @@
 // staging through shared memory with register prefetch is all the memory
 // pipeline needs.
 //
-// One kernel template serves DGEMM, ZGEMM, DSYRK (triangular tile grid),
-// DTRMM (triangular operand masking) and the DTRSM updates.
+// One kernel template serves xGEMM, xSYRK/xHERK and xSYR2K/xHER2K (triangular
+// tile grid), xSYMM/xHEMM (an operand read from one stored triangle), xTRMM
+// (triangular operand masking) and the xTRSM updates, for S, D, C and Z.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -18,6 +20,21 @@
 namespace gbx_gemm {
 
 struct dcplx { double x, y; };
+struct fcplx { float x, y; };
+
+// Complex quotient a / b by Smith's algorithm (R. L. Smith, "Algorithm 116:
+// Complex division", CACM 5(8), 1962): scales by the larger component of b
+// so that no intermediate overflows where the quotient does not.
+template <typename C, typename R>
+__device__ __forceinline__ C smith_div(C a, C b)
+{
+    if (fabs(b.y) <= fabs(b.x)) {
+        const R r = b.y / b.x, d = b.x + b.y * r;
+        return {(a.x + a.y * r) / d, (a.y - a.x * r) / d};
+    }
+    const R r = b.x / b.y, d = b.y + b.x * r;
+    return {(a.x * r + a.y) / d, (a.y * r - a.x) / d};
+}
 
 template <typename T> struct Ops;
 template <> struct Ops<double> {
@@ -27,7 +44,43 @@ template <> struct Ops<double> {
     static __device__ __forceinline__ double conj(double a) { return a; }
     static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
     static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    static __device__ __forceinline__ double neg(double a) { return -a; }
+    static __device__ __forceinline__ double real_only(double a) { return a; }
     static __device__ __forceinline__ bool is_zero(double a) { return a == 0.0; }
+};
+template <> struct Ops<float> {
+    static __device__ __forceinline__ float zero() { return 0.0f; }
+    static __device__ __forceinline__ float one() { return 1.0f; }
+    static __device__ __forceinline__ void fma_acc(float &acc, float a, float b) { acc = fmaf(a, b, acc); }
+    static __device__ __forceinline__ float conj(float a) { return a; }
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+    static __device__ __forceinline__ float neg(float a) { return -a; }
+    static __device__ __forceinline__ float real_only(float a) { return a; }
+    static __device__ __forceinline__ bool is_zero(float a) { return a == 0.0f; }
+};
+template <> struct Ops<fcplx> {
+    static __device__ __forceinline__ fcplx zero() { return {0.0f, 0.0f}; }
+    static __device__ __forceinline__ fcplx one() { return {1.0f, 0.0f}; }
+    static __device__ __forceinline__ void fma_acc(fcplx &acc, fcplx a, fcplx b)
+    {
+        acc.x = fmaf(a.x, b.x, acc.x);
+        acc.x = fmaf(-a.y, b.y, acc.x);
+        acc.y = fmaf(a.x, b.y, acc.y);
+        acc.y = fmaf(a.y, b.x, acc.y);
+    }
+    static __device__ __forceinline__ fcplx conj(fcplx a) { return {a.x, -a.y}; }
+    static __device__ __forceinline__ fcplx mul(fcplx a, fcplx b)
+    {
+        return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+    }
+    static __device__ __forceinline__ fcplx add(fcplx a, fcplx b) { return {a.x + b.x, a.y + b.y}; }
+    static __device__ __forceinline__ fcplx div(fcplx a, fcplx b) { return smith_div<fcplx, float>(a, b); }
+    static __device__ __forceinline__ fcplx neg(fcplx a) { return {-a.x, -a.y}; }
+    static __device__ __forceinline__ fcplx real_only(fcplx a) { return {a.x, 0.0f}; }
+    static __device__ __forceinline__ bool is_zero(fcplx a) { return a.x == 0.0f && a.y == 0.0f; }
 };
 template <> struct Ops<dcplx> {
     static __device__ __forceinline__ dcplx zero() { return {0.0, 0.0}; }
@@ -45,6 +98,9 @@ template <> struct Ops<dcplx> {
         return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
     }
     static __device__ __forceinline__ dcplx add(dcplx a, dcplx b) { return {a.x + b.x, a.y + b.y}; }
+    static __device__ __forceinline__ dcplx div(dcplx a, dcplx b) { return smith_div<dcplx, double>(a, b); }
+    static __device__ __forceinline__ dcplx neg(dcplx a) { return {-a.x, -a.y}; }
+    static __device__ __forceinline__ dcplx real_only(dcplx a) { return {a.x, 0.0}; }
     static __device__ __forceinline__ bool is_zero(dcplx a) { return a.x == 0.0 && a.y == 0.0; }
 };
 
@@ -53,6 +109,10 @@ template <> struct Ops<dcplx> {
 enum { TRI_NONE = 0, TRI_LOWER = 1, TRI_UPPER = 2, TRI_UNIT = 4 };
 // Which part of C is written.
 enum { C_FULL = 0, C_LOWER = 1, C_UPPER = 2 };
+// Symmetric / Hermitian operand (xSYMM, xHEMM): which triangle is stored;
+// the other is read from its mirror (conjugated for Hermitian, whose
+// diagonal is taken as real).
+enum { SYM_NONE = 0, SYM_LOWER = 1, SYM_UPPER = 2, SYM_HERM = 4 };
 
 template <typename T>
 struct GemmArgs {
@@ -62,7 +122,9 @@ struct GemmArgs {
     T alpha, beta;
     T *C; long long ldc;
     int tri_a, tri_b;   // triangular masks of op(A) (m x m) / op(B) (n x n)
+    int sym_a, sym_b;   // symmetric / Hermitian operand (square; op() ignored)
     int c_part;         // C_FULL / C_LOWER / C_UPPER (symmetric rank-k update)
+    int c_herm;         // Hermitian C: the diagonal's imaginary part is set to zero
     int tiles_m, tiles_n;
 };
 
@@ -78,7 +140,7 @@ struct PanelLoader {
 
     __device__ __forceinline__ void load(const T *__restrict__ X, long long ld, bool contig_mn,
                                          int mn0, int mn_lim, int k0, int k_lim, int conj, int tri,
-                                         bool is_a)
+                                         bool is_a, int sym)
     {
 #pragma unroll
         for (int q = 0; q < PER; q++) {
@@ -88,7 +150,17 @@ struct PanelLoader {
             else           { kk = idx % BK; mn = idx / BK; }
             const int gm = mn0 + mn, gk = k0 + kk;
             T v = Ops<T>::zero();
-            if (gm < mn_lim && gk < k_lim) {
+            if (sym) {
+                if (gm < mn_lim && gk < k_lim) {
+                    const int row = is_a ? gm : gk, col = is_a ? gk : gm;
+                    const bool stored = (sym & SYM_LOWER) ? row >= col : row <= col;
+                    v = stored ? X[(long long)col * ld + row] : X[(long long)row * ld + col];
+                    if (sym & SYM_HERM) {
+                        if (!stored) v = Ops<T>::conj(v);
+                        if (row == col) v = Ops<T>::real_only(v);
+                    }
+                }
+            } else if (gm < mn_lim && gk < k_lim) {
                 bool keep = true, unit_diag = false;
                 if (tri) {
                     // element of op(X) at (row, col): for A rows are mn, for B rows are k
@@ -169,8 +241,8 @@ gemm_simt_kernel(GemmArgs<T> p)
     PanelLoader<T, BN, BK> lb;
     int cur = 0;
     if (kbeg < kend) {
-        la.load(p.A, p.lda, a_contig_mn, m0, p.m, kbeg, p.k, p.conja, p.tri_a, true);
-        lb.load(p.B, p.ldb, b_contig_mn, n0, p.n, kbeg, p.k, p.conjb, p.tri_b, false);
+        la.load(p.A, p.lda, a_contig_mn, m0, p.m, kbeg, p.k, p.conja, p.tri_a, true, p.sym_a);
+        lb.load(p.B, p.ldb, b_contig_mn, n0, p.n, kbeg, p.k, p.conjb, p.tri_b, false, p.sym_b);
         la.store(As[0], a_contig_mn);
         lb.store(Bs[0], b_contig_mn);
     }
@@ -179,8 +251,8 @@ gemm_simt_kernel(GemmArgs<T> p)
     for (int k0 = kbeg; k0 < kend; k0 += BK) {
         const bool more = k0 + BK < kend;
         if (more) {
-            la.load(p.A, p.lda, a_contig_mn, m0, p.m, k0 + BK, p.k, p.conja, p.tri_a, true);
-            lb.load(p.B, p.ldb, b_contig_mn, n0, p.n, k0 + BK, p.k, p.conjb, p.tri_b, false);
+            la.load(p.A, p.lda, a_contig_mn, m0, p.m, k0 + BK, p.k, p.conja, p.tri_a, true, p.sym_a);
+            lb.load(p.B, p.ldb, b_contig_mn, n0, p.n, k0 + BK, p.k, p.conjb, p.tri_b, false, p.sym_b);
         }
 #pragma unroll
         for (int kk = 0; kk < BK; kk++) {
@@ -223,6 +295,7 @@ gemm_simt_kernel(GemmArgs<T> p)
             T *cp = p.C + (long long)col * p.ldc + row;
             T v = Ops<T>::mul(p.alpha, acc[i][j]);
             if (!beta0) v = Ops<T>::add(v, Ops<T>::mul(p.beta, *cp));
+            if (p.c_herm && row == col) v = Ops<T>::real_only(v);
             *cp = v;
         }
     }

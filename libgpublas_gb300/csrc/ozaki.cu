@@ -88,9 +88,13 @@ __device__ __forceinline__ double src_get(const SrcView &v, int r, int k)
 // estimate built from the exponent and top mantissa bits.
 constexpr int OZ_NONFINITE = 5;   // status word: an operand holds Inf/NaN
 
+// Bit pattern of |x|, taken in PTX: integer tests on a double's bits written
+// in C are folded back into FP64 compares, one FP64-pipe slot per element.
 __device__ __forceinline__ unsigned long long abs_bits(double x)
 {
-    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    unsigned long long b;
+    asm("and.b64 %0, %1, 0x7FFFFFFFFFFFFFFF;" : "=l"(b) : "l"(__double_as_longlong(x)));
+    return b;
 }
 
 // frexp exponent e (|x| < 2^e, |x| >= 2^(e-1)) of a finite |x| bit pattern.
@@ -173,12 +177,12 @@ oz_stats_rowk(SrcView v, int rows, int K, int *__restrict__ expo, double *__rest
 constexpr int OZ_STATS_KCH = 1024;
 
 __global__ void __launch_bounds__(256)
-oz_stats_colk(SrcView v, int rows, int K, SsAcc *__restrict__ part, int *status)
+oz_stats_colk(SrcView v, int rows, int K, int kch, SsAcc *__restrict__ part, int *status)
 {
     __shared__ SsAcc s_acc[8][32];
     const int rr = threadIdx.x & 31, kl = threadIdx.x >> 5;
     const int r = blockIdx.x * 32 + rr;
-    const int k0 = blockIdx.y * OZ_STATS_KCH, k1 = min(K, k0 + OZ_STATS_KCH);
+    const int k0 = blockIdx.y * kch, k1 = min(K, k0 + kch);
     SsAcc a;
     a.init();
     if (r < rows)
@@ -216,35 +220,40 @@ __device__ __forceinline__ uint32_t e4m3_of_digit(int d)
 }
 
 // Writes S digit planes X8[s][r][k] (K-major, rows padded to Rp, k to Kp)
-// for 16 consecutive k per thread.  Padding gets digit 0.  A 32-row x 128-k
-// tile is staged through shared memory so col_k sources are read coalesced.
+// for OZ_SPLIT_PER consecutive k per thread.  Padding gets digit 0.  A
+// 16-row x 128-k tile is staged through shared memory so col_k sources are
+// read coalesced (16 rows and 8 k per thread keep enough blocks in flight
+// for the small-K products of blocked factorizations).
+constexpr int OZ_SPLIT_ROWS = 16, OZ_SPLIT_PER = 8;
+
 __global__ void __launch_bounds__(256)
 oz_split(SrcView v, int rows, int K, int Rp, int Kp, const int *__restrict__ expo,
          const int *__restrict__ S_dev, uint8_t *__restrict__ X8)
 {
-    __shared__ double tile[32][129];
-    const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 128;
+    __shared__ double tile[OZ_SPLIT_ROWS][129];
+    const int r0 = blockIdx.y * OZ_SPLIT_ROWS, k0 = blockIdx.x * 128;
     const int S = *S_dev;
     // load: col_k -> threads along rows; row_k -> threads along k
-    for (int t = threadIdx.x; t < 32 * 128; t += blockDim.x) {
+    for (int t = threadIdx.x; t < OZ_SPLIT_ROWS * 128; t += blockDim.x) {
         int rr, kk;
         if (v.row_k) { kk = t & 127; rr = t >> 7; }
-        else         { rr = t & 31; kk = t >> 5; }
+        else         { rr = t % OZ_SPLIT_ROWS; kk = t / OZ_SPLIT_ROWS; }
         const int r = r0 + rr, k = k0 + kk;
         tile[rr][kk] = (r < rows && k < K) ? src_get(v, r, k) : 0.0;
     }
     __syncthreads();
-    const int rr = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 16;
+    constexpr int TPR = 128 / OZ_SPLIT_PER;   // threads per row
+    const int rr = threadIdx.x / TPR, kq = (threadIdx.x % TPR) * OZ_SPLIT_PER;
     const int r = r0 + rr;
     if (r >= Rp) return;
     const int e = r < rows ? expo[r] : 0;
     // N_j = round(|x_j| * 2^(4 - e + 5(S-1))) as a 128-bit integer hi:lo.
     // |x| < 2^e bounds N_j by 16 * 32^(S-1) <= 2^69.  Integer pipe only.
     const int top = 4 - e + 5 * (S - 1);
-    unsigned long long lo[16], hi[16];
+    unsigned long long lo[OZ_SPLIT_PER], hi[OZ_SPLIT_PER];
     unsigned neg = 0u;
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
+    for (int j = 0; j < OZ_SPLIT_PER; j++) {
         const unsigned long long b = (unsigned long long)__double_as_longlong(tile[rr][kq + j]);
         neg |= (unsigned)(b >> 63) << j;
         const int E = (int)((b >> 52) & 0x7FF);
@@ -258,9 +267,9 @@ oz_split(SrcView v, int rows, int K, int Rp, int Kp, const int *__restrict__ exp
     }
     // balanced base-32 digits, least significant first: d in [-15, 16]
     for (int s = S - 1; s >= 0; s--) {
-        uint32_t w[4] = {0u, 0u, 0u, 0u};
+        uint32_t w[OZ_SPLIT_PER / 4] = {};
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
+        for (int j = 0; j < OZ_SPLIT_PER; j++) {
             int d = (int)(lo[j] & 31ull);
             if (d > 16) {
                 d -= 32;
@@ -275,8 +284,8 @@ oz_split(SrcView v, int rows, int K, int Rp, int Kp, const int *__restrict__ exp
             const int sd = ((neg >> j) & 1u) ? -d : d;
             w[j >> 2] |= e4m3_of_digit(sd) << (8 * (j & 3));
         }
-        uint4 *dst = (uint4 *)(X8 + ((size_t)s * Rp + r) * Kp + k0 + kq);
-        *dst = make_uint4(w[0], w[1], w[2], w[3]);
+        uint2 *dst = (uint2 *)(X8 + ((size_t)s * Rp + r) * Kp + k0 + kq);
+        *dst = make_uint2(w[0], w[1]);
     }
 }
 
@@ -305,36 +314,50 @@ __device__ __forceinline__ double scaled_acc(uint32_t fb, int shift)
 // Slice count: relative Frobenius error ~ c * 2^(-5S) * gamma_A * gamma_B with
 // gamma^2 = (sum_i 2^(2 e_i)) / (sum_i 2^(2 e_i) * ss_i / K): the ratio of the
 // squared row maxima to the squared row norms (1 <= gamma <= sqrt(K)).
+// Block-wide reductions for the 256-thread slice-count kernel (fixed order,
+// so the result is deterministic); every thread gets the result.
+__device__ __forceinline__ int oz_block_max(int v)
+{
+    __shared__ int s[8];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = s[0];
+#pragma unroll
+    for (int i = 1; i < 8; i++) v = max(v, s[i]);
+    __syncthreads();
+    return v;
+}
+
+__device__ __forceinline__ double oz_block_sum(double v)
+{
+    __shared__ double s[8];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+    __syncthreads();
+    return v;
+}
+
 __device__ double oz_log2_gamma(const int *expo, const double *ss, int rows, int K)
 {
-    __shared__ double s_num[256], s_den[256];
-    __shared__ int s_emax[256];
     int emax = -100000;
     for (int i = threadIdx.x; i < rows; i += blockDim.x) emax = max(emax, expo[i]);
-    s_emax[threadIdx.x] = emax;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int i = 1; i < (int)blockDim.x; i++) emax = max(emax, s_emax[i]);
-        s_emax[0] = emax;
-    }
-    __syncthreads();
-    emax = s_emax[0];
+    emax = oz_block_max(emax);
     double num = 0.0, den = 0.0;
     for (int i = threadIdx.x; i < rows; i += blockDim.x) {
-        const double w = ldexp(1.0, 2 * (expo[i] - emax));
+        // 2^(2(e_i - emax)) from the exponent field (0 below the normal range)
+        const int d = 2 * (expo[i] - emax);
+        const double w = d < -1022 ? 0.0 : __longlong_as_double((long long)(1023 + d) << 52);
         num += w;
         den += w * ss[i];
     }
-    s_num[threadIdx.x] = num;
-    s_den[threadIdx.x] = den;
-    __syncthreads();
-    __shared__ double res;
-    if (threadIdx.x == 0) {
-        for (int i = 1; i < (int)blockDim.x; i++) { num += s_num[i]; den += s_den[i]; }
-        res = den > 0.0 ? 0.5 * log2(num * (double)K / den) : 0.0;
-    }
-    __syncthreads();
-    return res;
+    num = oz_block_sum(num);
+    den = oz_block_sum(den);
+    return den > 0.0 ? 0.5 * log2(num * (double)K / den) : 0.0;
 }
 
 __global__ void __launch_bounds__(256)
@@ -395,6 +418,77 @@ __device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, i
     if (p.c_part == 0) return true;
     const int r0 = tm * bm, r1 = r0 + bm - 1, c0 = tn * OZ_BN, c1 = c0 + OZ_BN - 1;
     return p.c_part == 1 ? (r1 >= c0) : (r0 <= c1);
+}
+
+// Drain one diagonal's accumulator for one row (row grow, the tile's OZ_BN
+// columns from gcol0) into the running sum W, or on the last pass into C.
+// The row is walked in 16-column chunks, software-pipelined: the global
+// loads of chunk c+1 (running sums, and C on the last pass) are issued
+// before chunk c is converted and stored.  Loads and stores are never
+// interleaved element by element: the compiler cannot prove that W and C do
+// not overlap, and a load/add/store per element serialised one L2 round trip
+// per element (that, not the MMAs, was the cost of a small-K product).
+__device__ __forceinline__ bool oz_c_keep(const OzParams &p, int grow, int gcol)
+{
+    return gcol < p.N && (p.c_part == 0 || (p.c_part == 1 ? grow >= gcol : grow <= gcol));
+}
+
+__device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, int grow, int gcol0, int rs,
+                                             bool first, bool last)
+{
+    constexpr int CH = 16, NCH = OZ_BN / CH;
+    const bool row_ok = grow < p.M;
+    const bool need_c = last && row_ok && p.beta != 0.0;
+    const double *wrow = p.W + (size_t)gcol0 * p.Mp + grow;
+    double *crow = p.C + (size_t)gcol0 * p.ldc + grow;
+    double wn[CH], cn[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) { wn[j] = 0.0; cn[j] = 0.0; }
+    if (!first) {
+#pragma unroll
+        for (int j = 0; j < CH; j++) wn[j] = __ldcg(wrow + (size_t)j * p.Mp);
+    }
+    if (need_c) {
+#pragma unroll
+        for (int j = 0; j < CH; j++) cn[j] = oz_c_keep(p, grow, gcol0 + j) ? crow[(size_t)j * p.ldc] : 0.0;
+    }
+#pragma unroll 1
+    for (int c = 0; c < NCH; c++) {
+        double wc[CH], cc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) { wc[j] = wn[j]; cc[j] = cn[j]; }
+        const int nc = (c + 1) * CH;
+        if (c + 1 < NCH) {
+            if (!first) {
+#pragma unroll
+                for (int j = 0; j < CH; j++) wn[j] = __ldcg(wrow + (size_t)(nc + j) * p.Mp);
+            }
+            if (need_c) {
+#pragma unroll
+                for (int j = 0; j < CH; j++)
+                    cn[j] = oz_c_keep(p, grow, gcol0 + nc + j) ? crow[(size_t)(nc + j) * p.ldc] : 0.0;
+            }
+        }
+        uint32_t r[CH];
+        tmem_ld_32x32b_x16(taddr + (uint32_t)(c * CH), r);
+        tmem_ld_wait();
+        const int cb = c * CH;
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            const double v = scaled_acc(r[j], rs + __ldg(p.col_exp + gcol0 + cb + j));
+            wc[j] = first ? v : wc[j] + v;
+        }
+        if (!last) {
+#pragma unroll
+            for (int j = 0; j < CH; j++) __stcg(p.W + (size_t)(gcol0 + cb + j) * p.Mp + grow, wc[j]);
+        } else if (row_ok) {
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                if (!oz_c_keep(p, grow, gcol0 + cb + j)) continue;
+                crow[(size_t)(cb + j) * p.ldc] = need_c ? fma(p.alpha, wc[j], p.beta * cc[j]) : p.alpha * wc[j];
+            }
+        }
+    }
 }
 
 __global__ void __launch_bounds__(OZ_THREADS, 1)
@@ -530,27 +624,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                     if (!ok) break;
                     tc_fence_after();
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * OZ_BN);
-                    for (int c = 0; c < OZ_BN / 32; c++) {
-                        uint32_t r[32];
-                        tmem_ld_32x32b_x32(taddr + c * 32, r);
-                        tmem_ld_wait();
-#pragma unroll
-                        for (int j = 0; j < 32; j++) {
-                            const int gcol = tn * OZ_BN + c * 32 + j;
-                            const double v = scaled_acc(r[j], rs + p.col_exp[gcol]);
-                            double *w = p.W + (size_t)gcol * p.Mp + grow;
-                            if (!last) {
-                                *w = first ? v : *w + v;
-                            } else {
-                                const double tot = first ? v : *w + v;
-                                if (grow < p.M && gcol < p.N &&
-                                    (p.c_part == 0 || (p.c_part == 1 ? grow >= gcol : grow <= gcol))) {
-                                    double *cp = p.C + (size_t)gcol * p.ldc + grow;
-                                    *cp = (p.beta == 0.0) ? p.alpha * tot : fma(p.alpha, tot, p.beta * *cp);
-                                }
-                            }
-                        }
-                    }
+                    oz_drain_row(p, taddr, grow, tn * OZ_BN, rs, first, last);
                     tc_fence_before();
                     mbar_arrive(&tempty[buf]);
                     first = false;
@@ -728,27 +802,7 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
                     if (!ok) break;
                     tc_fence_after();
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * OZ_BN);
-                    for (int c = 0; c < OZ_BN / 32; c++) {
-                        uint32_t r[32];
-                        tmem_ld_32x32b_x32(taddr + c * 32, r);
-                        tmem_ld_wait();
-#pragma unroll
-                        for (int j = 0; j < 32; j++) {
-                            const int gcol = tn * OZ_BN + c * 32 + j;
-                            const double v = scaled_acc(r[j], rs + p.col_exp[gcol]);
-                            double *w = p.W + (size_t)gcol * p.Mp + grow;
-                            if (!last) {
-                                *w = first ? v : *w + v;
-                            } else {
-                                const double tot = first ? v : *w + v;
-                                if (grow < p.M && gcol < p.N &&
-                                    (p.c_part == 0 || (p.c_part == 1 ? grow >= gcol : grow <= gcol))) {
-                                    double *cp = p.C + (size_t)gcol * p.ldc + grow;
-                                    *cp = (p.beta == 0.0) ? p.alpha * tot : fma(p.alpha, tot, p.beta * *cp);
-                                }
-                            }
-                        }
-                    }
+                    oz_drain_row(p, taddr, grow, tn * OZ_BN, rs, first, last);
                     tc_fence_before();
                     mbar_arrive_cluster(buf ? tempty_cl1 : tempty_cl0);
                     first = false;
@@ -879,12 +933,17 @@ gbx_status split_operand(gbx_ctx *ctx, const SrcView &v, int rows, int K, int Rp
             oz_stats_rowk<<<(rows * 32 + 255) / 256, 256, 0, s>>>(v, rows, K, expo, ss, status);
             gbx_count_launch(ctx, 1);
         } else {
-            const int nkb = (K + OZ_STATS_KCH - 1) / OZ_STATS_KCH;
+            // K chunk per block: at most OZ_STATS_KCH, smaller when the row
+            // blocks alone would leave SMs idle
+            int kch = OZ_STATS_KCH;
+            const long long rblocks = (rows + 31) / 32;
+            while (kch > 64 && rblocks * ((K + kch - 1) / kch) < 2LL * gbx_ctx_sms(ctx)) kch >>= 1;
+            const int nkb = (K + kch - 1) / kch;
             void *p;
             gbx_status st = gbx_ws(ctx, GBX_WS_TMP2, sizeof(SsAcc) * (size_t)nkb * rows, &p);
             if (st != GBX_OK) return st;
-            dim3 g((rows + 31) / 32, nkb);
-            oz_stats_colk<<<g, 256, 0, s>>>(v, rows, K, (SsAcc *)p, status);
+            dim3 g((unsigned)rblocks, nkb);
+            oz_stats_colk<<<g, 256, 0, s>>>(v, rows, K, kch, (SsAcc *)p, status);
             oz_stats_combine<<<std::min(1024, (rows + 255) / 256), 256, 0, s>>>((const SsAcc *)p, rows, nkb,
                                                                                 expo, ss);
             gbx_count_launch(ctx, 2);
@@ -893,7 +952,7 @@ gbx_status split_operand(gbx_ctx *ctx, const SrcView &v, int rows, int K, int Rp
         gbx_count_launch(ctx, 1);
         return gbx_check_launch(ctx, "ozaki stats");
     }
-    dim3 g(Kp / 128, Rp / 32);
+    dim3 g(Kp / 128, Rp / OZ_SPLIT_ROWS);
     oz_split<<<g, 256, 0, s>>>(v, rows, K, Rp, Kp, expo, S_dev, X8);
     gbx_count_launch(ctx, 1);
     return gbx_check_launch(ctx, "ozaki split");

@@ -1,15 +1,18 @@
-// trsm.cu — gbx_dtrsm: triangular solve with many right-hand sides.
+// trsm.cu — xTRSM (S, D, C, Z): triangular solve with many right-hand sides.
 //
-// Replaces cublasDtrsm behind the reference's wrapper (blas_level3/trsm.cc:
-// 40-73 launch, 76-132 argument checks; that file does not compile as shipped,
-// trsm.cc:55).  Recursive blocked algorithm:
-//   * all diagonal blocks of op(A) (64 x 64) are inverted in FP64 by one
-//     launch (one CTA per block, forward/back substitution against I);
+// Replaces cublas?trsm behind the reference's wrapper (blas_level3/trsm.cc:
+// 40-73 launch, 76-132 argument checks, 134-213 the four precisions; that
+// file does not compile as shipped, trsm.cc:55).  Recursive blocked
+// algorithm:
+//   * all diagonal blocks of op(A) (64 x 64) are inverted by one launch (one
+//     CTA per block, forward/back substitution against I, in the routine's
+//     own precision);
 //   * the solve recurses on halves: solve the leading half, update the
-//     trailing half with one large GEMM (k = half the order) on the DFMA GEMM
+//     trailing half with one large GEMM (k = half the order) on the SIMT GEMM
 //     core, solve the trailing half.  Leaves multiply by the inverted block.
 // The GEMM updates dominate (m^2*nrhs flops overall); the inverted-block leaves
-// add 2*64^2*nrhs flops per block (about 3% at m = 8192).
+// add 2*64^2*nrhs flops per block (about 3% at m = 8192).  op(A) = A^H
+// (transa 'C') conjugates the inverted blocks and the GEMM operands.
 #include "gbx_internal.h"
 #include "gemm_host.h"
 
@@ -24,27 +27,38 @@ constexpr int NB = 64;
 
 inline cudaStream_t S(gbx_ctx *ctx) { return (cudaStream_t)gbx_ctx_get_stream(ctx); }
 
+template <typename T> T unit_of(int v) { return T(v); }
+template <> fcplx unit_of<fcplx>(int v) { return {(float)v, 0.0f}; }
+template <> dcplx unit_of<dcplx>(int v) { return {(double)v, 0.0}; }
+
 // Inverse of each NB x NB diagonal block of op(A) (na x na).  Blocks shorter
 // than NB at the end are padded with the identity.  Inv holds the blocks one
-// after another, each column-major with leading dimension NB.
+// after another, each column-major with leading dimension NB.  One CTA of NB
+// threads per block, one column of the inverse per thread, in the routine's
+// precision; the divisions are the element type's own (IEEE for real,
+// Smith's algorithm for complex).
+template <typename T>
 __global__ void __launch_bounds__(NB)
-trinv_blocks(int na, const double *__restrict__ A, long long lda, int tr, int lower, int unit,
-             double *__restrict__ Inv)
+trinv_blocks(int na, const T *__restrict__ A, long long lda, int tr, int cj, int lower, int unit,
+             T *__restrict__ Inv)
 {
-    extern __shared__ double sm[];
-    double *L = sm;                   // L[i*(NB+1) + k] = op(A)(r0+i, r0+k)
-    double *X = sm + NB * (NB + 1);   // X[i*NB + j]
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T *L = (T *)sm_raw;               // L[i*(NB+1) + k] = op(A)(r0+i, r0+k)
+    T *X = L + NB * (NB + 1);         // X[i*NB + j]
     const int r0 = blockIdx.x * NB;
     const int nbb = min(NB, na - r0);
     for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
         const int i = t % NB, k = t / NB;
-        double v = 0.0;
+        T v = Ops<T>::zero();
         if (i < nbb && k < nbb) {
             const bool in = lower ? (k <= i) : (k >= i);
-            if (in) v = tr ? A[(long long)(r0 + i) * lda + r0 + k] : A[(long long)(r0 + k) * lda + r0 + i];
-            if (i == k && unit) v = 1.0;
+            if (in) {
+                v = tr ? A[(long long)(r0 + i) * lda + r0 + k] : A[(long long)(r0 + k) * lda + r0 + i];
+                if (cj) v = Ops<T>::conj(v);
+            }
+            if (i == k && unit) v = Ops<T>::one();
         } else if (i == k) {
-            v = 1.0;
+            v = Ops<T>::one();
         }
         L[i * (NB + 1) + k] = v;
     }
@@ -52,57 +66,64 @@ trinv_blocks(int na, const double *__restrict__ A, long long lda, int tr, int lo
     const int j = threadIdx.x;   // this thread owns column j of the inverse
     if (lower) {
         for (int i = 0; i < NB; i++) {
-            double s = (i == j) ? 1.0 : 0.0;
-            for (int k = 0; k < i; k++) s = fma(-L[i * (NB + 1) + k], X[k * NB + j], s);
-            X[i * NB + j] = s / L[i * (NB + 1) + i];
+            T s = (i == j) ? Ops<T>::one() : Ops<T>::zero();
+            for (int k = 0; k < i; k++) Ops<T>::fma_acc(s, Ops<T>::neg(L[i * (NB + 1) + k]), X[k * NB + j]);
+            X[i * NB + j] = Ops<T>::div(s, L[i * (NB + 1) + i]);
         }
     } else {
         for (int i = NB - 1; i >= 0; i--) {
-            double s = (i == j) ? 1.0 : 0.0;
-            for (int k = i + 1; k < NB; k++) s = fma(-L[i * (NB + 1) + k], X[k * NB + j], s);
-            X[i * NB + j] = s / L[i * (NB + 1) + i];
+            T s = (i == j) ? Ops<T>::one() : Ops<T>::zero();
+            for (int k = i + 1; k < NB; k++) Ops<T>::fma_acc(s, Ops<T>::neg(L[i * (NB + 1) + k]), X[k * NB + j]);
+            X[i * NB + j] = Ops<T>::div(s, L[i * (NB + 1) + i]);
         }
     }
-    double *out = Inv + (long long)blockIdx.x * NB * NB;
+    T *out = Inv + (long long)blockIdx.x * NB * NB;
     for (int i = 0; i < NB; i++) out[(long long)j * NB + i] = X[i * NB + j];
 }
 
+template <typename T>
 struct Trsm {
     gbx_ctx *ctx;
+    const char *nm;
     int m, n, na;
-    const double *A;
+    const T *A;
     long long lda;
-    int tr, lower;
-    double *B;
+    int tr, cj, lower;
+    T *B;
     long long ldb;
-    const double *Inv;
-    double *T;   // NB x n (left) or m x NB (right)
+    const T *Inv;
+    T *Tw;   // NB x n (left) or m x NB (right)
 
     // op(A)[r0:, c0:] as a GEMM operand: pointer and transposition flag
-    const double *opA(int r0, int c0, int &t) const
+    const T *opA(int r0, int c0, int &t) const
     {
         t = tr;
         return tr ? A + (long long)r0 * lda + c0 : A + (long long)c0 * lda + r0;
     }
 
-    gbx_status gemm(int mm, int nn, int kk, double alpha, const double *Ap, long long lda_, int ta,
-                    const double *Bp, long long ldb_, int tb, double beta, double *Cp, long long ldc)
+    // C = alpha op(X) op(Y) + beta C; conj_x / conj_y conjugate the operand
+    // (the slices of op(A) = A^H)
+    gbx_status gemm(int mm, int nn, int kk, T alpha, const T *Ap, long long lda_, int ta, int ca, const T *Bp,
+                    long long ldb_, int tb, int cb, T beta, T *Cp, long long ldc)
     {
-        GemmArgs<double> p{};
+        GemmArgs<T> p{};
         p.m = mm; p.n = nn; p.k = kk;
-        p.A = Ap; p.lda = lda_; p.ta = ta;
-        p.B = Bp; p.ldb = ldb_; p.tb = tb;
+        p.A = Ap; p.lda = lda_; p.ta = ta; p.conja = ca;
+        p.B = Bp; p.ldb = ldb_; p.tb = tb; p.conjb = cb;
         p.alpha = alpha; p.beta = beta;
         p.C = Cp; p.ldc = ldc;
-        return launch_gemm<double>(ctx, p, "dtrsm");
+        return launch_gemm<T>(ctx, p, nm);
     }
 
-    gbx_status copy_back(double *dst, long long ldd, const double *src, long long lds, int rows, int cols)
+    gbx_status copy_back(T *dst, long long ldd, const T *src, long long lds, int rows, int cols)
     {
-        cudaError_t e = cudaMemcpy2DAsync(dst, sizeof(double) * ldd, src, sizeof(double) * lds,
-                                          sizeof(double) * rows, cols, cudaMemcpyDeviceToDevice, S(ctx));
-        return e == cudaSuccess ? GBX_OK : gbx_fail(ctx, GBX_ERR_CUDA, "dtrsm copy: %s", cudaGetErrorString(e));
+        cudaError_t e = cudaMemcpy2DAsync(dst, sizeof(T) * ldd, src, sizeof(T) * lds, sizeof(T) * rows, cols,
+                                          cudaMemcpyDeviceToDevice, S(ctx));
+        return e == cudaSuccess ? GBX_OK : gbx_fail(ctx, GBX_ERR_CUDA, "%s copy: %s", nm, cudaGetErrorString(e));
     }
+
+    static T one() { return unit_of<T>(1); }
+    static T mone() { return unit_of<T>(-1); }
 
     // split point: a multiple of NB near the middle
     static int split(int len) { return std::max(NB, ((len / 2 + NB - 1) / NB) * NB); }
@@ -112,22 +133,23 @@ struct Trsm {
     {
         gbx_status st;
         if (len <= NB) {
-            const double *inv = Inv + (long long)(r0 / NB) * NB * NB;
-            if ((st = gemm(len, n, len, 1.0, inv, NB, 0, B + r0, ldb, 0, 0.0, T, NB)) != GBX_OK) return st;
-            return copy_back(B + r0, ldb, T, NB, len, n);
+            const T *inv = Inv + (long long)(r0 / NB) * NB * NB;
+            if ((st = gemm(len, n, len, one(), inv, NB, 0, 0, B + r0, ldb, 0, 0, T{}, Tw, NB)) != GBX_OK) return st;
+            return copy_back(B + r0, ldb, Tw, NB, len, n);
         }
         const int h = split(len);
         int t;
         if (lower) {
             if ((st = left(r0, h)) != GBX_OK) return st;
-            const double *a = opA(r0 + h, r0, t);
-            if ((st = gemm(len - h, n, h, -1.0, a, lda, t, B + r0, ldb, 0, 1.0, B + r0 + h, ldb)) != GBX_OK)
+            const T *a = opA(r0 + h, r0, t);
+            if ((st = gemm(len - h, n, h, mone(), a, lda, t, cj, B + r0, ldb, 0, 0, one(), B + r0 + h, ldb)) !=
+                GBX_OK)
                 return st;
             return left(r0 + h, len - h);
         }
         if ((st = left(r0 + h, len - h)) != GBX_OK) return st;
-        const double *a = opA(r0, r0 + h, t);
-        if ((st = gemm(h, n, len - h, -1.0, a, lda, t, B + r0 + h, ldb, 0, 1.0, B + r0, ldb)) != GBX_OK)
+        const T *a = opA(r0, r0 + h, t);
+        if ((st = gemm(h, n, len - h, mone(), a, lda, t, cj, B + r0 + h, ldb, 0, 0, one(), B + r0, ldb)) != GBX_OK)
             return st;
         return left(r0, h);
     }
@@ -137,63 +159,99 @@ struct Trsm {
     {
         gbx_status st;
         if (len <= NB) {
-            const double *inv = Inv + (long long)(c0 / NB) * NB * NB;
-            if ((st = gemm(m, len, len, 1.0, B + (long long)c0 * ldb, ldb, 0, inv, NB, 0, 0.0, T, m)) != GBX_OK)
+            const T *inv = Inv + (long long)(c0 / NB) * NB * NB;
+            if ((st = gemm(m, len, len, one(), B + (long long)c0 * ldb, ldb, 0, 0, inv, NB, 0, 0, T{}, Tw, m)) !=
+                GBX_OK)
                 return st;
-            return copy_back(B + (long long)c0 * ldb, ldb, T, m, m, len);
+            return copy_back(B + (long long)c0 * ldb, ldb, Tw, m, m, len);
         }
         const int h = split(len);
         int t;
         if (!lower) {
             // X_2 op(A)_22 = B_2 - X_1 op(A)_12
             if ((st = right(c0, h)) != GBX_OK) return st;
-            const double *a = opA(c0, c0 + h, t);
-            if ((st = gemm(m, len - h, h, -1.0, B + (long long)c0 * ldb, ldb, 0, a, lda, t, 1.0,
+            const T *a = opA(c0, c0 + h, t);
+            if ((st = gemm(m, len - h, h, mone(), B + (long long)c0 * ldb, ldb, 0, 0, a, lda, t, cj, one(),
                            B + (long long)(c0 + h) * ldb, ldb)) != GBX_OK)
                 return st;
             return right(c0 + h, len - h);
         }
         // lower: X_1 op(A)_11 = B_1 - X_2 op(A)_21
         if ((st = right(c0 + h, len - h)) != GBX_OK) return st;
-        const double *a = opA(c0 + h, c0, t);
-        if ((st = gemm(m, h, len - h, -1.0, B + (long long)(c0 + h) * ldb, ldb, 0, a, lda, t, 1.0,
+        const T *a = opA(c0 + h, c0, t);
+        if ((st = gemm(m, h, len - h, mone(), B + (long long)(c0 + h) * ldb, ldb, 0, 0, a, lda, t, cj, one(),
                        B + (long long)c0 * ldb, ldb)) != GBX_OK)
             return st;
         return right(c0, h);
     }
 };
 
-}  // namespace
-
-extern "C" gbx_status gbx_dtrsm(gbx_ctx *ctx, char side, char uplo, char ta, char diag, int m,
-                                int n, double alpha, const double *A, int lda, double *B, int ldb)
+template <typename T>
+gbx_status trsm_t(gbx_ctx *ctx, const char *nm, char side, char uplo, char ta, char diag, int m, int n, T alpha,
+                  bool alpha0, bool alpha1, const T *A, int lda, T *B, int ldb)
 {
     if (!ctx) return GBX_ERR_ARG;
     int info = gbx_check_trxm_args(side, uplo, ta, diag, m, n, lda, ldb);
-    if (info) return gbx_fail(ctx, GBX_ERR_ARG, "DTRSM parameter %d", info);
+    if (info) return gbx_fail(ctx, GBX_ERR_ARG, "%s parameter %d", nm, info);
     if (m == 0 || n == 0) return GBX_OK;
-    if (alpha == 0.0) return scale_matrix<double>(ctx, m, n, 0.0, B, ldb, C_FULL);
+    if (alpha0) return scale_matrix<T>(ctx, m, n, alpha, B, ldb, C_FULL);
     gbx_status st;
-    if (alpha != 1.0 && (st = scale_matrix<double>(ctx, m, n, alpha, B, ldb, C_FULL)) != GBX_OK) return st;
+    if (!alpha1 && (st = scale_matrix<T>(ctx, m, n, alpha, B, ldb, C_FULL)) != GBX_OK) return st;
 
     const bool lside = gbx_lsame(side, 'L');
     const int tri = gbx_op_tri(uplo, ta, diag);
-    Trsm t;
-    t.ctx = ctx; t.m = m; t.n = n; t.na = lside ? m : n;
-    t.A = A; t.lda = lda; t.tr = !gbx_lsame(ta, 'N'); t.lower = (tri & TRI_LOWER) != 0;
+    Trsm<T> t;
+    t.ctx = ctx; t.nm = nm; t.m = m; t.n = n; t.na = lside ? m : n;
+    t.A = A; t.lda = lda; t.tr = !gbx_lsame(ta, 'N'); t.cj = gbx_lsame(ta, 'C');
+    t.lower = (tri & TRI_LOWER) != 0;
     t.B = B; t.ldb = ldb;
     const int nblk = (t.na + NB - 1) / NB;
-    double *inv, *tmp;
-    if ((st = gbx_ws(ctx, 1, sizeof(double) * (size_t)nblk * NB * NB, (void **)&inv)) != GBX_OK) return st;
-    if ((st = gbx_ws(ctx, 2, sizeof(double) * (size_t)NB * (lside ? n : m), (void **)&tmp)) != GBX_OK) return st;
+    T *inv, *tmp;
+    if ((st = gbx_ws(ctx, GBX_WS_TMP1, sizeof(T) * (size_t)nblk * NB * NB, (void **)&inv)) != GBX_OK) return st;
+    if ((st = gbx_ws(ctx, GBX_WS_TMP2, sizeof(T) * (size_t)NB * (lside ? n : m), (void **)&tmp)) != GBX_OK)
+        return st;
     t.Inv = inv;
-    t.T = tmp;
+    t.Tw = tmp;
 
-    const size_t smem = sizeof(double) * (NB * (NB + 1) + NB * NB);
+    const size_t smem = sizeof(T) * (NB * (NB + 1) + NB * NB);
     // a per-device function attribute; setting it is a cheap host call
-    cudaFuncSetAttribute(trinv_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    trinv_blocks<<<nblk, NB, smem, S(ctx)>>>(t.na, A, lda, t.tr, t.lower, (tri & TRI_UNIT) != 0, inv);
+    cudaFuncSetAttribute(trinv_blocks<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    trinv_blocks<T><<<nblk, NB, smem, S(ctx)>>>(t.na, A, lda, t.tr, t.cj, t.lower, (tri & TRI_UNIT) != 0, inv);
     gbx_count_launch(ctx, 1);
-    if ((st = gbx_check_launch(ctx, "dtrsm inverse")) != GBX_OK) return st;
+    if ((st = gbx_check_launch(ctx, nm)) != GBX_OK) return st;
     return lside ? t.left(0, m) : t.right(0, n);
+}
+
+}  // namespace
+
+extern "C" gbx_status gbx_strsm(gbx_ctx *ctx, char side, char uplo, char ta, char diag, int m, int n, float alpha,
+                                const float *A, int lda, float *B, int ldb)
+{
+    return trsm_t<float>(ctx, "STRSM", side, uplo, ta, diag, m, n, alpha, alpha == 0.0f, alpha == 1.0f, A, lda, B,
+                         ldb);
+}
+
+extern "C" gbx_status gbx_dtrsm(gbx_ctx *ctx, char side, char uplo, char ta, char diag, int m, int n,
+                                double alpha, const double *A, int lda, double *B, int ldb)
+{
+    return trsm_t<double>(ctx, "DTRSM", side, uplo, ta, diag, m, n, alpha, alpha == 0.0, alpha == 1.0, A, lda, B,
+                          ldb);
+}
+
+extern "C" gbx_status gbx_ctrsm(gbx_ctx *ctx, char side, char uplo, char ta, char diag, int m, int n,
+                                const float *alpha, const float *A, int lda, float *B, int ldb)
+{
+    if (!alpha) return GBX_ERR_ARG;
+    const fcplx al{alpha[0], alpha[1]};
+    return trsm_t<fcplx>(ctx, "CTRSM", side, uplo, ta, diag, m, n, al, al.x == 0.0f && al.y == 0.0f,
+                         al.x == 1.0f && al.y == 0.0f, (const fcplx *)A, lda, (fcplx *)B, ldb);
+}
+
+extern "C" gbx_status gbx_ztrsm(gbx_ctx *ctx, char side, char uplo, char ta, char diag, int m, int n,
+                                const double *alpha, const double *A, int lda, double *B, int ldb)
+{
+    if (!alpha) return GBX_ERR_ARG;
+    const dcplx al{alpha[0], alpha[1]};
+    return trsm_t<dcplx>(ctx, "ZTRSM", side, uplo, ta, diag, m, n, al, al.x == 0.0 && al.y == 0.0,
+                         al.x == 1.0 && al.y == 0.0, (const dcplx *)A, lda, (dcplx *)B, ldb);
 }

@@ -83,6 +83,18 @@ class Oracle:
         L.orc_dtrsm_residual.restype = _c_dbl
         L.orc_dtrsm_residual.argtypes = [_c_char] * 4 + [_c_int, _c_int, _c_dbl, _P, _c_int,
                                                          _P, _c_int, _P, _c_int]
+        L.orc_zsymm.argtypes = [_c_char, _c_char, _c_int, _c_int, _P, _P, _c_int, _P, _c_int, _P, _P,
+                                _c_int, _c_int]
+        L.orc_zsyrk.argtypes = [_c_char, _c_char, _c_int, _c_int, _c_int, _P, _P, _c_int, _P, _P, _c_int,
+                                _c_int]
+        L.orc_zsyr2k.argtypes = [_c_char, _c_char, _c_int, _c_int, _c_int, _P, _P, _c_int, _P, _c_int, _P,
+                                 _P, _c_int, _c_int]
+        for f in ("orc_ztrmm", "orc_ztrsm"):
+            getattr(L, f).argtypes = [_c_char, _c_char, _c_char, _c_char, _c_int, _c_int, _P, _P, _c_int,
+                                      _P, _c_int]
+        L.orc_check_symm.argtypes = [_c_char, _c_char] + [_c_int] * 5
+        L.orc_check_rank_k.argtypes = [_c_char, _c_char] + [_c_int] * 5
+        L.orc_check_rank_2k.argtypes = [_c_char, _c_char] + [_c_int] * 6
         L.orc_rel_fro.restype = _c_dbl
         L.orc_rel_fro.argtypes = [_c_int, _c_int, _P, _c_int, _P, _c_int]
 
@@ -155,6 +167,47 @@ class Oracle:
                            _ptr(a), a.shape[0], _ptr(b), b.shape[0])
 
     # ---- argument checks ---------------------------------------------------
+    # ---- the rest of Level 3, on complex128 arrays (real or single-precision
+    # inputs are widened by the caller; ``z`` promotes a copy) -------------
+    @staticmethod
+    def z(a):
+        """Fortran-ordered complex128 copy of any numeric array."""
+        return np.asfortranarray(np.asarray(a, dtype=np.complex128))
+
+    def zsymm(self, side, uplo, m, n, alpha, a, b, beta, c, herm=False):
+        al = np.array([complex(alpha)]); be = np.array([complex(beta)])
+        self.lib.orc_zsymm(_ch(side), _ch(uplo), m, n, _ptr(al), _ptr(a), a.shape[0], _ptr(b), b.shape[0],
+                           _ptr(be), _ptr(c), c.shape[0], int(herm))
+
+    def zsyrk(self, uplo, trans, allowed, n, k, alpha, a, beta, c, herm=False):
+        al = np.array([complex(alpha)]); be = np.array([complex(beta)])
+        self.lib.orc_zsyrk(_ch(uplo), _ch(trans), allowed, n, k, _ptr(al), _ptr(a), a.shape[0], _ptr(be),
+                           _ptr(c), c.shape[0], int(herm))
+
+    def zsyr2k(self, uplo, trans, allowed, n, k, alpha, a, b, beta, c, herm=False):
+        al = np.array([complex(alpha)]); be = np.array([complex(beta)])
+        self.lib.orc_zsyr2k(_ch(uplo), _ch(trans), allowed, n, k, _ptr(al), _ptr(a), a.shape[0], _ptr(b),
+                            b.shape[0], _ptr(be), _ptr(c), c.shape[0], int(herm))
+
+    def ztrmm(self, side, uplo, ta, diag, m, n, alpha, a, b):
+        al = np.array([complex(alpha)])
+        self.lib.orc_ztrmm(_ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n, _ptr(al), _ptr(a), a.shape[0],
+                           _ptr(b), b.shape[0])
+
+    def ztrsm(self, side, uplo, ta, diag, m, n, alpha, a, b):
+        al = np.array([complex(alpha)])
+        self.lib.orc_ztrsm(_ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n, _ptr(al), _ptr(a), a.shape[0],
+                           _ptr(b), b.shape[0])
+
+    def check_symm(self, side, uplo, m, n, lda, ldb, ldc):
+        return self.lib.orc_check_symm(_ch(side), _ch(uplo), m, n, lda, ldb, ldc)
+
+    def check_rank_k(self, uplo, trans, allowed, n, k, lda, ldc):
+        return self.lib.orc_check_rank_k(_ch(uplo), _ch(trans), allowed, n, k, lda, ldc)
+
+    def check_rank_2k(self, uplo, trans, allowed, n, k, lda, ldb, ldc):
+        return self.lib.orc_check_rank_2k(_ch(uplo), _ch(trans), allowed, n, k, lda, ldb, ldc)
+
     def check_dgemm(self, ta, tb, m, n, k, lda, ldb, ldc):
         return self.lib.orc_check_dgemm(_ch(ta), _ch(tb), m, n, k, lda, ldb, ldc)
 

@@ -484,6 +484,279 @@ void orc_dtrmm(char side, char uplo, char ta, char diag, int m, int n,
 }
 
 /* ------------------------------------------------------------------------ */
+/* The rest of the Level-3 set in complex double: xSYMM/xHEMM, xSYRK/xHERK,  */
+/* xSYR2K/xHER2K, complex xTRMM/xTRSM.  Real (S, D) and single-precision     */
+/* (S, C) routines are checked against these with zero imaginary parts and   */
+/* inputs widened to double.  Semantics follow the netlib reference BLAS     */
+/* (zsymm.f, zhemm.f, zsyrk.f, zherk.f, zsyr2k.f, zher2k.f, ztrmm.f,         */
+/* ztrsm.f), which is what the reference's wrappers reproduce              */
+/* (blas_level3/symm.cc, hemm.cc, syrk.cc, herk.cc, syr2k.cc, her2k.cc,      */
+/* trmm.cc, trsm.cc argument checks) before handing the call to cuBLAS.      */
+/* ------------------------------------------------------------------------ */
+static inline zc zget(const double *m, int ld, int i, int j) { return zld(m + 2 * ((size_t)j * ld + i)); }
+static inline void zput(double *m, int ld, int i, int j, zc v)
+{
+    m[2 * ((size_t)j * ld + i)] = v.re;
+    m[2 * ((size_t)j * ld + i) + 1] = v.im;
+}
+static inline int zis(const double *a, double re) { return a[0] == re && a[1] == 0.0; }
+
+int orc_check_symm(char side, char uplo, int m, int n, int lda, int ldb, int ldc)
+{
+    int nrowa = same(side, 'L') ? m : n;
+    if (!same(side, 'L') && !same(side, 'R')) return 1;
+    if (!same(uplo, 'U') && !same(uplo, 'L')) return 2;
+    if (m < 0) return 3;
+    if (n < 0) return 4;
+    if (lda < imax(1, nrowa)) return 7;
+    if (ldb < imax(1, m)) return 9;
+    if (ldc < imax(1, m)) return 12;
+    return 0;
+}
+
+/* element (i,j) of the symmetric / Hermitian matrix stored in one triangle */
+static zc sym_elem(const double *a, int lda, char uplo, int i, int j, int herm)
+{
+    int stored = same(uplo, 'U') ? (i <= j) : (i >= j);
+    zc v = stored ? zget(a, lda, i, j) : zget(a, lda, j, i);
+    if (herm) {
+        if (!stored) v = zconj(v);
+        if (i == j) v.im = 0.0;
+    }
+    return v;
+}
+
+void orc_zsymm(char side, char uplo, int m, int n, const double *alpha, const double *a, int lda,
+               const double *b, int ldb, const double *beta, double *c, int ldc, int herm)
+{
+    if (orc_check_symm(side, uplo, m, n, lda, ldb, ldc)) return;
+    zc al = zld(alpha), be = zld(beta);
+    int alpha0 = zis(alpha, 0.0), beta0 = zis(beta, 0.0), beta1 = zis(beta, 1.0);
+    if (m == 0 || n == 0 || (alpha0 && beta1)) return;
+    int lside = same(side, 'L');
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            zc t = {0.0, 0.0};
+            if (!alpha0) {
+                if (lside) for (int l = 0; l < m; l++) t = zadd(t, zmul(sym_elem(a, lda, uplo, i, l, herm), zget(b, ldb, l, j)));
+                else       for (int l = 0; l < n; l++) t = zadd(t, zmul(zget(b, ldb, i, l), sym_elem(a, lda, uplo, l, j, herm)));
+            }
+            zc r = zmul(al, t);
+            if (!beta0) r = zadd(r, zmul(be, zget(c, ldc, i, j)));
+            zput(c, ldc, i, j, r);
+        }
+}
+
+/* transposition letters: 1 N, 2 T, 4 C (real routines take all three) */
+static int trans_ok(char t, int allowed)
+{
+    return (same(t, 'N') && (allowed & 1)) || (same(t, 'T') && (allowed & 2)) || (same(t, 'C') && (allowed & 4));
+}
+
+int orc_check_rank_k(char uplo, char trans, int allowed, int n, int k, int lda, int ldc)
+{
+    int nrowa = same(trans, 'N') ? n : k;
+    if (!same(uplo, 'U') && !same(uplo, 'L')) return 1;
+    if (!trans_ok(trans, allowed)) return 2;
+    if (n < 0) return 3;
+    if (k < 0) return 4;
+    if (lda < imax(1, nrowa)) return 7;
+    if (ldc < imax(1, n)) return 10;
+    return 0;
+}
+
+int orc_check_rank_2k(char uplo, char trans, int allowed, int n, int k, int lda, int ldb, int ldc)
+{
+    int nrowa = same(trans, 'N') ? n : k;
+    if (!same(uplo, 'U') && !same(uplo, 'L')) return 1;
+    if (!trans_ok(trans, allowed)) return 2;
+    if (n < 0) return 3;
+    if (k < 0) return 4;
+    if (lda < imax(1, nrowa)) return 7;
+    if (ldb < imax(1, nrowa)) return 9;
+    if (ldc < imax(1, n)) return 12;
+    return 0;
+}
+
+/* op(X)(i,l) for a rank-k operand: N -> X(i,l); T -> X(l,i); C -> conj X(l,i) */
+static zc rk_op(const double *x, int ld, int i, int l, char trans, int herm)
+{
+    if (same(trans, 'N')) return zget(x, ld, i, l);
+    zc v = zget(x, ld, l, i);
+    return herm ? zconj(v) : v;
+}
+/* op(X)'(l,j), the transposed (herm: conjugate-transposed) factor */
+static zc rk_opt(const double *x, int ld, int l, int j, char trans, int herm)
+{
+    if (!same(trans, 'N')) return zget(x, ld, l, j);
+    zc v = zget(x, ld, j, l);
+    return herm ? zconj(v) : v;
+}
+
+/* C = alpha op(A) op(A)' + beta C on the uplo triangle; herm: ' = ^H, alpha
+ * and beta real (imaginary parts ignored), diagonal of C made real */
+void orc_zsyrk(char uplo, char trans, int allowed, int n, int k, const double *alpha, const double *a, int lda,
+               const double *beta, double *c, int ldc, int herm)
+{
+    if (orc_check_rank_k(uplo, trans, allowed, n, k, lda, ldc)) return;
+    zc al = zld(alpha), be = zld(beta);
+    if (herm) { al.im = 0.0; be.im = 0.0; }
+    int alpha0 = al.re == 0.0 && al.im == 0.0, beta0 = be.re == 0.0 && be.im == 0.0;
+    int beta1 = be.re == 1.0 && be.im == 0.0;
+    if (n == 0 || ((alpha0 || k == 0) && beta1)) return;
+    int upper = same(uplo, 'U');
+    for (int j = 0; j < n; j++)
+        for (int i = upper ? 0 : j; i < (upper ? j + 1 : n); i++) {
+            zc t = {0.0, 0.0};
+            if (!alpha0)
+                for (int l = 0; l < k; l++)
+                    t = zadd(t, zmul(rk_op(a, lda, i, l, trans, herm), rk_opt(a, lda, l, j, trans, herm)));
+            zc r = zmul(al, t);
+            if (!beta0) r = zadd(r, zmul(be, zget(c, ldc, i, j)));
+            if (herm && i == j) r.im = 0.0;
+            zput(c, ldc, i, j, r);
+        }
+}
+
+/* C = alpha op(A) op(B)' + alpha' op(B) op(A)' + beta C; alpha' = alpha
+ * (symmetric) or conj(alpha) (herm, beta real, diagonal made real) */
+void orc_zsyr2k(char uplo, char trans, int allowed, int n, int k, const double *alpha, const double *a, int lda,
+                const double *b, int ldb, const double *beta, double *c, int ldc, int herm)
+{
+    if (orc_check_rank_2k(uplo, trans, allowed, n, k, lda, ldb, ldc)) return;
+    zc al = zld(alpha), be = zld(beta);
+    if (herm) be.im = 0.0;
+    zc al2 = herm ? zconj(al) : al;
+    int alpha0 = al.re == 0.0 && al.im == 0.0, beta0 = be.re == 0.0 && be.im == 0.0;
+    int beta1 = be.re == 1.0 && be.im == 0.0;
+    if (n == 0 || ((alpha0 || k == 0) && beta1)) return;
+    int upper = same(uplo, 'U');
+    for (int j = 0; j < n; j++)
+        for (int i = upper ? 0 : j; i < (upper ? j + 1 : n); i++) {
+            zc t1 = {0.0, 0.0}, t2 = {0.0, 0.0};
+            if (!alpha0)
+                for (int l = 0; l < k; l++) {
+                    t1 = zadd(t1, zmul(rk_op(a, lda, i, l, trans, herm), rk_opt(b, ldb, l, j, trans, herm)));
+                    t2 = zadd(t2, zmul(rk_op(b, ldb, i, l, trans, herm), rk_opt(a, lda, l, j, trans, herm)));
+                }
+            zc r = zadd(zmul(al, t1), zmul(al2, t2));
+            if (!beta0) r = zadd(r, zmul(be, zget(c, ldc, i, j)));
+            if (herm && i == j) r.im = 0.0;
+            zput(c, ldc, i, j, r);
+        }
+}
+
+static zc zdiv(zc a, zc b)
+{
+    double d = b.re * b.re + b.im * b.im;
+    zc r = {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+    return r;
+}
+
+/* explicit op(A) (na x na, complex) for TRMM/TRSM; returns 1 if lower */
+static int zexplicit_tri(char uplo, char ta, char diag, int na, const double *a, int lda, zc *t)
+{
+    int upper = same(uplo, 'U'), notr = same(ta, 'N'), unit = same(diag, 'U'), cj = same(ta, 'C');
+    for (int j = 0; j < na; j++)
+        for (int i = 0; i < na; i++) {
+            int ai = notr ? i : j, aj = notr ? j : i;
+            int in_tri = upper ? (ai <= aj) : (ai >= aj);
+            zc v = {0.0, 0.0};
+            if (in_tri) v = zget(a, lda, ai, aj);
+            if (cj) v = zconj(v);
+            if (i == j && unit) { v.re = 1.0; v.im = 0.0; }
+            t[(size_t)j * na + i] = v;
+        }
+    return upper ? !notr : notr;
+}
+
+void orc_ztrmm(char side, char uplo, char ta, char diag, int m, int n, const double *alpha, const double *a,
+               int lda, double *b, int ldb)
+{
+    if (orc_check_dtrsm(side, uplo, ta, diag, m, n, lda, ldb)) return;
+    if (m == 0 || n == 0) return;
+    zc al = zld(alpha);
+    int lside = same(side, 'L'), na = lside ? m : n;
+    zc *t = (zc *)malloc(sizeof(zc) * (size_t)na * na);
+    zc *r = (zc *)malloc(sizeof(zc) * (size_t)m * n);
+    zexplicit_tri(uplo, ta, diag, na, a, lda, t);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            zc s2 = {0.0, 0.0};
+            if (lside) for (int l = 0; l < m; l++) s2 = zadd(s2, zmul(t[(size_t)l * na + i], zget(b, ldb, l, j)));
+            else       for (int l = 0; l < n; l++) s2 = zadd(s2, zmul(zget(b, ldb, i, l), t[(size_t)j * na + l]));
+            r[(size_t)j * m + i] = zmul(al, s2);
+        }
+    if (al.re == 0.0 && al.im == 0.0)
+        for (size_t q = 0; q < (size_t)m * n; q++) { r[q].re = 0.0; r[q].im = 0.0; }
+    for (int j = 0; j < n; j++) for (int i = 0; i < m; i++) zput(b, ldb, i, j, r[(size_t)j * m + i]);
+    free(r); free(t);
+}
+
+void orc_ztrsm(char side, char uplo, char ta, char diag, int m, int n, const double *alpha, const double *a,
+               int lda, double *b, int ldb)
+{
+    if (orc_check_dtrsm(side, uplo, ta, diag, m, n, lda, ldb)) return;
+    if (m == 0 || n == 0) return;
+    zc al = zld(alpha);
+    if (al.re == 0.0 && al.im == 0.0) {
+        zc z = {0.0, 0.0};
+        for (int j = 0; j < n; j++) for (int i = 0; i < m; i++) zput(b, ldb, i, j, z);
+        return;
+    }
+    int lside = same(side, 'L'), unit = same(diag, 'U'), na = lside ? m : n;
+    zc *t = (zc *)malloc(sizeof(zc) * (size_t)na * na);
+    int lower = zexplicit_tri(uplo, ta, diag, na, a, lda, t);
+#define ZT(i, j) t[(size_t)(j) * na + (i)]
+#define ZB(i, j) zget(b, ldb, i, j)
+#define ZSET(i, j, v) zput(b, ldb, i, j, v)
+    for (int j = 0; j < n; j++) for (int i = 0; i < m; i++) ZSET(i, j, zmul(al, ZB(i, j)));
+    if (lside) {
+        for (int j = 0; j < n; j++) {
+            if (lower) {
+                for (int kk = 0; kk < m; kk++) {
+                    if (!unit) ZSET(kk, j, zdiv(ZB(kk, j), ZT(kk, kk)));
+                    for (int i = kk + 1; i < m; i++) {
+                        zc p = zmul(ZB(kk, j), ZT(i, kk));
+                        zc v = ZB(i, j); v.re -= p.re; v.im -= p.im; ZSET(i, j, v);
+                    }
+                }
+            } else {
+                for (int kk = m - 1; kk >= 0; kk--) {
+                    if (!unit) ZSET(kk, j, zdiv(ZB(kk, j), ZT(kk, kk)));
+                    for (int i = 0; i < kk; i++) {
+                        zc p = zmul(ZB(kk, j), ZT(i, kk));
+                        zc v = ZB(i, j); v.re -= p.re; v.im -= p.im; ZSET(i, j, v);
+                    }
+                }
+            }
+        }
+    } else if (!lower) {
+        for (int j = 0; j < n; j++) {
+            for (int kk = 0; kk < j; kk++)
+                for (int i = 0; i < m; i++) {
+                    zc p = zmul(ZT(kk, j), ZB(i, kk));
+                    zc v = ZB(i, j); v.re -= p.re; v.im -= p.im; ZSET(i, j, v);
+                }
+            if (!unit) for (int i = 0; i < m; i++) ZSET(i, j, zdiv(ZB(i, j), ZT(j, j)));
+        }
+    } else {
+        for (int j = n - 1; j >= 0; j--) {
+            for (int kk = j + 1; kk < n; kk++)
+                for (int i = 0; i < m; i++) {
+                    zc p = zmul(ZT(kk, j), ZB(i, kk));
+                    zc v = ZB(i, j); v.re -= p.re; v.im -= p.im; ZSET(i, j, v);
+                }
+            if (!unit) for (int i = 0; i < m; i++) ZSET(i, j, zdiv(ZB(i, j), ZT(j, j)));
+        }
+    }
+#undef ZT
+#undef ZB
+#undef ZSET
+    free(t);
+}
+
+/* ------------------------------------------------------------------------ */
 /* double-double checkers                                                    */
 /* ------------------------------------------------------------------------ */
 static double opd(const double *m, int ld, int i, int j, char t)

@@ -63,6 +63,24 @@ void orc_dtrmm(char side, char uplo, char transa, char diag, int m, int n,
 void orc_dtrsm(char side, char uplo, char transa, char diag, int m, int n,
                double alpha, const double *a, int lda, double *b, int ldb);
 
+/* The rest of the Level-3 set, complex double (real and single-precision
+ * routines are checked through these with zero imaginary parts).  allowed:
+ * transposition letters the routine takes, 1 N | 2 T | 4 C.  herm selects
+ * the Hermitian form (xHEMM, xHERK, xHER2K). */
+void orc_zsymm(char side, char uplo, int m, int n, const double *alpha, const double *a, int lda,
+               const double *b, int ldb, const double *beta, double *c, int ldc, int herm);
+void orc_zsyrk(char uplo, char trans, int allowed, int n, int k, const double *alpha, const double *a,
+               int lda, const double *beta, double *c, int ldc, int herm);
+void orc_zsyr2k(char uplo, char trans, int allowed, int n, int k, const double *alpha, const double *a,
+                int lda, const double *b, int ldb, const double *beta, double *c, int ldc, int herm);
+void orc_ztrmm(char side, char uplo, char ta, char diag, int m, int n, const double *alpha,
+               const double *a, int lda, double *b, int ldb);
+void orc_ztrsm(char side, char uplo, char ta, char diag, int m, int n, const double *alpha,
+               const double *a, int lda, double *b, int ldb);
+int orc_check_symm(char side, char uplo, int m, int n, int lda, int ldb, int ldc);
+int orc_check_rank_k(char uplo, char trans, int allowed, int n, int k, int lda, int ldc);
+int orc_check_rank_2k(char uplo, char trans, int allowed, int n, int k, int lda, int ldb, int ldc);
+
 /* ---- argument checks (netlib INFO numbering; 0 = valid) ----------------- */
 int orc_check_dgemm(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc);
 int orc_check_dtrsm(char side, char uplo, char ta, char diag, int m, int n, int lda, int ldb);
