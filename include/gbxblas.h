@@ -122,6 +122,17 @@ gbx_status gbx_dgemv(gbx_ctx *ctx, char trans, int m, int n, double alpha,
                      const double *A, int lda, const double *x, int incx,
                      double beta, double *y, int incy);
 
+/* A := alpha*x*y^T + A                replaces cublasDger, blas_level2/ger.cc:86-94 */
+gbx_status gbx_dger(gbx_ctx *ctx, int m, int n, double alpha, const double *x, int incx,
+                    const double *y, int incy, double *A, int lda);
+/* y := alpha*A*x + beta*y, A symmetric (one stored triangle)
+ *                                     replaces cublasDsymv, blas_level2/symv.cc:88-96 */
+gbx_status gbx_dsymv(gbx_ctx *ctx, char uplo, int n, double alpha, const double *A, int lda,
+                     const double *x, int incx, double beta, double *y, int incy);
+/* x := op(A)^-1 * x, A triangular     replaces cublasDtrsv, blas_level2/trsv.cc:81-87 */
+gbx_status gbx_dtrsv(gbx_ctx *ctx, char uplo, char trans, char diag, int n, const double *A, int lda,
+                     double *x, int incx);
+
 /* ---- Level 3 ---------------------------------------------------------------
  * C := alpha*op(A)*op(B) + beta*C     replaces cublasDgemm, blas_level3/gemm.cc:62-82,174
  * beta == 0 sets C (NaN/Inf in C are not propagated), as netlib does.          */

@@ -111,6 +111,15 @@ void ztrsm_(const char *side, const char *uplo, const char *transa, const char *
 void dgemv_(const char *trans, const int *m, const int *n, const double *alpha, const double *a,
             const int *lda, const double *x, const int *incx, const double *beta, double *y,
             const int *incy);
+/* F77_ger(d, double)  blas.h:94-100; CBLAS body blas_level2/ger.cc:86-94 (not built there) */
+void dger_(const int *m, const int *n, const double *alpha, const double *x, const int *incx, const double *y,
+           const int *incy, double *a, const int *lda);
+/* F77_symv(d, double)  blas.h:134-142; CBLAS body blas_level2/symv.cc:88-96 (not built there) */
+void dsymv_(const char *uplo, const int *n, const double *alpha, const double *a, const int *lda,
+            const double *x, const int *incx, const double *beta, double *y, const int *incy);
+/* F77_trsv(d, double)  blas.h:193-200; CBLAS body blas_level2/trsv.cc:81-87 (not built there) */
+void dtrsv_(const char *uplo, const char *trans, const char *diag, const int *n, const double *a, const int *lda,
+            double *x, const int *incx);
 /* F77_axpy(d, double)  blas.h:20-31 */
 void daxpy_(const int *n, const double *alpha, const double *x, const int *incx, double *y,
             const int *incy);
@@ -210,6 +219,12 @@ void cblas_ztrsm(int layout, int side, int uplo, int transa, int diag, int m, in
 /* cblas.h:283-297 */
 void cblas_dgemv(int layout, int trans, int m, int n, double alpha, const double *a, int lda,
                  const double *x, int incx, double beta, double *y, int incy);
+/* cblas_?ger cblas.h:301-314, cblas_?symv 506-521, cblas_?trsv 640-655 */
+void cblas_dger(int layout, int m, int n, double alpha, const double *x, int incx, const double *y, int incy,
+                double *a, int lda);
+void cblas_dsymv(int layout, int uplo, int n, double alpha, const double *a, int lda, const double *x, int incx,
+                 double beta, double *y, int incy);
+void cblas_dtrsv(int layout, int uplo, int trans, int diag, int n, const double *a, int lda, double *x, int incx);
 void cblas_daxpy(int n, double alpha, const double *x, int incx, double *y, int incy);
 double cblas_ddot(int n, const double *x, int incx, const double *y, int incy);
 double cblas_dnrm2(int n, const double *x, int incx);

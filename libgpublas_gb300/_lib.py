@@ -277,6 +277,18 @@ class F77:
     def idamin(self, n, x, incx):
         return self.L.idamin_(_byref_i(n), _hp(x), _byref_i(incx))
 
+    def dger(self, m, n, alpha, x, incx, y, incy, a, lda):
+        self.L.dger_(_byref_i(m), _byref_i(n), _byref_d(alpha), _hp(x), _byref_i(incx), _hp(y), _byref_i(incy),
+                     _hp(a), _byref_i(lda))
+
+    def dsymv(self, uplo, n, alpha, a, lda, x, incx, beta, y, incy):
+        self.L.dsymv_(C.c_char_p(_ch(uplo)), _byref_i(n), _byref_d(alpha), _hp(a), _byref_i(lda), _hp(x),
+                      _byref_i(incx), _byref_d(beta), _hp(y), _byref_i(incy))
+
+    def dtrsv(self, uplo, trans, diag, n, a, lda, x, incx):
+        self.L.dtrsv_(C.c_char_p(_ch(uplo)), C.c_char_p(_ch(trans)), C.c_char_p(_ch(diag)), _byref_i(n), _hp(a),
+                      _byref_i(lda), _hp(x), _byref_i(incx))
+
     # ---- the Level-3 family in every precision: p is 's', 'd', 'c' or 'z';
     # scalars are passed by reference in the routine's type (real for the
     # Hermitian alpha/beta that netlib declares real)

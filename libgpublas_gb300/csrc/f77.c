@@ -332,6 +332,79 @@ fail:
     report("DGEMV", ctx, st);
 }
 
+/* ----------------------------------------------- DGER / DSYMV / DTRSV */
+int gbx_check_ger_args(int m, int n, int incx, int incy, int lda);
+int gbx_check_symv_args(char uplo, int n, int lda, int incx, int incy);
+int gbx_check_trsv_args(char uplo, char trans, char diag, int n, int lda, int incx);
+
+void dger_(const int *m, const int *n, const double *alpha, const double *x, const int *incx, const double *y,
+           const int *incy, double *a, const int *lda)
+{
+    int info = gbx_check_ger_args(*m, *n, *incx, *incy, *lda);
+    if (info) { xerbla_("DGER  ", &info, 6); return; }
+    NOTE("dger_", x); NOTE("dger_", y); NOTE("dger_", a);
+    if (*m == 0 || *n == 0 || *alpha == 0.0) return;
+    gbx_ctx *ctx = ctx_or_report("DGER");
+    if (!ctx) return;
+    gbx_status st;
+    gbx_operand oa = {0}, ox = {0}, oy = {0};
+    TRY(gbx_place_vec(ctx, GBX_WS_STAGE_B, x, *m, *incx, 8, 1, &ox));
+    TRY(gbx_place_vec(ctx, GBX_WS_STAGE_C, y, *n, *incy, 8, 1, &oy));
+    TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, *m, *n, *lda, 8, 1, &oa));
+    TRY(gbx_dger(ctx, *m, *n, *alpha, ox.dev, *incx, oy.dev, *incy, oa.dev, oa.ld));
+    TRY(gbx_place_out(ctx, &oa, *m, *n, 8));
+    TRY(gbx_ctx_sync(ctx));
+    return;
+fail:
+    report("DGER", ctx, st);
+}
+
+void dsymv_(const char *uplo, const int *n, const double *alpha, const double *a, const int *lda,
+            const double *x, const int *incx, const double *beta, double *y, const int *incy)
+{
+    int info = gbx_check_symv_args(*uplo, *n, *lda, *incx, *incy);
+    if (info) { xerbla_("DSYMV ", &info, 6); return; }
+    NOTE("dsymv_", a); NOTE("dsymv_", x); NOTE("dsymv_", y);
+    if (*n == 0 || (*alpha == 0.0 && *beta == 1.0)) return;
+    gbx_ctx *ctx = ctx_or_report("DSYMV");
+    if (!ctx) return;
+    gbx_status st;
+    gbx_operand oa = {.ld = *lda}, ox = {0}, oy = {0};
+    if (*alpha != 0.0) {
+        TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, *n, *n, *lda, 8, 1, &oa));
+        TRY(gbx_place_vec(ctx, GBX_WS_STAGE_B, x, *n, *incx, 8, 1, &ox));
+    }
+    const int yin = *beta != 0.0 || (*incy != 1 && *incy != -1);
+    TRY(gbx_place_vec(ctx, GBX_WS_STAGE_C, y, *n, *incy, 8, yin, &oy));
+    TRY(gbx_dsymv(ctx, *uplo, *n, *alpha, oa.dev, oa.ld, ox.dev, *incx, *beta, oy.dev, *incy));
+    TRY(gbx_place_vec_out(ctx, &oy, *n, *incy, 8));
+    TRY(gbx_ctx_sync(ctx));
+    return;
+fail:
+    report("DSYMV", ctx, st);
+}
+
+void dtrsv_(const char *uplo, const char *trans, const char *diag, const int *n, const double *a, const int *lda,
+            double *x, const int *incx)
+{
+    int info = gbx_check_trsv_args(*uplo, *trans, *diag, *n, *lda, *incx);
+    if (info) { xerbla_("DTRSV ", &info, 6); return; }
+    NOTE("dtrsv_", a); NOTE("dtrsv_", x);
+    if (*n == 0) return;
+    gbx_ctx *ctx = ctx_or_report("DTRSV");
+    if (!ctx) return;
+    gbx_status st;
+    gbx_operand oa = {0}, ox = {0};
+    TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, *n, *n, *lda, 8, 1, &oa));
+    TRY(gbx_place_vec(ctx, GBX_WS_STAGE_B, x, *n, *incx, 8, 1, &ox));
+    TRY(gbx_dtrsv(ctx, *uplo, *trans, *diag, *n, oa.dev, oa.ld, ox.dev, *incx));
+    TRY(gbx_place_vec_out(ctx, &ox, *n, *incx, 8));
+    TRY(gbx_ctx_sync(ctx));
+    return;
+fail:
+    report("DTRSV", ctx, st);
+}
+
 /* ---------------------------------------------------------------- Level 1 */
 void daxpy_(const int *n, const double *alpha, const double *x, const int *incx, double *y,
             const int *incy)
@@ -502,6 +575,34 @@ void cblas_dgemv(int layout, int trans, int m, int n, double alpha, const double
         int tmp = m; m = n; n = tmp;
     }
     dgemv_(&t, &m, &n, &alpha, a, &lda, x, &incx, &beta, y, &incy);
+}
+
+/* row-major: A^T += alpha y x^T */
+void cblas_dger(int layout, int m, int n, double alpha, const double *x, int incx, const double *y, int incy,
+                double *a, int lda)
+{
+    if (bad_layout(layout, "DGER  ")) return;
+    if (layout == GbxColMajor) dger_(&m, &n, &alpha, x, &incx, y, &incy, a, &lda);
+    else dger_(&n, &m, &alpha, y, &incy, x, &incx, a, &lda);
+}
+
+/* row-major: the stored triangle flips (A^T = A) */
+void cblas_dsymv(int layout, int uplo, int n, double alpha, const double *a, int lda, const double *x, int incx,
+                 double beta, double *y, int incy)
+{
+    if (bad_layout(layout, "DSYMV ")) return;
+    char u = uch(uplo);
+    if (layout == GbxRowMajor) u = flip_u(u);
+    dsymv_(&u, &n, &alpha, a, &lda, x, &incx, &beta, y, &incy);
+}
+
+/* row-major: op(A) on A^T: the triangle flips and N <-> T */
+void cblas_dtrsv(int layout, int uplo, int trans, int diag, int n, const double *a, int lda, double *x, int incx)
+{
+    if (bad_layout(layout, "DTRSV ")) return;
+    char u = uch(uplo), t = tch(trans), d = dch(diag);
+    if (layout == GbxRowMajor) { u = flip_u(u); t = flip_t(t); }
+    dtrsv_(&u, &t, &d, &n, a, &lda, x, &incx);
 }
 
 void cblas_daxpy(int n, double alpha, const double *x, int incx, double *y, int incy)

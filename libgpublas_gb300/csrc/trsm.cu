@@ -224,6 +224,21 @@ gbx_status trsm_t(gbx_ctx *ctx, const char *nm, char side, char uplo, char ta, c
 
 }  // namespace
 
+namespace gbx_gemm {
+// Inverted 64x64 diagonal blocks of op(A) (na x na; lower: op(A) is lower
+// triangular), for the blocked DTRSV.
+gbx_status trinv_diag_blocks(gbx_ctx *ctx, int na, const double *A, long long lda, int tr, int lower, int unit,
+                             double *inv)
+{
+    const int nblk = (na + NB - 1) / NB;
+    const size_t smem = sizeof(double) * (NB * (NB + 1) + NB * NB);
+    cudaFuncSetAttribute(trinv_blocks<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    trinv_blocks<double><<<nblk, NB, smem, S(ctx)>>>(na, A, lda, tr, 0, lower, unit, inv);
+    gbx_count_launch(ctx, 1);
+    return gbx_check_launch(ctx, "trsv inverse");
+}
+}  // namespace gbx_gemm
+
 extern "C" gbx_status gbx_strsm(gbx_ctx *ctx, char side, char uplo, char ta, char diag, int m, int n, float alpha,
                                 const float *A, int lda, float *B, int ldb)
 {

@@ -92,6 +92,12 @@ class Oracle:
         for f in ("orc_ztrmm", "orc_ztrsm"):
             getattr(L, f).argtypes = [_c_char, _c_char, _c_char, _c_char, _c_int, _c_int, _P, _P, _c_int,
                                       _P, _c_int]
+        L.orc_dger.argtypes = [_c_int, _c_int, _c_dbl, _P, _c_int, _P, _c_int, _P, _c_int]
+        L.orc_dsymv.argtypes = [_c_char, _c_int, _c_dbl, _P, _c_int, _P, _c_int, _c_dbl, _P, _c_int]
+        L.orc_dtrsv.argtypes = [_c_char, _c_char, _c_char, _c_int, _P, _c_int, _P, _c_int]
+        L.orc_check_dger.argtypes = [_c_int] * 5
+        L.orc_check_dsymv.argtypes = [_c_char] + [_c_int] * 4
+        L.orc_check_dtrsv.argtypes = [_c_char] * 3 + [_c_int] * 3
         L.orc_check_symm.argtypes = [_c_char, _c_char] + [_c_int] * 5
         L.orc_check_rank_k.argtypes = [_c_char, _c_char] + [_c_int] * 5
         L.orc_check_rank_2k.argtypes = [_c_char, _c_char] + [_c_int] * 6
@@ -167,6 +173,16 @@ class Oracle:
                            _ptr(a), a.shape[0], _ptr(b), b.shape[0])
 
     # ---- argument checks ---------------------------------------------------
+    # ---- DGER / DSYMV / DTRSV (in place, leading dimension = first extent)
+    def dger(self, m, n, alpha, x, incx, y, incy, a):
+        self.lib.orc_dger(m, n, alpha, _ptr(x), incx, _ptr(y), incy, _ptr(a), a.shape[0])
+
+    def dsymv(self, uplo, n, alpha, a, x, incx, beta, y, incy):
+        self.lib.orc_dsymv(_ch(uplo), n, alpha, _ptr(a), a.shape[0], _ptr(x), incx, beta, _ptr(y), incy)
+
+    def dtrsv(self, uplo, trans, diag, n, a, x, incx):
+        self.lib.orc_dtrsv(_ch(uplo), _ch(trans), _ch(diag), n, _ptr(a), a.shape[0], _ptr(x), incx)
+
     # ---- the rest of Level 3, on complex128 arrays (real or single-precision
     # inputs are widened by the caller; ``z`` promotes a copy) -------------
     @staticmethod

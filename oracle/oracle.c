@@ -484,6 +484,98 @@ void orc_dtrmm(char side, char uplo, char ta, char diag, int m, int n,
 }
 
 /* ------------------------------------------------------------------------ */
+/* DGER, DSYMV, DTRSV (netlib dger.f, dsymv.f, dtrsv.f loop orders; the      */
+/* reference's CBLAS bodies blas_level2/ger.cc:86-94, symv.cc:88-96,         */
+/* trsv.cc:81-87 forward to cuBLAS)                                          */
+/* ------------------------------------------------------------------------ */
+int orc_check_dger(int m, int n, int incx, int incy, int lda)
+{
+    if (m < 0) return 1;
+    if (n < 0) return 2;
+    if (incx == 0) return 5;
+    if (incy == 0) return 7;
+    if (lda < imax(1, m)) return 9;
+    return 0;
+}
+
+void orc_dger(int m, int n, double alpha, const double *x, int incx, const double *y, int incy, double *a, int lda)
+{
+    if (orc_check_dger(m, n, incx, incy, lda)) return;
+    if (m == 0 || n == 0 || alpha == 0.0) return;
+    for (int j = 0; j < n; j++) {
+        double yj = y[vidx(j, n, incy)];
+        if (yj == 0.0) continue;
+        double t = alpha * yj;
+        for (int i = 0; i < m; i++) A_(i, j) += x[vidx(i, m, incx)] * t;
+    }
+}
+
+int orc_check_dsymv(char uplo, int n, int lda, int incx, int incy)
+{
+    if (!same(uplo, 'U') && !same(uplo, 'L')) return 1;
+    if (n < 0) return 2;
+    if (lda < imax(1, n)) return 5;
+    if (incx == 0) return 7;
+    if (incy == 0) return 10;
+    return 0;
+}
+
+void orc_dsymv(char uplo, int n, double alpha, const double *a, int lda, const double *x, int incx, double beta,
+               double *y, int incy)
+{
+    if (orc_check_dsymv(uplo, n, lda, incx, incy)) return;
+    if (n == 0 || (alpha == 0.0 && beta == 1.0)) return;
+    int upper = same(uplo, 'U');
+    for (int i = 0; i < n; i++) {
+        double s = 0.0;
+        if (alpha != 0.0)
+            for (int j = 0; j < n; j++) {
+                int stored = upper ? (i <= j) : (i >= j);
+                s += (stored ? A_(i, j) : A_(j, i)) * x[vidx(j, n, incx)];
+            }
+        double *yp = &y[vidx(i, n, incy)];
+        *yp = (beta == 0.0) ? alpha * s : alpha * s + beta * *yp;
+    }
+}
+
+int orc_check_dtrsv(char uplo, char trans, char diag, int n, int lda, int incx)
+{
+    if (!same(uplo, 'U') && !same(uplo, 'L')) return 1;
+    if (!same(trans, 'N') && !same(trans, 'T') && !same(trans, 'C')) return 2;
+    if (!same(diag, 'U') && !same(diag, 'N')) return 3;
+    if (n < 0) return 4;
+    if (lda < imax(1, n)) return 6;
+    if (incx == 0) return 8;
+    return 0;
+}
+
+void orc_dtrsv(char uplo, char trans, char diag, int n, const double *a, int lda, double *x, int incx)
+{
+    if (orc_check_dtrsv(uplo, trans, diag, n, lda, incx)) return;
+    if (n == 0) return;
+    double *t = (double *)malloc(sizeof(double) * (size_t)n * n);
+    int lower = explicit_tri(uplo, trans, diag, n, a, lda, t), unit = same(diag, 'U');
+    double *v = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int i = 0; i < n; i++) v[i] = x[vidx(i, n, incx)];
+    if (lower) {
+        for (int i = 0; i < n; i++) {
+            double s = v[i];
+            for (int j = 0; j < i; j++) s -= t[(size_t)j * n + i] * v[j];
+            v[i] = unit ? s : s / t[(size_t)i * n + i];
+        }
+    } else {
+        for (int i = n - 1; i >= 0; i--) {
+            double s = v[i];
+            for (int j = i + 1; j < n; j++) s -= t[(size_t)j * n + i] * v[j];
+            v[i] = unit ? s : s / t[(size_t)i * n + i];
+        }
+    }
+    for (int i = 0; i < n; i++) x[vidx(i, n, incx)] = v[i];
+    free(v);
+    free(t);
+}
+
+/* ------------------------------------------------------------------------ */
 /* The rest of the Level-3 set in complex double: xSYMM/xHEMM, xSYRK/xHERK,  */
 /* xSYR2K/xHER2K, complex xTRMM/xTRSM.  Real (S, D) and single-precision     */
 /* (S, C) routines are checked against these with zero imaginary parts and   */

@@ -63,6 +63,16 @@ void orc_dtrmm(char side, char uplo, char transa, char diag, int m, int n,
 void orc_dtrsm(char side, char uplo, char transa, char diag, int m, int n,
                double alpha, const double *a, int lda, double *b, int ldb);
 
+/* DGER / DSYMV / DTRSV (vectors follow netlib's increment rules) */
+void orc_dger(int m, int n, double alpha, const double *x, int incx, const double *y, int incy, double *a,
+              int lda);
+void orc_dsymv(char uplo, int n, double alpha, const double *a, int lda, const double *x, int incx, double beta,
+               double *y, int incy);
+void orc_dtrsv(char uplo, char trans, char diag, int n, const double *a, int lda, double *x, int incx);
+int orc_check_dger(int m, int n, int incx, int incy, int lda);
+int orc_check_dsymv(char uplo, int n, int lda, int incx, int incy);
+int orc_check_dtrsv(char uplo, char trans, char diag, int n, int lda, int incx);
+
 /* The rest of the Level-3 set, complex double (real and single-precision
  * routines are checked through these with zero imaginary parts).  allowed:
  * transposition letters the routine takes, 1 N | 2 T | 4 C.  herm selects
