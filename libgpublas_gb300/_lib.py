@@ -88,6 +88,24 @@ def _declare(L):
     L.gbx_dsyrk.argtypes = [_P, _CH, _CH, _I, _I, _D, _P, _I, _D, _P, _I]
     L.gbx_dtrsm.argtypes = [_P, _CH, _CH, _CH, _CH, _I, _I, _D, _P, _I, _P, _I]
     L.gbx_dtrmm.argtypes = [_P, _CH, _CH, _CH, _CH, _I, _I, _D, _P, _I, _P, _I]
+    L.gbx_dger.argtypes = [_P, _I, _I, _D, _P, _I, _P, _I, _P, _I]
+    L.gbx_dsymv.argtypes = [_P, _CH, _I, _D, _P, _I, _P, _I, _D, _P, _I]
+    L.gbx_dtrsv.argtypes = [_P, _CH, _CH, _CH, _I, _P, _I, _P, _I]
+    # the Level-3 set in S/D/C/Z (complex scalars: pointers to host pairs)
+    _F = C.c_float
+    for p, S in (("s", _F), ("d", _D), ("c", _P), ("z", _P)):
+        if p in "sc":
+            getattr(L, f"gbx_{p}gemm").argtypes = [_P, _CH, _CH, _I, _I, _I, S, _P, _I, _P, _I, S, _P, _I]
+        getattr(L, f"gbx_{p}symm").argtypes = [_P, _CH, _CH, _I, _I, S, _P, _I, _P, _I, S, _P, _I]
+        getattr(L, f"gbx_{p}syr2k").argtypes = [_P, _CH, _CH, _I, _I, S, _P, _I, _P, _I, S, _P, _I]
+        if p != "d":
+            getattr(L, f"gbx_{p}syrk").argtypes = [_P, _CH, _CH, _I, _I, S, _P, _I, S, _P, _I]
+            for r in ("trmm", "trsm"):
+                getattr(L, f"gbx_{p}{r}").argtypes = [_P, _CH, _CH, _CH, _CH, _I, _I, S, _P, _I, _P, _I]
+    for p, R in (("c", _F), ("z", _D)):
+        getattr(L, f"gbx_{p}hemm").argtypes = [_P, _CH, _CH, _I, _I, _P, _P, _I, _P, _I, _P, _P, _I]
+        getattr(L, f"gbx_{p}herk").argtypes = [_P, _CH, _CH, _I, _I, R, _P, _I, R, _P, _I]
+        getattr(L, f"gbx_{p}her2k").argtypes = [_P, _CH, _CH, _I, _I, _P, _P, _I, _P, _I, R, _P, _I]
     L.gbx_dgemm_ozaki.argtypes = [_P, _CH, _CH, _I, _I, _I, _D, _P, _I, _P, _I, _D, _P, _I,
                                   _D, _I, C.POINTER(_I)]
     L.gbx_zgemm_ozaki.argtypes = [_P, _CH, _CH, _I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _I,

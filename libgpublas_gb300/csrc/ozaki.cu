@@ -41,13 +41,13 @@ using namespace gbx_tc;
 
 namespace {
 
-constexpr int OZ_BM = 128, OZ_BN = 256, OZ_BK = 128, OZ_STAGES = 4;
+// Tile: OZ_BM rows by OZ_BN (256) or 128 columns (oz_gemm_kernel<BN>), K in
+// blocks of OZ_BK digits.  OZ_THREADS is the CTA-pair kernel's block.
+constexpr int OZ_BM = 128, OZ_BN = 256, OZ_BK = 128;
 constexpr int OZ_THREADS = 192;
 constexpr int OZ_SMAX = 14;
 constexpr int OZ_KEXT_MAX = 65536;   // 2^24 / 16^2
-constexpr int OZ_A_BYTES = OZ_BM * OZ_BK, OZ_B_BYTES = OZ_BN * OZ_BK;
-constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
-constexpr size_t OZ_SMEM = (size_t)OZ_STAGES * OZ_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int OZ_A_BYTES = OZ_BM * OZ_BK;
 
 inline cudaStream_t S_(gbx_ctx *ctx) { return (cudaStream_t)gbx_ctx_get_stream(ctx); }
 inline long long rup(long long v, long long m) { return (v + m - 1) / m * m; }
@@ -149,16 +149,38 @@ __device__ __forceinline__ void flag_nonfinite(unsigned long long b, int *status
     if ((b >> 52) == 0x7FFull) atomicCAS(status, 0, OZ_NONFINITE);
 }
 
-// row_k sources (K contiguous per row): one warp per row.
-__global__ void __launch_bounds__(256)
-oz_stats_rowk(SrcView v, int rows, int K, int *__restrict__ expo, double *__restrict__ ss, int *status)
+// ---- per-call operand preparation, fused over both operands ----------------
+// One call of the Ozaki product prepares op(A) (rows M) and op(B)^T (rows N)
+// in three launches: statistics of both operands, the combination of the
+// statistics with the scale exponents and (in the last CTA to finish) the
+// slice count, and the slicing of both operands.  Small products (the
+// trailing updates of a blocked factorization) are dominated by per-launch
+// cost, not by these kernels' bytes.
+struct OzPrepOp {
+    SrcView v;
+    int rows, K, Rp, Kp;
+    int kch, nkb, rblocks;   // col_k statistics: 32-row blocks x kch-wide K chunks
+    int stat_blocks;         // CTAs of the statistics launch (0: no statistics)
+    int split_blocks;        // CTAs of the slicing launch: (Kp/128) x (Rp/OZ_SPLIT_ROWS)
+    SsAcc *part;             // col_k partials [nkb][rows]
+    int *expo;               // frexp exponent of each row's max |x|
+    double *ss;              // scaled sum of squares per row
+    int *scale;              // Rp scale exponents e-4 (padded rows 0)
+    int *scale2;             // optional second copy over Rp2 rows (symmetric rank-k)
+    int Rp2;
+    uint8_t *X8;             // S digit planes [s][Rp][Kp]
+};
+
+__device__ __forceinline__ void oz_stats_rowk_block(const SrcView &v, int rows, int K, int blk, int *expo,
+                                                    double *ss, int *status)
 {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= rows) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blk * 8 + warp;   // one warp per row, 8 rows per CTA
+    if (r >= rows) return;
     SsAcc a;
     a.init();
     for (int k = lane; k < K; k += 32) {
-        const unsigned long long b = abs_bits(src_get(v, warp, k));
+        const unsigned long long b = abs_bits(src_get(v, r, k));
         flag_nonfinite(b, status);
         a.add(b);
     }
@@ -169,20 +191,18 @@ oz_stats_rowk(SrcView v, int rows, int K, int *__restrict__ expo, double *__rest
         t.ss = __shfl_xor_sync(0xffffffffu, a.ss, o);
         a.merge(t);
     }
-    if (lane == 0) a.finish(expo[warp], ss[warp]);
+    if (lane == 0) a.finish(expo[r], ss[r]);
 }
 
-// col_k sources (rows contiguous): 32 rows x 8 k-lanes per block, one block
-// column per chunk of OZ_STATS_KCH k; partials merged by oz_stats_combine.
-constexpr int OZ_STATS_KCH = 1024;
-
-__global__ void __launch_bounds__(256)
-oz_stats_colk(SrcView v, int rows, int K, int kch, SsAcc *__restrict__ part, int *status)
+// col_k sources (rows contiguous): 32 rows x 8 k-lanes per CTA over one K
+// chunk; partials merged in oz_prep_finish.
+__device__ __forceinline__ void oz_stats_colk_block(const SrcView &v, int rows, int K, int kch, int rblocks,
+                                                    int blk, SsAcc *part, int *status)
 {
     __shared__ SsAcc s_acc[8][32];
     const int rr = threadIdx.x & 31, kl = threadIdx.x >> 5;
-    const int r = blockIdx.x * 32 + rr;
-    const int k0 = blockIdx.y * kch, k1 = min(K, k0 + kch);
+    const int r = (blk % rblocks) * 32 + rr, kb = blk / rblocks;
+    const int k0 = kb * kch, k1 = min(K, k0 + kch);
     SsAcc a;
     a.init();
     if (r < rows)
@@ -195,17 +215,121 @@ oz_stats_colk(SrcView v, int rows, int K, int kch, SsAcc *__restrict__ part, int
     __syncthreads();
     if (kl == 0 && r < rows) {
         for (int q = 1; q < 8; q++) a.merge(s_acc[q][rr]);
-        part[(size_t)blockIdx.y * rows + r] = a;
+        part[(size_t)kb * rows + r] = a;
     }
 }
 
-__global__ void oz_stats_combine(const SsAcc *__restrict__ part, int rows, int nkb, int *__restrict__ expo,
-                                 double *__restrict__ ss)
+__global__ void __launch_bounds__(256)
+oz_prep_stats(OzPrepOp a, OzPrepOp b, int *status, unsigned *counter)
 {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
-        SsAcc a = part[r];
-        for (int q = 1; q < nkb; q++) a.merge(part[(size_t)q * rows + r]);
-        a.finish(expo[r], ss[r]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *counter = 0u;   // for oz_prep_finish (next launch)
+    int blk = blockIdx.x;
+    if (blk < a.stat_blocks) {
+        if (a.v.row_k) oz_stats_rowk_block(a.v, a.rows, a.K, blk, a.expo, a.ss, status);
+        else oz_stats_colk_block(a.v, a.rows, a.K, a.kch, a.rblocks, blk, a.part, status);
+    } else {
+        blk -= a.stat_blocks;
+        if (b.v.row_k) oz_stats_rowk_block(b.v, b.rows, b.K, blk, b.expo, b.ss, status);
+        else oz_stats_colk_block(b.v, b.rows, b.K, b.kch, b.rblocks, blk, b.part, status);
+    }
+}
+
+// Per row: merge col_k partials into (expo, ss), then the scale exponent.
+__device__ __forceinline__ void oz_finish_row(const OzPrepOp &o, int r)
+{
+    int e = 0;
+    if (r < o.rows) {
+        if (!o.v.row_k) {
+            SsAcc acc = o.part[r];
+            for (int q = 1; q < o.nkb; q++) acc.merge(o.part[(size_t)q * o.rows + r]);
+            acc.finish(o.expo[r], o.ss[r]);
+            e = o.expo[r] - 4;
+        } else {
+            e = o.expo[r] - 4;
+        }
+    }
+    if (r < o.Rp) o.scale[r] = e;
+    if (o.scale2 && r < o.Rp2) o.scale2[r] = e;
+}
+
+// Block-wide reductions for 256 threads (fixed order: deterministic); every
+// thread gets the result.
+__device__ __forceinline__ int oz_block_max(int v)
+{
+    __shared__ int s[8];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = s[0];
+#pragma unroll
+    for (int i = 1; i < 8; i++) v = max(v, s[i]);
+    __syncthreads();
+    return v;
+}
+
+__device__ __forceinline__ double oz_block_sum(double v)
+{
+    __shared__ double s[8];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+    __syncthreads();
+    return v;
+}
+
+// Slice count: relative Frobenius error ~ c * 2^(-5S) * gamma_A * gamma_B with
+// gamma^2 = (sum_i 2^(2 e_i)) / (sum_i 2^(2 e_i) * ss_i / K): the ratio of the
+// squared row maxima to the squared row norms (1 <= gamma <= sqrt(K)).  The
+// statistics were written by other CTAs of the same launch: read through L2.
+__device__ double oz_log2_gamma(const int *expo, const double *ss, int rows, int K)
+{
+    int emax = -100000;
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) emax = max(emax, __ldcg(expo + i));
+    emax = oz_block_max(emax);
+    double num = 0.0, den = 0.0;
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) {
+        // 2^(2(e_i - emax)) from the exponent field (0 below the normal range)
+        const int d = 2 * (__ldcg(expo + i) - emax);
+        const double w = d < -1022 ? 0.0 : __longlong_as_double((long long)(1023 + d) << 52);
+        num += w;
+        den += w * __ldcg(ss + i);
+    }
+    num = oz_block_sum(num);
+    den = oz_block_sum(den);
+    return den > 0.0 ? 0.5 * log2(num * (double)K / den) : 0.0;
+}
+
+// Finishes the statistics of both operands (b_stats: b has its own) and, in
+// the last CTA to finish, chooses the slice count:
+//   error ~ c * 2^(-5S) * gamma_A * gamma_B; c = 2^1.5 covers the truncated
+//   cross terms and the FP64 recombination (measured c ~ 1.4 against the
+//   double-double oracle on uniform inputs).
+__global__ void __launch_bounds__(256)
+oz_prep_finish(OzPrepOp a, OzPrepOp b, int b_stats, double tol, int forced, unsigned *counter, int *S_dev)
+{
+    const int na = max(a.Rp, a.scale2 ? a.Rp2 : 0);
+    const int nb = b_stats ? b.Rp : 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < na + nb; t += gridDim.x * blockDim.x) {
+        if (t < na) oz_finish_row(a, t);
+        else oz_finish_row(b, t - na);
+    }
+    __threadfence();
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const double ga = oz_log2_gamma(a.expo, a.ss, a.rows, a.K);
+    const double gb = b_stats ? oz_log2_gamma(b.expo, b.ss, b.rows, b.K) : ga;
+    if (threadIdx.x == 0) {
+        int S;
+        if (forced > 0) S = forced;
+        else S = (int)ceil((-log2(tol) + ga + gb + 1.5) / 5.0);
+        S_dev[0] = max(1, min(OZ_SMAX, S));
     }
 }
 
@@ -219,20 +343,18 @@ __device__ __forceinline__ uint32_t e4m3_of_digit(int d)
     return ((d < 0) ? 0x80u : 0u) | (uint32_t)((E + 7) << 3) | (uint32_t)mant;
 }
 
-// Writes S digit planes X8[s][r][k] (K-major, rows padded to Rp, k to Kp)
-// for OZ_SPLIT_PER consecutive k per thread.  Padding gets digit 0.  A
-// 16-row x 128-k tile is staged through shared memory so col_k sources are
-// read coalesced (16 rows and 8 k per thread keep enough blocks in flight
-// for the small-K products of blocked factorizations).
+// Slices one 16-row x 128-k tile of an operand: S digit planes X8[s][r][k]
+// (K-major, rows padded to Rp, k to Kp), OZ_SPLIT_PER consecutive k per
+// thread; padding gets digit 0.  The tile is staged through shared memory so
+// col_k sources are read coalesced.
 constexpr int OZ_SPLIT_ROWS = 16, OZ_SPLIT_PER = 8;
 
-__global__ void __launch_bounds__(256)
-oz_split(SrcView v, int rows, int K, int Rp, int Kp, const int *__restrict__ expo,
-         const int *__restrict__ S_dev, uint8_t *__restrict__ X8)
+__device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K, int Rp, int Kp, const int *expo,
+                                              int S, uint8_t *X8, int blk)
 {
     __shared__ double tile[OZ_SPLIT_ROWS][129];
-    const int r0 = blockIdx.y * OZ_SPLIT_ROWS, k0 = blockIdx.x * 128;
-    const int S = *S_dev;
+    const int kblocks = Kp / 128;
+    const int r0 = (blk / kblocks) * OZ_SPLIT_ROWS, k0 = (blk % kblocks) * 128;
     // load: col_k -> threads along rows; row_k -> threads along k
     for (int t = threadIdx.x; t < OZ_SPLIT_ROWS * 128; t += blockDim.x) {
         int rr, kk;
@@ -289,12 +411,12 @@ oz_split(SrcView v, int rows, int K, int Rp, int Kp, const int *__restrict__ exp
     }
 }
 
-// Scale exponents e-4 of the slices' power-of-two scale 2^(e-4) (padded
-// rows: 0; their digits are zero).
-__global__ void oz_scales(const int *__restrict__ expo, int rows, int Rp, int *__restrict__ scale)
+__global__ void __launch_bounds__(256)
+oz_prep_split(OzPrepOp a, OzPrepOp b, const int *__restrict__ S_dev)
 {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < Rp; r += gridDim.x * blockDim.x)
-        scale[r] = r < rows ? expo[r] - 4 : 0;
+    const int S = *S_dev;
+    if ((int)blockIdx.x < a.split_blocks) oz_split_tile(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, S, a.X8, blockIdx.x);
+    else oz_split_tile(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, S, b.X8, blockIdx.x - a.split_blocks);
 }
 
 // acc * 2^shift as a double, built from the FP32 accumulator's bit pattern
@@ -310,76 +432,6 @@ __device__ __forceinline__ double scaled_acc(uint32_t fb, int shift)
     return __longlong_as_double(
         (long long)(sign | ((unsigned long long)ex << 52) | ((unsigned long long)(fb & 0x7FFFFFu) << 29)));
 }
-
-// Slice count: relative Frobenius error ~ c * 2^(-5S) * gamma_A * gamma_B with
-// gamma^2 = (sum_i 2^(2 e_i)) / (sum_i 2^(2 e_i) * ss_i / K): the ratio of the
-// squared row maxima to the squared row norms (1 <= gamma <= sqrt(K)).
-// Block-wide reductions for the 256-thread slice-count kernel (fixed order,
-// so the result is deterministic); every thread gets the result.
-__device__ __forceinline__ int oz_block_max(int v)
-{
-    __shared__ int s[8];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
-    __syncthreads();
-    v = s[0];
-#pragma unroll
-    for (int i = 1; i < 8; i++) v = max(v, s[i]);
-    __syncthreads();
-    return v;
-}
-
-__device__ __forceinline__ double oz_block_sum(double v)
-{
-    __shared__ double s[8];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
-    __syncthreads();
-    v = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
-    __syncthreads();
-    return v;
-}
-
-__device__ double oz_log2_gamma(const int *expo, const double *ss, int rows, int K)
-{
-    int emax = -100000;
-    for (int i = threadIdx.x; i < rows; i += blockDim.x) emax = max(emax, expo[i]);
-    emax = oz_block_max(emax);
-    double num = 0.0, den = 0.0;
-    for (int i = threadIdx.x; i < rows; i += blockDim.x) {
-        // 2^(2(e_i - emax)) from the exponent field (0 below the normal range)
-        const int d = 2 * (expo[i] - emax);
-        const double w = d < -1022 ? 0.0 : __longlong_as_double((long long)(1023 + d) << 52);
-        num += w;
-        den += w * ss[i];
-    }
-    num = oz_block_sum(num);
-    den = oz_block_sum(den);
-    return den > 0.0 ? 0.5 * log2(num * (double)K / den) : 0.0;
-}
-
-__global__ void __launch_bounds__(256)
-oz_choose_slices(const int *ea, const double *ssa, int M, const int *eb, const double *ssb, int N, int K,
-                 double tol, int forced, int *S_dev)
-{
-    const double ga = oz_log2_gamma(ea, ssa, M, K);
-    const double gb = oz_log2_gamma(eb, ssb, N, K);
-    if (threadIdx.x == 0) {
-        int S;
-        if (forced > 0) S = forced;
-        else {
-            // error ~ c * 2^(-5S) * gamma_A * gamma_B; c = 2^1.5 covers the
-            // truncated cross terms and the FP64 recombination (measured
-            // c ~ 1.4 against the double-double oracle on uniform inputs).
-            const double bits = -log2(tol) + ga + gb + 1.5;
-            S = (int)ceil(bits / 5.0);
-        }
-        S_dev[0] = max(1, min(OZ_SMAX, S));
-    }
-}
-
 // ---------------------------------------------------------------------------
 // the tensor-core kernel
 // ---------------------------------------------------------------------------
@@ -413,30 +465,38 @@ struct GroupPlan {
     }
 };
 
-__device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, int bm = OZ_BM)
+__device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, int bm = OZ_BM, int bn = OZ_BN)
 {
     if (p.c_part == 0) return true;
-    const int r0 = tm * bm, r1 = r0 + bm - 1, c0 = tn * OZ_BN, c1 = c0 + OZ_BN - 1;
+    const int r0 = tm * bm, r1 = r0 + bm - 1, c0 = tn * bn, c1 = c0 + bn - 1;
     return p.c_part == 1 ? (r1 >= c0) : (r0 <= c1);
 }
 
-// Drain one diagonal's accumulator for one row (row grow, the tile's OZ_BN
-// columns from gcol0) into the running sum W, or on the last pass into C.
-// The row is walked in 16-column chunks, software-pipelined: the global
-// loads of chunk c+1 (running sums, and C on the last pass) are issued
-// before chunk c is converted and stored.  Loads and stores are never
-// interleaved element by element: the compiler cannot prove that W and C do
-// not overlap, and a load/add/store per element serialised one L2 round trip
-// per element (that, not the MMAs, was the cost of a small-K product).
+// Drain one diagonal's accumulator for one row (row grow, NCOL columns from
+// gcol0) into the running sum W, or on the last pass into C.  The row is
+// walked in CH-column chunks, software-pipelined: the global loads of chunk
+// c+1 (running sums, and C on the last pass) are issued before chunk c is
+// converted and stored.  Loads and stores are never interleaved element by
+// element: the compiler cannot prove that W and C do not overlap, and a
+// load/add/store per element serialised one L2 round trip per element
+// (that, not the MMAs, was the cost of a small-K product).
 __device__ __forceinline__ bool oz_c_keep(const OzParams &p, int grow, int gcol)
 {
     return gcol < p.N && (p.c_part == 0 || (p.c_part == 1 ? grow >= gcol : grow <= gcol));
 }
 
+template <int CH>
+__device__ __forceinline__ void tmem_ld_chunk(uint32_t taddr, uint32_t (&r)[CH]);
+template <>
+__device__ __forceinline__ void tmem_ld_chunk<16>(uint32_t taddr, uint32_t (&r)[16]) { tmem_ld_32x32b_x16(taddr, r); }
+template <>
+__device__ __forceinline__ void tmem_ld_chunk<8>(uint32_t taddr, uint32_t (&r)[8]) { tmem_ld_32x32b_x8(taddr, r); }
+
+template <int NCOL, int CH>
 __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, int grow, int gcol0, int rs,
                                              bool first, bool last)
 {
-    constexpr int CH = 16, NCH = OZ_BN / CH;
+    constexpr int NCH = NCOL / CH;
     const bool row_ok = grow < p.M;
     const bool need_c = last && row_ok && p.beta != 0.0;
     const double *wrow = p.W + (size_t)gcol0 * p.Mp + grow;
@@ -470,7 +530,7 @@ __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, 
             }
         }
         uint32_t r[CH];
-        tmem_ld_32x32b_x16(taddr + (uint32_t)(c * CH), r);
+        tmem_ld_chunk<CH>(taddr + (uint32_t)(c * CH), r);
         tmem_ld_wait();
         const int cb = c * CH;
 #pragma unroll
@@ -491,22 +551,44 @@ __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, 
     }
 }
 
-__global__ void __launch_bounds__(OZ_THREADS, 1)
+// 1-CTA kernel, BM = 128 rows by BN = 256 or 128 columns.  Warp 0 issues the
+// TMA loads, warp 1 the MMAs, warps 2..9 drain: two warps per TMEM lane
+// quarter (a warp may only read the 32 TMEM lanes of its rank within its
+// warpgroup), each taking half of the tile's columns.  TMEM holds 512/BN
+// accumulator buffers, so the MMAs run up to that many diagonal groups ahead
+// of the drain.
+template <int BN>
+struct OzCfg {
+    static constexpr int NBUF = 512 / BN;
+    static constexpr int B_BYTES = BN * OZ_BK;
+    static constexpr int STAGE_BYTES = OZ_A_BYTES + B_BYTES;
+    static constexpr int STAGES = (BN == 256) ? 4 : 6;
+    static constexpr int EPI_WARPS = 8;
+    static constexpr int THREADS = 64 + 32 * EPI_WARPS;
+    static constexpr int DRAIN_COLS = BN / 2;
+    static constexpr int DRAIN_CH = 8;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(OzCfg<BN>::THREADS, 1)
 oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
 {
+    using Cfg = OzCfg<BN>;
+    constexpr int STAGES = Cfg::STAGES, NBUF = Cfg::NBUF, STAGE_BYTES = Cfg::STAGE_BYTES;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *bars = (uint64_t *)(smem + OZ_STAGES * OZ_STAGE_BYTES);
-    uint64_t *full = bars, *empty = bars + OZ_STAGES;
-    uint64_t *tfull = bars + 2 * OZ_STAGES, *tempty = tfull + 2;
-    uint32_t *tmem_slot = (uint32_t *)(tempty + 2);
+    uint64_t *bars = (uint64_t *)(smem + STAGES * STAGE_BYTES);
+    uint64_t *full = bars, *empty = bars + STAGES;
+    uint64_t *tfull = bars + 2 * STAGES, *tempty = tfull + NBUF;
+    uint32_t *tmem_slot = (uint32_t *)(tempty + NBUF);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int *status = p.status;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < OZ_STAGES; i++) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
-        for (int i = 0; i < 2; i++) { mbar_init(&tfull[i], 1); mbar_init(&tempty[i], 128); }
+        for (int i = 0; i < STAGES; i++) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
+        for (int i = 0; i < NBUF; i++) { mbar_init(&tfull[i], 1); mbar_init(&tempty[i], 32 * Cfg::EPI_WARPS); }
         fence_barrier_init();
         prefetch_tmap(&tmA);
         prefetch_tmap(&tmB);
@@ -532,7 +614,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int tm = t % p.tiles_m, tn = t / p.tiles_m;
-                if (!tile_needed(p, tm, tn)) continue;
+                if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
                 for (int q = gp.S - 1; q >= 0 && ok; q--) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
@@ -541,32 +623,32 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         const int kb0 = ch * gp.kch_blocks, kb1 = min(gp.nkb, kb0 + gp.kch_blocks);
                         for (int kb = kb0; kb < kb1; kb++) {
                             if (!mbar_wait(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
-                            uint8_t *sa = smem + stage * OZ_STAGE_BYTES;
-                            mbar_arrive_expect_tx(&full[stage], OZ_STAGE_BYTES);
+                            uint8_t *sa = smem + stage * STAGE_BYTES;
+                            mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
                             tma_load_2d(sa, &tmA, &full[stage], kb * OZ_BK, s * p.Mp + tm * OZ_BM);
-                            tma_load_2d(sa + OZ_A_BYTES, &tmB, &full[stage], kb * OZ_BK, t2 * p.Np + tn * OZ_BN);
-                            if (++stage == OZ_STAGES) { stage = 0; phase ^= 1u; }
+                            tma_load_2d(sa + OZ_A_BYTES, &tmB, &full[stage], kb * OZ_BK, t2 * p.Np + tn * BN);
+                            if (++stage == STAGES) { stage = 0; phase ^= 1u; }
                         }
                     }
                 }
             }
             // drain: wait (bounded) until every issued load has landed
-            for (int i = 0; i < OZ_STAGES; i++) {
+            for (int i = 0; i < STAGES; i++) {
                 mbar_wait(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY);
-                if (++stage == OZ_STAGES) { stage = 0; phase ^= 1u; }
+                if (++stage == STAGES) { stage = 0; phase ^= 1u; }
             }
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_e4m3_f32(OZ_BM, OZ_BN);
+            constexpr uint32_t idesc = idesc_e4m3_f32(OZ_BM, BN);
             int stage = 0, buf = 0;
             uint32_t phase = 0, tphase = 0;
             bool ok = true;
             const uint32_t smem_base = smem_u32(smem);
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int tm = t % p.tiles_m, tn = t / p.tiles_m;
-                if (!tile_needed(p, tm, tn)) continue;
+                if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
                 for (int q = gp.S - 1; q >= 0 && ok; q--) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
@@ -574,7 +656,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         const int g1 = min(nitems, g0 + gp.items_per_group);
                         if (!mbar_wait(&tempty[buf], tphase ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
                         tc_fence_after();
-                        const uint32_t d_tmem = tmem_base + (uint32_t)(buf * OZ_BN);
+                        const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
                         uint32_t acc = 0;
                         for (int it = g0; it < g1 && ok; it++) {
                             const int ch = it % gp.nchunks;
@@ -582,7 +664,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                             for (int kb = kb0; kb < kb1; kb++) {
                                 if (!mbar_wait(&full[stage], phase, status, TC_TIMEOUT_FULL)) { ok = false; break; }
                                 tc_fence_after();
-                                const uint32_t a_addr = smem_base + stage * OZ_STAGE_BYTES;
+                                const uint32_t a_addr = smem_base + stage * STAGE_BYTES;
                                 const uint32_t b_addr = a_addr + OZ_A_BYTES;
 #pragma unroll
                                 for (int kk = 0; kk < OZ_BK / 32; kk++) {
@@ -591,25 +673,26 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                                     acc = 1;
                                 }
                                 mma_commit(&empty[stage]);
-                                if (++stage == OZ_STAGES) { stage = 0; phase ^= 1u; }
+                                if (++stage == STAGES) { stage = 0; phase ^= 1u; }
                             }
                         }
                         mma_commit(&tfull[buf]);
-                        if (++buf == 2) { buf = 0; tphase ^= 1u; }
+                        if (++buf == NBUF) { buf = 0; tphase ^= 1u; }
                     }
                 }
             }
         }
     } else {
-        // ---------------- epilogue (warps 2..5) ----------------
+        // ---------------- drain (warps 2..9) ----------------
         const int quarter = warp & 3;               // TMEM lane window of this warp
+        const int half = (warp - 2) >> 2;           // which half of the tile's columns
         const int row = quarter * 32 + lane;
         int buf = 0;
         uint32_t tphase = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
             const int tm = t % p.tiles_m, tn = t / p.tiles_m;
-            if (!tile_needed(p, tm, tn)) continue;
+            if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
             const int grow = tm * OZ_BM + row;
             const int rexp = p.row_exp[grow];
             bool first = true;
@@ -623,12 +706,14 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                     ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tphase, status, TC_TIMEOUT_TMEM_FULL));
                     if (!ok) break;
                     tc_fence_after();
-                    const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * OZ_BN);
-                    oz_drain_row(p, taddr, grow, tn * OZ_BN, rs, first, last);
+                    const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) +
+                                           (uint32_t)(buf * BN + half * Cfg::DRAIN_COLS);
+                    oz_drain_row<Cfg::DRAIN_COLS, Cfg::DRAIN_CH>(p, taddr, grow, tn * BN + half * Cfg::DRAIN_COLS,
+                                                                 rs, first, last);
                     tc_fence_before();
                     mbar_arrive(&tempty[buf]);
                     first = false;
-                    if (++buf == 2) { buf = 0; tphase ^= 1u; }
+                    if (++buf == NBUF) { buf = 0; tphase ^= 1u; }
                 }
             }
         }
@@ -802,7 +887,7 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
                     if (!ok) break;
                     tc_fence_after();
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * OZ_BN);
-                    oz_drain_row(p, taddr, grow, tn * OZ_BN, rs, first, last);
+                    oz_drain_row<OZ_BN, 16>(p, taddr, grow, tn * OZ_BN, rs, first, last);
                     tc_fence_before();
                     mbar_arrive_cluster(buf ? tempty_cl1 : tempty_cl0);
                     first = false;
@@ -891,6 +976,18 @@ bool oz_use_pair(int M)
     return env != 0 && M > OZ_BM;
 }
 
+// Column tile: 128 when N fits in it (the rank-nb updates of blocked
+// factorizations have N = nb = 128) or when 256-wide tiles would leave most
+// SMs idle; 256 otherwise (half the A-tile reloads per output column).  The
+// CTA-pair kernel always uses 256.
+int oz_tile_n(int M, int N, int sms, bool pair)
+{
+    if (pair) return OZ_BN;
+    if (N <= 128) return 128;
+    const long long tiles256 = ((M + OZ_BM - 1) / OZ_BM) * (long long)((N + OZ_BN - 1) / OZ_BN);
+    return tiles256 < sms ? 128 : OZ_BN;
+}
+
 // Workspace layout for one Ozaki product.
 struct OzBuffers {
     uint8_t *A8, *B8;
@@ -924,38 +1021,52 @@ gbx_status oz_buffers(gbx_ctx *ctx, int Mp, int Np, int Kp, int nW, OzBuffers &b
     return GBX_OK;
 }
 
-gbx_status split_operand(gbx_ctx *ctx, const SrcView &v, int rows, int K, int Rp, int Kp, int *expo, double *ss,
-                         const int *S_dev, uint8_t *X8, int *scale, bool stats_only, int *status)
+// col_k statistics partition: K chunk per CTA of at most OZ_STATS_KCH,
+// smaller when the 32-row blocks alone would leave SMs idle.
+constexpr int OZ_STATS_KCH = 1024;
+
+OzPrepOp oz_prep_op(gbx_ctx *ctx, const SrcView &v, int rows, int K, int Rp, int Kp, int *expo, double *ss,
+                    int *scale, uint8_t *X8, bool stats)
+{
+    OzPrepOp o{};
+    o.v = v; o.rows = rows; o.K = K; o.Rp = Rp; o.Kp = Kp;
+    o.expo = expo; o.ss = ss; o.scale = scale; o.X8 = X8;
+    o.rblocks = (rows + 31) / 32;
+    o.kch = OZ_STATS_KCH;
+    if (!v.row_k)
+        while (o.kch > 64 && (long long)o.rblocks * ((K + o.kch - 1) / o.kch) < 2LL * gbx_ctx_sms(ctx)) o.kch >>= 1;
+    o.nkb = (K + o.kch - 1) / o.kch;
+    o.stat_blocks = !stats ? 0 : (v.row_k ? (rows + 7) / 8 : o.rblocks * o.nkb);
+    o.split_blocks = (Kp / 128) * (Rp / OZ_SPLIT_ROWS);
+    return o;
+}
+
+// The three preparation launches (statistics, finish + slice count, slicing)
+// for op(A) and, unless it is op(A) itself, op(B)^T.
+gbx_status oz_prepare(gbx_ctx *ctx, OzPrepOp &a, OzPrepOp &b, bool b_stats, double tol, int forced, int *status,
+                      unsigned *counter, int *S_dev)
 {
     cudaStream_t s = S_(ctx);
-    if (stats_only) {
-        if (v.row_k) {
-            oz_stats_rowk<<<(rows * 32 + 255) / 256, 256, 0, s>>>(v, rows, K, expo, ss, status);
-            gbx_count_launch(ctx, 1);
-        } else {
-            // K chunk per block: at most OZ_STATS_KCH, smaller when the row
-            // blocks alone would leave SMs idle
-            int kch = OZ_STATS_KCH;
-            const long long rblocks = (rows + 31) / 32;
-            while (kch > 64 && rblocks * ((K + kch - 1) / kch) < 2LL * gbx_ctx_sms(ctx)) kch >>= 1;
-            const int nkb = (K + kch - 1) / kch;
-            void *p;
-            gbx_status st = gbx_ws(ctx, GBX_WS_TMP2, sizeof(SsAcc) * (size_t)nkb * rows, &p);
-            if (st != GBX_OK) return st;
-            dim3 g((unsigned)rblocks, nkb);
-            oz_stats_colk<<<g, 256, 0, s>>>(v, rows, K, kch, (SsAcc *)p, status);
-            oz_stats_combine<<<std::min(1024, (rows + 255) / 256), 256, 0, s>>>((const SsAcc *)p, rows, nkb,
-                                                                                expo, ss);
-            gbx_count_launch(ctx, 2);
-        }
-        oz_scales<<<std::min(1024, (Rp + 255) / 256), 256, 0, s>>>(expo, rows, Rp, scale);
-        gbx_count_launch(ctx, 1);
-        return gbx_check_launch(ctx, "ozaki stats");
+    const size_t pa = a.v.row_k ? 0 : (size_t)a.nkb * a.rows, pb = (!b_stats || b.v.row_k) ? 0 : (size_t)b.nkb * b.rows;
+    if (pa + pb) {
+        void *p;
+        gbx_status st = gbx_ws(ctx, GBX_WS_TMP2, sizeof(SsAcc) * (pa + pb), &p);
+        if (st != GBX_OK) return st;
+        a.part = (SsAcc *)p;
+        b.part = (SsAcc *)p + pa;
     }
-    dim3 g(Kp / 128, Rp / OZ_SPLIT_ROWS);
-    oz_split<<<g, 256, 0, s>>>(v, rows, K, Rp, Kp, expo, S_dev, X8);
-    gbx_count_launch(ctx, 1);
-    return gbx_check_launch(ctx, "ozaki split");
+    if (!b_stats) b.stat_blocks = 0;
+    const long long nstat = (long long)a.stat_blocks + b.stat_blocks;
+    const long long nsplit = (long long)a.split_blocks + b.split_blocks;
+    if (nstat > 0x7fffffffLL || nsplit > 0x7fffffffLL)
+        return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: operands too large");
+    oz_prep_stats<<<(unsigned)nstat, 256, 0, s>>>(a, b, status, counter);
+    const long long rows = (long long)std::max(a.Rp, a.scale2 ? a.Rp2 : 0) + (b_stats ? b.Rp : 0);
+    const int fin = (int)std::max(1LL, std::min<long long>(2LL * gbx_ctx_sms(ctx), (rows + 255) / 256));
+    oz_prep_finish<<<fin, 256, 0, s>>>(a, b, b_stats ? 1 : 0, tol, forced, counter, S_dev);
+    oz_prep_split<<<(unsigned)nsplit, 256, 0, s>>>(a, b, S_dev);
+    gbx_count_launch(ctx, 3);
+    return gbx_check_launch(ctx, "ozaki prepare");
 }
 
 struct OzProblem {
@@ -973,7 +1084,8 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
 {
     if (pr.K > 0x3fffffff) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: K too large");
     const bool pair = oz_use_pair(pr.M);
-    const int Mp = (int)rup(pr.M, pair ? OZ2_BM : OZ_BM), Np = (int)rup(pr.N, OZ_BN);
+    const int bn = oz_tile_n(pr.M, pr.N, gbx_ctx_sms(ctx), pair);
+    const int Mp = (int)rup(pr.M, pair ? OZ2_BM : OZ_BM), Np = (int)rup(pr.N, bn);
     const int Kp = (int)rup(std::max(pr.K, 1), OZ_BK);
     OzBuffers b;
     gbx_status st;
@@ -984,49 +1096,37 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     cudaMemsetAsync(b.status, 0, 64, s);
 
     gbx_timer_begin(ctx, GBX_TIMER_OZAKI_SPLIT);
-    if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Mp, Kp, b.ea, b.ssa, b.S, b.A8, b.rsa, true, b.status)) !=
-        GBX_OK)
-        return st;
-    if (!pr.same_ab && (st = split_operand(ctx, pr.b, pr.N, pr.K, Np, Kp, b.eb, b.ssb, b.S, b.B8, b.csb, true,
-                                           b.status)) != GBX_OK)
-        return st;
-    const int *eb = pr.same_ab ? b.ea : b.eb;
-    const double *ssb = pr.same_ab ? b.ssa : b.ssb;
-    oz_choose_slices<<<1, 256, 0, s>>>(b.ea, b.ssa, pr.M, eb, ssb, pr.N, pr.K, tol, forced, b.S);
-    gbx_count_launch(ctx, 1);
-    if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Mp, Kp, b.ea, b.ssa, b.S, b.A8, b.rsa, false, b.status)) !=
-        GBX_OK)
-        return st;
+    // op(A): statistics and slices; op(B)^T: its own, or for a symmetric
+    // rank-k update the A slices themselves (re-sliced into the Np-row layout
+    // of the B tiles when Np != Mp, with scales mirrored from op(A)'s rows)
+    OzPrepOp oa = oz_prep_op(ctx, pr.a, pr.M, pr.K, Mp, Kp, b.ea, b.ssa, b.rsa, b.A8, true);
+    OzPrepOp ob{};
     uint8_t *B8 = b.B8;
     const int *csb = b.csb;
-    if (pr.same_ab) {
-        // B slices are the A slices; rows padded to Np (Np >= Mp here since M == N)
+    bool b_stats = false;
+    if (!pr.same_ab) {
+        ob = oz_prep_op(ctx, pr.b, pr.N, pr.K, Np, Kp, b.eb, b.ssb, b.csb, b.B8, true);
+        b_stats = true;
+    } else if (Np != Mp) {
+        ob = oz_prep_op(ctx, pr.a, pr.M, pr.K, Np, Kp, b.ea, b.ssa, b.csb, b.B8, false);
+        oa.scale2 = b.csb;
+        oa.Rp2 = Np;
+    } else {
         B8 = b.A8;
         csb = b.rsa;
-        if (Np != Mp) {
-            // re-split into the Np-row layout the B tiles expect
-            if ((st = split_operand(ctx, pr.a, pr.M, pr.K, Np, Kp, b.ea, b.ssa, b.S, b.B8, b.csb, false,
-                                    b.status)) != GBX_OK)
-                return st;
-            oz_scales<<<std::min(1024, (Np + 255) / 256), 256, 0, s>>>(b.ea, pr.M, Np, b.csb);
-            gbx_count_launch(ctx, 1);
-            B8 = b.B8;
-            csb = b.csb;
-        }
-    } else if ((st = split_operand(ctx, pr.b, pr.N, pr.K, Np, Kp, b.eb, b.ssb, b.S, b.B8, b.csb, false,
-                                   b.status)) != GBX_OK) {
-        return st;
     }
+    if ((st = oz_prepare(ctx, oa, ob, b_stats, tol, forced, b.status, (unsigned *)(b.S + 4), b.S)) != GBX_OK)
+        return st;
     gbx_timer_end(ctx);
 
     CUtensorMap tmA, tmB;
     if (!make_map(&tmA, b.A8, (long long)OZ_SMAX * Mp, Kp, OZ_BM) ||
-        !make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : OZ_BN))
+        !make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : bn))
         return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
 
     OzParams p{};
     p.M = pr.M; p.N = pr.N; p.Mp = Mp; p.Np = Np; p.Kp = Kp;
-    p.tiles_m = Mp / (pair ? OZ2_BM : OZ_BM); p.tiles_n = Np / OZ_BN;
+    p.tiles_m = Mp / (pair ? OZ2_BM : OZ_BM); p.tiles_n = Np / bn;
     p.S = b.S;
     p.row_exp = b.rsa;
     p.col_exp = csb;
@@ -1046,8 +1146,10 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         std::lock_guard<std::mutex> lk(attr_mu);
         max_pairs = (dev >= 0 && dev < 64) ? max_pairs_of[dev] : 0;
         if (max_pairs == 0) {
-            if (cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM) !=
-                    cudaSuccess ||
+            if (cudaFuncSetAttribute(oz_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)OzCfg<256>::SMEM) != cudaSuccess ||
+                cudaFuncSetAttribute(oz_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)OzCfg<128>::SMEM) != cudaSuccess ||
                 cudaFuncSetAttribute(oz_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OZ2_SMEM) != cudaSuccess)
                 return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: shared memory attribute");
@@ -1072,7 +1174,10 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         oz_gemm2_kernel<<<2 * npairs, OZ_THREADS, OZ2_SMEM, s>>>(tmA, tmB, p);
     } else {
         const int grid = std::min(ntiles, gbx_ctx_sms(ctx));
-        oz_gemm_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(tmA, tmB, p);
+        if (bn == 128)
+            oz_gemm_kernel<128><<<grid, OzCfg<128>::THREADS, OzCfg<128>::SMEM, s>>>(tmA, tmB, p);
+        else
+            oz_gemm_kernel<256><<<grid, OzCfg<256>::THREADS, OzCfg<256>::SMEM, s>>>(tmA, tmB, p);
     }
     gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);

@@ -3,14 +3,16 @@
 // on one cuBLAS handle and the legacy stream, runtime-blas.c:14-23).
 //
 // Host threads submit operations on device-resident operands and wait on a
-// ticket.  A dispatcher thread repeatedly takes everything queued, groups
-// the small DGEMM/DTRSM requests into one grouped kernel launch and runs the
-// large ones with the regular routines, each on the stream of a free slot
-// (one context per slot), so work that arrives while other work is on the
-// GPU is admitted as slots free up and overlaps with it.  A completion
-// thread watches the slots' events, completes tickets and records per-call
-// latency (submit to completion) for p50/p99.
-//
+// ticket.  Each slot (one context: stream and workspace) has a worker
+// thread.  A free worker takes the next queued work -- every small
+// DGEMM/DTRSM request queued at that moment, grouped into one kernel
+// launch, or the next large request -- launches it on its own stream,
+// waits for it, completes the tickets and records per-call latency (submit
+// to completion) for p50/p99.  Work that arrives while other work is on the
+// GPU is admitted as slots free up and overlaps with it; the host-side cost
+// of enqueueing (argument checks, tensor-map encoding, launches) is spread
+// over the workers instead of one dispatcher thread.
+
 // Routing depends only on the operation (small GEMM: m, n <= 512 and
 // k <= 4096; small TRSM: order <= 256; everything else runs alone), so a
 // result is bit-identical whether the call was served alone or in a mix.
@@ -48,10 +50,6 @@ struct Request {
 
 struct Slot {
     gbx_ctx *ctx = nullptr;
-    cudaEvent_t ev = nullptr;
-    bool busy = false;       // taken by the dispatcher
-    bool launched = false;   // its event was recorded behind the work
-    std::vector<Request *> reqs;
 };
 
 bool is_small(const gbx_op &o)
@@ -72,7 +70,7 @@ struct gbx_server {
     std::vector<Request *> finished;   // completed, not yet waited for
     uint64_t next_ticket = 1;
     bool stop = false;
-    std::thread dispatcher, completer;
+    std::vector<std::thread> workers;
     // latency record (microseconds), ring of the last 1M calls
     std::vector<float> lat;
     size_t lat_next = 0, completed = 0, batches = 0, grouped_calls = 0;
@@ -124,121 +122,66 @@ extern "C" gbx_status gbx_ops_run(gbx_ctx *ctx, const gbx_op *ops, int count)
 
 namespace {
 
-void dispatcher_loop(gbx_server *s)
+void complete(gbx_server *s, const std::vector<Request *> &reqs, gbx_status st)
 {
-    cudaSetDevice(s->device);
-    std::unique_lock<std::mutex> lk(s->mu);
-    while (true) {
-        s->cv_work.wait(lk, [&] {
-            if (s->stop) return true;
-            if (s->queue.empty()) return false;
-            for (auto &sl : s->slots)
-                if (!sl.busy) return true;
-            return false;
-        });
-        if (s->stop && s->queue.empty()) break;
-        if (s->queue.empty()) continue;
-        // take everything queued; small ones go together into one slot
-        std::vector<Request *> small, large;
-        while (!s->queue.empty()) {
-            Request *r = s->queue.front();
-            s->queue.pop_front();
-            (is_small(r->op) ? small : large).push_back(r);
-        }
-        auto take_slot = [&]() -> Slot * {
-            for (auto &sl : s->slots)
-                if (!sl.busy) return &sl;
-            return nullptr;
-        };
-        std::vector<Request *> leftover;
-        if (!small.empty()) {
-            Slot *sl = take_slot();
-            if (sl) {
-                sl->busy = true;
-                sl->reqs = small;
-                std::vector<gbx_op> ops;
-                ops.reserve(small.size());
-                for (auto *r : small) ops.push_back(r->op);
-                lk.unlock();
-                gbx_status st = gbx_grouped_launch_inline(sl->ctx, ops.data(), (int)ops.size());
-                cudaEventRecord(sl->ev, (cudaStream_t)gbx_ctx_get_stream(sl->ctx));
-                lk.lock();
-                sl->launched = true;
-                for (auto *r : small) r->status = st;
-                s->batches++;
-                s->grouped_calls += small.size();
-            } else {
-                leftover.insert(leftover.end(), small.begin(), small.end());
-            }
-        }
-        for (auto *r : large) {
-            Slot *sl = take_slot();
-            if (!sl) {
-                leftover.push_back(r);
-                continue;
-            }
-            sl->busy = true;
-            sl->reqs.assign(1, r);
-            lk.unlock();
-            gbx_status st = run_request(sl->ctx, r->op);
-            cudaEventRecord(sl->ev, (cudaStream_t)gbx_ctx_get_stream(sl->ctx));
-            lk.lock();
-            sl->launched = true;
-            r->status = st;
-            s->batches++;
-        }
-        // requests that found no free slot go back to the front, in order
-        for (auto it = leftover.rbegin(); it != leftover.rend(); ++it) s->queue.push_front(*it);
-        s->cv_done.notify_all();   // wake the completer
+    const auto now = clk::now();
+    for (auto *r : reqs) {
+        if (r->status == GBX_OK) r->status = st;
+        r->t_done = now;
+        r->done = true;
+        const float us = (float)std::chrono::duration<double, std::micro>(r->t_done - r->t_submit).count();
+        if (s->lat.size() < (1u << 20)) s->lat.push_back(us);
+        else s->lat[s->lat_next++ % s->lat.size()] = us;
+        s->completed++;
+        s->finished.push_back(r);
     }
 }
 
-void completer_loop(gbx_server *s)
+void worker_loop(gbx_server *s, Slot *sl)
 {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
     while (true) {
-        bool any_busy = false, progressed = false;
-        for (auto &sl : s->slots) {
-            if (!sl.busy) continue;
-            any_busy = true;
-            if (!sl.launched) continue;   // the dispatcher is still enqueueing
-            lk.unlock();
-            cudaError_t q = cudaEventQuery(sl.ev);
-            lk.lock();
-            if (q == cudaErrorNotReady) continue;
-            gbx_status st = GBX_OK;
-            if (q != cudaSuccess) st = GBX_ERR_CUDA;
-            else st = gbx_ctx_sync(sl.ctx);   // collects bounded-wait status words
-            const auto now = clk::now();
-            for (auto *r : sl.reqs) {
-                if (r->status == GBX_OK) r->status = st;
-                r->t_done = now;
-                r->done = true;
-                const float us =
-                    (float)std::chrono::duration<double, std::micro>(r->t_done - r->t_submit).count();
-                if (s->lat.size() < (1u << 20)) s->lat.push_back(us);
-                else s->lat[s->lat_next++ % s->lat.size()] = us;
-                s->completed++;
-                s->finished.push_back(r);
+        s->cv_work.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+        if (s->queue.empty()) {
+            if (s->stop) break;
+            continue;
+        }
+        // take the front request; if it is small, every small request queued
+        // now goes with it into one grouped launch
+        std::vector<Request *> mine;
+        const bool small = is_small(s->queue.front()->op);
+        if (small) {
+            for (auto it = s->queue.begin(); it != s->queue.end();) {
+                if (is_small((*it)->op)) {
+                    mine.push_back(*it);
+                    it = s->queue.erase(it);
+                } else {
+                    ++it;
+                }
             }
-            sl.reqs.clear();
-            sl.busy = false;
-            sl.launched = false;
-            progressed = true;
+        } else {
+            mine.push_back(s->queue.front());
+            s->queue.pop_front();
         }
-        if (progressed) {
-            s->cv_done.notify_all();
-            s->cv_work.notify_all();
+        if (!s->queue.empty()) s->cv_work.notify_one();   // more work for another worker
+        lk.unlock();
+        gbx_status st;
+        if (small) {
+            std::vector<gbx_op> ops;
+            ops.reserve(mine.size());
+            for (auto *r : mine) ops.push_back(r->op);
+            st = gbx_grouped_launch_inline(sl->ctx, ops.data(), (int)ops.size());
+        } else {
+            st = run_request(sl->ctx, mine[0]->op);
         }
-        if (s->stop && !any_busy && s->queue.empty()) break;
-        if (!any_busy) {
-            s->cv_done.wait_for(lk, std::chrono::milliseconds(5));
-        } else if (!progressed) {
-            lk.unlock();
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
-            lk.lock();
-        }
+        const gbx_status sync = gbx_ctx_sync(sl->ctx);   // also collects bounded-wait status words
+        if (st == GBX_OK) st = sync;
+        lk.lock();
+        s->batches++;
+        if (small) s->grouped_calls += mine.size();
+        complete(s, mine, st);
+        s->cv_done.notify_all();
     }
 }
 
@@ -253,12 +196,9 @@ extern "C" gbx_status gbx_server_create(int device, int nslots, size_t mem_budge
     s->device = device;
     s->slots.resize(nslots);
     for (auto &sl : s->slots) {
-        if (gbx_ctx_create(&sl.ctx, device) != GBX_OK ||
-            cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
-            for (auto &q : s->slots) {
+        if (gbx_ctx_create(&sl.ctx, device) != GBX_OK) {
+            for (auto &q : s->slots)
                 if (q.ctx) gbx_ctx_destroy(q.ctx);
-                if (q.ev) cudaEventDestroy(q.ev);
-            }
             delete s;
             return GBX_ERR_CUDA;
         }
@@ -267,8 +207,7 @@ extern "C" gbx_status gbx_server_create(int device, int nslots, size_t mem_budge
     cudaMemGetInfo(&free_b, &total_b);
     const size_t auto_budget = free_b / 10 * 8;   // 80% of what is free now
     s->budget = mem_budget ? std::min(mem_budget, auto_budget) : auto_budget;
-    s->dispatcher = std::thread(dispatcher_loop, s);
-    s->completer = std::thread(completer_loop, s);
+    for (auto &sl : s->slots) s->workers.emplace_back(worker_loop, s, &sl);
     *out = s;
     return GBX_OK;
 }
@@ -392,13 +331,11 @@ extern "C" gbx_status gbx_server_destroy(gbx_server *s)
     }
     s->cv_work.notify_all();
     s->cv_done.notify_all();
-    if (s->dispatcher.joinable()) s->dispatcher.join();
-    if (s->completer.joinable()) s->completer.join();
+    for (auto &w : s->workers)
+        if (w.joinable()) w.join();
     for (auto *r : s->finished) delete r;
-    for (auto &sl : s->slots) {
+    for (auto &sl : s->slots)
         if (sl.ctx) gbx_ctx_destroy(sl.ctx);
-        if (sl.ev) cudaEventDestroy(sl.ev);
-    }
     delete s;
     return GBX_OK;
 }

@@ -128,7 +128,7 @@ def test_cblas_row_major_equals_column_major(lib, f77, p):
     assert np.linalg.norm(Cr[iu] - Cf[iu]) <= tol * np.linalg.norm(Cf[iu])
     # trsm: row-major B (m x n) := alpha * inv(A) B, A lower m x m
     m, n = 21, 9
-    A = rnd(m, m) / m + np.eye(m) * 2
+    A = (rnd(m, m) / m + np.eye(m) * 2).astype(dt)
     B0 = rnd(m, n)
     Br = np.ascontiguousarray(B0.copy())
     _cb(lib, p + "trsm")(101, 141, 122, 111, 131, m, n, sc(al), ptr(np.ascontiguousarray(A)), m, ptr(Br), n)
