@@ -43,6 +43,9 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# The serving workload keeps 16 slot streams busy at once; with the default 8
+# hardware work queues, streams would share queues and falsely serialise.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np  # noqa: E402
 
@@ -61,6 +64,8 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", choices=WORKLOADS, default="dgemm")
     p.add_argument("--n", type=int, default=0, help="problem size (0: the workload's default)")
+    p.add_argument("--m", type=int, default=0, help="dgemm/ozaki: rows of C (0: n)")
+    p.add_argument("--k", type=int, default=0, help="dgemm/ozaki: inner dimension (0: n)")
     p.add_argument("--trans", default="N", help="dgemv transposition")
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -186,12 +191,13 @@ class Work:
         o = self.orc
         if w in ("dgemm", "ozaki"):
             n = args.n or 8192
-            self.n = n
-            self.a, s = o.matrix(n, n, seed)
-            self.b, s = o.matrix(n, n, s)
-            self.c, s = o.matrix(n, n, s)
-            self.units, self.unit, self.metric = 2.0 * n ** 3 / 1e12, "TFLOP/s", f"{w}_tflops"
-            self.config = {"workload": f"{w}_NN_m{n}_n{n}_k{n}", "m": n, "n": n, "k": n, "lda": n,
+            m, k = args.m or n, args.k or n
+            self.n, self.m, self.k = n, m, k
+            self.a, s = o.matrix(m, k, seed)
+            self.b, s = o.matrix(k, n, s)
+            self.c, s = o.matrix(m, n, s)
+            self.units, self.unit, self.metric = 2.0 * m * n * k / 1e12, "TFLOP/s", f"{w}_tflops"
+            self.config = {"workload": f"{w}_NN_m{m}_n{n}_k{k}", "m": m, "n": n, "k": k, "lda": m,
                            "alpha": 1.0, "beta": 0.5}
         elif w in ("daxpy", "ddot", "dnrm2", "idamax"):
             n = args.n or (1 << 28)
@@ -253,12 +259,12 @@ class Work:
     def device_step(self, dev):
         d, w = self.d, self.kind
         if w == "dgemm":
-            n = self.n
-            dev.dgemm_checked("N", "N", n, n, n, 1.0, d["a"], n, d["b"], n, 0.5, d["c"], n)
+            m, n, k = self.m, self.n, self.k
+            dev.dgemm_checked("N", "N", m, n, k, 1.0, d["a"], m, d["b"], k, 0.5, d["c"], m)
         elif w == "ozaki":
-            n = self.n
-            self.slices = dev.dgemm_ozaki("N", "N", n, n, n, 1.0, d["a"], n, d["b"], n, 0.5,
-                                          d["c"], n)
+            m, n, k = self.m, self.n, self.k
+            self.slices = dev.dgemm_ozaki("N", "N", m, n, k, 1.0, d["a"], m, d["b"], k, 0.5,
+                                          d["c"], m)
         elif w == "daxpy":
             dev.daxpy(self.n, 0.5, d["x"], 1, d["y"], 1)
         elif w == "ddot":
@@ -287,8 +293,8 @@ class Work:
     def f77_step(self, f):
         p, w = self.hp, self.kind
         if w in ("dgemm", "ozaki"):
-            n = self.n
-            f.dgemm("N", "N", n, n, n, 1.0, p["a"], n, p["b"], n, 0.5, p["c"], n)
+            m, n, k = self.m, self.n, self.k
+            f.dgemm("N", "N", m, n, k, 1.0, p["a"], m, p["b"], k, 0.5, p["c"], m)
         elif w == "daxpy":
             f.daxpy(self.n, 0.5, p["x"], 1, p["y"], 1)
         elif w == "ddot":
@@ -313,8 +319,7 @@ class Work:
     def cpu_step(self, cb):
         c, w = self.cc, self.kind
         if w in ("dgemm", "ozaki"):
-            n = self.n
-            cb.dgemm("N", "N", n, n, n, 1.0, c["a"], c["b"], 0.5, c["c"])
+            cb.dgemm("N", "N", self.m, self.n, self.k, 1.0, c["a"], c["b"], 0.5, c["c"])
         elif w == "daxpy":
             cb.daxpy(self.n, 0.5, c["x"], 1, c["y"], 1)
         elif w == "ddot":
@@ -522,30 +527,30 @@ def ozaki_accuracy(dev, work):
     """Relative Frobenius error of one fresh Ozaki call against the
     double-double oracle on 2048 sampled entries."""
     import torch
-    n = work.n
+    m, n, k = work.m, work.n, work.k
     dc = torch.from_numpy(work.c.ravel(order="F")).cuda()
-    used = dev.dgemm_ozaki("N", "N", n, n, n, 1.0, work.d["a"], n, work.d["b"], n, 0.5, dc, n)
-    got = dc.cpu().numpy().reshape(n, n, order="F")
+    used = dev.dgemm_ozaki("N", "N", m, n, k, 1.0, work.d["a"], m, work.d["b"], k, 0.5, dc, m)
+    got = dc.cpu().numpy().reshape(m, n, order="F")
     rng = np.random.default_rng(0)
-    rows = rng.integers(0, n, 2048)
+    rows = rng.integers(0, m, 2048)
     cols = rng.integers(0, n, 2048)
-    ref = work.orc.dgemm_dd_sample("N", "N", n, 1.0, work.a, work.b, 0.5, work.c, rows, cols)
+    ref = work.orc.dgemm_dd_sample("N", "N", k, 1.0, work.a, work.b, 0.5, work.c, rows, cols)
     err = float(np.linalg.norm(got[rows, cols] - ref) / np.linalg.norm(ref))
     return {"rel_err_fro_sampled": err, "slices": used, "samples": 2048, "tol": 1e-14}
 
 
 def bench_ozaki(args, dev, work, stream):
     import torch
-    n = work.n
+    m, n, k = work.m, work.n, work.k
     d = work.d
     for _ in range(max(1, args.warmup - 1)):
-        dev.dgemm_ozaki("N", "N", n, n, n, 1.0, d["a"], n, d["b"], n, 0.5, d["c"], n)
+        dev.dgemm_ozaki("N", "N", m, n, k, 1.0, d["a"], m, d["b"], k, 0.5, d["c"], m)
     dev.sync()
     dev.enable_timing(True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for _ in range(args.steps):
-        dev.dgemm_ozaki("N", "N", n, n, n, 1.0, d["a"], n, d["b"], n, 0.5, d["c"], n)
+        dev.dgemm_ozaki("N", "N", m, n, k, 1.0, d["a"], m, d["b"], k, 0.5, d["c"], m)
     ev1.record(stream)
     ev1.synchronize()
     t = ev0.elapsed_time(ev1) / 1e3
@@ -689,6 +694,10 @@ def run_batched(args):
 # thread calls the library on its own stream and waits) against the serving
 # loop (every thread submits to one server and waits).
 # --------------------------------------------------------------------------
+OP_NAMES = {1: "dgemm", 2: "dtrsm", 3: "dsyrk", 4: "ddot", 5: "dnrm2", 6: "dpotrf", 7: "dgemm_ozaki",
+            8: "dsyrk_ozaki", 9: "dtrsm_ozaki"}
+
+
 def cholesky_calls(n, nb, base, lda, info_ptr, ozaki=False):
     import libgpublas_gb300 as g
     calls = []
@@ -700,7 +709,7 @@ def cholesky_calls(n, nb, base, lda, info_ptr, ozaki=False):
         if rest <= 0:
             continue
         # L21 = A21 L11^-T
-        calls.append(g.GbxOp(kind=2, side=b"R", uplo=b"L", transa=b"T", diag=b"N", m=rest, n=kb,
+        calls.append(g.GbxOp(kind=9 if ozaki else 2, side=b"R", uplo=b"L", transa=b"T", diag=b"N", m=rest, n=kb,
                              alpha=1.0, A=at(k, k), lda=lda, C=at(k + kb, k), ldc=lda))
         # trailing update, block column by block column
         for j in range(k + kb, n, nb):
@@ -743,11 +752,13 @@ def run_serving(args):
     results = {}
 
     def run_mode(mode):
-        server = g.Server(0, slots=8) if mode != "plain" else None
+        server = g.Server(0, slots=nthreads) if mode != "plain" else None
         work = [o.clone() for o in origs]
         torch.cuda.synchronize()
         lat, ncalls, errs = [], [0], []
+        by_kind, thread_s = {}, [0.0] * nthreads
         lock = threading.Lock()
+        t_start = [0.0]
 
         def worker(t):
             A = work[t]
@@ -760,7 +771,7 @@ def run_serving(args):
                     t0 = time.perf_counter()
                     st = d.L.gbx_ops_run(d.ctx, ctypes_ref(op), 1)
                     st2 = d.L.gbx_ctx_sync(d.ctx)
-                    local.append((time.perf_counter() - t0) * 1e6)
+                    local.append((op.kind, (time.perf_counter() - t0) * 1e6))
                     if st or st2:
                         errs.append((t, st, st2))
                         break
@@ -768,16 +779,21 @@ def run_serving(args):
             else:
                 for op in calls:
                     st, us = server.call(op)
-                    local.append(us)
+                    local.append((op.kind, us))
                     if st:
                         errs.append((t, st))
                         break
             with lock:
-                lat.extend(local)
+                lat.extend(us for _, us in local)
                 ncalls[0] += len(local)
+                for kind, us in local:
+                    e = by_kind.setdefault(kind, [0, 0.0])
+                    e[0] += 1
+                    e[1] += us
+                thread_s[t] = time.perf_counter() - t_start[0]
 
         threads = [threading.Thread(target=worker, args=(t,)) for t in range(nthreads)]
-        t0 = time.perf_counter()
+        t0 = t_start[0] = time.perf_counter()
         for th in threads:
             th.start()
         for th in threads:
@@ -810,7 +826,12 @@ def run_serving(args):
                          "tflops": flops / wall / 1e12,
                          "residual_sampled": (res_num / res_den) ** 0.5 if res_den else None,
                          "info_nonzero": int((info != 0).sum().item()), "errors": errs[:4],
-                         "server": srv_stats}
+                         "server": srv_stats,
+                         # per operation kind: calls, mean and summed latency
+                         "by_kind": {OP_NAMES.get(k, str(k)): {"calls": c, "mean_us": tot / c, "sum_s": tot / 1e6}
+                                     for k, (c, tot) in sorted(by_kind.items())},
+                         # each thread's finish time: the slowest thread's call chain bounds the wall
+                         "thread_finish_s": [round(x, 3) for x in thread_s]}
         del work
         torch.cuda.synchronize()
 

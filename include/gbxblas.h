@@ -259,6 +259,13 @@ gbx_status gbx_zgemm_ozaki(gbx_ctx *ctx, char transa, char transb, int m, int n,
 gbx_status gbx_dsyrk_ozaki(gbx_ctx *ctx, char uplo, char trans, int n, int k, double alpha,
                            const double *A, int lda, double beta, double *C, int ldc,
                            double tol, int slices, int *slices_used);
+/* B := alpha*op(A)^-1*B or alpha*B*op(A)^-1 for a triangle of order <= 1024:
+ * op(A)^-1 is formed in FP64 (the triangular solve against I on the DFMA
+ * path), then applied to B as one Ozaki product.  Larger orders run the FP64
+ * DTRSM.  Same arguments as gbx_dtrsm. */
+gbx_status gbx_dtrsm_ozaki(gbx_ctx *ctx, char side, char uplo, char transa, char diag, int m, int n,
+                           double alpha, const double *A, int lda, double *B, int ldb, double tol,
+                           int slices, int *slices_used);
 
 /* ---- grouped execution of many small calls (no reference counterpart) ------
  * A plan turns a list of independent DGEMM / DTRSM operations (device
@@ -280,7 +287,8 @@ enum {
     GBX_OP_POTRF = 6,      /* serving loop: lower Cholesky of the n x n block at
                               C (ldc), n <= 256; int info at (int *)B          */
     GBX_OP_GEMM_OZAKI = 7, /* serving loop: DGEMM through the Ozaki path       */
-    GBX_OP_SYRK_OZAKI = 8  /* serving loop: DSYRK through the Ozaki path       */
+    GBX_OP_SYRK_OZAKI = 8, /* serving loop: DSYRK through the Ozaki path       */
+    GBX_OP_TRSM_OZAKI = 9  /* serving loop: DTRSM through gbx_dtrsm_ozaki      */
 };
 typedef struct {
     int kind;                 /* GBX_OP_GEMM or GBX_OP_TRSM                     */

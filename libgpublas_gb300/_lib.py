@@ -88,6 +88,7 @@ def _declare(L):
     L.gbx_dsyrk.argtypes = [_P, _CH, _CH, _I, _I, _D, _P, _I, _D, _P, _I]
     L.gbx_dtrsm.argtypes = [_P, _CH, _CH, _CH, _CH, _I, _I, _D, _P, _I, _P, _I]
     L.gbx_dtrmm.argtypes = [_P, _CH, _CH, _CH, _CH, _I, _I, _D, _P, _I, _P, _I]
+    L.gbx_dtrsm_ozaki.argtypes = [_P, _CH, _CH, _CH, _CH, _I, _I, _D, _P, _I, _P, _I, _D, _I, C.POINTER(_I)]
     L.gbx_dger.argtypes = [_P, _I, _I, _D, _P, _I, _P, _I, _P, _I]
     L.gbx_dsymv.argtypes = [_P, _CH, _I, _D, _P, _I, _P, _I, _D, _P, _I]
     L.gbx_dtrsv.argtypes = [_P, _CH, _CH, _CH, _I, _P, _I, _P, _I]
@@ -521,4 +522,10 @@ class Device:
         self._ok(self.L.gbx_dsyrk_ozaki(self.ctx, _ch(uplo), _ch(trans), n, k, alpha, _dp(a), lda,
                                         beta, _dp(c), ldc, tol, slices, C.byref(used)),
                  "dsyrk_ozaki")
+        return used.value
+
+    def dtrsm_ozaki(self, side, uplo, ta, diag, m, n, alpha, a, lda, b, ldb, tol=0.0, slices=0):
+        used = C.c_int(0)
+        self._ok(self.L.gbx_dtrsm_ozaki(self.ctx, _ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n, alpha, _dp(a),
+                                        lda, _dp(b), ldb, tol, slices, C.byref(used)), "dtrsm_ozaki")
         return used.value

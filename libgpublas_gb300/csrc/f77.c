@@ -269,13 +269,17 @@ static void trxm(const char *name, trxm_fn fn, const char *side, const char *upl
     gbx_operand oa = {.ld = *lda}, ob = {0};
     if (*alpha != 0.0) TRY(gbx_place_in(ctx, GBX_WS_STAGE_A, a, na, na, *lda, 8, 1, &oa));
     TRY(gbx_place_in(ctx, GBX_WS_STAGE_B, b, *m, *n, *ldb, 8, *alpha != 0.0, &ob));
+    const int ozaki = fn == gbx_dtrsm && gbx_get_config()->precision_ozaki && *alpha != 0.0;
     if (srv) {
         gbx_op op = {0};
-        op.kind = GBX_OP_TRSM;
+        op.kind = ozaki ? GBX_OP_TRSM_OZAKI : GBX_OP_TRSM;
         op.side = *side; op.uplo = *uplo; op.transa = *transa; op.diag = *diag;
         op.m = *m; op.n = *n; op.alpha = *alpha;
         op.A = oa.dev; op.lda = oa.ld; op.C = ob.dev; op.ldc = ob.ld;
         TRY(served(ctx, srv, &op));
+    } else if (ozaki) {
+        TRY(gbx_dtrsm_ozaki(ctx, *side, *uplo, *transa, *diag, *m, *n, *alpha, oa.dev, oa.ld, ob.dev, ob.ld,
+                            gbx_get_config()->ozaki_tol, 0, NULL));
     } else {
         TRY(fn(ctx, *side, *uplo, *transa, *diag, *m, *n, *alpha, oa.dev, oa.ld, ob.dev, ob.ld));
     }

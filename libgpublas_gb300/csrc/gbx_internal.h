@@ -34,6 +34,8 @@ gbx_status gbx_fail(gbx_ctx *ctx, gbx_status st, const char *fmt, ...);
 #define GBX_WS_OZ3      9
 #define GBX_WS_BATCH    10  /* grouped/batched descriptors                  */
 #define GBX_WS_STAGE_D  11
+#define GBX_WS_TRSM_X   12  /* dtrsm_ozaki: inverse of the triangle          */
+#define GBX_WS_TRSM_B   13  /* dtrsm_ozaki: copy of the right-hand sides     */
 #define GBX_WS_GEMV     14  /* gemv partial sums                            */
 #define GBX_WS_RED      15  /* reduction partials                           */
 gbx_status gbx_ws(gbx_ctx *ctx, int slot, size_t bytes, void **ptr);

@@ -14,18 +14,19 @@
 //     slices is exact;
 //   * products with the same s + t = q share one TMEM accumulator (and one
 //     power-of-two weight 2^-5q); only q <= S-1 are formed (S(S+1)/2 slice
-//     products); the epilogue adds acc_q * 2^(e_i+f_j-8-5q) into an FP64
-//     running sum, smallest q first, and the last group writes
+//     products); the drain adds each diagonal sum exactly into a 128-bit
+//     integer running sum (smallest q first), and the last group converts
+//     it once to FP64, scales it by 2^(e_i+f_j-8-5(S-1)) and writes
 //     C = alpha*sum + beta*C;
 //   * S is chosen on the device from the operands' exponent statistics for a
 //     target relative Frobenius error (or forced by the caller).
-// Everything FP64 (scaling, recombination, alpha/beta) stays FP64.
+// The scaling, the final recombination and alpha/beta are FP64.
 //
-// Kernel layout: persistent, one CTA per SM, 192 threads: warp 0 issues TMA
-// loads of 128x128-byte (A) and 256x128-byte (B) slice tiles into a 4-stage
-// shared-memory ring; warp 1 allocates all 512 TMEM columns and issues the
-// tcgen05.mma.kind::f8f6f4 (M=128, N=256, K=32) into one of two 256-column
-// accumulators; warps 2-5 drain the other accumulator into FP64.
+// Kernel layout: persistent, one CTA per SM, 320 threads: warp 0 issues TMA
+// loads of 128x128-byte (A) and BNx128-byte (B, BN = 256 or 128) slice tiles
+// into a shared-memory ring; warp 1 allocates all 512 TMEM columns and
+// issues the tcgen05.mma.kind::f8f6f4 (M=128, N=BN, K=32) into one of
+// 512/BN accumulators; warps 2-9 drain the others.
 #include "gbx_internal.h"
 #include "gemm_host.h"
 #include "tc_ptx.cuh"
@@ -419,19 +420,88 @@ oz_prep_split(OzPrepOp a, OzPrepOp b, const int *__restrict__ S_dev)
     else oz_split_tile(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, S, b.X8, blockIdx.x - a.split_blocks);
 }
 
-// acc * 2^shift as a double, built from the FP32 accumulator's bit pattern
-// with integer operations (acc is an integer-valued float, |acc| <= 2^24).
-// Results below the binary64 normal range flush to zero, above it give Inf.
-__device__ __forceinline__ double scaled_acc(uint32_t fb, int shift)
+// ---- small K: the whole preparation in one launch ---------------------------
+// Each CTA owns 16 complete rows of one operand: a first pass over their K
+// extent gives the row statistics (maximum and sum of squares), a second
+// writes all OZ_SMAX digit planes (the slice count is not known yet; the
+// leading S planes of the OZ_SMAX-digit balanced expansion represent the
+// row to within 16.5 * 2^(-5S) of its maximum, the same bound as rounding
+// at S digits).  The last CTA to finish chooses S from the statistics of
+// both operands.  One launch instead of three: small products are
+// dominated by per-launch cost.
+__device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, int Rp, int Kp, int *expo, double *ss,
+                                             int *scale, uint8_t *X8, int rblk, int *status)
 {
-    if ((fb & 0x7FFFFFFFu) == 0u) return 0.0;
-    const int ex = (int)((fb >> 23) & 0xFFu) - 127 + 1023 + shift;
-    const unsigned long long sign = (unsigned long long)(fb >> 31) << 63;
-    if (ex <= 0) return __longlong_as_double((long long)sign);
-    if (ex >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
-    return __longlong_as_double(
-        (long long)(sign | ((unsigned long long)ex << 52) | ((unsigned long long)(fb & 0x7FFFFFu) << 29)));
+    __shared__ double tile[OZ_SPLIT_ROWS][129];
+    const int r0 = rblk * OZ_SPLIT_ROWS;
+    const int rr = threadIdx.x >> 4, lane16 = threadIdx.x & 15;   // 16 threads per row
+    SsAcc acc;
+    acc.init();
+    for (int k0 = 0; k0 < K; k0 += 128) {
+        for (int t = threadIdx.x; t < OZ_SPLIT_ROWS * 128; t += blockDim.x) {
+            int tr, kk;
+            if (v.row_k) { kk = t & 127; tr = t >> 7; }
+            else         { tr = t % OZ_SPLIT_ROWS; kk = t / OZ_SPLIT_ROWS; }
+            const int r = r0 + tr, k = k0 + kk;
+            tile[tr][kk] = (r < rows && k < K) ? src_get(v, r, k) : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const unsigned long long b = abs_bits(tile[rr][lane16 + 16 * j]);
+            flag_nonfinite(b, status);
+            acc.add(b);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int o = 8; o; o >>= 1) {   // the 16 threads of a row are one half-warp
+        SsAcc t;
+        t.maxb = __shfl_xor_sync(0xffffffffu, acc.maxb, o);
+        t.mref = __shfl_xor_sync(0xffffffffu, acc.mref, o);
+        t.ss = __shfl_xor_sync(0xffffffffu, acc.ss, o);
+        acc.merge(t);
+    }
+    const int r = r0 + rr;
+    if (lane16 == 0 && r < Rp) {
+        if (r < rows) {
+            acc.finish(expo[r], ss[r]);
+            scale[r] = expo[r] - 4;
+        } else {
+            scale[r] = 0;
+        }
+    }
+    __syncthreads();   // the row exponents are visible to the whole CTA
+    const int kblocks = Kp / 128;
+    for (int kb = 0; kb < kblocks; kb++) oz_split_tile(v, rows, K, Rp, Kp, expo, OZ_SMAX, X8, rblk * kblocks + kb);
 }
+
+__global__ void __launch_bounds__(256)
+oz_prep_small(OzPrepOp a, OzPrepOp b, double tol, int forced, int *status, unsigned *counter, int *S_dev)
+{
+    const int na = a.Rp / OZ_SPLIT_ROWS;
+    if ((int)blockIdx.x < na)
+        oz_prep_rows(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, a.ss, a.scale, a.X8, blockIdx.x, status);
+    else
+        oz_prep_rows(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, b.ss, b.scale, b.X8, blockIdx.x - na, status);
+    __threadfence();
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const double ga = oz_log2_gamma(a.expo, a.ss, a.rows, a.K);
+    const double gb = oz_log2_gamma(b.expo, b.ss, b.rows, b.K);
+    if (threadIdx.x == 0) {
+        int S;
+        if (forced > 0) S = forced;
+        else S = (int)ceil((-log2(tol) + ga + gb + 1.5) / 5.0);
+        S_dev[0] = max(1, min(OZ_SMAX, S));
+        *counter = 0u;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the tensor-core kernel
 // ---------------------------------------------------------------------------
@@ -441,7 +511,7 @@ struct OzParams {
     const int *S;
     const int *row_exp;        // Mp: e_i - 4
     const int *col_exp;        // Np: f_j - 4
-    double *W;                 // Mp x Np, column-major
+    long long *W;              // Mp x Np running sums, two words per element, column-major
     double *C;
     long long ldc;
     double alpha, beta;
@@ -472,14 +542,23 @@ __device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, i
     return p.c_part == 1 ? (r1 >= c0) : (r0 <= c1);
 }
 
-// Drain one diagonal's accumulator for one row (row grow, NCOL columns from
-// gcol0) into the running sum W, or on the last pass into C.  The row is
-// walked in CH-column chunks, software-pipelined: the global loads of chunk
-// c+1 (running sums, and C on the last pass) are issued before chunk c is
-// converted and stored.  Loads and stores are never interleaved element by
-// element: the compiler cannot prove that W and C do not overlap, and a
-// load/add/store per element serialised one L2 round trip per element
-// (that, not the MMAs, was the cost of a small-K product).
+// The drain: per output element, the diagonal sums D_q (integers, |D_q| <
+// 2^24 per accumulation group, exact in the FP32 TMEM accumulator) are
+// summed exactly as one signed 128-bit integer in units of the last
+// diagonal's weight,
+//     V = sum_q D_q 2^(5(S-1-q)),     C_ij = V 2^(e_i + f_j - 8 - 5(S-1)),
+// held in W (two 64-bit words per element, column-major Mp x Np) between
+// diagonals.  Each diagonal costs an FP32->int conversion and a 128-bit
+// shift-and-add on the integer pipe per element; the FP64 pipe (the scarce
+// one on GB300) is used once per element, for the final conversion, scale
+// and alpha/beta.  |V| < 2^(24 + 65 + 14) for S <= 14 and K <= 2^30.
+//
+// One row (grow) and NCOL columns from gcol0 per call, walked in CH-column
+// chunks and software-pipelined: the global loads of chunk c+1 (running
+// sums, and C on the last pass) are issued before chunk c is converted and
+// stored.  Loads and stores are never interleaved element by element: the
+// compiler cannot prove that W and C do not overlap, and a load/add/store
+// per element serialised one L2 round trip per element.
 __device__ __forceinline__ bool oz_c_keep(const OzParams &p, int grow, int gcol)
 {
     return gcol < p.N && (p.c_part == 0 || (p.c_part == 1 ? grow >= gcol : grow <= gcol));
@@ -492,18 +571,58 @@ __device__ __forceinline__ void tmem_ld_chunk<16>(uint32_t taddr, uint32_t (&r)[
 template <>
 __device__ __forceinline__ void tmem_ld_chunk<8>(uint32_t taddr, uint32_t (&r)[8]) { tmem_ld_32x32b_x8(taddr, r); }
 
+// d * 2^sh as a signed 128-bit (lo, hi) pair, 0 <= sh <= 70 (sh is uniform
+// across the warp: every lane drains the same diagonal)
+__device__ __forceinline__ void oz_shift128(long long d, int sh, unsigned long long &lo, long long &hi)
+{
+    if (sh == 0) {
+        lo = (unsigned long long)d;
+        hi = d >> 63;
+    } else if (sh < 64) {
+        lo = (unsigned long long)d << sh;
+        hi = d >> (64 - sh);
+    } else {
+        lo = 0ull;
+        hi = d << (sh - 64);
+    }
+}
+
+// V (128-bit) as a double: the exact integer rounded once to 53 bits when it
+// fits 64 bits, else hi * 2^64 + lo (the low word rounded first, within one
+// unit of the last place).
+__device__ __forceinline__ double oz_to_double(unsigned long long lo, long long hi)
+{
+    if (hi == ((long long)lo >> 63)) return (double)(long long)lo;
+    return fma((double)hi, 0x1p64, (double)lo);
+}
+
+// alpha * 2^e, exact: the exponent field moved on the integer pipe when the
+// result stays a normal number, ldexp otherwise.  Then alpha * (V * 2^e) is
+// one FP64 multiply of V by this factor.
+__device__ __forceinline__ double oz_alpha_pow2(double alpha, int e)
+{
+    const long long b = __double_as_longlong(alpha);
+    const int ea = (int)((b >> 52) & 0x7FF);
+    if (ea != 0 && ea != 0x7FF && ea + e >= 1 && ea + e <= 2046)
+        return __longlong_as_double(b + ((long long)e << 52));
+    return ldexp(alpha, e);
+}
+
 template <int NCOL, int CH>
-__device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, int grow, int gcol0, int rs,
-                                             bool first, bool last)
+__device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, int grow, int gcol0, int q, int S,
+                                             int rexp, bool first, bool last)
 {
     constexpr int NCH = NCOL / CH;
+    const int sh = 5 * (S - 1 - q);
+    const int erow = rexp - 5 * (S - 1);   // scale of V without the column part
     const bool row_ok = grow < p.M;
     const bool need_c = last && row_ok && p.beta != 0.0;
-    const double *wrow = p.W + (size_t)gcol0 * p.Mp + grow;
+    const longlong2 *wrow = (const longlong2 *)p.W + (size_t)gcol0 * p.Mp + grow;
     double *crow = p.C + (size_t)gcol0 * p.ldc + grow;
-    double wn[CH], cn[CH];
+    longlong2 wn[CH];
+    double cn[CH];
 #pragma unroll
-    for (int j = 0; j < CH; j++) { wn[j] = 0.0; cn[j] = 0.0; }
+    for (int j = 0; j < CH; j++) { wn[j] = make_longlong2(0, 0); cn[j] = 0.0; }
     if (!first) {
 #pragma unroll
         for (int j = 0; j < CH; j++) wn[j] = __ldcg(wrow + (size_t)j * p.Mp);
@@ -514,7 +633,8 @@ __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, 
     }
 #pragma unroll 1
     for (int c = 0; c < NCH; c++) {
-        double wc[CH], cc[CH];
+        longlong2 wc[CH];
+        double cc[CH];
 #pragma unroll
         for (int j = 0; j < CH; j++) { wc[j] = wn[j]; cc[j] = cn[j]; }
         const int nc = (c + 1) * CH;
@@ -535,17 +655,30 @@ __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, 
         const int cb = c * CH;
 #pragma unroll
         for (int j = 0; j < CH; j++) {
-            const double v = scaled_acc(r[j], rs + __ldg(p.col_exp + gcol0 + cb + j));
-            wc[j] = first ? v : wc[j] + v;
+            unsigned long long slo;
+            long long shi;
+            oz_shift128((long long)__float2int_rn(__uint_as_float(r[j])), sh, slo, shi);
+            if (first) {
+                wc[j].x = (long long)slo;
+                wc[j].y = shi;
+            } else {
+                const unsigned long long lo = (unsigned long long)wc[j].x + slo;
+                wc[j].y = wc[j].y + shi + (lo < slo ? 1 : 0);
+                wc[j].x = (long long)lo;
+            }
         }
         if (!last) {
+            longlong2 *wdst = (longlong2 *)p.W + (size_t)(gcol0 + cb) * p.Mp + grow;
 #pragma unroll
-            for (int j = 0; j < CH; j++) __stcg(p.W + (size_t)(gcol0 + cb + j) * p.Mp + grow, wc[j]);
+            for (int j = 0; j < CH; j++) __stcg(wdst + (size_t)j * p.Mp, wc[j]);
         } else if (row_ok) {
 #pragma unroll
             for (int j = 0; j < CH; j++) {
-                if (!oz_c_keep(p, grow, gcol0 + cb + j)) continue;
-                crow[(size_t)(cb + j) * p.ldc] = need_c ? fma(p.alpha, wc[j], p.beta * cc[j]) : p.alpha * wc[j];
+                const int gcol = gcol0 + cb + j;
+                if (!oz_c_keep(p, grow, gcol)) continue;
+                const double v = oz_to_double((unsigned long long)wc[j].x, wc[j].y);
+                const double sa = oz_alpha_pow2(p.alpha, erow + __ldg(p.col_exp + gcol));
+                crow[(size_t)(cb + j) * p.ldc] = need_c ? fma(sa, v, p.beta * cc[j]) : sa * v;
             }
         }
     }
@@ -699,7 +832,6 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             for (int q = gp.S - 1; q >= 0 && ok; q--) {
                 const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                 const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
-                const int rs = rexp - 5 * q;   // weight 2^(e_i - 4 - 5q)
                 for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
                     const bool last = (q == 0) && (g0 + gp.items_per_group >= nitems);
                     // warp-uniform outcome: tcgen05.ld below is .sync.aligned
@@ -709,11 +841,209 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) +
                                            (uint32_t)(buf * BN + half * Cfg::DRAIN_COLS);
                     oz_drain_row<Cfg::DRAIN_COLS, Cfg::DRAIN_CH>(p, taddr, grow, tn * BN + half * Cfg::DRAIN_COLS,
-                                                                 rs, first, last);
+                                                                 q, gp.S, rexp, first, last);
                     tc_fence_before();
                     mbar_arrive(&tempty[buf]);
                     first = false;
                     if (++buf == NBUF) { buf = 0; tphase ^= 1u; }
+                }
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, 512);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Small-K kernel: every diagonal accumulator resident in TMEM
+// ---------------------------------------------------------------------------
+// When Kp * OZ_SMAX <= 65536, each diagonal's accumulation over the whole K
+// extent stays exact in one FP32 accumulator, so a 128 x 32 tile keeps all
+// S (<= 14) diagonal sums in TMEM at once (S x 32 of the 512 columns).  The
+// MMAs of all S(S+1)/2 slice products then run back to back, and one drain
+// per tile combines the S sums exactly in registers (128-bit integers) and
+// writes C: no running-sum traffic and no per-diagonal hand-off between the
+// MMA issuer and the drain, which bound the wide-tile kernel on the small-K
+// products of blocked factorizations.  Slices stream through two rings: A_s
+// (16 KB) for s = 0..S-1 and, under each A_s, B_t (4 KB) for t = 0..S-1-s.
+// Tiles are ordered column-fastest so the CTAs sharing an A row block run
+// together and its slices come from L2.
+// Warp 0: TMA; warp 1: MMA issuer; warps 2..9: drain (two per TMEM lane
+// quarter, 16 columns each).  The accumulators are released before C is
+// converted and written, so the next tile's MMAs overlap that work.
+constexpr int OZS_BN = 32, OZS_AST = 3, OZS_BST = 16, OZS_DRAIN_WARPS = 8;
+constexpr int OZS_B_BYTES = OZS_BN * OZ_BK;   // 4 KB
+constexpr int OZS_THREADS = 64 + 32 * OZS_DRAIN_WARPS;
+constexpr size_t OZS_SMEM = (size_t)OZS_AST * OZ_A_BYTES + (size_t)OZS_BST * OZS_B_BYTES + 1024 + 512;
+constexpr int OZS_KMAX = 65536 / OZ_SMAX / OZ_BK * OZ_BK;   // 4608: exact for any slice count
+
+__global__ void __launch_bounds__(OZS_THREADS, 1)
+oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + OZS_AST * OZ_A_BYTES;
+    uint64_t *bars = (uint64_t *)(sB + OZS_BST * OZS_B_BYTES);
+    uint64_t *fullA = bars, *emptyA = fullA + OZS_AST;
+    uint64_t *fullB = emptyA + OZS_AST, *emptyB = fullB + OZS_BST;
+    uint64_t *tfull = emptyB + OZS_BST, *tempty = tfull + 1;
+    uint32_t *tmem_slot = (uint32_t *)(tempty + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    volatile int *status = p.status;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < OZS_AST; i++) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], 1); }
+        for (int i = 0; i < OZS_BST; i++) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], 1); }
+        mbar_init(tfull, 1);
+        mbar_init(tempty, 32 * OZS_DRAIN_WARPS);
+        fence_barrier_init();
+        prefetch_tmap(&tmA);
+        prefetch_tmap(&tmB);
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    const int S = *p.S;
+    const int nkb = p.Kp / OZ_BK;
+    const int ntiles = p.tiles_m * p.tiles_n;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            int as = 0, bs = 0;
+            uint32_t ap = 0, bp = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int tm = t / p.tiles_n, tn = t % p.tiles_n;
+                if (!tile_needed(p, tm, tn, OZ_BM, OZS_BN)) continue;
+                for (int kb = 0; kb < nkb && ok; kb++)
+                    for (int sa = 0; sa < S && ok; sa++) {
+                        if (!mbar_wait(&emptyA[as], ap ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
+                        mbar_arrive_expect_tx(&fullA[as], OZ_A_BYTES);
+                        tma_load_2d(sA + as * OZ_A_BYTES, &tmA, &fullA[as], kb * OZ_BK, sa * p.Mp + tm * OZ_BM);
+                        if (++as == OZS_AST) { as = 0; ap ^= 1u; }
+                        for (int tb = 0; tb < S - sa && ok; tb++) {
+                            if (!mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
+                            mbar_arrive_expect_tx(&fullB[bs], OZS_B_BYTES);
+                            tma_load_2d(sB + bs * OZS_B_BYTES, &tmB, &fullB[bs], kb * OZ_BK, tb * p.Np + tn * OZS_BN);
+                            if (++bs == OZS_BST) { bs = 0; bp ^= 1u; }
+                        }
+                    }
+            }
+            // wait (bounded) until every issued load has been consumed
+            for (int i = 0; i < OZS_AST; i++) {
+                mbar_wait(&emptyA[as], ap ^ 1u, status, TC_TIMEOUT_EMPTY);
+                if (++as == OZS_AST) { as = 0; ap ^= 1u; }
+            }
+            for (int i = 0; i < OZS_BST; i++) {
+                mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY);
+                if (++bs == OZS_BST) { bs = 0; bp ^= 1u; }
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_e4m3_f32(OZ_BM, OZS_BN);
+            int as = 0, bs = 0;
+            uint32_t ap = 0, bp = 0, tp = 0;
+            bool ok = true;
+            const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int tm = t / p.tiles_n, tn = t % p.tiles_n;
+                if (!tile_needed(p, tm, tn, OZ_BM, OZS_BN)) continue;
+                // the previous tile's sums have been read out of TMEM
+                if (!mbar_wait(tempty, tp ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
+                tc_fence_after();
+                for (int kb = 0; kb < nkb && ok; kb++)
+                    for (int sa = 0; sa < S && ok; sa++) {
+                        if (!mbar_wait(&fullA[as], ap, status, TC_TIMEOUT_FULL)) { ok = false; break; }
+                        tc_fence_after();
+                        const uint32_t a_addr = a_base + as * OZ_A_BYTES;
+                        for (int tb = 0; tb < S - sa && ok; tb++) {
+                            if (!mbar_wait(&fullB[bs], bp, status, TC_TIMEOUT_FULL)) { ok = false; break; }
+                            tc_fence_after();
+                            const uint32_t b_addr = b_base + bs * OZS_B_BYTES;
+                            const uint32_t d_tmem = tmem_base + (uint32_t)((sa + tb) * OZS_BN);
+#pragma unroll
+                            for (int kk = 0; kk < OZ_BK / 32; kk++)
+                                // the first product into diagonal q = tb (s = 0, kb = 0) starts it
+                                mma_f8f6f4(d_tmem, smem_desc_k128(a_addr + kk * 32), smem_desc_k128(b_addr + kk * 32),
+                                           idesc, (kb == 0 && sa == 0 && kk == 0) ? 0u : 1u);
+                            mma_commit(&emptyB[bs]);
+                            if (++bs == OZS_BST) { bs = 0; bp ^= 1u; }
+                        }
+                        mma_commit(&emptyA[as]);
+                        if (++as == OZS_AST) { as = 0; ap ^= 1u; }
+                    }
+                mma_commit(tfull);
+                tp ^= 1u;
+            }
+        }
+    } else {
+        // ---------------- drain (warps 2..9) ----------------
+        const int quarter = warp & 3;               // TMEM lane window of this warp
+        const int half = (warp - 2) >> 2;           // columns half*16 .. +15 of the tile
+        const int row = quarter * 32 + lane;
+        uint32_t tp = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+            const int tm = t / p.tiles_n, tn = t % p.tiles_n;
+            if (!tile_needed(p, tm, tn, OZ_BM, OZS_BN)) continue;
+            ok = __all_sync(0xffffffffu, mbar_wait(tfull, tp, status, TC_TIMEOUT_TMEM_FULL));
+            if (!ok) break;
+            tc_fence_after();
+            tp ^= 1u;
+            unsigned long long lo[16];
+            long long hi[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) { lo[j] = 0ull; hi[j] = 0; }
+            const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(half * 16);
+            for (int q = 0; q < S; q++) {
+                uint32_t r[16];
+                tmem_ld_32x32b_x16(tbase + (uint32_t)(q * OZS_BN), r);
+                tmem_ld_wait();
+                const int sh = 5 * (S - 1 - q);
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    unsigned long long slo;
+                    long long shi;
+                    oz_shift128((long long)__float2int_rn(__uint_as_float(r[j])), sh, slo, shi);
+                    const unsigned long long nl = lo[j] + slo;
+                    hi[j] = hi[j] + shi + (nl < slo ? 1 : 0);
+                    lo[j] = nl;
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(tempty);   // TMEM free: the next tile's MMAs may start
+            const int grow = tm * OZ_BM + row;
+            if (grow < p.M) {
+                const int erow = p.row_exp[grow] - 5 * (S - 1);
+                const int gc0 = tn * OZS_BN + half * 16;
+                double *cp = p.C + (size_t)gc0 * p.ldc + grow;
+                double cold[16];
+                if (p.beta != 0.0) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) cold[j] = oz_c_keep(p, grow, gc0 + j) ? cp[(size_t)j * p.ldc] : 0.0;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    if (!oz_c_keep(p, grow, gc0 + j)) continue;
+                    const double v = oz_to_double(lo[j], hi[j]);
+                    const double sa = oz_alpha_pow2(p.alpha, erow + __ldg(p.col_exp + gc0 + j));
+                    cp[(size_t)j * p.ldc] = p.beta != 0.0 ? fma(sa, v, p.beta * cold[j]) : sa * v;
                 }
             }
         }
@@ -880,14 +1210,13 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
             for (int q = gp.S - 1; q >= 0 && ok; q--) {
                 const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                 const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
-                const int rs = rexp - 5 * q;
                 for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
                     const bool last = (q == 0) && (g0 + gp.items_per_group >= nitems);
                     ok = __all_sync(0xffffffffu, mbar_wait_cl(&tfull[buf], tphase, status, TC_TIMEOUT_TMEM_FULL));
                     if (!ok) break;
                     tc_fence_after();
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * OZ_BN);
-                    oz_drain_row<OZ_BN, 16>(p, taddr, grow, tn * OZ_BN, rs, first, last);
+                    oz_drain_row<OZ_BN, 8>(p, taddr, grow, tn * OZ_BN, q, gp.S, rexp, first, last);
                     tc_fence_before();
                     mbar_arrive_cluster(buf ? tempty_cl1 : tempty_cl0);
                     first = false;
@@ -988,12 +1317,24 @@ int oz_tile_n(int M, int N, int sms, bool pair)
     return tiles256 < sms ? 128 : OZ_BN;
 }
 
+// Small-K products (the rank-nb updates of blocked factorizations) take the
+// kernel with every diagonal in TMEM; GBX_OZAKI_SMALLK=0 turns it off.
+bool oz_small_k(int K)
+{
+    static int env = [] {
+        const char *s = getenv("GBX_OZAKI_SMALLK");
+        return s ? atoi(s) : 1;
+    }();
+    return env != 0 && K <= 1024;
+}
+
 // Workspace layout for one Ozaki product.
 struct OzBuffers {
     uint8_t *A8, *B8;
     int *ea, *eb, *S;
     int *rsa, *csb;   // scale exponents e-4 (rows of op(A), columns of op(B))
-    double *ssa, *ssb, *W;
+    double *ssa, *ssb;
+    long long *W;     // nW planes of Mp x Np 128-bit running sums
     int *status;
 };
 
@@ -1005,8 +1346,8 @@ gbx_status oz_buffers(gbx_ctx *ctx, int Mp, int Np, int Kp, int nW, OzBuffers &b
     b.A8 = (uint8_t *)p;
     if ((st = gbx_ws(ctx, GBX_WS_OZ1, (size_t)OZ_SMAX * Np * Kp, &p)) != GBX_OK) return st;
     b.B8 = (uint8_t *)p;
-    if ((st = gbx_ws(ctx, GBX_WS_OZ2, sizeof(double) * (size_t)Mp * Np * nW, &p)) != GBX_OK) return st;
-    b.W = (double *)p;
+    if ((st = gbx_ws(ctx, GBX_WS_OZ2, 2 * sizeof(long long) * (size_t)Mp * Np * nW, &p)) != GBX_OK) return st;
+    b.W = (long long *)p;
     const size_t small = 256 + sizeof(int) * (size_t)(Mp + Np) + sizeof(double) * 4 * (size_t)(Mp + Np) + 1024;
     if ((st = gbx_ws(ctx, GBX_WS_OZ3, small, &p)) != GBX_OK) return st;
     uint8_t *q = (uint8_t *)p;
@@ -1084,7 +1425,8 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
 {
     if (pr.K > 0x3fffffff) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: K too large");
     const bool pair = oz_use_pair(pr.M);
-    const int bn = oz_tile_n(pr.M, pr.N, gbx_ctx_sms(ctx), pair);
+    const bool small_k = !pair && rup(std::max(pr.K, 1), OZ_BK) <= OZS_KMAX && oz_small_k(pr.K);
+    const int bn = small_k ? OZS_BN : oz_tile_n(pr.M, pr.N, gbx_ctx_sms(ctx), pair);
     const int Mp = (int)rup(pr.M, pair ? OZ2_BM : OZ_BM), Np = (int)rup(pr.N, bn);
     const int Kp = (int)rup(std::max(pr.K, 1), OZ_BK);
     OzBuffers b;
@@ -1115,8 +1457,25 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         B8 = b.A8;
         csb = b.rsa;
     }
-    if ((st = oz_prepare(ctx, oa, ob, b_stats, tol, forced, b.status, (unsigned *)(b.S + 4), b.S)) != GBX_OK)
+    if (small_k) {
+        // one launch; both operands carry their own statistics (for a
+        // symmetric rank-k update the second copy repeats op(A)'s)
+        if (pr.same_ab) {
+            ob = oz_prep_op(ctx, pr.a, pr.M, pr.K, Np, Kp, b.eb, b.ssb, b.csb, b.B8, true);
+            oa.scale2 = nullptr;
+            B8 = b.B8;
+            csb = b.csb;
+        }
+        const long long blocks = (long long)Mp / OZ_SPLIT_ROWS + (long long)Np / OZ_SPLIT_ROWS;
+        if (blocks > 0x7fffffffLL) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: operands too large");
+        oz_prep_small<<<(unsigned)blocks, 256, 0, s>>>(oa, ob, tol, forced, b.status, (unsigned *)(b.status + 8),
+                                                      b.S);
+        gbx_count_launch(ctx, 1);
+        if ((st = gbx_check_launch(ctx, "ozaki prepare")) != GBX_OK) return st;
+    } else if ((st = oz_prepare(ctx, oa, ob, b_stats, tol, forced, b.status, (unsigned *)(b.S + 4), b.S)) !=
+               GBX_OK) {
         return st;
+    }
     gbx_timer_end(ctx);
 
     CUtensorMap tmA, tmB;
@@ -1130,7 +1489,7 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     p.S = b.S;
     p.row_exp = b.rsa;
     p.col_exp = csb;
-    p.W = b.W + (size_t)w_index * Mp * Np;
+    p.W = b.W + 2 * (size_t)w_index * Mp * Np;
     p.C = pr.C; p.ldc = pr.ldc;
     p.alpha = pr.alpha; p.beta = pr.beta;
     p.c_part = pr.c_part;
@@ -1146,7 +1505,9 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         std::lock_guard<std::mutex> lk(attr_mu);
         max_pairs = (dev >= 0 && dev < 64) ? max_pairs_of[dev] : 0;
         if (max_pairs == 0) {
-            if (cudaFuncSetAttribute(oz_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            if (cudaFuncSetAttribute(oz_gemm_sk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)OZS_SMEM) != cudaSuccess ||
+                cudaFuncSetAttribute(oz_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OzCfg<256>::SMEM) != cudaSuccess ||
                 cudaFuncSetAttribute(oz_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OzCfg<128>::SMEM) != cudaSuccess ||
@@ -1174,7 +1535,9 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         oz_gemm2_kernel<<<2 * npairs, OZ_THREADS, OZ2_SMEM, s>>>(tmA, tmB, p);
     } else {
         const int grid = std::min(ntiles, gbx_ctx_sms(ctx));
-        if (bn == 128)
+        if (small_k)
+            oz_gemm_sk_kernel<<<grid, OZS_THREADS, OZS_SMEM, s>>>(tmA, tmB, p);
+        else if (bn == 128)
             oz_gemm_kernel<128><<<grid, OzCfg<128>::THREADS, OzCfg<128>::SMEM, s>>>(tmA, tmB, p);
         else
             oz_gemm_kernel<256><<<grid, OzCfg<256>::THREADS, OzCfg<256>::SMEM, s>>>(tmA, tmB, p);
@@ -1245,6 +1608,56 @@ extern "C" gbx_status gbx_dsyrk_ozaki(gbx_ctx *ctx, char uplo, char trans, int n
     return run_ozaki(ctx, pr, tol, slices, slices_used);
 }
 
+// DTRSM via the inverse: X = op(A)^-1 is formed in FP64 (the FP64 DTRSM of
+// the identity: the diagonal-block solves stay FP64), then B is multiplied
+// by it as one Ozaki product (B := alpha X B or alpha B X).  For the
+// well-conditioned diagonal blocks of a Cholesky factorization the extra
+// error of applying the inverse is a factor cond(op(A)) on the rounding of X.
+namespace {
+__global__ void oz_set_identity(int n, double *X, long long ldx)
+{
+    const long long total = (long long)n * n;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % n), j = (int)(t / n);
+        X[(long long)j * ldx + i] = i == j ? 1.0 : 0.0;
+    }
+}
+}  // namespace
+
+extern "C" gbx_status gbx_dtrsm_ozaki(gbx_ctx *ctx, char side, char uplo, char ta, char diag, int m, int n,
+                                      double alpha, const double *A, int lda, double *B, int ldb, double tol,
+                                      int slices, int *slices_used)
+{
+    if (!ctx) return GBX_ERR_ARG;
+    const int info = gbx_check_trxm_args(side, uplo, ta, diag, m, n, lda, ldb);
+    if (info) return gbx_fail(ctx, GBX_ERR_ARG, "DTRSM parameter %d", info);
+    if (slices < 0 || slices > OZ_SMAX) return gbx_fail(ctx, GBX_ERR_ARG, "ozaki: slices must be 0..%d", OZ_SMAX);
+    if (slices_used) *slices_used = 0;
+    if (m == 0 || n == 0) return GBX_OK;
+    const bool lside = gbx_lsame(side, 'L');
+    const int na = lside ? m : n;
+    if (alpha == 0.0 || na > 1024) return gbx_dtrsm(ctx, side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb);
+    gbx_status st;
+    void *px, *pb;
+    if ((st = gbx_ws(ctx, GBX_WS_TRSM_X, sizeof(double) * (size_t)na * na, &px)) != GBX_OK) return st;
+    if ((st = gbx_ws(ctx, GBX_WS_TRSM_B, sizeof(double) * (size_t)m * n, &pb)) != GBX_OK) return st;
+    double *X = (double *)px, *Bc = (double *)pb;
+    cudaStream_t s = S_(ctx);
+    const long long total = (long long)na * na;
+    oz_set_identity<<<(int)std::min<long long>((total + 255) / 256, (long long)gbx_ctx_sms(ctx) * 4), 256, 0, s>>>(
+        na, X, na);
+    gbx_count_launch(ctx, 1);
+    if ((st = gbx_check_launch(ctx, "dtrsm_ozaki identity")) != GBX_OK) return st;
+    if ((st = gbx_dtrsm(ctx, 'L', uplo, ta, diag, na, na, 1.0, A, lda, X, na)) != GBX_OK) return st;
+    cudaError_t e = cudaMemcpy2DAsync(Bc, sizeof(double) * (size_t)m, B, sizeof(double) * (size_t)ldb,
+                                      sizeof(double) * (size_t)m, n, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "dtrsm_ozaki copy: %s", cudaGetErrorString(e));
+    if (lside)
+        return gbx_dgemm_ozaki(ctx, 'N', 'N', m, n, m, alpha, X, na, Bc, m, 0.0, B, ldb, tol, slices, slices_used);
+    return gbx_dgemm_ozaki(ctx, 'N', 'N', m, n, n, alpha, Bc, m, X, na, 0.0, B, ldb, tol, slices, slices_used);
+}
+
 // ZGEMM: Re = [Ar | Ai] x [Br ; -Bi],  Im = [Ar | Ai] x [Bi ; Br]  (K' = 2K),
 // both real Ozaki products into FP64 workspace, then C = alpha*(Re + i Im) +
 // beta*C.  Conjugation ('C') negates the imaginary part while slicing.
@@ -1278,7 +1691,7 @@ extern "C" gbx_status gbx_zgemm_ozaki(gbx_ctx *ctx, char ta, char tb, int m, int
     pr.b.X = B; pr.b.ld = ldb; pr.b.row_k = gbx_lsame(tb, 'N'); pr.b.cplx = 1;
     pr.b.conj = gbx_lsame(tb, 'C'); pr.b.part0 = 0; pr.b.part1 = 2; pr.b.Ksplit = k;   // [Br ; -Bi]
     pr.alpha = 1.0; pr.beta = 0.0; pr.c_part = 0;
-    double *Wre = b.W + (size_t)Mp * Np;       // second plane holds the real part result
+    double *Wre = (double *)(b.W + 2 * (size_t)Mp * Np);   // second plane holds the real part result
     pr.C = Wre; pr.ldc = Mp;
     int used_re = 0, used_im = 0;
     // W plane 0 is the running-sum workspace of each product; plane 1 keeps Re.

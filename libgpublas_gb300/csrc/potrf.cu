@@ -1,60 +1,86 @@
-// potrf.cu — Cholesky factorisation of one small diagonal block (n <= 256),
-// lower triangle, in one CTA.  Not a BLAS routine: it is the diagonal step of
-// the blocked right-looking Cholesky that drives the serving trace (the
-// other steps are the intercepted dtrsm_/dsyrk_/dgemm_ calls).
+// potrf.cu — Cholesky factorisation of one diagonal block, lower triangle.
+// Not a BLAS routine: it is the diagonal step of the blocked right-looking
+// Cholesky that drives the serving trace (the other steps are the
+// intercepted dtrsm_/dsyrk_/dgemm_ calls).
 //
-// Right-looking, column by column, in place in global memory (the block is
-// small and stays in L1/L2): a_kk = sqrt(a_kk); a_ik /= a_kk; a_ij -= a_ik a_jk
-// for i >= j > k.  A non-positive pivot sets *info = k+1 (1-based, LAPACK
-// convention) and stops.
+// Blocked in 64-column steps.  On GB300 one SM does about 4 GFLOP/s of FP64,
+// so a factorisation of a 256 x 256 block confined to one CTA costs over a
+// millisecond; here only the 64 x 64 diagonal factorisations are serial:
+//   * potrf_step(j0): every CTA factors the 64 x 64 diagonal block at j0 in
+//     shared memory (redundantly: 44k FMAs), CTA 0 writes it back, and each
+//     CTA solves 64 rows of the panel below against it (x L^T = a, one row
+//     per thread);
+//   * the trailing update A22 -= A21 A21^T is one DSYRK on the GEMM core.
+// A non-positive pivot sets *info to its 1-based column (LAPACK convention,
+// first failure wins); the rest of the block is then unspecified.
 #include "gbx_internal.h"
 
 #include <cuda_runtime.h>
 
+extern "C" gbx_status gbx_dsyrk(gbx_ctx *ctx, char uplo, char trans, int n, int k, double alpha, const double *A,
+                                int lda, double beta, double *C, int ldc);
+
 namespace {
 
+constexpr int PB = 64;          // panel width
 constexpr int PT_THREADS = 256;
 
 __global__ void __launch_bounds__(PT_THREADS)
-potrf_small_lower(int n, double *__restrict__ A, long long lda, int *__restrict__ info)
+potrf_step(int n, int j0, double *__restrict__ A, long long lda, int *__restrict__ info)
 {
-    __shared__ double s_piv;
+    extern __shared__ double sm[];
+    double(*L)[PB + 1] = (double(*)[PB + 1])sm;                   // diagonal block
+    double(*X)[PB + 1] = (double(*)[PB + 1])(sm + PB * (PB + 1));  // panel rows, one per thread
     __shared__ int s_bad;
-    if (threadIdx.x == 0) s_bad = 0;
+    const int tid = threadIdx.x;
+    const int b = min(PB, n - j0);
+    for (int t = tid; t < PB * PB; t += PT_THREADS) {
+        const int i = t % PB, k = t / PB;
+        L[i][k] = (i < b && k < b && i >= k) ? A[(long long)(j0 + k) * lda + j0 + i] : (i == k ? 1.0 : 0.0);
+    }
+    if (tid == 0) s_bad = 0;
     __syncthreads();
-    for (int k = 0; k < n; k++) {
-        if (threadIdx.x == 0) {
-            const double d = A[(long long)k * lda + k];
-            if (!(d > 0.0)) {
-                s_bad = k + 1;
-            } else {
-                const double r = sqrt(d);
-                A[(long long)k * lda + k] = r;
-                s_piv = r;
-            }
+    // right-looking factorisation of the diagonal block in shared memory
+    for (int k = 0; k < b; k++) {
+        if (tid == 0) {
+            const double d = L[k][k];
+            if (!(d > 0.0)) s_bad = k + 1;
+            else L[k][k] = sqrt(d);
         }
         __syncthreads();
         if (s_bad) break;
-        const double piv = s_piv;
-        for (int i = k + 1 + threadIdx.x; i < n; i += PT_THREADS) A[(long long)k * lda + i] /= piv;
+        const double piv = L[k][k];
+        for (int i = k + 1 + tid; i < b; i += PT_THREADS) L[i][k] /= piv;
         __syncthreads();
-        // trailing update of the lower triangle, one (i, j) pair per step
-        const int m = n - k - 1;
-        const long long pairs = (long long)m * (m + 1) / 2;
-        for (long long t = threadIdx.x; t < pairs; t += PT_THREADS) {
-            // t -> (jj, ii) with ii >= jj, column-major over the trailing triangle
-            int jj = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-            while ((long long)(jj + 1) * (jj + 2) / 2 <= t) jj++;
-            while ((long long)jj * (jj + 1) / 2 > t) jj--;
-            const int ii = (int)(t - (long long)jj * (jj + 1) / 2);
-            // map (jj, ii) with ii <= jj to row = k+1+jj, col = k+1+ii (row >= col)
-            const int row = k + 1 + jj, col = k + 1 + ii;
-            A[(long long)col * lda + row] =
-                fma(-A[(long long)k * lda + row], A[(long long)k * lda + col], A[(long long)col * lda + row]);
+        const int m = b - k - 1;
+        for (int t = tid; t < m * m; t += PT_THREADS) {
+            const int i = k + 1 + t % m, j = k + 1 + t / m;
+            if (j <= i) L[i][j] = fma(-L[i][k], L[j][k], L[i][j]);
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) *info = s_bad;
+    if (s_bad) {
+        if (blockIdx.x == 0 && tid == 0) atomicCAS(info, 0, j0 + s_bad);
+        return;
+    }
+    if (blockIdx.x == 0)
+        for (int t = tid; t < b * b; t += PT_THREADS) {
+            const int i = t % b, k = t / b;
+            if (i >= k) A[(long long)(j0 + k) * lda + j0 + i] = L[i][k];
+        }
+    // panel: rows r below the block solve x L11^T = a (forward substitution)
+    const int r = j0 + b + blockIdx.x * PB + tid;
+    const bool mine = tid < PB && r < n;
+    if (mine)
+        for (int k = 0; k < b; k++) X[tid][k] = A[(long long)(j0 + k) * lda + r];
+    if (mine) {
+        for (int k = 0; k < b; k++) {
+            double s = X[tid][k];
+            for (int l = 0; l < k; l++) s = fma(-X[tid][l], L[k][l], s);
+            X[tid][k] = s / L[k][k];
+        }
+        for (int k = 0; k < b; k++) A[(long long)(j0 + k) * lda + r] = X[tid][k];
+    }
 }
 
 }  // namespace
@@ -65,11 +91,23 @@ extern "C" gbx_status gbx_dpotrf_small(gbx_ctx *ctx, char uplo, int n, double *A
     if (!gbx_lsame(uplo, 'L')) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "dpotrf_small: lower only");
     if (n < 0 || n > 256 || lda < (n > 1 ? n : 1))
         return gbx_fail(ctx, GBX_ERR_ARG, "dpotrf_small: n = %d (<= 256), lda = %d", n, lda);
-    if (n == 0) {
-        cudaMemsetAsync(info, 0, sizeof(int), (cudaStream_t)gbx_ctx_get_stream(ctx));
-        return GBX_OK;
+    cudaStream_t s = (cudaStream_t)gbx_ctx_get_stream(ctx);
+    cudaMemsetAsync(info, 0, sizeof(int), s);
+    constexpr size_t SMEM = 2 * sizeof(double) * PB * (PB + 1);
+    cudaFuncSetAttribute(potrf_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    gbx_status st;
+    for (int j0 = 0; j0 < n; j0 += PB) {
+        const int b = n - j0 < PB ? n - j0 : PB;
+        const int rows = n - j0 - b;
+        const int grid = rows > 0 ? (rows + PB - 1) / PB : 1;
+        potrf_step<<<grid, PT_THREADS, SMEM, s>>>(n, j0, A, lda, info);
+        gbx_count_launch(ctx, 1);
+        if ((st = gbx_check_launch(ctx, "dpotrf_small")) != GBX_OK) return st;
+        if (rows > 0) {
+            double *A21 = A + (long long)j0 * lda + j0 + b;
+            double *A22 = A + (long long)(j0 + b) * lda + j0 + b;
+            if ((st = gbx_dsyrk(ctx, 'L', 'N', rows, b, -1.0, A21, lda, 1.0, A22, lda)) != GBX_OK) return st;
+        }
     }
-    potrf_small_lower<<<1, PT_THREADS, 0, (cudaStream_t)gbx_ctx_get_stream(ctx)>>>(n, A, lda, info);
-    gbx_count_launch(ctx, 1);
-    return gbx_check_launch(ctx, "dpotrf_small");
+    return GBX_OK;
 }

@@ -50,6 +50,7 @@ struct Request {
 
 struct Slot {
     gbx_ctx *ctx = nullptr;
+    bool busy = false;   // taken by its worker or by a calling thread (under the server mutex)
 };
 
 bool is_small(const gbx_op &o)
@@ -100,6 +101,9 @@ gbx_status run_request(gbx_ctx *ctx, const gbx_op &o)
     case GBX_OP_GEMM_OZAKI:
         return gbx_dgemm_ozaki(ctx, o.transa, o.transb, o.m, o.n, o.k, o.alpha, o.A, o.lda, o.B, o.ldb,
                                o.beta, o.C, o.ldc, 0.0, 0, nullptr);
+    case GBX_OP_TRSM_OZAKI:
+        return gbx_dtrsm_ozaki(ctx, o.side, o.uplo, o.transa, o.diag, o.m, o.n, o.alpha, o.A, o.lda, o.C, o.ldc,
+                               0.0, 0, nullptr);
     case GBX_OP_SYRK_OZAKI:
         return gbx_dsyrk_ozaki(ctx, o.uplo, o.transa, o.n, o.k, o.alpha, o.A, o.lda, o.beta, o.C, o.ldc, 0.0, 0,
                                nullptr);
@@ -122,6 +126,14 @@ extern "C" gbx_status gbx_ops_run(gbx_ctx *ctx, const gbx_op *ops, int count)
 
 namespace {
 
+void record(gbx_server *s, clk::time_point t0, clk::time_point t1)
+{
+    const float us = (float)std::chrono::duration<double, std::micro>(t1 - t0).count();
+    if (s->lat.size() < (1u << 20)) s->lat.push_back(us);
+    else s->lat[s->lat_next++ % s->lat.size()] = us;
+    s->completed++;
+}
+
 void complete(gbx_server *s, const std::vector<Request *> &reqs, gbx_status st)
 {
     const auto now = clk::now();
@@ -129,10 +141,7 @@ void complete(gbx_server *s, const std::vector<Request *> &reqs, gbx_status st)
         if (r->status == GBX_OK) r->status = st;
         r->t_done = now;
         r->done = true;
-        const float us = (float)std::chrono::duration<double, std::micro>(r->t_done - r->t_submit).count();
-        if (s->lat.size() < (1u << 20)) s->lat.push_back(us);
-        else s->lat[s->lat_next++ % s->lat.size()] = us;
-        s->completed++;
+        record(s, r->t_submit, r->t_done);
         s->finished.push_back(r);
     }
 }
@@ -142,11 +151,12 @@ void worker_loop(gbx_server *s, Slot *sl)
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
     while (true) {
-        s->cv_work.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+        s->cv_work.wait(lk, [&] { return s->stop || (!s->queue.empty() && !sl->busy); });
         if (s->queue.empty()) {
             if (s->stop) break;
             continue;
         }
+        sl->busy = true;
         // take the front request; if it is small, every small request queued
         // now goes with it into one grouped launch
         std::vector<Request *> mine;
@@ -178,10 +188,12 @@ void worker_loop(gbx_server *s, Slot *sl)
         const gbx_status sync = gbx_ctx_sync(sl->ctx);   // also collects bounded-wait status words
         if (st == GBX_OK) st = sync;
         lk.lock();
+        sl->busy = false;
         s->batches++;
         if (small) s->grouped_calls += mine.size();
         complete(s, mine, st);
         s->cv_done.notify_all();
+        if (!s->queue.empty()) s->cv_work.notify_all();
     }
 }
 
@@ -256,8 +268,44 @@ extern "C" gbx_status gbx_server_wait(gbx_server *s, uint64_t ticket, double *la
     return st;
 }
 
+// A large request whose caller would only wait for it runs on the calling
+// thread, on a free slot's stream: the slot pool still bounds how much work
+// is on the GPU, and no hand-off to and back from a worker thread is added
+// to a latency that sits on the caller's critical path.  Small requests (and
+// large ones that find every slot busy) go through the queue and are grouped.
 extern "C" gbx_status gbx_server_call(gbx_server *s, const gbx_op *op, double *latency_us)
 {
+    if (!s || !op) return GBX_ERR_ARG;
+    if (!is_small(*op)) {
+        Slot *sl = nullptr;
+        const auto t0 = clk::now();
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (s->stop) return GBX_ERR_ARG;
+            for (auto &q : s->slots)
+                if (!q.busy) {
+                    sl = &q;
+                    q.busy = true;
+                    break;
+                }
+        }
+        if (sl) {
+            cudaSetDevice(s->device);
+            gbx_status st = run_request(sl->ctx, *op);
+            const gbx_status sync = gbx_ctx_sync(sl->ctx);
+            if (st == GBX_OK) st = sync;
+            const auto t1 = clk::now();
+            {
+                std::lock_guard<std::mutex> lk(s->mu);
+                sl->busy = false;
+                s->batches++;
+                record(s, t0, t1);
+            }
+            s->cv_work.notify_all();   // a worker may be waiting for this slot
+            if (latency_us) *latency_us = std::chrono::duration<double, std::micro>(t1 - t0).count();
+            return st;
+        }
+    }
     uint64_t t;
     gbx_status st = gbx_server_submit(s, op, &t);
     if (st != GBX_OK) return st;

@@ -31,8 +31,10 @@ def from_dev(t, rows, cols):
     return t.cpu().numpy().reshape(rows, cols, order="F")
 
 
-@pytest.mark.parametrize("K", [4096, 65536])
+@pytest.mark.parametrize("K", [1024, 4096, 65536])
 def test_fp8_accumulation_is_exact(dev, K):
+    # K = 1024 runs the small-K kernel (all diagonals resident in TMEM), the
+    # others the wide-tile kernel
     # Rows/columns hold even integers with |x| <= 30 and a 30 in every row and
     # column: e = 5, one digit d = x/2 (|d| <= 15) represents x exactly, so
     # slices=1 makes the result exactly 4 * sum d_a d_b.
@@ -159,6 +161,66 @@ def test_zgemm_ozaki(orc, dev, ta, tb):
     dev.zgemm_ozaki(ta, tb, m, n, k, alpha, A, ra, B, rb, beta, C, m)
     got = C.cpu().numpy().view(np.complex128).reshape(m, n, order="F")
     assert rel(got[rows, cols], ref) <= TOL
+
+
+@pytest.mark.parametrize("side", "LR")
+@pytest.mark.parametrize("uplo", "LU")
+@pytest.mark.parametrize("ta", "NT")
+@pytest.mark.parametrize("diag", "NU")
+def test_dtrsm_ozaki(orc, dev, side, uplo, ta, diag):
+    # op(A)^-1 formed in FP64, applied as one Ozaki product; well-conditioned
+    # triangles (diagonal uniform[1,2], off-diagonal uniform[-1,1]/n)
+    m, n = 300, 190
+    na = m if side == "L" else n
+    a, s = orc.trsm_matrix(na, 40 + na)
+    b, _ = orc.matrix(m, n, s)
+    want = b.copy(order="F")
+    orc.dtrsm(side, uplo, ta, diag, m, n, -0.75, a, want)
+    B = to_dev(b)
+    used = dev.dtrsm_ozaki(side, uplo, ta, diag, m, n, -0.75, to_dev(a), na, B, m)
+    assert 1 <= used <= 14
+    assert rel(from_dev(B, m, n), want) <= 1e-13
+
+
+@pytest.mark.parametrize("m,n,k", [(1500, 128, 128), (700, 256, 256), (4100, 96, 64)])
+def test_trailing_update_shapes(orc, dev, m, n, k):
+    # the rank-nb updates of a blocked Cholesky: C -= A B^T with operands that
+    # are sub-blocks of one larger matrix (leading dimension > rows)
+    ld = m + n + 37
+    big, s = orc.matrix(ld, k, 321 + m)
+    a = np.asfortranarray(big[:m])
+    b = np.asfortranarray(big[m:m + n])
+    c, _ = orc.matrix(m, n, s)
+    ref = orc.dgemm_dd("N", "T", m, n, k, -1.0, a, b, 1.0, c)
+    BIG = to_dev(big)
+    C = to_dev(c)
+    dev.dgemm_ozaki("N", "T", m, n, k, -1.0, BIG, ld, BIG[m:], ld, 1.0, C, m)
+    assert rel(from_dev(C, m, n), ref) <= TOL
+    # the diagonal block: symmetric rank-k on the first n rows
+    cs, _ = orc.matrix(n, n, 5)
+    want = cs.copy(order="F")
+    orc.dsyrk("L", "N", n, k, -1.0, np.asfortranarray(big[:n]), 1.0, want)
+    CS = to_dev(cs)
+    dev.dsyrk_ozaki("L", "N", n, k, -1.0, BIG, ld, 1.0, CS, n)
+    got = from_dev(CS, n, n)
+    assert rel(np.tril(got), np.tril(want)) <= TOL
+    assert np.array_equal(np.triu(got, 1), np.triu(cs, 1))
+
+
+@pytest.mark.skipif(__import__("os").environ.get("GBX_OZAKI_SMALLK") == "0",
+                    reason="already running without the small-K kernel")
+def test_wide_tile_kernel_for_small_k():
+    # the small-K kernel is the default for K <= 1024; rerun the small-K tests
+    # with the wide-tile kernel selected
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GBX_OZAKI_SMALLK="0", PYTHONPATH=root)
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider",
+                        os.path.abspath(__file__), "-k", "shapes or spread or syrk or zgemm or tolerance"],
+                       capture_output=True, text=True, env=env, cwd=root, timeout=600)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
 
 
 @pytest.mark.skipif(__import__("os").environ.get("GBX_OZAKI_PAIR") == "1",
