@@ -71,6 +71,7 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ozaki", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-open-loop", action="store_true", help="serving: skip the Poisson-arrival sweep")
     return p.parse_args()
 
 
@@ -263,8 +264,9 @@ class Work:
             dev.dgemm_checked("N", "N", m, n, k, 1.0, d["a"], m, d["b"], k, 0.5, d["c"], m)
         elif w == "ozaki":
             m, n, k = self.m, self.n, self.k
-            self.slices = dev.dgemm_ozaki("N", "N", m, n, k, 1.0, d["a"], m, d["b"], k, 0.5,
-                                          d["c"], m)
+            # asynchronous like a C caller's: no slice-count read-back per call
+            dev.dgemm_ozaki("N", "N", m, n, k, 1.0, d["a"], m, d["b"], k, 0.5, d["c"], m,
+                            want_slices=False)
         elif w == "daxpy":
             dev.daxpy(self.n, 0.5, d["x"], 1, d["y"], 1)
         elif w == "ddot":
@@ -457,11 +459,15 @@ def run_ours(args):
                             "traffic": traffic_from_profiles(f"{w}_{work.config['workload']}"),
                             "kernel_launches_timed": int(k_n)}
     elif w == "ozaki":
-        s = getattr(work, "slices", 0)
+        d = work.d
+        # the slice count of this workload (one more call, outside the timed region)
+        s = dev.dgemm_ozaki("N", "N", work.m, work.n, work.k, 1.0, d["a"], work.m, d["b"], work.k, 0.5,
+                            d["c"], work.m)
         raw = s * (s + 1) / 2 * work.units   # FP8 tensor TFLOP per step
         peak = 2.0 * peaks.get("bf16_tflops", 1900.0)
         achieved = raw / per_launch_s if per_launch_s > 0 else None
-        line["roofline"] = {"bound": "tensor", "kernel": "oz_gemm_kernel (tcgen05 kind::f8f6f4)",
+        kname = "oz_gemm_sk_kernel" if work.k <= 1024 else "oz_gemm_kernel"
+        line["roofline"] = {"bound": "tensor", "kernel": f"{kname} (tcgen05 kind::f8f6f4)",
                             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                             "frac": achieved / peak if achieved else None,
                             "peak_source": f"2 x bf16_tflops of {peak_src} (FP8 dense = 2x bf16 "
@@ -838,18 +844,126 @@ def run_serving(args):
     for mode in ("plain", "served", "ozaki"):
         info.zero_()
         run_mode(mode)
-    line = {"metric": "serving_calls_per_s", "value": results["served"]["calls_per_s"],
+    origs.clear()
+    torch.cuda.synchronize()
+    open_loop = None if args.no_open_loop else run_serving_open_loop(g, results)
+    head = results["ozaki"]
+    line = {"metric": "serving_calls_per_s", "value": head["calls_per_s"],
             "unit": "calls/s", "n_gpus": 1, "steps": 1, "warmup": 0,
-            "ms_per_step": results["served"]["wall_s"] * 1e3, "higher_is_better": True,
+            "ms_per_step": head["wall_s"] * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "cholesky_trace_16threads", "n": sizes, "nb": nbs,
                        "matrix": "A = G G^T + n I, G uniform[-1,1] (device generator, seed 5)",
-                       "calls": "dpotrf(diag) dtrsm dsyrk dgemm + ddot residual checks"},
+                       "calls": "dpotrf(diag) dtrsm dsyrk dgemm + ddot residual checks",
+                       "headline_mode": "ozaki: serving loop, dgemm/dsyrk/dtrsm through the Ozaki path "
+                                        "(tolerance 1e-14, FP64 results), dpotrf in FP64"},
             "modes": results,
-            "speedup_vs_plain_dispatch": results["served"]["calls_per_s"] / results["plain"]["calls_per_s"],
+            "speedup_vs_plain_dispatch": {
+                "ozaki": head["calls_per_s"] / results["plain"]["calls_per_s"],
+                "served_fp64": results["served"]["calls_per_s"] / results["plain"]["calls_per_s"]},
+            "residual_sampled": {m: results[m]["residual_sampled"] for m in results},
+            "open_loop": open_loop,
             "e2e": {"unavailable": "operands are device-resident by design of this workload"}}
     print(json.dumps(line), flush=True)
     dev.close()
+
+
+def run_serving_open_loop(g, closed, njobs=48, nmax=4096, workers=16, seed=11):
+    """Open-loop form of the Cholesky trace: factorisation jobs (n
+    log-uniform in [1024, nmax], nb in {128, 256}) arrive as a Poisson
+    process at swept rates and a pool of worker threads takes them in
+    arrival order.  Reports, per mode and offered rate, the achieved calls/s,
+    per-call latency p50/p99 and job latency (arrival to last call) p50/p99.
+    The rates are fractions of each mode's closed-loop capacity in jobs/s,
+    estimated from the closed-loop calls/s and the jobs' mean call count."""
+    import threading
+    import torch
+    rng = np.random.default_rng(seed)
+    sizes = [int(v) for v in loguni(rng, 1024, nmax, njobs)]
+    nbs = [int(v) for v in rng.choice([128, 256], njobs)]
+    dev = g.Device(0)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    origs = []
+    for n in sizes:
+        G = torch.empty(n * n, dtype=torch.float64, device="cuda").uniform_(-1.0, 1.0, generator=gen)
+        A = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        dev.dgemm_ozaki("N", "T", n, n, n, 1.0, G, n, G, n, 0.0, A, n)
+        A.view(n, n).diagonal().add_(float(n))
+        dev.sync()
+        del G
+        origs.append(A)
+    info = torch.zeros(njobs, dtype=torch.int32, device="cuda")
+    ncalls = [len(cholesky_calls(n, nb, 0, n, 0)) for n, nb in zip(sizes, nbs)]
+    out = {}
+    for mode in ("plain", "served", "ozaki"):
+        cap = closed[mode]["calls_per_s"] / (sum(ncalls) / njobs)   # jobs/s at closed-loop throughput
+        rows = []
+        for frac in (0.25, 0.5, 0.75, 1.0):
+            rate = frac * cap
+            arrivals = np.cumsum(np.random.default_rng(seed + 1).exponential(1.0 / rate, njobs))
+            work = [o.clone() for o in origs]
+            info.zero_()
+            torch.cuda.synchronize()
+            server = g.Server(0, slots=workers) if mode != "plain" else None
+            lat, job_lat, errs = [], [0.0] * njobs, []
+            lock = threading.Lock()
+            nxt = [0]
+            t0 = time.perf_counter()
+
+            def worker():
+                d = g.Device(0) if server is None else None
+                local = []
+                while True:
+                    with lock:
+                        j = nxt[0]
+                        nxt[0] += 1
+                    if j >= njobs:
+                        break
+                    wait = t0 + arrivals[j] - time.perf_counter()
+                    if wait > 0:
+                        time.sleep(wait)
+                    calls = cholesky_calls(sizes[j], nbs[j], work[j].data_ptr(), sizes[j],
+                                           info.data_ptr() + 4 * j, ozaki=(mode == "ozaki"))
+                    for op in calls:
+                        if server is None:
+                            c0 = time.perf_counter()
+                            st = d.L.gbx_ops_run(d.ctx, ctypes_ref(op), 1) or d.L.gbx_ctx_sync(d.ctx)
+                            us = (time.perf_counter() - c0) * 1e6
+                        else:
+                            st, us = server.call(op)
+                        local.append(us)
+                        if st:
+                            errs.append((j, st))
+                            break
+                    job_lat[j] = time.perf_counter() - (t0 + arrivals[j])
+                if d is not None:
+                    d.close()
+                with lock:
+                    lat.extend(local)
+
+            threads = [threading.Thread(target=worker) for _ in range(workers)]
+            for th in threads:
+                th.start()
+            for th in threads:
+                th.join()
+            wall = time.perf_counter() - t0
+            if server:
+                server.close()
+            torch.cuda.synchronize()
+            lat.sort()
+            jl = sorted(job_lat)
+            rows.append({"offered_jobs_per_s": rate, "load_fraction": frac, "calls": len(lat),
+                         "wall_s": wall, "calls_per_s": len(lat) / wall,
+                         "p50_us": lat[len(lat) // 2], "p99_us": lat[int(0.99 * (len(lat) - 1))],
+                         "job_p50_ms": jl[njobs // 2] * 1e3, "job_p99_ms": jl[int(0.99 * (njobs - 1))] * 1e3,
+                         "info_nonzero": int((info != 0).sum().item()), "errors": errs[:4]})
+            del work
+        out[mode] = rows
+    dev.close()
+    return {"jobs": njobs, "n": sizes, "nb": nbs, "workers": workers,
+            "arrivals": f"Poisson, seed {seed + 1}; rate = fraction x closed-loop capacity in jobs/s",
+            "modes": out}
 
 
 # --------------------------------------------------------------------------

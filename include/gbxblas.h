@@ -14,9 +14,10 @@
  *     This is the "thin C ABI" the host code calls; it never reads host
  *     operand memory and never synchronises unless the function says so.
  *
- * Everything is column-major FP64 (complex: interleaved re/im pairs, leading
- * dimensions counted in complex elements).  Integer arguments are 32-bit, as
- * in the LP64 Fortran ABI.
+ * Everything is column-major, in the precision the routine's letter names
+ * (s: float, d: double, c: float complex, z: double complex; complex values
+ * are interleaved re/im pairs, leading dimensions counted in complex
+ * elements).  Integer arguments are 32-bit, as in the LP64 Fortran ABI.
  */
 #ifndef GBXBLAS_H
 #define GBXBLAS_H

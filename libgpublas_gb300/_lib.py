@@ -501,12 +501,15 @@ class Device:
         self._ok(self.L.gbx_dtrmm(self.ctx, _ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n, alpha,
                                   _dp(a), lda, _dp(b), ldb), "dtrmm")
 
-    def dgemm_ozaki(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, tol=0.0, slices=0):
+    def dgemm_ozaki(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, tol=0.0, slices=0,
+                    want_slices=True):
+        """Returns the slice count used (a stream synchronisation), or None
+        with want_slices=False (the call stays asynchronous)."""
         used = C.c_int(0)
         self._ok(self.L.gbx_dgemm_ozaki(self.ctx, _ch(ta), _ch(tb), m, n, k, alpha, _dp(a), lda,
                                         _dp(b), ldb, beta, _dp(c), ldc, tol, slices,
-                                        C.byref(used)), "dgemm_ozaki")
-        return used.value
+                                        C.byref(used) if want_slices else None), "dgemm_ozaki")
+        return used.value if want_slices else None
 
     def zgemm_ozaki(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, tol=0.0, slices=0):
         al = (C.c_double * 2)(complex(alpha).real, complex(alpha).imag)

@@ -45,9 +45,13 @@ void gbx_count_launch(gbx_ctx *ctx, int n);
 /* Event bracket around one launch (no-op unless timing is enabled). */
 void gbx_timer_begin(gbx_ctx *ctx, int tag);
 void gbx_timer_end(gbx_ctx *ctx);
-/* Queue a copy of a device status word (nonzero = a bounded wait gave up);
- * gbx_ctx_sync reports it as GBX_ERR_TIMEOUT. */
-void gbx_watch_status(gbx_ctx *ctx, const int *dev_status);
+/* The context's status words for kernels with bounded waits (64 bytes of
+ * device memory, zero while nothing failed) and the device address of their
+ * mapped host mirror, which such kernels set to the status when it is
+ * nonzero as they finish.  gbx_ctx_sync reports a nonzero mirror (5: a
+ * non-finite Ozaki operand, GBX_ERR_ARG; else GBX_ERR_TIMEOUT) and clears
+ * both. */
+gbx_status gbx_ctx_status(gbx_ctx *ctx, int **dev_status, int **host_mirror);
 /* Check cudaGetLastError after a launch, record and map it. */
 gbx_status gbx_check_launch(gbx_ctx *ctx, const char *what);
 int gbx_ctx_device(const gbx_ctx *ctx);

@@ -40,8 +40,10 @@ struct gbx_ctx {
     void  *pinned;
     size_t pinned_bytes;
     uint64_t launches;
-    int *watch_host;     // pinned copies of device status words (bounded waits)
-    int watch_pending;
+    int *status_dev;     // device status words of kernels with bounded waits ([0]; [8] a counter)
+    int *status_host;    // mapped pinned mirror of status_dev[0], written by the kernels on failure
+    int *status_mirror;  // the mirror's device address
+    int status_armed;    // a kernel that reports through the mirror ran since the last sync
     int timing;
     int timer_next;
     int timer_open;
@@ -167,7 +169,8 @@ extern "C" gbx_status gbx_ctx_destroy(gbx_ctx *c)
     for (int i = 0; i < GBX_WS_SLOTS; i++)
         if (c->ws[i]) cudaFree(c->ws[i]);
     if (c->pinned) cudaFreeHost(c->pinned);
-    if (c->watch_host) cudaFreeHost(c->watch_host);
+    if (c->status_dev) cudaFree(c->status_dev);
+    if (c->status_host) cudaFreeHost(c->status_host);
     for (int i = 0; i < GBX_TIMER_PAIRS; i++) {
         if (c->timers[i].start) cudaEventDestroy(c->timers[i].start);
         if (c->timers[i].stop) cudaEventDestroy(c->timers[i].stop);
@@ -210,27 +213,32 @@ extern "C" gbx_status gbx_ctx_set_stream(gbx_ctx *c, void *stream)
 
 extern "C" void *gbx_ctx_get_stream(gbx_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
-#define GBX_WATCH_SLOTS 64
-
-// Kernels with bounded device-side waits write a status word; the word is
-// copied to pinned memory behind the kernel and checked at the next sync.
-extern "C" void gbx_watch_status(gbx_ctx *c, const int *dev_status)
+// Kernels with bounded device-side waits share one status word per context
+// (zero while nothing failed; first error wins) and copy it, when it is
+// nonzero, into a mapped pinned mirror as they finish.  A sync reads the
+// mirror: no copy or reset is queued per call, only after a failure.
+extern "C" gbx_status gbx_ctx_status(gbx_ctx *c, int **dev_status, int **host_mirror)
 {
-    if (!c) return;
-    if (!c->watch_host) {
-        if (cudaMallocHost((void **)&c->watch_host, sizeof(int) * GBX_WATCH_SLOTS) != cudaSuccess) {
+    if (!c) return GBX_ERR_ARG;
+    if (!c->status_dev) {
+        if (cudaMalloc((void **)&c->status_dev, 64) != cudaSuccess)
+            return gbx_fail(c, GBX_ERR_ALLOC, "status word");
+        if (cudaMemset(c->status_dev, 0, 64) != cudaSuccess ||
+            cudaHostAlloc((void **)&c->status_host, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&c->status_mirror, c->status_host, 0) != cudaSuccess) {
             cudaGetLastError();
-            c->watch_host = nullptr;
-            return;
+            if (c->status_host) cudaFreeHost(c->status_host);
+            cudaFree(c->status_dev);
+            c->status_dev = nullptr;
+            c->status_host = nullptr;
+            return gbx_fail(c, GBX_ERR_ALLOC, "status mirror");
         }
-        memset(c->watch_host, 0, sizeof(int) * GBX_WATCH_SLOTS);
+        *(volatile int *)c->status_host = 0;
     }
-    if (c->watch_pending >= GBX_WATCH_SLOTS) {
-        // all slots in use: settle them before reusing
-        gbx_ctx_sync(c);
-    }
-    cudaMemcpyAsync(&c->watch_host[c->watch_pending++], dev_status, sizeof(int), cudaMemcpyDeviceToHost,
-                    c->stream);
+    c->status_armed = 1;
+    *dev_status = c->status_dev;
+    *host_mirror = c->status_mirror;
+    return GBX_OK;
 }
 
 extern "C" gbx_status gbx_ctx_sync(gbx_ctx *c)
@@ -238,15 +246,18 @@ extern "C" gbx_status gbx_ctx_sync(gbx_ctx *c)
     if (!c) return GBX_ERR_ARG;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return gbx_fail(c, GBX_ERR_CUDA, "stream sync: %s", cudaGetErrorString(e));
-    int bad = 0;
-    for (int i = 0; i < c->watch_pending; i++) {
-        if (c->watch_host[i] != 0 && !bad) bad = c->watch_host[i];
-        c->watch_host[i] = 0;
-    }
-    c->watch_pending = 0;
+    if (!c->status_armed) return GBX_OK;
+    c->status_armed = 0;
+    const int bad = *(volatile int *)c->status_host;
+    if (!bad) return GBX_OK;
+    // clear the words for the next call (the prep counter at [8] is reset by
+    // the kernel that uses it, but a failed call may have left it behind)
+    cudaMemsetAsync(c->status_dev, 0, 64, c->stream);
+    e = cudaStreamSynchronize(c->stream);
+    *(volatile int *)c->status_host = 0;
+    if (e != cudaSuccess) return gbx_fail(c, GBX_ERR_CUDA, "status reset: %s", cudaGetErrorString(e));
     if (bad == 5) return gbx_fail(c, GBX_ERR_ARG, "non-finite operand: the Ozaki path needs finite inputs");
-    if (bad) return gbx_fail(c, GBX_ERR_TIMEOUT, "a bounded device wait gave up (code %d)", bad);
-    return GBX_OK;
+    return gbx_fail(c, GBX_ERR_TIMEOUT, "a bounded device wait gave up (code %d)", bad);
 }
 
 extern "C" uint64_t gbx_ctx_launches(const gbx_ctx *c) { return c ? c->launches : 0; }

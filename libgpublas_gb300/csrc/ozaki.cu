@@ -170,6 +170,7 @@ struct OzPrepOp {
     int *scale2;             // optional second copy over Rp2 rows (symmetric rank-k)
     int Rp2;
     uint8_t *X8;             // S digit planes [s][Rp][Kp]
+    float *gpart;            // one-launch path: (emax, num, den) per 16-row block
 };
 
 __device__ __forceinline__ void oz_stats_rowk_block(const SrcView &v, int rows, int K, int blk, int *expo,
@@ -284,23 +285,87 @@ __device__ __forceinline__ double oz_block_sum(double v)
 // Slice count: relative Frobenius error ~ c * 2^(-5S) * gamma_A * gamma_B with
 // gamma^2 = (sum_i 2^(2 e_i)) / (sum_i 2^(2 e_i) * ss_i / K): the ratio of the
 // squared row maxima to the squared row norms (1 <= gamma <= sqrt(K)).  The
-// statistics were written by other CTAs of the same launch: read through L2.
+// statistics were written by other CTAs of the same launch: read through L2,
+// four rows per thread in flight.  The logarithm is one thread's (FP64
+// transcendental work by a whole CTA costs microseconds on this part).
+__device__ __forceinline__ double oz_gamma_finish(double num, double den, int K)
+{
+    __shared__ double g;
+    num = oz_block_sum(num);
+    den = oz_block_sum(den);
+    if (threadIdx.x == 0) g = den > 0.0 ? 0.5 * log2(num * (double)K / den) : 0.0;
+    __syncthreads();
+    const double r = g;
+    __syncthreads();   // g is reused by the next call
+    return r;
+}
+
+// 2^(2d) for d <= 0 from the exponent field (0 below the normal range)
+__device__ __forceinline__ double oz_pow4(int d)
+{
+    return 2 * d < -1022 ? 0.0 : __longlong_as_double((long long)(1023 + 2 * d) << 52);
+}
+
 __device__ double oz_log2_gamma(const int *expo, const double *ss, int rows, int K)
 {
     int emax = -100000;
+#pragma unroll 4
     for (int i = threadIdx.x; i < rows; i += blockDim.x) emax = max(emax, __ldcg(expo + i));
     emax = oz_block_max(emax);
     double num = 0.0, den = 0.0;
+#pragma unroll 4
     for (int i = threadIdx.x; i < rows; i += blockDim.x) {
-        // 2^(2(e_i - emax)) from the exponent field (0 below the normal range)
-        const int d = 2 * (__ldcg(expo + i) - emax);
-        const double w = d < -1022 ? 0.0 : __longlong_as_double((long long)(1023 + d) << 52);
+        const double w = oz_pow4(__ldcg(expo + i) - emax);
         num += w;
         den += w * __ldcg(ss + i);
     }
-    num = oz_block_sum(num);
-    den = oz_block_sum(den);
-    return den > 0.0 ? 0.5 * log2(num * (double)K / den) : 0.0;
+    return oz_gamma_finish(num, den, K);
+}
+
+// The same from per-CTA partials (emax_c, num_c, den_c) of 16 rows each,
+// num_c = sum 2^(2(e_i - emax_c)) and den_c likewise weighted by ss_i: the
+// one-launch preparation leaves one partial per CTA, so the last CTA merges
+// Rp/16 partials instead of reading every row.  FP32 throughout (the
+// statistic only steers the slice count; rows 2^-63 below the largest
+// maximum contribute nothing either way) and one warp-level reduction pass:
+// FP64 and block-wide barrier rounds cost microseconds on the critical path
+// of a small product.
+__device__ float oz_log2_gamma_parts(const float *part, int n, int K)
+{
+    __shared__ int s_emax[8];
+    __shared__ float s_num[8], s_den[8], s_g;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int emax = -100000;
+#pragma unroll 4
+    for (int i = threadIdx.x; i < n; i += blockDim.x) emax = max(emax, (int)__ldcg(part + 3 * i));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if (lane == 0) s_emax[warp] = emax;
+    __syncthreads();
+#pragma unroll
+    for (int w = 0; w < 8; w++) emax = max(emax, s_emax[w]);
+    float num = 0.f, den = 0.f;
+#pragma unroll 4
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int d = 2 * ((int)__ldcg(part + 3 * i) - emax);
+        const float w = d < -126 ? 0.f : __int_as_float((127 + d) << 23);
+        num = fmaf(w, __ldcg(part + 3 * i + 1), num);
+        den = fmaf(w, __ldcg(part + 3 * i + 2), den);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        num += __shfl_xor_sync(0xffffffffu, num, o);
+        den += __shfl_xor_sync(0xffffffffu, den, o);
+    }
+    if (lane == 0) { s_num[warp] = num; s_den[warp] = den; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float tn = 0.f, td = 0.f;
+        for (int w = 0; w < 8; w++) { tn += s_num[w]; td += s_den[w]; }
+        s_g = td > 0.f ? 0.5f * __log2f(tn * (float)K / td) : 0.f;
+    }
+    __syncthreads();
+    return s_g;
 }
 
 // Finishes the statistics of both operands (b_stats: b has its own) and, in
@@ -350,20 +415,26 @@ __device__ __forceinline__ uint32_t e4m3_of_digit(int d)
 // col_k sources are read coalesced.
 constexpr int OZ_SPLIT_ROWS = 16, OZ_SPLIT_PER = 8;
 
+// pre: the same tile already staged by the caller (one-launch path, K <= 128)
 __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K, int Rp, int Kp, const int *expo,
-                                              int S, uint8_t *X8, int blk)
+                                              int S, uint8_t *X8, int blk, const double (*pre)[129] = nullptr)
 {
     __shared__ double tile[OZ_SPLIT_ROWS][129];
+    __shared__ uint32_t e4m3_tbl[33];   // E4M3 byte of the digit d at [16 + d], d in [-16, 16]
     const int kblocks = Kp / 128;
     const int r0 = (blk / kblocks) * OZ_SPLIT_ROWS, k0 = (blk % kblocks) * 128;
+    __syncthreads();   // a previous call's readers of tile are done
+    if (threadIdx.x < 33) e4m3_tbl[threadIdx.x] = e4m3_of_digit((int)threadIdx.x - 16);
     // load: col_k -> threads along rows; row_k -> threads along k
-    for (int t = threadIdx.x; t < OZ_SPLIT_ROWS * 128; t += blockDim.x) {
-        int rr, kk;
-        if (v.row_k) { kk = t & 127; rr = t >> 7; }
-        else         { rr = t % OZ_SPLIT_ROWS; kk = t / OZ_SPLIT_ROWS; }
-        const int r = r0 + rr, k = k0 + kk;
-        tile[rr][kk] = (r < rows && k < K) ? src_get(v, r, k) : 0.0;
-    }
+    if (!pre)
+        for (int t = threadIdx.x; t < OZ_SPLIT_ROWS * 128; t += blockDim.x) {
+            int rr, kk;
+            if (v.row_k) { kk = t & 127; rr = t >> 7; }
+            else         { rr = t % OZ_SPLIT_ROWS; kk = t / OZ_SPLIT_ROWS; }
+            const int r = r0 + rr, k = k0 + kk;
+            tile[rr][kk] = (r < rows && k < K) ? src_get(v, r, k) : 0.0;
+        }
+    const double (*T)[129] = pre ? pre : tile;
     __syncthreads();
     constexpr int TPR = 128 / OZ_SPLIT_PER;   // threads per row
     const int rr = threadIdx.x / TPR, kq = (threadIdx.x % TPR) * OZ_SPLIT_PER;
@@ -377,7 +448,7 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
     unsigned neg = 0u;
 #pragma unroll
     for (int j = 0; j < OZ_SPLIT_PER; j++) {
-        const unsigned long long b = (unsigned long long)__double_as_longlong(tile[rr][kq + j]);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(T[rr][kq + j]);
         neg |= (unsigned)(b >> 63) << j;
         const int E = (int)((b >> 52) & 0x7FF);
         const unsigned long long M = (b & 0xFFFFFFFFFFFFFull) | (E ? (1ull << 52) : 0ull);
@@ -388,24 +459,36 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
         else if (sh < 64) { lo[j] = M << sh; hi[j] = M >> (64 - sh); }
         else { lo[j] = 0ull; hi[j] = M << (sh - 64); }
     }
-    // balanced base-32 digits, least significant first: d in [-15, 16]
+    // Balanced base-32 digits d_s in [-16, 16] with N = sum_s d_s 32^(S-1-s):
+    // adding C = 16 * sum_{s<S} 32^s once turns every 5-bit chunk c of N + C
+    // into the digit c - 16 (the carries are resolved by the one addition);
+    // the top chunk is taken unmasked (N <= 16 * 32^(S-1) bounds it by 32).
+    unsigned long long clo = 0ull, chi = 0ull;
+    for (int s = 0; s < S; s++) {
+        const int b = 5 * s + 4;
+        if (b < 64) clo |= 1ull << b;
+        else chi |= 1ull << (b - 64);
+    }
+#pragma unroll
+    for (int j = 0; j < OZ_SPLIT_PER; j++) {
+        const unsigned long long nl = lo[j] + clo;
+        hi[j] = hi[j] + chi + (nl < clo ? 1ull : 0ull);
+        lo[j] = nl;
+    }
     for (int s = S - 1; s >= 0; s--) {
+        const int sh = 5 * (S - 1 - s);   // plane s holds the chunk at bit sh
+        const unsigned mask = s == 0 ? 63u : 31u;
         uint32_t w[OZ_SPLIT_PER / 4] = {};
 #pragma unroll
         for (int j = 0; j < OZ_SPLIT_PER; j++) {
-            int d = (int)(lo[j] & 31ull);
-            if (d > 16) {
-                d -= 32;
-                const unsigned long long nl = lo[j] + (unsigned long long)(-d);
-                hi[j] += (nl < lo[j]) ? 1ull : 0ull;
-                lo[j] = nl;
-            } else {
-                lo[j] -= (unsigned long long)d;   // clears the low 5 bits, no borrow
-            }
-            lo[j] = (lo[j] >> 5) | (hi[j] << 59);
-            hi[j] >>= 5;
-            const int sd = ((neg >> j) & 1u) ? -d : d;
-            w[j >> 2] |= e4m3_of_digit(sd) << (8 * (j & 3));
+            unsigned c;
+            if (sh == 0) c = (unsigned)lo[j];
+            else if (sh < 64) c = (unsigned)((lo[j] >> sh) | (hi[j] << (64 - sh)));
+            else c = (unsigned)(hi[j] >> (sh - 64));
+            const int d = (int)(c & mask) - 16;
+            // the digit of x = sign(x) * d, as an E4M3 byte from the table
+            const int idx = ((neg >> j) & 1u) ? 16 - d : 16 + d;
+            w[j >> 2] |= e4m3_tbl[idx] << (8 * (j & 3));
         }
         uint2 *dst = (uint2 *)(X8 + ((size_t)s * Rp + r) * Kp + k0 + kq);
         *dst = make_uint2(w[0], w[1]);
@@ -430,7 +513,7 @@ oz_prep_split(OzPrepOp a, OzPrepOp b, const int *__restrict__ S_dev)
 // both operands.  One launch instead of three: small products are
 // dominated by per-launch cost.
 __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, int Rp, int Kp, int *expo, double *ss,
-                                             int *scale, uint8_t *X8, int rblk, int *status)
+                                             int *scale, uint8_t *X8, float *gpart, int rblk, int *status)
 {
     __shared__ double tile[OZ_SPLIT_ROWS][129];
     const int r0 = rblk * OZ_SPLIT_ROWS;
@@ -472,8 +555,33 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
         }
     }
     __syncthreads();   // the row exponents are visible to the whole CTA
+    if (gpart && threadIdx.x < 32) {
+        // this block's partial of the slice-count statistic (oz_log2_gamma_parts)
+        const int rg = r0 + (threadIdx.x & 15);
+        const bool valid = threadIdx.x < 16 && rg < rows;
+        const int e = valid ? expo[rg] : -100000;
+        int em = e;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
+        const int d = 2 * (e - em);
+        const float w = (!valid || d < -126) ? 0.f : __int_as_float((127 + d) << 23);
+        float nu = w, de = valid ? w * (float)ss[rg] : 0.f;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            nu += __shfl_xor_sync(0xffffffffu, nu, o);
+            de += __shfl_xor_sync(0xffffffffu, de, o);
+        }
+        if (threadIdx.x == 0) {
+            gpart[3 * rblk] = (float)em;
+            gpart[3 * rblk + 1] = nu;
+            gpart[3 * rblk + 2] = de;
+        }
+    }
     const int kblocks = Kp / 128;
-    for (int kb = 0; kb < kblocks; kb++) oz_split_tile(v, rows, K, Rp, Kp, expo, OZ_SMAX, X8, rblk * kblocks + kb);
+    if (kblocks == 1)   // the statistics pass left this block's only tile in shared memory
+        oz_split_tile(v, rows, K, Rp, Kp, expo, OZ_SMAX, X8, rblk, tile);
+    else
+        for (int kb = 0; kb < kblocks; kb++) oz_split_tile(v, rows, K, Rp, Kp, expo, OZ_SMAX, X8, rblk * kblocks + kb);
 }
 
 __global__ void __launch_bounds__(256)
@@ -481,9 +589,9 @@ oz_prep_small(OzPrepOp a, OzPrepOp b, double tol, int forced, int *status, unsig
 {
     const int na = a.Rp / OZ_SPLIT_ROWS;
     if ((int)blockIdx.x < na)
-        oz_prep_rows(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, a.ss, a.scale, a.X8, blockIdx.x, status);
+        oz_prep_rows(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, a.ss, a.scale, a.X8, a.gpart, blockIdx.x, status);
     else
-        oz_prep_rows(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, b.ss, b.scale, b.X8, blockIdx.x - na, status);
+        oz_prep_rows(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, b.ss, b.scale, b.X8, b.gpart, blockIdx.x - na, status);
     __threadfence();
     __syncthreads();
     __shared__ bool last;
@@ -491,12 +599,12 @@ oz_prep_small(OzPrepOp a, OzPrepOp b, double tol, int forced, int *status, unsig
     __syncthreads();
     if (!last) return;
     __threadfence();
-    const double ga = oz_log2_gamma(a.expo, a.ss, a.rows, a.K);
-    const double gb = oz_log2_gamma(b.expo, b.ss, b.rows, b.K);
+    const float ga = oz_log2_gamma_parts(a.gpart, a.Rp / OZ_SPLIT_ROWS, a.K);
+    const float gb = oz_log2_gamma_parts(b.gpart, b.Rp / OZ_SPLIT_ROWS, b.K);
     if (threadIdx.x == 0) {
         int S;
         if (forced > 0) S = forced;
-        else S = (int)ceil((-log2(tol) + ga + gb + 1.5) / 5.0);
+        else S = (int)ceilf((-__log2f((float)tol) + ga + gb + 1.5f) / 5.0f);
         S_dev[0] = max(1, min(OZ_SMAX, S));
         *counter = 0u;
     }
@@ -516,8 +624,31 @@ struct OzParams {
     long long ldc;
     double alpha, beta;
     int c_part;                // 0 full, 1 lower (row >= col), 2 upper
-    int *status;
+    int *status;               // the context's status word (zero while nothing failed)
+    int *status_host;          // its mapped host mirror
 };
+
+// A call whose operands were found non-finite (or whose earlier kernel gave
+// up a wait) skips the product kernel: every thread of the CTA takes the
+// same decision before any copy or MMA is issued, so no asynchronous work is
+// left behind.
+__device__ __forceinline__ bool oz_skip_kernel(const OzParams &p)
+{
+    __shared__ int s_st;
+    if (threadIdx.x == 0) s_st = *(volatile int *)p.status;
+    __syncthreads();
+    return s_st != 0;
+}
+
+// A nonzero status is copied to the host mirror as the CTA finishes (the
+// host reads the mirror after its stream synchronisation).
+__device__ __forceinline__ void oz_report(const OzParams &p)
+{
+    if (threadIdx.x == 0) {
+        const int st = *(volatile int *)p.status;
+        if (st) *(volatile int *)p.status_host = st;
+    }
+}
 
 // Group enumeration shared by the three roles.  Items are (pair, k chunk);
 // a group is a run of consecutive items of one diagonal whose K extent stays
@@ -548,10 +679,12 @@ __device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, i
 // diagonal's weight,
 //     V = sum_q D_q 2^(5(S-1-q)),     C_ij = V 2^(e_i + f_j - 8 - 5(S-1)),
 // held in W (two 64-bit words per element, column-major Mp x Np) between
-// diagonals.  Each diagonal costs an FP32->int conversion and a 128-bit
-// shift-and-add on the integer pipe per element; the FP64 pipe (the scarce
-// one on GB300) is used once per element, for the final conversion, scale
-// and alpha/beta.  |V| < 2^(24 + 65 + 14) for S <= 14 and K <= 2^30.
+// diagonals.  Each diagonal costs a decode of the FP32 value and a 128-bit
+// shift-and-add on the integer pipe per element; the final conversion and
+// scale are integer work too (oz_i128_ldexp), so the FP64 pipe (the scarce
+// one on GB300) sees one multiply-add per element, for beta, and one
+// multiply when alpha is not a power of two.  |V| < 2^(24 + 65 + 14) for
+// S <= 14 and K <= 2^30.
 //
 // One row (grow) and NCOL columns from gcol0 per call, walked in CH-column
 // chunks and software-pipelined: the global loads of chunk c+1 (running
@@ -566,8 +699,6 @@ __device__ __forceinline__ bool oz_c_keep(const OzParams &p, int grow, int gcol)
 
 template <int CH>
 __device__ __forceinline__ void tmem_ld_chunk(uint32_t taddr, uint32_t (&r)[CH]);
-template <>
-__device__ __forceinline__ void tmem_ld_chunk<16>(uint32_t taddr, uint32_t (&r)[16]) { tmem_ld_32x32b_x16(taddr, r); }
 template <>
 __device__ __forceinline__ void tmem_ld_chunk<8>(uint32_t taddr, uint32_t (&r)[8]) { tmem_ld_32x32b_x8(taddr, r); }
 
@@ -606,6 +737,152 @@ __device__ __forceinline__ double oz_alpha_pow2(double alpha, int e)
     if (ea != 0 && ea != 0x7FF && ea + e >= 1 && ea + e <= 2046)
         return __longlong_as_double(b + ((long long)e << 52));
     return ldexp(alpha, e);
+}
+
+// FP32 accumulator values are integers.  Float-to-integer conversion
+// instructions issue to the FP64 pipe, which on this part retires two lanes
+// per clock per SM (one drain of a 128 x 32 tile with ten diagonals spent
+// 20k cycles there), so the drains decode the value on the FMA and integer
+// pipes instead.
+//   |v| < 2^22: adding 1.5 * 2^23 (exact, round to nearest) leaves v in the
+//   low mantissa bits, bits = 0x4B400000 + v.
+__device__ __forceinline__ int oz_f2i22(float v)
+{
+    return __float_as_int(__fadd_rn(v, 12582912.0f)) - 0x4B400000;
+}
+
+//   |v| <= 2^24: v = m * 2^(e - 150) with the 24-bit significand m, so a
+//   right shift by 150 - e (a left shift by one for 2^24 itself); zero has
+//   e = 0 and shifts out.
+__device__ __forceinline__ int oz_f2i24(float v)
+{
+    const int b = __float_as_int(v);
+    const int e = (b >> 23) & 0xFF;
+    const unsigned m = ((unsigned)b & 0x7FFFFFu) | 0x800000u;
+    const unsigned mag = e > 150 ? (m << 1) : (m >> min(150 - e, 31));
+    const int s = b >> 31;
+    return ((int)mag ^ s) - s;
+}
+
+// The signed 128-bit integer (hi:lo) times 2^e as a double, rounded to
+// nearest even, built on the integer pipe: magnitude, leading-zero count,
+// normalisation, rounding of the 75 discarded bits, exponent field.  ok is
+// false when the result would not be a normal number (the caller then takes
+// the FP64 route); zero is exact.
+__device__ __forceinline__ double oz_i128_ldexp(unsigned long long lo, long long hi, int e, bool &ok)
+{
+    const unsigned long long s = (unsigned long long)(hi >> 63);
+    const unsigned long long ml = (lo ^ s) - s;
+    const unsigned long long mh = ((unsigned long long)hi ^ s) + (s & (ml == 0ull ? 1ull : 0ull));
+    if ((mh | ml) == 0ull) {
+        ok = true;
+        return 0.0;
+    }
+    const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
+    unsigned long long nh, nl;
+    if (lz >= 64) {
+        nh = ml << (lz - 64);
+        nl = 0ull;
+    } else if (lz == 0) {
+        nh = mh;
+        nl = ml;
+    } else {
+        nh = (mh << lz) | (ml >> (64 - lz));
+        nl = ml << lz;
+    }
+    unsigned long long mant = nh >> 11;   // 53 bits, the leading one at bit 52
+    const unsigned long long rem = nh & 0x7FFull;
+    if (rem > 0x400ull || (rem == 0x400ull && (nl != 0ull || (mant & 1ull)))) mant++;
+    const int eb = 127 - lz + e + 1023;   // biased exponent (a rounding carry adds one through mant)
+    ok = eb >= 1 && eb <= 2045;
+    return __longlong_as_double((long long)((((unsigned long long)(eb - 1)) << 52) + mant) |
+                                (long long)(s & 0x8000000000000000ull));
+}
+
+// alpha as +-2^ea when it is a power of two (folded into the exponent on the
+// integer pipe), else kept for one FP64 multiply.
+struct OzAlpha {
+    bool pow2;
+    int ea;
+    unsigned long long sign;
+};
+__device__ __forceinline__ OzAlpha oz_alpha_split(double alpha)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(alpha);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    OzAlpha a;
+    a.pow2 = (b & 0xFFFFFFFFFFFFFull) == 0ull && ex != 0 && ex != 0x7FF;
+    a.ea = ex - 1023;
+    a.sign = b & 0x8000000000000000ull;
+    return a;
+}
+
+// v * 2^e as a double for |v| < 2^53 (exact), built on the integer pipe;
+// eb receives the biased exponent of the result (1023 for v = 0), which the
+// caller checks against the normal range.
+__device__ __forceinline__ double oz_i53_ldexp(long long v, int e, int &eb)
+{
+    const unsigned long long s = (unsigned long long)(v >> 63);
+    const unsigned long long m = ((unsigned long long)v ^ s) - s;
+    const int lz = __clzll((long long)m);   // >= 11; 64 for v = 0
+    eb = m ? 1086 - lz + e : 1023;
+    const unsigned long long bits = ((unsigned long long)(eb - 1) << 52) + (m << (lz - 11));
+    return __longlong_as_double((long long)((m ? bits : 0ull) | (s & 0x8000000000000000ull)));
+}
+
+// The output value alpha * V * 2^e + beta * cold for the signed 128-bit V:
+// one rounding of V * 2^e (exact scaling), then one multiply-add with beta.
+__device__ __forceinline__ double oz_result(unsigned long long lo, long long hi, int e, double alpha,
+                                            const OzAlpha &as, double beta, double cold)
+{
+    bool ok;
+    double r;
+    if (as.pow2) {
+        r = oz_i128_ldexp(lo, hi, e + as.ea, ok);
+        r = __longlong_as_double(__double_as_longlong(r) ^ (long long)as.sign);
+    } else {
+        r = alpha * oz_i128_ldexp(lo, hi, e, ok);
+    }
+    if (!ok) r = oz_alpha_pow2(alpha, e) * oz_to_double(lo, hi);
+    return beta != 0.0 ? fma(beta, cold, r) : r;
+}
+
+// The same for V = vh * 2^lsh + vl with |vh|, |vl| < 2^53 (0 <= lsh < 64):
+// both parts convert exactly on the integer pipe and one FP64 addition
+// rounds their sum once, so V * 2^e is correctly rounded with two FP64
+// instructions per element (the addition and the beta multiply-add) and no
+// 128-bit normalisation.  Parts outside the normal range take the 128-bit
+// route.
+__device__ __forceinline__ double oz_result_split(long long vh, long long vl, int lsh, int e, double alpha,
+                                                  const OzAlpha &as, double beta, double cold)
+{
+    const int ee = as.pow2 ? e + as.ea : e;
+    int ebh, ebl;
+    double dh = oz_i53_ldexp(vh, ee + lsh, ebh);
+    double dl = oz_i53_ldexp(vl, ee, ebl);
+    if (ebh >= 1 && ebh <= 2045 && ebl >= 1 && ebl <= 2045) {
+        double r;
+        if (as.pow2) {
+            dh = __longlong_as_double(__double_as_longlong(dh) ^ (long long)as.sign);
+            dl = __longlong_as_double(__double_as_longlong(dl) ^ (long long)as.sign);
+            r = dh + dl;
+        } else {
+            r = alpha * (dh + dl);
+        }
+        return beta != 0.0 ? fma(beta, cold, r) : r;
+    }
+    unsigned long long lo;
+    long long hi;
+    if (lsh == 0) {
+        lo = (unsigned long long)vh;
+        hi = vh >> 63;
+    } else {
+        lo = (unsigned long long)vh << lsh;
+        hi = vh >> (64 - lsh);
+    }
+    const unsigned long long nlo = lo + (unsigned long long)vl;
+    hi = hi + (vl >> 63) + (nlo < lo ? 1 : 0);
+    return oz_result(nlo, hi, e, alpha, as, beta, cold);
 }
 
 template <int NCOL, int CH>
@@ -657,7 +934,7 @@ __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, 
         for (int j = 0; j < CH; j++) {
             unsigned long long slo;
             long long shi;
-            oz_shift128((long long)__float2int_rn(__uint_as_float(r[j])), sh, slo, shi);
+            oz_shift128((long long)oz_f2i24(__uint_as_float(r[j])), sh, slo, shi);
             if (first) {
                 wc[j].x = (long long)slo;
                 wc[j].y = shi;
@@ -672,13 +949,14 @@ __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, 
 #pragma unroll
             for (int j = 0; j < CH; j++) __stcg(wdst + (size_t)j * p.Mp, wc[j]);
         } else if (row_ok) {
+            const OzAlpha as = oz_alpha_split(p.alpha);
+            const double beta = need_c ? p.beta : 0.0;
 #pragma unroll
             for (int j = 0; j < CH; j++) {
                 const int gcol = gcol0 + cb + j;
                 if (!oz_c_keep(p, grow, gcol)) continue;
-                const double v = oz_to_double((unsigned long long)wc[j].x, wc[j].y);
-                const double sa = oz_alpha_pow2(p.alpha, erow + __ldg(p.col_exp + gcol));
-                crow[(size_t)(cb + j) * p.ldc] = need_c ? fma(sa, v, p.beta * cc[j]) : sa * v;
+                crow[(size_t)(cb + j) * p.ldc] = oz_result((unsigned long long)wc[j].x, wc[j].y,
+                                                           erow + __ldg(p.col_exp + gcol), p.alpha, as, beta, cc[j]);
             }
         }
     }
@@ -707,6 +985,10 @@ template <int BN>
 __global__ void __launch_bounds__(OzCfg<BN>::THREADS, 1)
 oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
 {
+    if (oz_skip_kernel(p)) {
+        oz_report(p);
+        return;
+    }
     using Cfg = OzCfg<BN>;
     constexpr int STAGES = Cfg::STAGES, NBUF = Cfg::NBUF, STAGE_BYTES = Cfg::STAGE_BYTES;
     extern __shared__ uint8_t smem_raw[];
@@ -857,42 +1139,68 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         tc_fence_after();
         tmem_dealloc(tmem_base, 512);
     }
+    oz_report(p);
 }
 
 // ---------------------------------------------------------------------------
 // Small-K kernel: every diagonal accumulator resident in TMEM
 // ---------------------------------------------------------------------------
-// When Kp * OZ_SMAX <= 65536, each diagonal's accumulation over the whole K
-// extent stays exact in one FP32 accumulator, so a 128 x 32 tile keeps all
-// S (<= 14) diagonal sums in TMEM at once (S x 32 of the 512 columns).  The
-// MMAs of all S(S+1)/2 slice products then run back to back, and one drain
-// per tile combines the S sums exactly in registers (128-bit integers) and
-// writes C: no running-sum traffic and no per-diagonal hand-off between the
-// MMA issuer and the drain, which bound the wide-tile kernel on the small-K
-// products of blocked factorizations.  Slices stream through two rings: A_s
-// (16 KB) for s = 0..S-1 and, under each A_s, B_t (4 KB) for t = 0..S-1-s.
-// Tiles are ordered column-fastest so the CTAs sharing an A row block run
-// together and its slices come from L2.
-// Warp 0: TMA; warp 1: MMA issuer; warps 2..9: drain (two per TMEM lane
-// quarter, 16 columns each).  The accumulators are released before C is
-// converted and written, so the next tile's MMAs overlap that work.
-constexpr int OZS_BN = 32, OZS_AST = 3, OZS_BST = 16, OZS_DRAIN_WARPS = 8;
-constexpr int OZS_B_BYTES = OZS_BN * OZ_BK;   // 4 KB
+// For Kp <= 1024 each diagonal sum over the whole K extent is an integer of
+// magnitude below 14 * 1024 * 16 * 16 < 2^22, exact in one FP32 accumulator,
+// so a 128 x 32 tile keeps all S (<= 14) diagonal sums in TMEM at once:
+// diagonal q in columns [32q, 32q + 32).  One drain per tile combines the S
+// sums exactly in registers and writes C: no running-sum traffic and no
+// per-diagonal hand-off between the MMA issuer and the drain.
+//
+// The B slices of one k block are loaded side by side, B_0..B_{S-1} as the
+// rows 32t..32t+31 of one S*32 x 128-byte stage.  Then a single MMA of
+// N = 32(S - s) columns multiplies A_s by B_0..B_{S-1-s} at once and writes
+// A_s B_t into columns 32(s + t): exactly diagonal s + t's accumulator.  A
+// tcgen05.mma costs the issuing thread about 70 cycles whatever its N up to
+// 128 (N = 256: 128 cycles; diag/utc_probe.cu), so S(S+1)/2 products of
+// N = 32 would leave the tensor pipe three quarters idle; concatenated, a
+// 128-wide k block of a tile is sum_s ceil(32(S - s) / 256) * 4 MMAs (48 for
+// S = 10 instead of 220).  The A slices (16 KB each) stream through a ring;
+// the B stage is double-buffered so the next k block's (or tile's) slices
+// load under the current MMAs.
+//
+// The drain prefetches its row's C values while the MMAs run, then decodes each FP32 sum on the FMA and integer pipes (oz_f2i22)
+// and folds diagonals by Horner's rule, V = (...(D_0 * 32 + D_1) * 32 ...) +
+// D_{S-1}, in two signed 64-bit halves (diagonals 0..g-1 and g..S-1, g =
+// ceil(S/2): at most seven each, |half| < 2^22 * 32^6 * 1.04 < 2^53); each
+// half converts exactly to a double on the integer pipe and one FP64 addition
+// rounds V once (oz_result_split).  Tiles are ordered column-fastest so the
+// CTAs sharing an A row block run together and its slices come from L2.
+// Warp 0: TMA; warp 1: MMA issuer; warps 2..17: drain (four per TMEM lane
+// quarter, 8 columns each: the per-element conversion work of one tile is
+// what bounds a CTA with several tiles, so it gets most of the warps).  The
+// accumulators are released before C is written, so the next tile's MMAs
+// overlap that work.
+constexpr int OZS_BN = 32, OZS_AST = 4, OZS_BSTG = 2, OZS_DRAIN_WARPS = 16;
+constexpr int OZS_DCOLS = OZS_BN / (OZS_DRAIN_WARPS / 4);   // columns per drain thread
+constexpr int OZS_B_BYTES = OZS_BN * OZ_BK;                 // 4 KB: one slice's 32 rows
+constexpr int OZS_BSTAGE_BYTES = OZ_SMAX * OZS_B_BYTES;     // 56 KB: all slices of one k block
 constexpr int OZS_THREADS = 64 + 32 * OZS_DRAIN_WARPS;
-constexpr size_t OZS_SMEM = (size_t)OZS_AST * OZ_A_BYTES + (size_t)OZS_BST * OZS_B_BYTES + 1024 + 512;
-constexpr int OZS_KMAX = 65536 / OZ_SMAX / OZ_BK * OZ_BK;   // 4608: exact for any slice count
+constexpr size_t OZS_SMEM = (size_t)OZS_AST * OZ_A_BYTES + (size_t)OZS_BSTG * OZS_BSTAGE_BYTES + 1024 + 256;
+constexpr int OZS_KMAX = 1024;
+static_assert((long long)OZ_SMAX * OZS_KMAX * 256 < (1LL << 22), "small-K diagonal sums must stay below 2^22");
+static_assert(OZ_SMAX * OZS_BN <= 512, "small-K accumulators must fit TMEM");
 
 __global__ void __launch_bounds__(OZS_THREADS, 1)
 oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
 {
+    if (oz_skip_kernel(p)) {
+        oz_report(p);
+        return;
+    }
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
     uint8_t *sB = smem + OZS_AST * OZ_A_BYTES;
-    uint64_t *bars = (uint64_t *)(sB + OZS_BST * OZS_B_BYTES);
+    uint64_t *bars = (uint64_t *)(sB + OZS_BSTG * OZS_BSTAGE_BYTES);
     uint64_t *fullA = bars, *emptyA = fullA + OZS_AST;
-    uint64_t *fullB = emptyA + OZS_AST, *emptyB = fullB + OZS_BST;
-    uint64_t *tfull = emptyB + OZS_BST, *tempty = tfull + 1;
+    uint64_t *fullB = emptyA + OZS_AST, *emptyB = fullB + OZS_BSTG;
+    uint64_t *tfull = emptyB + OZS_BSTG, *tempty = tfull + 1;
     uint32_t *tmem_slot = (uint32_t *)(tempty + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -900,7 +1208,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < OZS_AST; i++) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], 1); }
-        for (int i = 0; i < OZS_BST; i++) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], 1); }
+        for (int i = 0; i < OZS_BSTG; i++) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], 1); }
         mbar_init(tfull, 1);
         mbar_init(tempty, 32 * OZS_DRAIN_WARPS);
         fence_barrier_init();
@@ -929,34 +1237,36 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int tm = t / p.tiles_n, tn = t % p.tiles_n;
                 if (!tile_needed(p, tm, tn, OZ_BM, OZS_BN)) continue;
-                for (int kb = 0; kb < nkb && ok; kb++)
-                    for (int sa = 0; sa < S && ok; sa++) {
+                for (int kb = 0; kb < nkb && ok; kb++) {
+                    // the B stage: slices 0..S-1 of the tile's 32 columns, side by side
+                    if (!mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
+                    mbar_arrive_expect_tx(&fullB[bs], (uint32_t)(S * OZS_B_BYTES));
+                    for (int tb = 0; tb < S; tb++)
+                        tma_load_2d(sB + bs * OZS_BSTAGE_BYTES + tb * OZS_B_BYTES, &tmB, &fullB[bs], kb * OZ_BK,
+                                    tb * p.Np + tn * OZS_BN);
+                    if (++bs == OZS_BSTG) { bs = 0; bp ^= 1u; }
+                    // then the A slices
+                    for (int sa = 0; sa < S; sa++) {
                         if (!mbar_wait(&emptyA[as], ap ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
                         mbar_arrive_expect_tx(&fullA[as], OZ_A_BYTES);
                         tma_load_2d(sA + as * OZ_A_BYTES, &tmA, &fullA[as], kb * OZ_BK, sa * p.Mp + tm * OZ_BM);
                         if (++as == OZS_AST) { as = 0; ap ^= 1u; }
-                        for (int tb = 0; tb < S - sa && ok; tb++) {
-                            if (!mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
-                            mbar_arrive_expect_tx(&fullB[bs], OZS_B_BYTES);
-                            tma_load_2d(sB + bs * OZS_B_BYTES, &tmB, &fullB[bs], kb * OZ_BK, tb * p.Np + tn * OZS_BN);
-                            if (++bs == OZS_BST) { bs = 0; bp ^= 1u; }
-                        }
                     }
+                }
             }
             // wait (bounded) until every issued load has been consumed
             for (int i = 0; i < OZS_AST; i++) {
                 mbar_wait(&emptyA[as], ap ^ 1u, status, TC_TIMEOUT_EMPTY);
                 if (++as == OZS_AST) { as = 0; ap ^= 1u; }
             }
-            for (int i = 0; i < OZS_BST; i++) {
+            for (int i = 0; i < OZS_BSTG; i++) {
                 mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY);
-                if (++bs == OZS_BST) { bs = 0; bp ^= 1u; }
+                if (++bs == OZS_BSTG) { bs = 0; bp ^= 1u; }
             }
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_e4m3_f32(OZ_BM, OZS_BN);
             int as = 0, bs = 0;
             uint32_t ap = 0, bp = 0, tp = 0;
             bool ok = true;
@@ -967,84 +1277,102 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 // the previous tile's sums have been read out of TMEM
                 if (!mbar_wait(tempty, tp ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
                 tc_fence_after();
-                for (int kb = 0; kb < nkb && ok; kb++)
-                    for (int sa = 0; sa < S && ok; sa++) {
+                for (int kb = 0; kb < nkb && ok; kb++) {
+                    if (!mbar_wait(&fullB[bs], bp, status, TC_TIMEOUT_FULL)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t b_addr = b_base + bs * OZS_BSTAGE_BYTES;
+                    for (int sa = 0; sa < S; sa++) {
                         if (!mbar_wait(&fullA[as], ap, status, TC_TIMEOUT_FULL)) { ok = false; break; }
                         tc_fence_after();
                         const uint32_t a_addr = a_base + as * OZ_A_BYTES;
-                        for (int tb = 0; tb < S - sa && ok; tb++) {
-                            if (!mbar_wait(&fullB[bs], bp, status, TC_TIMEOUT_FULL)) { ok = false; break; }
-                            tc_fence_after();
-                            const uint32_t b_addr = b_base + bs * OZS_B_BYTES;
-                            const uint32_t d_tmem = tmem_base + (uint32_t)((sa + tb) * OZS_BN);
+                        // A_s against B_0..B_{S-1-s}: columns 32s.. of TMEM, N <= 256 per MMA
+                        const int ntot = OZS_BN * (S - sa);
+                        for (int c0 = 0; c0 < ntot; c0 += 256) {
+                            const int n = min(256, ntot - c0);
+                            const uint32_t idesc = idesc_e4m3_f32(OZ_BM, n);
+                            const uint32_t d_tmem = tmem_base + (uint32_t)(OZS_BN * sa + c0);
 #pragma unroll
                             for (int kk = 0; kk < OZ_BK / 32; kk++)
-                                // the first product into diagonal q = tb (s = 0, kb = 0) starts it
-                                mma_f8f6f4(d_tmem, smem_desc_k128(a_addr + kk * 32), smem_desc_k128(b_addr + kk * 32),
-                                           idesc, (kb == 0 && sa == 0 && kk == 0) ? 0u : 1u);
-                            mma_commit(&emptyB[bs]);
-                            if (++bs == OZS_BST) { bs = 0; bp ^= 1u; }
+                                // the first k block's s = 0 products start every diagonal
+                                mma_f8f6f4(d_tmem, smem_desc_k128(a_addr + kk * 32),
+                                           smem_desc_k128(b_addr + (uint32_t)c0 * OZ_BK + kk * 32), idesc,
+                                           (kb == 0 && sa == 0 && kk == 0) ? 0u : 1u);
                         }
                         mma_commit(&emptyA[as]);
                         if (++as == OZS_AST) { as = 0; ap ^= 1u; }
                     }
+                    if (!ok) break;
+                    mma_commit(&emptyB[bs]);
+                    if (++bs == OZS_BSTG) { bs = 0; bp ^= 1u; }
+                }
+                if (!ok) break;
                 mma_commit(tfull);
                 tp ^= 1u;
             }
         }
     } else {
-        // ---------------- drain (warps 2..9) ----------------
+        // ---------------- drain (warps 2..17) ----------------
         const int quarter = warp & 3;               // TMEM lane window of this warp
-        const int half = (warp - 2) >> 2;           // columns half*16 .. +15 of the tile
+        const int cg = (warp - 2) >> 2;             // columns cg*OZS_DCOLS .. of the tile
         const int row = quarter * 32 + lane;
+        const OzAlpha as = oz_alpha_split(p.alpha);
+        const int g = (S + 1) >> 1;                 // diagonals of the high half
+        const int lsh = 5 * (S - g);                // weight of the high half over the low one
         uint32_t tp = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
             const int tm = t / p.tiles_n, tn = t % p.tiles_n;
             if (!tile_needed(p, tm, tn, OZ_BM, OZS_BN)) continue;
+            // this row's C values and scale exponents, loaded while the MMAs run
+            const int grow = tm * OZ_BM + row;
+            const bool row_ok = grow < p.M;
+            const int gc0 = tn * OZS_BN + cg * OZS_DCOLS;
+            double *cp = p.C + (size_t)gc0 * p.ldc + grow;
+            double cold[OZS_DCOLS];
+            int ecol[OZS_DCOLS];
+#pragma unroll
+            for (int j = 0; j < OZS_DCOLS; j++) {
+                cold[j] = (row_ok && p.beta != 0.0 && oz_c_keep(p, grow, gc0 + j)) ? cp[(size_t)j * p.ldc] : 0.0;
+                ecol[j] = __ldg(p.col_exp + gc0 + j);
+            }
+            const int erow = row_ok ? p.row_exp[grow] - 5 * (S - 1) : 0;
+
             ok = __all_sync(0xffffffffu, mbar_wait(tfull, tp, status, TC_TIMEOUT_TMEM_FULL));
             if (!ok) break;
             tc_fence_after();
             tp ^= 1u;
-            unsigned long long lo[16];
-            long long hi[16];
+            long long vh[OZS_DCOLS], vl[OZS_DCOLS];
 #pragma unroll
-            for (int j = 0; j < 16; j++) { lo[j] = 0ull; hi[j] = 0; }
-            const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(half * 16);
-            for (int q = 0; q < S; q++) {
-                uint32_t r[16];
-                tmem_ld_32x32b_x16(tbase + (uint32_t)(q * OZS_BN), r);
+            for (int j = 0; j < OZS_DCOLS; j++) { vh[j] = 0; vl[j] = 0; }
+            const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cg * OZS_DCOLS);
+            for (int q = 0; q < g; q++) {
+                uint32_t r[OZS_DCOLS];
+                tmem_ld_32x32b_x8(tbase + (uint32_t)(q * OZS_BN), r);
                 tmem_ld_wait();
-                const int sh = 5 * (S - 1 - q);
 #pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    unsigned long long slo;
-                    long long shi;
-                    oz_shift128((long long)__float2int_rn(__uint_as_float(r[j])), sh, slo, shi);
-                    const unsigned long long nl = lo[j] + slo;
-                    hi[j] = hi[j] + shi + (nl < slo ? 1 : 0);
-                    lo[j] = nl;
-                }
+                for (int j = 0; j < OZS_DCOLS; j++)
+                    vh[j] = (long long)(((unsigned long long)vh[j] << 5) +
+                                        (unsigned long long)(long long)oz_f2i22(__uint_as_float(r[j])));
+            }
+            for (int q = g; q < S; q++) {
+                uint32_t r[OZS_DCOLS];
+                tmem_ld_32x32b_x8(tbase + (uint32_t)(q * OZS_BN), r);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < OZS_DCOLS; j++)
+                    vl[j] = (long long)(((unsigned long long)vl[j] << 5) +
+                                        (unsigned long long)(long long)oz_f2i22(__uint_as_float(r[j])));
             }
             tc_fence_before();
             mbar_arrive(tempty);   // TMEM free: the next tile's MMAs may start
-            const int grow = tm * OZ_BM + row;
-            if (grow < p.M) {
-                const int erow = p.row_exp[grow] - 5 * (S - 1);
-                const int gc0 = tn * OZS_BN + half * 16;
-                double *cp = p.C + (size_t)gc0 * p.ldc + grow;
-                double cold[16];
-                if (p.beta != 0.0) {
+            if (row_ok) {
+                double res[OZS_DCOLS];
 #pragma unroll
-                    for (int j = 0; j < 16; j++) cold[j] = oz_c_keep(p, grow, gc0 + j) ? cp[(size_t)j * p.ldc] : 0.0;
-                }
+                for (int j = 0; j < OZS_DCOLS; j++)   // V = vh * 2^lsh + vl
+                    res[j] = oz_result_split(vh[j], vl[j], lsh, erow + ecol[j], p.alpha, as, p.beta, cold[j]);
 #pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    if (!oz_c_keep(p, grow, gc0 + j)) continue;
-                    const double v = oz_to_double(lo[j], hi[j]);
-                    const double sa = oz_alpha_pow2(p.alpha, erow + __ldg(p.col_exp + gc0 + j));
-                    cp[(size_t)j * p.ldc] = p.beta != 0.0 ? fma(sa, v, p.beta * cold[j]) : sa * v;
-                }
+                for (int j = 0; j < OZS_DCOLS; j++)
+                    if (oz_c_keep(p, grow, gc0 + j)) cp[(size_t)j * p.ldc] = res[j];
             }
         }
     }
@@ -1055,6 +1383,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         tc_fence_after();
         tmem_dealloc(tmem_base, 512);
     }
+    oz_report(p);
 }
 
 // ---------------------------------------------------------------------------
@@ -1079,6 +1408,10 @@ constexpr size_t OZ2_SMEM = (size_t)OZ2_STAGES * OZ2_STAGE_BYTES + 1024 + 256;
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(OZ_THREADS, 1)
 oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
 {
+    if (oz_skip_kernel(p)) {
+        oz_report(p);
+        return;
+    }
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + OZ2_STAGES * OZ2_STAGE_BYTES);
@@ -1233,6 +1566,7 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         tc_fence_after();
         tmem_dealloc_pair(tmem_base, 512);
     }
+    oz_report(p);
 }
 
 // complex combine: C = alpha*(Wr + i Wi) + beta*C
@@ -1335,7 +1669,9 @@ struct OzBuffers {
     int *rsa, *csb;   // scale exponents e-4 (rows of op(A), columns of op(B))
     double *ssa, *ssb;
     long long *W;     // nW planes of Mp x Np 128-bit running sums
-    int *status;
+    float *gpart;     // (Mp + Np) / 16 slice-count partials of the one-launch preparation
+    int *status;      // the context's status words
+    int *status_host; // device address of their host mirror
 };
 
 gbx_status oz_buffers(gbx_ctx *ctx, int Mp, int Np, int Kp, int nW, OzBuffers &b)
@@ -1348,17 +1684,21 @@ gbx_status oz_buffers(gbx_ctx *ctx, int Mp, int Np, int Kp, int nW, OzBuffers &b
     b.B8 = (uint8_t *)p;
     if ((st = gbx_ws(ctx, GBX_WS_OZ2, 2 * sizeof(long long) * (size_t)Mp * Np * nW, &p)) != GBX_OK) return st;
     b.W = (long long *)p;
-    const size_t small = 256 + sizeof(int) * (size_t)(Mp + Np) + sizeof(double) * 4 * (size_t)(Mp + Np) + 1024;
+    const size_t small = 256 + sizeof(int) * (size_t)(Mp + Np) + sizeof(double) * 4 * (size_t)(Mp + Np) + 1024 +
+                         3 * sizeof(double) * (size_t)((Mp + Np) / 16 + 2);
     if ((st = gbx_ws(ctx, GBX_WS_OZ3, small, &p)) != GBX_OK) return st;
     uint8_t *q = (uint8_t *)p;
-    b.status = (int *)q; q += 64;
+    if ((st = gbx_ctx_status(ctx, &b.status, &b.status_host)) != GBX_OK) return st;
+    q += 64;
     b.S = (int *)q; q += 64;
     b.ssa = (double *)q; q += sizeof(double) * Mp;
     b.ssb = (double *)q; q += sizeof(double) * Np;
     b.rsa = (int *)q; q += sizeof(double) * Mp;
     b.csb = (int *)q; q += sizeof(double) * Np;
     b.ea = (int *)q; q += sizeof(int) * Mp;
-    b.eb = (int *)q;
+    b.eb = (int *)q; q += sizeof(int) * Np;
+    q = (uint8_t *)(((uintptr_t)q + 15) & ~(uintptr_t)15);
+    b.gpart = (float *)q;
     return GBX_OK;
 }
 
@@ -1435,7 +1775,6 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     else if ((st = oz_buffers(ctx, Mp, Np, Kp, nW, b)) != GBX_OK) return st;
     cudaStream_t s = S_(ctx);
     if (tol <= 0.0) tol = 1e-14;
-    cudaMemsetAsync(b.status, 0, 64, s);
 
     gbx_timer_begin(ctx, GBX_TIMER_OZAKI_SPLIT);
     // op(A): statistics and slices; op(B)^T: its own, or for a symmetric
@@ -1468,6 +1807,8 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         }
         const long long blocks = (long long)Mp / OZ_SPLIT_ROWS + (long long)Np / OZ_SPLIT_ROWS;
         if (blocks > 0x7fffffffLL) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: operands too large");
+        oa.gpart = b.gpart;
+        ob.gpart = b.gpart + 3 * (size_t)(Mp / OZ_SPLIT_ROWS);
         oz_prep_small<<<(unsigned)blocks, 256, 0, s>>>(oa, ob, tol, forced, b.status, (unsigned *)(b.status + 8),
                                                       b.S);
         gbx_count_launch(ctx, 1);
@@ -1494,6 +1835,7 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     p.alpha = pr.alpha; p.beta = pr.beta;
     p.c_part = pr.c_part;
     p.status = b.status;
+    p.status_host = b.status_host;
 
     // kernel attributes (per device) and the resident CTA-pair count; calls
     // arrive from many host threads
@@ -1545,7 +1887,6 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);
     if ((st = gbx_check_launch(ctx, "ozaki gemm")) != GBX_OK) return st;
-    gbx_watch_status(ctx, b.status);
     if (slices_used) {
         int h = 0;
         cudaMemcpyAsync(&h, b.S, sizeof(int), cudaMemcpyDeviceToHost, s);

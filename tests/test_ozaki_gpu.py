@@ -123,6 +123,26 @@ def test_dgemm_ozaki_beta0_nan_and_determinism(orc, dev):
     assert all(np.array_equal(outs[0], o) for o in outs[1:])
 
 
+@pytest.mark.parametrize("k", [128, 2048])        # small-K kernel, wide-tile kernel
+@pytest.mark.parametrize("bad", [np.inf, np.nan])
+def test_nonfinite_operand_is_reported_and_context_recovers(orc, dev, k, bad):
+    # the preparation flags the operand, the product kernel skips, the sync
+    # reports it; the next call on the same context runs normally
+    from libgpublas_gb300._lib import GbxError
+    m, n = 256, 128
+    a, s = orc.matrix(m, k, 3)
+    b, s = orc.matrix(k, n, s)
+    c, s = orc.matrix(m, n, s)
+    a_bad = a.copy()
+    a_bad[5, 7] = bad
+    with pytest.raises(GbxError, match="non-finite"):
+        dev.dgemm_ozaki("N", "N", m, n, k, 1.0, to_dev(a_bad), m, to_dev(b), k, 0.5, to_dev(c), m)
+    C = to_dev(c)
+    dev.dgemm_ozaki("N", "N", m, n, k, 1.0, to_dev(a), m, to_dev(b), k, 0.5, C, m)
+    ref = orc.dgemm_dd("N", "N", m, n, k, 1.0, a, b, 0.5, c)
+    assert rel(from_dev(C, m, n), ref) <= TOL
+
+
 @pytest.mark.parametrize("uplo", ["L", "U"])
 @pytest.mark.parametrize("trans", ["N", "T"])
 def test_dsyrk_ozaki(orc, dev, uplo, trans):
