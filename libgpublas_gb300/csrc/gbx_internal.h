@@ -35,7 +35,7 @@ gbx_status gbx_fail(gbx_ctx *ctx, gbx_status st, const char *fmt, ...);
 #define GBX_WS_BATCH    10  /* grouped/batched descriptors                  */
 #define GBX_WS_STAGE_D  11
 #define GBX_WS_TRSM_X   12  /* dtrsm_ozaki: inverse of the triangle          */
-#define GBX_WS_TRSM_B   13  /* dtrsm_ozaki: copy of the right-hand sides     */
+#define GBX_WS_SPARE13  13  /* unused                                      */
 #define GBX_WS_GEMV     14  /* gemv partial sums                            */
 #define GBX_WS_RED      15  /* reduction partials                           */
 gbx_status gbx_ws(gbx_ctx *ctx, int slot, size_t bytes, void **ptr);
@@ -50,7 +50,8 @@ void gbx_timer_end(gbx_ctx *ctx);
  * mapped host mirror, which such kernels set to the status when it is
  * nonzero as they finish.  gbx_ctx_sync reports a nonzero mirror (5: a
  * non-finite Ozaki operand, GBX_ERR_ARG; else GBX_ERR_TIMEOUT) and clears
- * both. */
+ * both.  Word 0 is the status; words 8 (Ozaki one-launch preparation) and
+ * 12 (DPOTRF step) are last-CTA counters that their kernels reset. */
 gbx_status gbx_ctx_status(gbx_ctx *ctx, int **dev_status, int **host_mirror);
 /* Check cudaGetLastError after a launch, record and map it. */
 gbx_status gbx_check_launch(gbx_ctx *ctx, const char *what);

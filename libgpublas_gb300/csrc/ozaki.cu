@@ -587,6 +587,9 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
 __global__ void __launch_bounds__(256)
 oz_prep_small(OzPrepOp a, OzPrepOp b, double tol, int forced, int *status, unsigned *counter, int *S_dev)
 {
+    // the product kernel may be scheduled now: its set-up needs none of this
+    // launch's results, and it waits for them (griddepcontrol.wait)
+    asm volatile("griddepcontrol.launch_dependents;");
     const int na = a.Rp / OZ_SPLIT_ROWS;
     if ((int)blockIdx.x < na)
         oz_prep_rows(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, a.ss, a.scale, a.X8, a.gpart, blockIdx.x, status);
@@ -1160,11 +1163,14 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 // 128 (N = 256: 128 cycles; diag/utc_probe.cu), so S(S+1)/2 products of
 // N = 32 would leave the tensor pipe three quarters idle; concatenated, a
 // 128-wide k block of a tile is sum_s ceil(32(S - s) / 256) * 4 MMAs (48 for
-// S = 10 instead of 220).  The A slices (16 KB each) stream through a ring;
-// the B stage is double-buffered so the next k block's (or tile's) slices
-// load under the current MMAs.
+// S = 10 instead of 220).  The A slices (16 KB each) stream through a ring
+// of up to eight stages: an A slice whose product has a narrow N is used
+// up in a few hundred cycles, so with K > 128 the ring depth, not the tensor
+// pipe, set the pace at four stages.  The B stage is double-buffered so the
+// next k block's (or tile's) slices load under the current MMAs.
 //
-// The drain prefetches its row's C values while the MMAs run, then decodes each FP32 sum on the FMA and integer pipes (oz_f2i22)
+// The drain prefetches its row's C values and scale exponents while the
+// MMAs run, then decodes each FP32 sum on the FMA and integer pipes (oz_f2i22)
 // and folds diagonals by Horner's rule, V = (...(D_0 * 32 + D_1) * 32 ...) +
 // D_{S-1}, in two signed 64-bit halves (diagonals 0..g-1 and g..S-1, g =
 // ceil(S/2): at most seven each, |half| < 2^22 * 32^6 * 1.04 < 2^53); each
@@ -1176,12 +1182,15 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 // what bounds a CTA with several tiles, so it gets most of the warps).  The
 // accumulators are released before C is written, so the next tile's MMAs
 // overlap that work.
-constexpr int OZS_BN = 32, OZS_AST = 4, OZS_BSTG = 2, OZS_DRAIN_WARPS = 16;
+constexpr int OZS_BN = 32, OZS_AMAX = 8, OZS_BSTG = 2, OZS_DRAIN_WARPS = 16;
 constexpr int OZS_DCOLS = OZS_BN / (OZS_DRAIN_WARPS / 4);   // columns per drain thread
 constexpr int OZS_B_BYTES = OZS_BN * OZ_BK;                 // 4 KB: one slice's 32 rows
-constexpr int OZS_BSTAGE_BYTES = OZ_SMAX * OZS_B_BYTES;     // 56 KB: all slices of one k block
 constexpr int OZS_THREADS = 64 + 32 * OZS_DRAIN_WARPS;
-constexpr size_t OZS_SMEM = (size_t)OZS_AST * OZ_A_BYTES + (size_t)OZS_BSTG * OZS_BSTAGE_BYTES + 1024 + 256;
+// Dynamic shared memory: the two B stages (S x 4 KB each) and as many 16 KB
+// A stages as fit (8 for S <= 10, 6 for S = 14), barriers at the end.
+constexpr size_t OZS_SMEM = 220 * 1024;
+constexpr size_t OZS_DATA = OZS_SMEM - 1024 - 512;   // alignment slack, barriers
+static_assert(OZS_DATA >= 2 * OZ_SMAX * OZS_B_BYTES + 4 * (size_t)OZ_A_BYTES, "small-K stages");
 constexpr int OZS_KMAX = 1024;
 static_assert((long long)OZ_SMAX * OZS_KMAX * 256 < (1LL << 22), "small-K diagonal sums must stay below 2^22");
 static_assert(OZ_SMAX * OZS_BN <= 512, "small-K accumulators must fit TMEM");
@@ -1189,17 +1198,11 @@ static_assert(OZ_SMAX * OZS_BN <= 512, "small-K accumulators must fit TMEM");
 __global__ void __launch_bounds__(OZS_THREADS, 1)
 oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
 {
-    if (oz_skip_kernel(p)) {
-        oz_report(p);
-        return;
-    }
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem;
-    uint8_t *sB = smem + OZS_AST * OZ_A_BYTES;
-    uint64_t *bars = (uint64_t *)(sB + OZS_BSTG * OZS_BSTAGE_BYTES);
-    uint64_t *fullA = bars, *emptyA = fullA + OZS_AST;
-    uint64_t *fullB = emptyA + OZS_AST, *emptyB = fullB + OZS_BSTG;
+    uint64_t *bars = (uint64_t *)(smem + OZS_DATA);
+    uint64_t *fullA = bars, *emptyA = fullA + OZS_AMAX;
+    uint64_t *fullB = emptyA + OZS_AMAX, *emptyB = fullB + OZS_BSTG;
     uint64_t *tfull = emptyB + OZS_BSTG, *tempty = tfull + 1;
     uint32_t *tmem_slot = (uint32_t *)(tempty + 1);
 
@@ -1207,7 +1210,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     volatile int *status = p.status;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < OZS_AST; i++) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], 1); }
+        for (int i = 0; i < OZS_AMAX; i++) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], 1); }
         for (int i = 0; i < OZS_BSTG; i++) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], 1); }
         mbar_init(tfull, 1);
         mbar_init(tempty, 32 * OZS_DRAIN_WARPS);
@@ -1224,8 +1227,26 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
 
+    // Launched as a programmatic dependent of the preparation: the set-up
+    // above overlaps its tail; its slices, scales and S are complete and
+    // visible after this wait (a no-op for an ordinary launch).
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (oz_skip_kernel(p)) {
+        if (warp == 1) {
+            tc_fence_after();
+            tmem_dealloc(tmem_base, 512);
+        }
+        oz_report(p);
+        return;
+    }
+
     const int S = *p.S;
     const int nkb = p.Kp / OZ_BK;
+    // B stages first (S slices of 4 KB each), then the A ring
+    const int bstage = S * OZS_B_BYTES;
+    uint8_t *sB = smem;
+    uint8_t *sA = smem + OZS_BSTG * bstage;
+    const int nA = min(OZS_AMAX, (int)((OZS_DATA - (size_t)OZS_BSTG * bstage) / OZ_A_BYTES));
     const int ntiles = p.tiles_m * p.tiles_n;
 
     if (warp == 0) {
@@ -1242,7 +1263,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     if (!mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
                     mbar_arrive_expect_tx(&fullB[bs], (uint32_t)(S * OZS_B_BYTES));
                     for (int tb = 0; tb < S; tb++)
-                        tma_load_2d(sB + bs * OZS_BSTAGE_BYTES + tb * OZS_B_BYTES, &tmB, &fullB[bs], kb * OZ_BK,
+                        tma_load_2d(sB + bs * bstage + tb * OZS_B_BYTES, &tmB, &fullB[bs], kb * OZ_BK,
                                     tb * p.Np + tn * OZS_BN);
                     if (++bs == OZS_BSTG) { bs = 0; bp ^= 1u; }
                     // then the A slices
@@ -1250,14 +1271,14 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                         if (!mbar_wait(&emptyA[as], ap ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
                         mbar_arrive_expect_tx(&fullA[as], OZ_A_BYTES);
                         tma_load_2d(sA + as * OZ_A_BYTES, &tmA, &fullA[as], kb * OZ_BK, sa * p.Mp + tm * OZ_BM);
-                        if (++as == OZS_AST) { as = 0; ap ^= 1u; }
+                        if (++as == nA) { as = 0; ap ^= 1u; }
                     }
                 }
             }
             // wait (bounded) until every issued load has been consumed
-            for (int i = 0; i < OZS_AST; i++) {
+            for (int i = 0; i < nA; i++) {
                 mbar_wait(&emptyA[as], ap ^ 1u, status, TC_TIMEOUT_EMPTY);
-                if (++as == OZS_AST) { as = 0; ap ^= 1u; }
+                if (++as == nA) { as = 0; ap ^= 1u; }
             }
             for (int i = 0; i < OZS_BSTG; i++) {
                 mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY);
@@ -1280,7 +1301,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 for (int kb = 0; kb < nkb && ok; kb++) {
                     if (!mbar_wait(&fullB[bs], bp, status, TC_TIMEOUT_FULL)) { ok = false; break; }
                     tc_fence_after();
-                    const uint32_t b_addr = b_base + bs * OZS_BSTAGE_BYTES;
+                    const uint32_t b_addr = b_base + bs * bstage;
                     for (int sa = 0; sa < S; sa++) {
                         if (!mbar_wait(&fullA[as], ap, status, TC_TIMEOUT_FULL)) { ok = false; break; }
                         tc_fence_after();
@@ -1299,7 +1320,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                                            (kb == 0 && sa == 0 && kk == 0) ? 0u : 1u);
                         }
                         mma_commit(&emptyA[as]);
-                        if (++as == OZS_AST) { as = 0; ap ^= 1u; }
+                        if (++as == nA) { as = 0; ap ^= 1u; }
                     }
                     if (!ok) break;
                     mma_commit(&emptyB[bs]);
@@ -1877,9 +1898,24 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         oz_gemm2_kernel<<<2 * npairs, OZ_THREADS, OZ2_SMEM, s>>>(tmA, tmB, p);
     } else {
         const int grid = std::min(ntiles, gbx_ctx_sms(ctx));
-        if (small_k)
-            oz_gemm_sk_kernel<<<grid, OZS_THREADS, OZS_SMEM, s>>>(tmA, tmB, p);
-        else if (bn == 128)
+        if (small_k) {
+            // a programmatic dependent of the one-launch preparation before it
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)grid);
+            cfg.blockDim = dim3(OZS_THREADS);
+            cfg.dynamicSmemBytes = OZS_SMEM;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            const cudaError_t le = cudaLaunchKernelEx(&cfg, oz_gemm_sk_kernel, tmA, tmB, p);
+            if (le != cudaSuccess) {
+                cudaGetLastError();
+                return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki gemm: %s", cudaGetErrorString(le));
+            }
+        } else if (bn == 128)
             oz_gemm_kernel<128><<<grid, OzCfg<128>::THREADS, OzCfg<128>::SMEM, s>>>(tmA, tmB, p);
         else
             oz_gemm_kernel<256><<<grid, OzCfg<256>::THREADS, OzCfg<256>::SMEM, s>>>(tmA, tmB, p);
@@ -1980,10 +2016,9 @@ extern "C" gbx_status gbx_dtrsm_ozaki(gbx_ctx *ctx, char side, char uplo, char t
     const int na = lside ? m : n;
     if (alpha == 0.0 || na > 1024) return gbx_dtrsm(ctx, side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb);
     gbx_status st;
-    void *px, *pb;
+    void *px;
     if ((st = gbx_ws(ctx, GBX_WS_TRSM_X, sizeof(double) * (size_t)na * na, &px)) != GBX_OK) return st;
-    if ((st = gbx_ws(ctx, GBX_WS_TRSM_B, sizeof(double) * (size_t)m * n, &pb)) != GBX_OK) return st;
-    double *X = (double *)px, *Bc = (double *)pb;
+    double *X = (double *)px;
     cudaStream_t s = S_(ctx);
     const long long total = (long long)na * na;
     oz_set_identity<<<(int)std::min<long long>((total + 255) / 256, (long long)gbx_ctx_sms(ctx) * 4), 256, 0, s>>>(
@@ -1991,12 +2026,12 @@ extern "C" gbx_status gbx_dtrsm_ozaki(gbx_ctx *ctx, char side, char uplo, char t
     gbx_count_launch(ctx, 1);
     if ((st = gbx_check_launch(ctx, "dtrsm_ozaki identity")) != GBX_OK) return st;
     if ((st = gbx_dtrsm(ctx, 'L', uplo, ta, diag, na, na, 1.0, A, lda, X, na)) != GBX_OK) return st;
-    cudaError_t e = cudaMemcpy2DAsync(Bc, sizeof(double) * (size_t)m, B, sizeof(double) * (size_t)ldb,
-                                      sizeof(double) * (size_t)m, n, cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return gbx_fail(ctx, GBX_ERR_CUDA, "dtrsm_ozaki copy: %s", cudaGetErrorString(e));
+    // B is both an operand and the result: the Ozaki product reads its FP64
+    // operands only in the preparation launches, which complete before the
+    // product kernel writes C, and with beta = 0 it never reads C.
     if (lside)
-        return gbx_dgemm_ozaki(ctx, 'N', 'N', m, n, m, alpha, X, na, Bc, m, 0.0, B, ldb, tol, slices, slices_used);
-    return gbx_dgemm_ozaki(ctx, 'N', 'N', m, n, n, alpha, Bc, m, X, na, 0.0, B, ldb, tol, slices, slices_used);
+        return gbx_dgemm_ozaki(ctx, 'N', 'N', m, n, m, alpha, X, na, B, ldb, 0.0, B, ldb, tol, slices, slices_used);
+    return gbx_dgemm_ozaki(ctx, 'N', 'N', m, n, n, alpha, B, ldb, X, na, 0.0, B, ldb, tol, slices, slices_used);
 }
 
 // ZGEMM: Re = [Ar | Ai] x [Br ; -Bi],  Im = [Ar | Ai] x [Bi ; Br]  (K' = 2K),

@@ -16,6 +16,8 @@
 // Routing depends only on the operation (small GEMM: m, n <= 512 and
 // k <= 4096; small TRSM: order <= 256; everything else runs alone), so a
 // result is bit-identical whether the call was served alone or in a mix.
+// Critical-path requests (DPOTRF of a diagonal block, DTRSM of a panel) run
+// on a high-priority stream of their slot.
 //
 // Admission by memory: callers that stage host operands reserve their bytes
 // with gbx_server_admit (blocks while the reserved total would exceed the
@@ -50,6 +52,7 @@ struct Request {
 
 struct Slot {
     gbx_ctx *ctx = nullptr;
+    cudaStream_t hi = nullptr;   // high-priority stream for critical-path requests
     bool busy = false;   // taken by its worker or by a calling thread (under the server mutex)
 };
 
@@ -110,6 +113,28 @@ gbx_status run_request(gbx_ctx *ctx, const gbx_op &o)
     default:
         return GBX_ERR_ARG;
     }
+}
+
+// The sequential steps of blocked factorizations (the diagonal-block
+// Cholesky and the panel solves) gate every later call of their chain, while
+// the trailing updates they release are many and independent: they run on
+// the slot's high-priority stream, so their CTAs are scheduled ahead of
+// queued trailing-update CTAs as SMs free up.
+bool is_critical(const gbx_op &o)
+{
+    return o.kind == GBX_OP_POTRF || o.kind == GBX_OP_TRSM || o.kind == GBX_OP_TRSM_OZAKI;
+}
+
+// One request on a slot, synchronised (the slot's stream, or its
+// high-priority stream for a critical-path request).
+gbx_status run_on_slot(Slot *sl, const gbx_op &o)
+{
+    const bool hi = sl->hi && is_critical(o);
+    if (hi) gbx_ctx_set_stream(sl->ctx, sl->hi);
+    gbx_status st = run_request(sl->ctx, o);
+    const gbx_status sync = gbx_ctx_sync(sl->ctx);   // also collects bounded-wait status words
+    if (hi) gbx_ctx_set_stream(sl->ctx, nullptr);
+    return st == GBX_OK ? sync : st;
 }
 
 }  // namespace
@@ -182,11 +207,11 @@ void worker_loop(gbx_server *s, Slot *sl)
             ops.reserve(mine.size());
             for (auto *r : mine) ops.push_back(r->op);
             st = gbx_grouped_launch_inline(sl->ctx, ops.data(), (int)ops.size());
+            const gbx_status sync = gbx_ctx_sync(sl->ctx);   // also collects bounded-wait status words
+            if (st == GBX_OK) st = sync;
         } else {
-            st = run_request(sl->ctx, mine[0]->op);
+            st = run_on_slot(sl, mine[0]->op);
         }
-        const gbx_status sync = gbx_ctx_sync(sl->ctx);   // also collects bounded-wait status words
-        if (st == GBX_OK) st = sync;
         lk.lock();
         sl->busy = false;
         s->batches++;
@@ -207,10 +232,16 @@ extern "C" gbx_status gbx_server_create(int device, int nslots, size_t mem_budge
     gbx_server *s = new gbx_server();
     s->device = device;
     s->slots.resize(nslots);
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
     for (auto &sl : s->slots) {
-        if (gbx_ctx_create(&sl.ctx, device) != GBX_OK) {
-            for (auto &q : s->slots)
+        if (gbx_ctx_create(&sl.ctx, device) != GBX_OK ||
+            cudaStreamCreateWithPriority(&sl.hi, cudaStreamNonBlocking, prio_high) != cudaSuccess) {
+            cudaGetLastError();
+            for (auto &q : s->slots) {
                 if (q.ctx) gbx_ctx_destroy(q.ctx);
+                if (q.hi) cudaStreamDestroy(q.hi);
+            }
             delete s;
             return GBX_ERR_CUDA;
         }
@@ -291,9 +322,7 @@ extern "C" gbx_status gbx_server_call(gbx_server *s, const gbx_op *op, double *l
         }
         if (sl) {
             cudaSetDevice(s->device);
-            gbx_status st = run_request(sl->ctx, *op);
-            const gbx_status sync = gbx_ctx_sync(sl->ctx);
-            if (st == GBX_OK) st = sync;
+            const gbx_status st = run_on_slot(sl, *op);
             const auto t1 = clk::now();
             {
                 std::lock_guard<std::mutex> lk(s->mu);
@@ -382,8 +411,10 @@ extern "C" gbx_status gbx_server_destroy(gbx_server *s)
     for (auto &w : s->workers)
         if (w.joinable()) w.join();
     for (auto *r : s->finished) delete r;
-    for (auto &sl : s->slots)
+    for (auto &sl : s->slots) {
         if (sl.ctx) gbx_ctx_destroy(sl.ctx);
+        if (sl.hi) cudaStreamDestroy(sl.hi);
+    }
     delete s;
     return GBX_OK;
 }
