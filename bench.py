@@ -731,7 +731,6 @@ def cholesky_calls(n, nb, base, lda, info_ptr, ozaki=False):
 
 
 def run_serving(args):
-    import threading
     import torch
     import libgpublas_gb300 as g
     from libgpublas_gb300 import build
@@ -758,53 +757,18 @@ def run_serving(args):
     results = {}
 
     def run_mode(mode):
+        # the 16 caller threads are native (gbx_diag_cholesky_trace): C++
+        # threads calling the library as a C or Fortran application would,
+        # without interpreter time or lock contention on every call
         server = g.Server(0, slots=nthreads) if mode != "plain" else None
         work = [o.clone() for o in origs]
         torch.cuda.synchronize()
-        lat, ncalls, errs = [], [0], []
-        by_kind, thread_s = {}, [0.0] * nthreads
-        lock = threading.Lock()
-        t_start = [0.0]
-
-        def worker(t):
-            A = work[t]
-            calls = cholesky_calls(sizes[t], nbs[t], A.data_ptr(), sizes[t], info.data_ptr() + 4 * t,
-                                   ozaki=(mode == "ozaki"))
-            local = []
-            if server is None:
-                d = g.Device(0)
-                for op in calls:
-                    t0 = time.perf_counter()
-                    st = d.L.gbx_ops_run(d.ctx, ctypes_ref(op), 1)
-                    st2 = d.L.gbx_ctx_sync(d.ctx)
-                    local.append((op.kind, (time.perf_counter() - t0) * 1e6))
-                    if st or st2:
-                        errs.append((t, st, st2))
-                        break
-                d.close()
-            else:
-                for op in calls:
-                    st, us = server.call(op)
-                    local.append((op.kind, us))
-                    if st:
-                        errs.append((t, st))
-                        break
-            with lock:
-                lat.extend(us for _, us in local)
-                ncalls[0] += len(local)
-                for kind, us in local:
-                    e = by_kind.setdefault(kind, [0, 0.0])
-                    e[0] += 1
-                    e[1] += us
-                thread_s[t] = time.perf_counter() - t_start[0]
-
-        threads = [threading.Thread(target=worker, args=(t,)) for t in range(nthreads)]
-        t0 = t_start[0] = time.perf_counter()
-        for th in threads:
-            th.start()
-        for th in threads:
-            th.join()
-        wall = time.perf_counter() - t0
+        r = g.cholesky_trace(server, 0, sizes, nbs, [w.data_ptr() for w in work], info.data_ptr(),
+                             mode == "ozaki")
+        wall = r["wall_s"]
+        errs = [r["first_error"]] if r["first_error"] else []
+        by_kind = {k: (c, r["kind_sum_us"][k]) for k, c in enumerate(r["kind_calls"]) if c}
+        thread_s = r["thread_finish_s"]
         srv_stats = server.stats() if server else None
         if server:
             server.close()
@@ -824,11 +788,9 @@ def run_serving(args):
                 res_num += (out.item() - aij) ** 2
                 res_den += aij ** 2
         d.close()
-        lat.sort()
         flops = sum(float(n) ** 3 / 3 for n in sizes)
-        results[mode] = {"calls": ncalls[0], "wall_s": wall, "calls_per_s": ncalls[0] / wall,
-                         "p50_us": lat[len(lat) // 2] if lat else None,
-                         "p99_us": lat[int(0.99 * (len(lat) - 1))] if lat else None,
+        results[mode] = {"calls": r["calls"], "wall_s": wall, "calls_per_s": r["calls"] / wall,
+                         "p50_us": r["p50_us"], "p99_us": r["p99_us"],
                          "tflops": flops / wall / 1e12,
                          "residual_sampled": (res_num / res_den) ** 0.5 if res_den else None,
                          "info_nonzero": int((info != 0).sum().item()), "errors": errs[:4],
@@ -854,6 +816,7 @@ def run_serving(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "cholesky_trace_16threads", "n": sizes, "nb": nbs,
                        "matrix": "A = G G^T + n I, G uniform[-1,1] (device generator, seed 5)",
+                       "driver": "16 native host threads (gbx_diag_cholesky_trace), one call at a time each",
                        "calls": "dpotrf(diag) dtrsm dsyrk dgemm + ddot residual checks",
                        "headline_mode": "ozaki: serving loop, dgemm/dsyrk/dtrsm through the Ozaki path "
                                         "(tolerance 1e-14, FP64 results), dpotrf in FP64"},

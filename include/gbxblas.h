@@ -336,6 +336,29 @@ gbx_status gbx_server_stats(gbx_server *srv, uint64_t *completed, uint64_t *batc
 gbx_status gbx_server_reset_stats(gbx_server *srv);
 gbx_status gbx_server_destroy(gbx_server *srv);
 
+/* Native driver of the serving workload (diagnostic; no reference
+ * counterpart): nthreads host threads, thread t running the calls of a
+ * blocked right-looking Cholesky of the n[t] x n[t] matrix A[t] (leading
+ * dimension lda[t], block nb[t] <= 256, lower triangle, info[t] its INFO)
+ * through server (or plain per-call dispatch on one context per thread when
+ * server is NULL); ozaki selects the Ozaki forms of dtrsm/dsyrk/dgemm.  The
+ * threads start together; per-call latency is taken on the calling thread.
+ * Op kinds index kind_calls / kind_sum_us. */
+#define GBX_TRACE_MAX_THREADS 64
+#define GBX_TRACE_KINDS 16
+typedef struct {
+    uint64_t calls;
+    double wall_s;
+    double p50_us, p99_us;
+    uint64_t kind_calls[GBX_TRACE_KINDS];
+    double kind_sum_us[GBX_TRACE_KINDS];
+    double thread_finish_s[GBX_TRACE_MAX_THREADS];
+    int first_error;   /* status of the first failed call (0: none) */
+} gbx_trace_stats;
+gbx_status gbx_diag_cholesky_trace(gbx_server *server, int device, int nthreads, const int *n, const int *nb,
+                                   double *const *A, const int *lda, int *info, int ozaki,
+                                   gbx_trace_stats *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,4 +7,4 @@ Python package only builds it (``build.build_library``) and binds it with
 ctypes (``_lib``) for tests and benchmarks.
 """
 from ._lib import (F77, OP_DOT, OP_GEMM, OP_NRM2, OP_SYRK, OP_TRSM, Device, GbxError, GbxOp,  # noqa: F401
-                   LIB_PATH, Server, declared_symbols, load, stats)
+                   LIB_PATH, Server, cholesky_trace, declared_symbols, load, stats)

@@ -146,6 +146,8 @@ def _declare(L):
     L.gbx_ctx_enable_timing.argtypes = [_P, _I]
     L.gbx_ctx_kernel_time.argtypes = [_P, _I, C.POINTER(_D), C.POINTER(C.c_uint64)]
     L.gbx_diag_fp64_peak.argtypes = [_P, C.POINTER(_D)]
+    L.gbx_diag_cholesky_trace.argtypes = [_P, _I, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_P),
+                                          C.POINTER(_I), _P, _I, C.POINTER(TraceStats)]
 
 
 class GbxOp(C.Structure):
@@ -159,6 +161,38 @@ class GbxOp(C.Structure):
 
 
 OP_GEMM, OP_TRSM, OP_SYRK, OP_DOT, OP_NRM2 = 1, 2, 3, 4, 5
+
+TRACE_MAX_THREADS, TRACE_KINDS = 64, 16
+
+
+class TraceStats(C.Structure):
+    """gbx_trace_stats of include/gbxblas.h."""
+    _fields_ = [("calls", C.c_uint64), ("wall_s", C.c_double), ("p50_us", C.c_double),
+                ("p99_us", C.c_double), ("kind_calls", C.c_uint64 * TRACE_KINDS),
+                ("kind_sum_us", C.c_double * TRACE_KINDS),
+                ("thread_finish_s", C.c_double * TRACE_MAX_THREADS), ("first_error", C.c_int)]
+
+
+def cholesky_trace(server, device, n, nb, mats, info_ptr, ozaki):
+    """Runs the native Cholesky-trace driver (gbx_diag_cholesky_trace):
+    len(n) host threads, thread t factorising the device matrix whose address
+    is mats[t] (n[t] x n[t], leading dimension n[t], block nb[t]); server is
+    a Server or None (plain per-call dispatch).  Returns gbx_trace_stats as a
+    dict."""
+    L = load()
+    k = len(n)
+    ni = (_I * k)(*n)
+    nbi = (_I * k)(*nb)
+    ai = (_P * k)(*mats)
+    ld = (_I * k)(*n)
+    out = TraceStats()
+    st = L.gbx_diag_cholesky_trace(server.h if server else None, device, k, ni, nbi, ai, ld, info_ptr,
+                                   1 if ozaki else 0, C.byref(out))
+    if st != 0:
+        raise GbxError(f"gbx_diag_cholesky_trace failed with status {st}")
+    return {"calls": out.calls, "wall_s": out.wall_s, "p50_us": out.p50_us, "p99_us": out.p99_us,
+            "kind_calls": list(out.kind_calls), "kind_sum_us": list(out.kind_sum_us),
+            "thread_finish_s": list(out.thread_finish_s)[:k], "first_error": out.first_error}
 
 
 class Server:

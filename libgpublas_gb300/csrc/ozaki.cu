@@ -36,6 +36,8 @@
 #include <math.h>
 #include <stdint.h>
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 using namespace gbx_tc;
@@ -506,14 +508,15 @@ oz_prep_split(OzPrepOp a, OzPrepOp b, const int *__restrict__ S_dev)
 // ---- small K: the whole preparation in one launch ---------------------------
 // Each CTA owns 16 complete rows of one operand: a first pass over their K
 // extent gives the row statistics (maximum and sum of squares), a second
-// writes all OZ_SMAX digit planes (the slice count is not known yet; the
-// leading S planes of the OZ_SMAX-digit balanced expansion represent the
-// row to within 16.5 * 2^(-5S) of its maximum, the same bound as rounding
-// at S digits).  The last CTA to finish chooses S from the statistics of
-// both operands.  One launch instead of three: small products are
-// dominated by per-launch cost.
+// writes P digit planes, P the largest slice count the tolerance can call
+// for (the slice count itself is not known yet; the leading S planes of the
+// P-digit balanced expansion represent the row to within 16.5 * 2^(-5S) of
+// its maximum, the same bound as rounding at S digits); every CTA leaves a partial of the slice-count statistic,
+// from which the product kernel chooses S.  One launch instead of three:
+// small products are dominated by per-launch cost.
 __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, int Rp, int Kp, int *expo, double *ss,
-                                             int *scale, uint8_t *X8, float *gpart, int rblk, int *status)
+                                             int *scale, uint8_t *X8, float *gpart, int planes, int rblk,
+                                             int *status)
 {
     __shared__ double tile[OZ_SPLIT_ROWS][129];
     const int r0 = rblk * OZ_SPLIT_ROWS;
@@ -579,38 +582,23 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
     }
     const int kblocks = Kp / 128;
     if (kblocks == 1)   // the statistics pass left this block's only tile in shared memory
-        oz_split_tile(v, rows, K, Rp, Kp, expo, OZ_SMAX, X8, rblk, tile);
+        oz_split_tile(v, rows, K, Rp, Kp, expo, planes, X8, rblk, tile);
     else
-        for (int kb = 0; kb < kblocks; kb++) oz_split_tile(v, rows, K, Rp, Kp, expo, OZ_SMAX, X8, rblk * kblocks + kb);
+        for (int kb = 0; kb < kblocks; kb++) oz_split_tile(v, rows, K, Rp, Kp, expo, planes, X8, rblk * kblocks + kb);
 }
 
 __global__ void __launch_bounds__(256)
-oz_prep_small(OzPrepOp a, OzPrepOp b, double tol, int forced, int *status, unsigned *counter, int *S_dev)
+oz_prep_small(OzPrepOp a, OzPrepOp b, int planes, int *status)
 {
     // the product kernel may be scheduled now: its set-up needs none of this
     // launch's results, and it waits for them (griddepcontrol.wait)
     asm volatile("griddepcontrol.launch_dependents;");
     const int na = a.Rp / OZ_SPLIT_ROWS;
     if ((int)blockIdx.x < na)
-        oz_prep_rows(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, a.ss, a.scale, a.X8, a.gpart, blockIdx.x, status);
+        oz_prep_rows(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, a.ss, a.scale, a.X8, a.gpart, planes, blockIdx.x, status);
     else
-        oz_prep_rows(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, b.ss, b.scale, b.X8, b.gpart, blockIdx.x - na, status);
-    __threadfence();
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    const float ga = oz_log2_gamma_parts(a.gpart, a.Rp / OZ_SPLIT_ROWS, a.K);
-    const float gb = oz_log2_gamma_parts(b.gpart, b.Rp / OZ_SPLIT_ROWS, b.K);
-    if (threadIdx.x == 0) {
-        int S;
-        if (forced > 0) S = forced;
-        else S = (int)ceilf((-__log2f((float)tol) + ga + gb + 1.5f) / 5.0f);
-        S_dev[0] = max(1, min(OZ_SMAX, S));
-        *counter = 0u;
-    }
+        oz_prep_rows(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, b.ss, b.scale, b.X8, b.gpart, planes, blockIdx.x - na,
+                     status);
 }
 
 // ---------------------------------------------------------------------------
@@ -619,7 +607,7 @@ oz_prep_small(OzPrepOp a, OzPrepOp b, double tol, int forced, int *status, unsig
 struct OzParams {
     int M, N, Mp, Np, Kp;
     int tiles_m, tiles_n;
-    const int *S;
+    int *S;                    // slice count (written by the small-K kernel, read by the others)
     const int *row_exp;        // Mp: e_i - 4
     const int *col_exp;        // Np: f_j - 4
     long long *W;              // Mp x Np running sums, two words per element, column-major
@@ -629,7 +617,76 @@ struct OzParams {
     int c_part;                // 0 full, 1 lower (row >= col), 2 upper
     int *status;               // the context's status word (zero while nothing failed)
     int *status_host;          // its mapped host mirror
+    // small-K kernel: the slice count is chosen in the kernel from the
+    // preparation's per-block partials (and written to *S by CTA 0)
+    const float *gpa, *gpb;    // partials of op(A) and op(B)^T
+    int npa, npb;              // their counts
+    int K;
+    float tol_bits;            // -log2(tol)
+    int forced;                // fixed slice count, or 0
+    int smax;                  // digit planes prepared (upper bound of S)
 };
+
+// The small-K product kernel's slice count, computed by every CTA from the
+// preparation's per-block partials of both operands (the same data in the
+// same order in every CTA: one S per call) with the model oz_prep_finish
+// applies, clamped to the planes the preparation wrote; CTA 0 records it.
+__device__ int oz_choose_S(const OzParams &p)
+{
+    __shared__ int s_e[2][32];
+    __shared__ float s_v[4][32];
+    __shared__ int s_S;
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (p.forced > 0) {
+        const int S = min(p.forced, p.smax);
+        if (blockIdx.x == 0 && threadIdx.x == 0) *p.S = S;
+        return S;
+    }
+    int ea = -100000, eb = -100000;
+    for (int i = threadIdx.x; i < p.npa; i += blockDim.x) ea = max(ea, (int)__ldcg(p.gpa + 3 * i));
+    for (int i = threadIdx.x; i < p.npb; i += blockDim.x) eb = max(eb, (int)__ldcg(p.gpb + 3 * i));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        ea = max(ea, __shfl_xor_sync(0xffffffffu, ea, o));
+        eb = max(eb, __shfl_xor_sync(0xffffffffu, eb, o));
+    }
+    if (lane == 0) { s_e[0][warp] = ea; s_e[1][warp] = eb; }
+    __syncthreads();
+    for (int w = 0; w < nw; w++) { ea = max(ea, s_e[0][w]); eb = max(eb, s_e[1][w]); }
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int i = threadIdx.x; i < p.npa; i += blockDim.x) {
+        const int d = 2 * ((int)__ldcg(p.gpa + 3 * i) - ea);
+        const float w = d < -126 ? 0.f : __int_as_float((127 + d) << 23);
+        v[0] = fmaf(w, __ldcg(p.gpa + 3 * i + 1), v[0]);
+        v[1] = fmaf(w, __ldcg(p.gpa + 3 * i + 2), v[1]);
+    }
+    for (int i = threadIdx.x; i < p.npb; i += blockDim.x) {
+        const int d = 2 * ((int)__ldcg(p.gpb + 3 * i) - eb);
+        const float w = d < -126 ? 0.f : __int_as_float((127 + d) << 23);
+        v[2] = fmaf(w, __ldcg(p.gpb + 3 * i + 1), v[2]);
+        v[3] = fmaf(w, __ldcg(p.gpb + 3 * i + 2), v[3]);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], o);
+        if (lane == 0) s_v[j][warp] = v[j];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int w = 0; w < nw; w++)
+            for (int j = 0; j < 4; j++) t[j] += s_v[j][w];
+        const float ga = t[1] > 0.f ? 0.5f * __log2f(t[0] * (float)p.K / t[1]) : 0.f;
+        const float gb = t[3] > 0.f ? 0.5f * __log2f(t[2] * (float)p.K / t[3]) : 0.f;
+        int S = (int)ceilf((p.tol_bits + ga + gb + 1.5f) / 5.0f);
+        S = max(1, min(p.smax, S));
+        s_S = S;
+        if (blockIdx.x == 0) *p.S = S;
+    }
+    __syncthreads();
+    return s_S;
+}
 
 // A call whose operands were found non-finite (or whose earlier kernel gave
 // up a wait) skips the product kernel: every thread of the CTA takes the
@@ -818,6 +875,17 @@ __device__ __forceinline__ OzAlpha oz_alpha_split(double alpha)
     a.ea = ex - 1023;
     a.sign = b & 0x8000000000000000ull;
     return a;
+}
+
+// One Horner step v = 32 v + D for each of the OZS_DCOLS-wide row segment
+// (D: FP32 accumulator values below 2^22, decoded off the FP64 pipe).
+template <int N>
+__device__ __forceinline__ void oz_horner(long long (&v)[N], const uint32_t (&r)[N])
+{
+#pragma unroll
+    for (int j = 0; j < N; j++)
+        v[j] = (long long)(((unsigned long long)v[j] << 5) +
+                           (unsigned long long)(long long)oz_f2i22(__uint_as_float(r[j])));
 }
 
 // v * 2^e as a double for |v| < 2^53 (exact), built on the integer pipe;
@@ -1240,7 +1308,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         return;
     }
 
-    const int S = *p.S;
+    const int S = oz_choose_S(p);
     const int nkb = p.Kp / OZ_BK;
     // B stages first (S slices of 4 KB each), then the A ring
     const int bstage = S * OZS_B_BYTES;
@@ -1366,23 +1434,16 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
             for (int j = 0; j < OZS_DCOLS; j++) { vh[j] = 0; vl[j] = 0; }
             const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cg * OZS_DCOLS);
-            for (int q = 0; q < g; q++) {
-                uint32_t r[OZS_DCOLS];
-                tmem_ld_32x32b_x8(tbase + (uint32_t)(q * OZS_BN), r);
+            // two diagonals per TMEM round trip; q < g folds into the high half
+            for (int q = 0; q < S; q += 2) {
+                uint32_t r0[OZS_DCOLS], r1[OZS_DCOLS];
+                tmem_ld_32x32b_x8(tbase + (uint32_t)(q * OZS_BN), r0);
+                if (q + 1 < S) tmem_ld_32x32b_x8(tbase + (uint32_t)((q + 1) * OZS_BN), r1);
                 tmem_ld_wait();
-#pragma unroll
-                for (int j = 0; j < OZS_DCOLS; j++)
-                    vh[j] = (long long)(((unsigned long long)vh[j] << 5) +
-                                        (unsigned long long)(long long)oz_f2i22(__uint_as_float(r[j])));
-            }
-            for (int q = g; q < S; q++) {
-                uint32_t r[OZS_DCOLS];
-                tmem_ld_32x32b_x8(tbase + (uint32_t)(q * OZS_BN), r);
-                tmem_ld_wait();
-#pragma unroll
-                for (int j = 0; j < OZS_DCOLS; j++)
-                    vl[j] = (long long)(((unsigned long long)vl[j] << 5) +
-                                        (unsigned long long)(long long)oz_f2i22(__uint_as_float(r[j])));
+                if (q < g) oz_horner(vh, r0);
+                else oz_horner(vl, r0);
+                if (q + 1 < g) oz_horner(vh, r1);
+                else if (q + 1 < S) oz_horner(vl, r1);
             }
             tc_fence_before();
             mbar_arrive(tempty);   // TMEM free: the next tile's MMAs may start
@@ -1634,7 +1695,7 @@ EncodeTiledFn get_encode()
 }
 
 // 2-D byte tensor [rows][Kp] with a (box_rows x 128-byte) box, 128B swizzle.
-bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int box_rows)
+bool make_map_uncached(CUtensorMap *map, void *base, long long rows, long long Kp, int box_rows)
 {
     EncodeTiledFn enc = get_encode();
     if (!enc) return false;
@@ -1645,6 +1706,36 @@ bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int bo
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The digit planes live in workspace slots that persist across calls, so a
+// calling thread sees the same few (base, rows, K, box) over and over: the
+// encoded maps are kept per thread (8 entries, round robin) instead of
+// re-encoding two per call on the host.
+bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int box_rows)
+{
+    struct Entry {
+        void *base;
+        long long rows, Kp;
+        int box;
+        CUtensorMap map;
+    };
+    thread_local Entry cache[8] = {};
+    thread_local int next = 0;
+    for (auto &e : cache)
+        if (e.base == base && e.rows == rows && e.Kp == Kp && e.box == box_rows) {
+            *map = e.map;
+            return true;
+        }
+    if (!make_map_uncached(map, base, rows, Kp, box_rows)) return false;
+    Entry &e = cache[next];
+    next = (next + 1) & 7;
+    e.base = base;
+    e.rows = rows;
+    e.Kp = Kp;
+    e.box = box_rows;
+    e.map = *map;
+    return true;
 }
 
 // The CTA-pair kernel is selected with GBX_OZAKI_PAIR=1 for problems with
@@ -1790,12 +1881,18 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     const int bn = small_k ? OZS_BN : oz_tile_n(pr.M, pr.N, gbx_ctx_sms(ctx), pair);
     const int Mp = (int)rup(pr.M, pair ? OZ2_BM : OZ_BM), Np = (int)rup(pr.N, bn);
     const int Kp = (int)rup(std::max(pr.K, 1), OZ_BK);
+    if (tol <= 0.0) tol = 1e-14;
+    // small K: the digit planes to prepare, the largest S the tolerance can
+    // call for (gamma <= 2 sqrt(K) per operand in the slice-count model)
+    const int planes = forced > 0 ? forced
+                                  : std::max(1, std::min(OZ_SMAX, (int)ceil((-log2(tol) + 2.0 +
+                                                                             log2((double)std::max(pr.K, 1)) +
+                                                                             1.5) / 5.0)));
     OzBuffers b;
     gbx_status st;
     if (keep) b = *keep;
     else if ((st = oz_buffers(ctx, Mp, Np, Kp, nW, b)) != GBX_OK) return st;
     cudaStream_t s = S_(ctx);
-    if (tol <= 0.0) tol = 1e-14;
 
     gbx_timer_begin(ctx, GBX_TIMER_OZAKI_SPLIT);
     // op(A): statistics and slices; op(B)^T: its own, or for a symmetric
@@ -1830,8 +1927,7 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         if (blocks > 0x7fffffffLL) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: operands too large");
         oa.gpart = b.gpart;
         ob.gpart = b.gpart + 3 * (size_t)(Mp / OZ_SPLIT_ROWS);
-        oz_prep_small<<<(unsigned)blocks, 256, 0, s>>>(oa, ob, tol, forced, b.status, (unsigned *)(b.status + 8),
-                                                      b.S);
+        oz_prep_small<<<(unsigned)blocks, 256, 0, s>>>(oa, ob, planes, b.status);
         gbx_count_launch(ctx, 1);
         if ((st = gbx_check_launch(ctx, "ozaki prepare")) != GBX_OK) return st;
     } else if ((st = oz_prepare(ctx, oa, ob, b_stats, tol, forced, b.status, (unsigned *)(b.S + 4), b.S)) !=
@@ -1857,6 +1953,14 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     p.c_part = pr.c_part;
     p.status = b.status;
     p.status_host = b.status_host;
+    p.gpa = b.gpart;
+    p.gpb = b.gpart + 3 * (size_t)(Mp / OZ_SPLIT_ROWS);
+    p.npa = Mp / OZ_SPLIT_ROWS;
+    p.npb = Np / OZ_SPLIT_ROWS;
+    p.K = pr.K;
+    p.tol_bits = (float)(-log2(tol));
+    p.forced = forced;
+    p.smax = planes;
 
     // kernel attributes (per device) and the resident CTA-pair count; calls
     // arrive from many host threads

@@ -235,3 +235,48 @@ def test_fortran_calls_through_the_serving_loop(orc):
                        timeout=300)
     assert r.returncode == 0, r.stderr[-3000:]
     assert "ERRS []" in r.stdout, r.stdout + r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("mode", ["plain", "served", "ozaki"])
+def test_native_cholesky_trace(lib, mode):
+    # the serving benchmark's native driver: 3 threads factorise SPD matrices
+    # through the serving loop (or plain dispatch); each factor L must
+    # reproduce A = L L^T on the lower triangle
+    import torch
+    import libgpublas_gb300 as g
+    sizes, nbs = [300, 517, 256], [128, 256, 128]
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(21)
+    mats, origs = [], []
+    for n in sizes:
+        G = torch.empty(n, n, dtype=torch.float64, device="cuda").uniform_(-1.0, 1.0, generator=gen)
+        A = (G @ G.T + n * torch.eye(n, dtype=torch.float64, device="cuda")).T.contiguous()
+        origs.append(A.clone())
+        mats.append(A)
+    info = torch.zeros(len(sizes), dtype=torch.int32, device="cuda")
+    # the library's streams do not order with torch's: the operands must be
+    # complete before the calls start
+    torch.cuda.synchronize()
+    server = g.Server(0, slots=4) if mode != "plain" else None
+    try:
+        r = g.cholesky_trace(server, 0, sizes, nbs, [m.data_ptr() for m in mats], info.data_ptr(),
+                             mode == "ozaki")
+    finally:
+        if server:
+            server.close()
+    assert r["first_error"] == 0
+    assert int((info != 0).sum()) == 0
+    expect = 0
+    for n, nb in zip(sizes, nbs):
+        steps = (n + nb - 1) // nb
+        for s in range(steps):
+            rest = steps - s - 1
+            expect += 1 + (1 if rest else 0) + rest + max(rest - 1, 0)
+    assert r["calls"] == expect
+    assert len(r["thread_finish_s"]) == len(sizes) and max(r["thread_finish_s"]) <= r["wall_s"] + 1e-3
+    for n, A, A0 in zip(sizes, mats, origs):
+        # column-major storage: the lower triangle of the n x n matrix is the
+        # upper triangle of the row-major view
+        Lm = torch.tril(A.T)
+        R = torch.tril(Lm @ Lm.T - A0.T)
+        assert float(R.norm() / torch.tril(A0.T).norm()) <= (1e-14 if mode != "ozaki" else 1e-13)
