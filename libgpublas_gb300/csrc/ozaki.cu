@@ -324,52 +324,6 @@ __device__ double oz_log2_gamma(const int *expo, const double *ss, int rows, int
     return oz_gamma_finish(num, den, K);
 }
 
-// The same from per-CTA partials (emax_c, num_c, den_c) of 16 rows each,
-// num_c = sum 2^(2(e_i - emax_c)) and den_c likewise weighted by ss_i: the
-// one-launch preparation leaves one partial per CTA, so the last CTA merges
-// Rp/16 partials instead of reading every row.  FP32 throughout (the
-// statistic only steers the slice count; rows 2^-63 below the largest
-// maximum contribute nothing either way) and one warp-level reduction pass:
-// FP64 and block-wide barrier rounds cost microseconds on the critical path
-// of a small product.
-__device__ float oz_log2_gamma_parts(const float *part, int n, int K)
-{
-    __shared__ int s_emax[8];
-    __shared__ float s_num[8], s_den[8], s_g;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int emax = -100000;
-#pragma unroll 4
-    for (int i = threadIdx.x; i < n; i += blockDim.x) emax = max(emax, (int)__ldcg(part + 3 * i));
-#pragma unroll
-    for (int o = 16; o; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-    if (lane == 0) s_emax[warp] = emax;
-    __syncthreads();
-#pragma unroll
-    for (int w = 0; w < 8; w++) emax = max(emax, s_emax[w]);
-    float num = 0.f, den = 0.f;
-#pragma unroll 4
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int d = 2 * ((int)__ldcg(part + 3 * i) - emax);
-        const float w = d < -126 ? 0.f : __int_as_float((127 + d) << 23);
-        num = fmaf(w, __ldcg(part + 3 * i + 1), num);
-        den = fmaf(w, __ldcg(part + 3 * i + 2), den);
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        num += __shfl_xor_sync(0xffffffffu, num, o);
-        den += __shfl_xor_sync(0xffffffffu, den, o);
-    }
-    if (lane == 0) { s_num[warp] = num; s_den[warp] = den; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float tn = 0.f, td = 0.f;
-        for (int w = 0; w < 8; w++) { tn += s_num[w]; td += s_den[w]; }
-        s_g = td > 0.f ? 0.5f * __log2f(tn * (float)K / td) : 0.f;
-    }
-    __syncthreads();
-    return s_g;
-}
-
 // Finishes the statistics of both operands (b_stats: b has its own) and, in
 // the last CTA to finish, chooses the slice count:
 //   error ~ c * 2^(-5S) * gamma_A * gamma_B; c = 2^1.5 covers the truncated
@@ -416,11 +370,18 @@ __device__ __forceinline__ uint32_t e4m3_of_digit(int d)
 // thread; padding gets digit 0.  The tile is staged through shared memory so
 // col_k sources are read coalesced.
 constexpr int OZ_SPLIT_ROWS = 16, OZ_SPLIT_PER = 8;
+// the one-launch preparation: 256 threads per 16-row block (16 per row for
+// the statistics, 8 k per thread for the digits; 512 threads and 4 k per
+// thread measured faster only for products of a few thousand rows)
+constexpr int OZ_SMALL_THREADS = 256, OZ_SMALL_PER = 8;
 
-// pre: the same tile already staged by the caller (one-launch path, K <= 128)
+// PER consecutive k per thread (blockDim = 16 * 128 / PER); pre: the same
+// tile already staged by the caller (one-launch path, K <= 128)
+template <int PER>
 __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K, int Rp, int Kp, const int *expo,
                                               int S, uint8_t *X8, int blk, const double (*pre)[129] = nullptr)
 {
+    static_assert(PER == 4 || PER == 8, "split width");
     __shared__ double tile[OZ_SPLIT_ROWS][129];
     __shared__ uint32_t e4m3_tbl[33];   // E4M3 byte of the digit d at [16 + d], d in [-16, 16]
     const int kblocks = Kp / 128;
@@ -438,18 +399,18 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
         }
     const double (*T)[129] = pre ? pre : tile;
     __syncthreads();
-    constexpr int TPR = 128 / OZ_SPLIT_PER;   // threads per row
-    const int rr = threadIdx.x / TPR, kq = (threadIdx.x % TPR) * OZ_SPLIT_PER;
+    constexpr int TPR = 128 / PER;   // threads per row
+    const int rr = threadIdx.x / TPR, kq = (threadIdx.x % TPR) * PER;
     const int r = r0 + rr;
     if (r >= Rp) return;
     const int e = r < rows ? expo[r] : 0;
     // N_j = round(|x_j| * 2^(4 - e + 5(S-1))) as a 128-bit integer hi:lo.
     // |x| < 2^e bounds N_j by 16 * 32^(S-1) <= 2^69.  Integer pipe only.
     const int top = 4 - e + 5 * (S - 1);
-    unsigned long long lo[OZ_SPLIT_PER], hi[OZ_SPLIT_PER];
+    unsigned long long lo[PER], hi[PER];
     unsigned neg = 0u;
 #pragma unroll
-    for (int j = 0; j < OZ_SPLIT_PER; j++) {
+    for (int j = 0; j < PER; j++) {
         const unsigned long long b = (unsigned long long)__double_as_longlong(T[rr][kq + j]);
         neg |= (unsigned)(b >> 63) << j;
         const int E = (int)((b >> 52) & 0x7FF);
@@ -472,7 +433,7 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
         else chi |= 1ull << (b - 64);
     }
 #pragma unroll
-    for (int j = 0; j < OZ_SPLIT_PER; j++) {
+    for (int j = 0; j < PER; j++) {
         const unsigned long long nl = lo[j] + clo;
         hi[j] = hi[j] + chi + (nl < clo ? 1ull : 0ull);
         lo[j] = nl;
@@ -480,9 +441,9 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
     for (int s = S - 1; s >= 0; s--) {
         const int sh = 5 * (S - 1 - s);   // plane s holds the chunk at bit sh
         const unsigned mask = s == 0 ? 63u : 31u;
-        uint32_t w[OZ_SPLIT_PER / 4] = {};
+        uint32_t w[PER / 4] = {};
 #pragma unroll
-        for (int j = 0; j < OZ_SPLIT_PER; j++) {
+        for (int j = 0; j < PER; j++) {
             unsigned c;
             if (sh == 0) c = (unsigned)lo[j];
             else if (sh < 64) c = (unsigned)((lo[j] >> sh) | (hi[j] << (64 - sh)));
@@ -492,8 +453,9 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
             const int idx = ((neg >> j) & 1u) ? 16 - d : 16 + d;
             w[j >> 2] |= e4m3_tbl[idx] << (8 * (j & 3));
         }
-        uint2 *dst = (uint2 *)(X8 + ((size_t)s * Rp + r) * Kp + k0 + kq);
-        *dst = make_uint2(w[0], w[1]);
+        uint8_t *dst = X8 + ((size_t)s * Rp + r) * Kp + k0 + kq;
+        if constexpr (PER == 8) *(uint2 *)dst = make_uint2(w[0], w[PER / 4 - 1]);
+        else *(uint32_t *)dst = w[0];
     }
 }
 
@@ -501,8 +463,10 @@ __global__ void __launch_bounds__(256)
 oz_prep_split(OzPrepOp a, OzPrepOp b, const int *__restrict__ S_dev)
 {
     const int S = *S_dev;
-    if ((int)blockIdx.x < a.split_blocks) oz_split_tile(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, S, a.X8, blockIdx.x);
-    else oz_split_tile(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, S, b.X8, blockIdx.x - a.split_blocks);
+    if ((int)blockIdx.x < a.split_blocks)
+        oz_split_tile<OZ_SPLIT_PER>(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, S, a.X8, blockIdx.x);
+    else
+        oz_split_tile<OZ_SPLIT_PER>(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, S, b.X8, blockIdx.x - a.split_blocks);
 }
 
 // ---- small K: the whole preparation in one launch ---------------------------
@@ -559,7 +523,8 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
     }
     __syncthreads();   // the row exponents are visible to the whole CTA
     if (gpart && threadIdx.x < 32) {
-        // this block's partial of the slice-count statistic (oz_log2_gamma_parts)
+        // this block's partial of the slice-count statistic (oz_choose_S):
+        // (emax_c, sum 2^(2(e_i - emax_c)), sum 2^(2(e_i - emax_c)) ss_i)
         const int rg = r0 + (threadIdx.x & 15);
         const bool valid = threadIdx.x < 16 && rg < rows;
         const int e = valid ? expo[rg] : -100000;
@@ -582,12 +547,13 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
     }
     const int kblocks = Kp / 128;
     if (kblocks == 1)   // the statistics pass left this block's only tile in shared memory
-        oz_split_tile(v, rows, K, Rp, Kp, expo, planes, X8, rblk, tile);
+        oz_split_tile<OZ_SMALL_PER>(v, rows, K, Rp, Kp, expo, planes, X8, rblk, tile);
     else
-        for (int kb = 0; kb < kblocks; kb++) oz_split_tile(v, rows, K, Rp, Kp, expo, planes, X8, rblk * kblocks + kb);
+        for (int kb = 0; kb < kblocks; kb++)
+            oz_split_tile<OZ_SMALL_PER>(v, rows, K, Rp, Kp, expo, planes, X8, rblk * kblocks + kb);
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(OZ_SMALL_THREADS)
 oz_prep_small(OzPrepOp a, OzPrepOp b, int planes, int *status)
 {
     // the product kernel may be scheduled now: its set-up needs none of this
@@ -860,18 +826,22 @@ __device__ __forceinline__ double oz_i128_ldexp(unsigned long long lo, long long
 }
 
 // alpha as +-2^ea when it is a power of two (folded into the exponent on the
-// integer pipe), else kept for one FP64 multiply.
+// integer pipe), else kept for one FP64 multiply; and whether beta is
+// nonzero, decided once per thread (an FP64 compare per element costs a slot
+// on the 2-lane FP64 pipe like any FP64 instruction).
 struct OzAlpha {
     bool pow2;
+    bool beta_on;
     int ea;
     unsigned long long sign;
 };
-__device__ __forceinline__ OzAlpha oz_alpha_split(double alpha)
+__device__ __forceinline__ OzAlpha oz_alpha_split(double alpha, double beta)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(alpha);
     const int ex = (int)((b >> 52) & 0x7FF);
     OzAlpha a;
     a.pow2 = (b & 0xFFFFFFFFFFFFFull) == 0ull && ex != 0 && ex != 0x7FF;
+    a.beta_on = beta != 0.0;
     a.ea = ex - 1023;
     a.sign = b & 0x8000000000000000ull;
     return a;
@@ -915,7 +885,7 @@ __device__ __forceinline__ double oz_result(unsigned long long lo, long long hi,
         r = alpha * oz_i128_ldexp(lo, hi, e, ok);
     }
     if (!ok) r = oz_alpha_pow2(alpha, e) * oz_to_double(lo, hi);
-    return beta != 0.0 ? fma(beta, cold, r) : r;
+    return as.beta_on ? fma(beta, cold, r) : r;
 }
 
 // The same for V = vh * 2^lsh + vl with |vh|, |vl| < 2^53 (0 <= lsh < 64):
@@ -940,7 +910,7 @@ __device__ __forceinline__ double oz_result_split(long long vh, long long vl, in
         } else {
             r = alpha * (dh + dl);
         }
-        return beta != 0.0 ? fma(beta, cold, r) : r;
+        return as.beta_on ? fma(beta, cold, r) : r;
     }
     unsigned long long lo;
     long long hi;
@@ -1020,8 +990,8 @@ __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, 
 #pragma unroll
             for (int j = 0; j < CH; j++) __stcg(wdst + (size_t)j * p.Mp, wc[j]);
         } else if (row_ok) {
-            const OzAlpha as = oz_alpha_split(p.alpha);
-            const double beta = need_c ? p.beta : 0.0;
+            const OzAlpha as = oz_alpha_split(p.alpha, need_c ? p.beta : 0.0);
+            const double beta = p.beta;
 #pragma unroll
             for (int j = 0; j < CH; j++) {
                 const int gcol = gcol0 + cb + j;
@@ -1404,7 +1374,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const int quarter = warp & 3;               // TMEM lane window of this warp
         const int cg = (warp - 2) >> 2;             // columns cg*OZS_DCOLS .. of the tile
         const int row = quarter * 32 + lane;
-        const OzAlpha as = oz_alpha_split(p.alpha);
+        const OzAlpha as = oz_alpha_split(p.alpha, p.beta);
         const int g = (S + 1) >> 1;                 // diagonals of the high half
         const int lsh = 5 * (S - g);                // weight of the high half over the low one
         uint32_t tp = 0;
@@ -1421,7 +1391,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             int ecol[OZS_DCOLS];
 #pragma unroll
             for (int j = 0; j < OZS_DCOLS; j++) {
-                cold[j] = (row_ok && p.beta != 0.0 && oz_c_keep(p, grow, gc0 + j)) ? cp[(size_t)j * p.ldc] : 0.0;
+                cold[j] = (row_ok && as.beta_on && oz_c_keep(p, grow, gc0 + j)) ? cp[(size_t)j * p.ldc] : 0.0;
                 ecol[j] = __ldg(p.col_exp + gc0 + j);
             }
             const int erow = row_ok ? p.row_exp[grow] - 5 * (S - 1) : 0;
@@ -1927,7 +1897,7 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         if (blocks > 0x7fffffffLL) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: operands too large");
         oa.gpart = b.gpart;
         ob.gpart = b.gpart + 3 * (size_t)(Mp / OZ_SPLIT_ROWS);
-        oz_prep_small<<<(unsigned)blocks, 256, 0, s>>>(oa, ob, planes, b.status);
+        oz_prep_small<<<(unsigned)blocks, OZ_SMALL_THREADS, 0, s>>>(oa, ob, planes, b.status);
         gbx_count_launch(ctx, 1);
         if ((st = gbx_check_launch(ctx, "ozaki prepare")) != GBX_OK) return st;
     } else if ((st = oz_prepare(ctx, oa, ob, b_stats, tol, forced, b.status, (unsigned *)(b.S + 4), b.S)) !=
