@@ -2065,6 +2065,80 @@ extern "C" gbx_status gbx_dsyrk_ozaki(gbx_ctx *ctx, char uplo, char trans, int n
 // well-conditioned diagonal blocks of a Cholesky factorization the extra
 // error of applying the inverse is a factor cond(op(A)) on the rounding of X.
 namespace {
+// Inverse of a triangular matrix of order n <= 256 in FP64, one warp per
+// column of the inverse.  An upper triangle U is handled as the lower
+// triangle L' = P U P (P the order-reversing permutation; U^-1 = P L'^-1 P).
+// Column j of W = L'^-1 solves L' w = e_j by forward substitution, lane l
+// holding rows l, l + 32, ...: at step i the owner lane scales w_i by the
+// inverse diagonal entry, broadcasts it, and every lane subtracts
+// w_i L'(r, i) from its rows r > i.  The columns of L' stream through shared
+// memory 16 at a time.  Each step costs one FP64 warp instruction per
+// 32-row slot still below the pivot, and an FP64 warp instruction occupies
+// the SM's 2-lane FP64 pipe for 16 cycles whatever its predicate: CTAs of 2
+// warps spread the columns over as many SMs as possible, and slots above
+// the pivot are skipped.  The FP64 DTRSM of the identity this replaces ran
+// its small GEMM updates on one or two SMs (~270 µs for n = 128).
+// X = W, or W^T for op = 'T'/'C'.
+constexpr int OZ_TI_WARPS = 2, OZ_TI_PANEL = 16, OZ_TI_NMAX = 256;
+
+__global__ void __launch_bounds__(OZ_TI_WARPS * 32)
+oz_trinv_kernel(int n, const double *__restrict__ T, long long ldt, int lower, int unit, int trans,
+                double *__restrict__ X, long long ldx)
+{
+    __shared__ double sT[OZ_TI_PANEL][OZ_TI_NMAX];
+    __shared__ double sR[OZ_TI_NMAX];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // L'(r, c) for r >= c
+    auto tget = [&](int r, int c) -> double {
+        const int rr = lower ? r : n - 1 - r, cc = lower ? c : n - 1 - c;
+        return T[(long long)cc * ldt + rr];
+    };
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sR[i] = unit ? 1.0 : 1.0 / tget(i, i);
+    const int jfirst = blockIdx.x * OZ_TI_WARPS;
+    const int j = jfirst + warp;   // this warp's column of L'^-1
+    double w[OZ_TI_NMAX / 32];
+#pragma unroll
+    for (int s = 0; s < OZ_TI_NMAX / 32; s++) w[s] = (s * 32 + lane == j) ? 1.0 : 0.0;
+    for (int p0 = jfirst / OZ_TI_PANEL * OZ_TI_PANEL; p0 < n; p0 += OZ_TI_PANEL) {
+        __syncthreads();   // the previous panel is consumed (and sR written)
+        const int rows = n - p0;
+        for (int t = threadIdx.x; t < OZ_TI_PANEL * rows; t += blockDim.x) {
+            const int c = t / rows, r = p0 + t % rows;
+            sT[c][r] = (p0 + c < n && r >= p0 + c) ? tget(r, p0 + c) : 0.0;
+        }
+        __syncthreads();
+        if (j >= n) continue;
+        for (int c = 0; c < OZ_TI_PANEL; c++) {
+            const int i = p0 + c;
+            if (i >= n) break;
+            if (i < j) continue;   // uniform over the warp
+            const int slot = i >> 5;
+            double wo = 0.0;
+#pragma unroll
+            for (int s = 0; s < OZ_TI_NMAX / 32; s++)
+                if (s == slot) wo = w[s];
+            const double wi = __shfl_sync(0xffffffffu, wo * sR[i], i & 31);
+#pragma unroll
+            for (int s = 0; s < OZ_TI_NMAX / 32; s++) {
+                if (s < slot || s * 32 >= n) continue;   // warp-uniform: no FP64 issue
+                const int r = s * 32 + lane;
+                if (r > i && r < n) w[s] = fma(-sT[c][r], wi, w[s]);
+                else if (r == i) w[s] = wi;
+            }
+        }
+    }
+    if (j >= n) return;
+#pragma unroll
+    for (int s = 0; s < OZ_TI_NMAX / 32; s++) {
+        const int r = s * 32 + lane;
+        if (r >= n) continue;
+        const double v = r >= j ? w[s] : 0.0;
+        const int R = lower ? r : n - 1 - r, J = lower ? j : n - 1 - j;   // entry (R, J) of T^-1
+        if (trans) X[(long long)R * ldx + J] = v;
+        else X[(long long)J * ldx + R] = v;
+    }
+}
+
 __global__ void oz_set_identity(int n, double *X, long long ldx)
 {
     const long long total = (long long)n * n;
@@ -2094,12 +2168,21 @@ extern "C" gbx_status gbx_dtrsm_ozaki(gbx_ctx *ctx, char side, char uplo, char t
     if ((st = gbx_ws(ctx, GBX_WS_TRSM_X, sizeof(double) * (size_t)na * na, &px)) != GBX_OK) return st;
     double *X = (double *)px;
     cudaStream_t s = S_(ctx);
-    const long long total = (long long)na * na;
-    oz_set_identity<<<(int)std::min<long long>((total + 255) / 256, (long long)gbx_ctx_sms(ctx) * 4), 256, 0, s>>>(
-        na, X, na);
-    gbx_count_launch(ctx, 1);
-    if ((st = gbx_check_launch(ctx, "dtrsm_ozaki identity")) != GBX_OK) return st;
-    if ((st = gbx_dtrsm(ctx, 'L', uplo, ta, diag, na, na, 1.0, A, lda, X, na)) != GBX_OK) return st;
+    if (na <= OZ_TI_NMAX) {
+        // X = op(A)^-1 by the warp-per-column substitution kernel
+        oz_trinv_kernel<<<(na + OZ_TI_WARPS - 1) / OZ_TI_WARPS, OZ_TI_WARPS * 32, 0, s>>>(
+            na, A, lda, gbx_lsame(uplo, 'L') ? 1 : 0, gbx_lsame(diag, 'U') ? 1 : 0, gbx_lsame(ta, 'N') ? 0 : 1, X, na);
+        gbx_count_launch(ctx, 1);
+        if ((st = gbx_check_launch(ctx, "dtrsm_ozaki inverse")) != GBX_OK) return st;
+    } else {
+        // X = op(A)^-1 I by the FP64 DTRSM
+        const long long total = (long long)na * na;
+        oz_set_identity<<<(int)std::min<long long>((total + 255) / 256, (long long)gbx_ctx_sms(ctx) * 4), 256, 0,
+                          s>>>(na, X, na);
+        gbx_count_launch(ctx, 1);
+        if ((st = gbx_check_launch(ctx, "dtrsm_ozaki identity")) != GBX_OK) return st;
+        if ((st = gbx_dtrsm(ctx, 'L', uplo, ta, diag, na, na, 1.0, A, lda, X, na)) != GBX_OK) return st;
+    }
     // B is both an operand and the result: the Ozaki product reads its FP64
     // operands only in the preparation launches, which complete before the
     // product kernel writes C, and with beta = 0 it never reads C.

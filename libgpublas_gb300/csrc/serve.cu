@@ -324,13 +324,18 @@ extern "C" gbx_status gbx_server_call(gbx_server *s, const gbx_op *op, double *l
             cudaSetDevice(s->device);
             const gbx_status st = run_on_slot(sl, *op);
             const auto t1 = clk::now();
+            bool waiting;
             {
                 std::lock_guard<std::mutex> lk(s->mu);
                 sl->busy = false;
                 s->batches++;
                 record(s, t0, t1);
+                waiting = !s->queue.empty();
             }
-            s->cv_work.notify_all();   // a worker may be waiting for this slot
+            // a queued request may be waiting for this slot; with an empty
+            // queue nobody is (waking every worker per call cost the host
+            // cores as many futex round trips as there are slots)
+            if (waiting) s->cv_work.notify_all();
             if (latency_us) *latency_us = std::chrono::duration<double, std::micro>(t1 - t0).count();
             return st;
         }

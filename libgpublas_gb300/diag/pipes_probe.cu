@@ -1,7 +1,7 @@
 // pipes_probe.cu — throughput of the arithmetic pipes a BLAS library can use
 // on this GPU: SIMT DFMA, FP64 mma.sync (m8n8k4), s8 IMMA (m16n8k32), bf16
-// HMMA (m16n8k16) and E4M3 mma.sync (m16n8k32), and whether DFMA and DMMA
-// overlap.  Each probe keeps 4–8
+// HMMA (m16n8k16) and E4M3 mma.sync (m16n8k32), whether DFMA and DMMA
+// overlap, and the latency of dependent FP64 and FP32 chains.  Each probe keeps 4–8
 // independent accumulator chains per thread over 1–8 CTAs per SM and reports
 // the best of three timed launches.  It decides which pipe the FP64 GEMM core
 // runs on (DFMA or DMMA) and sizes the Ozaki tensor-core path against the
@@ -120,6 +120,34 @@ float timeit(F f) {
   return best;
 }
 
+// Latency of dependent chains (clock64 cycles per operation, one CTA): FP64
+// FMA and multiply, FP32 FMA, and the shared-memory and shuffle hops of a
+// substitution step, with 1, 32 and 256 threads (8 warps share the SM's FP64
+// pipe).  Serial FP64 work -- pivots, substitutions -- is bound by these.
+__global__ void lat_probe(double* out, long long* cyc, double a, double b, int n, float af, float bf) {
+  double x = threadIdx.x * 1e-3 + 1.0;
+  long long t0 = clock64();
+  for (int i = 0; i < n; i++) x = fma(x, a, b);
+  long long t1 = clock64();
+  float y = threadIdx.x * 1e-3f + 1.0f;
+  for (int i = 0; i < n; i++) y = fmaf(y, af, bf);
+  long long t2 = clock64();
+  double z = x;
+  for (int i = 0; i < n; i++) z = z * a;
+  long long t3 = clock64();
+  __shared__ double sh[64];
+  sh[threadIdx.x & 63] = z;
+  __syncwarp();
+  double w = z;
+  for (int i = 0; i < n; i++) w = fma(sh[(i + threadIdx.x) & 63], w, b);
+  long long t4 = clock64();
+  double v = w;
+  for (int i = 0; i < n; i++) v = __shfl_sync(0xffffffffu, v, i & 31) * a;
+  long long t5 = clock64();
+  out[threadIdx.x] = x + y + z + w + v;
+  if (threadIdx.x == 0) { cyc[0] = t1 - t0; cyc[1] = t2 - t1; cyc[2] = t3 - t2; cyc[3] = t4 - t3; cyc[4] = t5 - t4; }
+}
+
 int main() {
   cudaDeviceProp p; CK(cudaGetDeviceProperties(&p,0));
   printf("device %s sms %d cc %d.%d\n", p.name, p.multiProcessorCount, p.major, p.minor);
@@ -170,6 +198,18 @@ int main() {
     const double fl = mode == 0 ? warps * fma_fl : mode == 1 ? warps * mma_fl : warps / 2 * (fma_fl + mma_fl);
     printf("mix %d (%s): %.3f ms  %.3f TFLOP/s\n", mode, mode == 0 ? "DFMA" : mode == 1 ? "DMMA" : "half/half", ms,
            fl / ms / 1e9);
+  }
+  {
+    long long* dcyc; CK(cudaMalloc(&dcyc, 64));
+    for (int threads : {1, 32, 256}) {
+      lat_probe<<<1, threads>>>(dout, dcyc, 1.0000001, 1e-9, 4096, 1.0000001f, 1e-9f);
+      CK(cudaGetLastError());
+      CK(cudaDeviceSynchronize());
+      long long h[5]; CK(cudaMemcpy(h, dcyc, sizeof(h), cudaMemcpyDeviceToHost));
+      printf("latency threads=%d: DFMA %.1f  FFMA %.1f  DMUL %.1f  LDS+DFMA %.1f  SHFL+DMUL %.1f cycles\n", threads,
+             h[0] / 4096.0, h[1] / 4096.0, h[2] / 4096.0, h[3] / 4096.0, h[4] / 4096.0);
+    }
+    CK(cudaFree(dcyc));
   }
   CK(cudaDeviceSynchronize());
   return 0;
