@@ -371,15 +371,20 @@ __device__ __forceinline__ uint32_t e4m3_of_digit(int d)
 // col_k sources are read coalesced.
 constexpr int OZ_SPLIT_ROWS = 16, OZ_SPLIT_PER = 8;
 // the one-launch preparation: 256 threads per 16-row block (16 per row for
-// the statistics, 8 k per thread for the digits; 512 threads and 4 k per
-// thread measured faster only for products of a few thousand rows)
-constexpr int OZ_SMALL_THREADS = 256, OZ_SMALL_PER = 8;
+// the statistics, 8 k per thread for the digits), or 512 (4 k per thread for
+// the digits) when the blocks fit on the SMs at once: the digit split is then
+// the block's longest step, and more warps per block shorten it (with more
+// blocks than SMs, 512-thread blocks measured slower)
+constexpr int OZ_SMALL_THREADS = 256;
 
 // PER consecutive k per thread (blockDim = 16 * 128 / PER); pre: the same
-// tile already staged by the caller (one-launch path, K <= 128)
+// tile already staged by the caller (one-launch path, K <= 128); expo_s: the
+// 16 rows' exponents in the caller's shared memory (one-launch path), else
+// they are read from expo
 template <int PER>
 __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K, int Rp, int Kp, const int *expo,
-                                              int S, uint8_t *X8, int blk, const double (*pre)[129] = nullptr)
+                                              int S, uint8_t *X8, int blk, const double (*pre)[129] = nullptr,
+                                              const int *expo_s = nullptr)
 {
     static_assert(PER == 4 || PER == 8, "split width");
     __shared__ double tile[OZ_SPLIT_ROWS][129];
@@ -403,7 +408,7 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
     const int rr = threadIdx.x / TPR, kq = (threadIdx.x % TPR) * PER;
     const int r = r0 + rr;
     if (r >= Rp) return;
-    const int e = r < rows ? expo[r] : 0;
+    const int e = r < rows ? (expo_s ? expo_s[rr] : expo[r]) : 0;
     // N_j = round(|x_j| * 2^(4 - e + 5(S-1))) as a 128-bit integer hi:lo.
     // |x| < 2^e bounds N_j by 16 * 32^(S-1) <= 2^69.  Integer pipe only.
     const int top = 4 - e + 5 * (S - 1);
@@ -478,11 +483,16 @@ oz_prep_split(OzPrepOp a, OzPrepOp b, const int *__restrict__ S_dev)
 // its maximum, the same bound as rounding at S digits); every CTA leaves a partial of the slice-count statistic,
 // from which the product kernel chooses S.  One launch instead of three:
 // small products are dominated by per-launch cost.
+template <int THREADS>
 __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, int Rp, int Kp, int *expo, double *ss,
                                              int *scale, uint8_t *X8, float *gpart, int planes, int rblk,
                                              int *status)
 {
+    static_assert(THREADS == 256 || THREADS == 512, "the statistics map 16 threads to a row of a 16-row block");
+    constexpr int PER = OZ_SPLIT_ROWS * 128 / THREADS;   // k per thread in the digit split
     __shared__ double tile[OZ_SPLIT_ROWS][129];
+    __shared__ int s_ex[OZ_SPLIT_ROWS];       // the rows' exponents and sums of squares, also kept here
+    __shared__ double s_ss[OZ_SPLIT_ROWS];    // for the partial and the split (no global round trip)
     const int r0 = rblk * OZ_SPLIT_ROWS;
     const int rr = threadIdx.x >> 4, lane16 = threadIdx.x & 15;   // 16 threads per row
     SsAcc acc;
@@ -496,30 +506,40 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
             tile[tr][kk] = (r < rows && k < K) ? src_get(v, r, k) : 0.0;
         }
         __syncthreads();
+        if (threadIdx.x < 256) {   // warp-uniform: the first eight warps
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const unsigned long long b = abs_bits(tile[rr][lane16 + 16 * j]);
-            flag_nonfinite(b, status);
-            acc.add(b);
+            for (int j = 0; j < 8; j++) {
+                const unsigned long long b = abs_bits(tile[rr][lane16 + 16 * j]);
+                flag_nonfinite(b, status);
+                acc.add(b);
+            }
         }
         __syncthreads();
     }
+    if (threadIdx.x < 256) {
 #pragma unroll
-    for (int o = 8; o; o >>= 1) {   // the 16 threads of a row are one half-warp
-        SsAcc t;
-        t.maxb = __shfl_xor_sync(0xffffffffu, acc.maxb, o);
-        t.mref = __shfl_xor_sync(0xffffffffu, acc.mref, o);
-        t.ss = __shfl_xor_sync(0xffffffffu, acc.ss, o);
-        acc.merge(t);
+        for (int o = 8; o; o >>= 1) {   // the 16 threads of a row are one half-warp
+            SsAcc t;
+            t.maxb = __shfl_xor_sync(0xffffffffu, acc.maxb, o);
+            t.mref = __shfl_xor_sync(0xffffffffu, acc.mref, o);
+            t.ss = __shfl_xor_sync(0xffffffffu, acc.ss, o);
+            acc.merge(t);
+        }
     }
     const int r = r0 + rr;
-    if (lane16 == 0 && r < Rp) {
+    if (threadIdx.x < 256 && lane16 == 0 && r < Rp) {
+        int ex = 0;
+        double sv = 0.0;
         if (r < rows) {
-            acc.finish(expo[r], ss[r]);
-            scale[r] = expo[r] - 4;
+            acc.finish(ex, sv);
+            expo[r] = ex;
+            ss[r] = sv;
+            scale[r] = ex - 4;
         } else {
             scale[r] = 0;
         }
+        s_ex[rr] = ex;
+        s_ss[rr] = sv;
     }
     __syncthreads();   // the row exponents are visible to the whole CTA
     if (gpart && threadIdx.x < 32) {
@@ -527,13 +547,13 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
         // (emax_c, sum 2^(2(e_i - emax_c)), sum 2^(2(e_i - emax_c)) ss_i)
         const int rg = r0 + (threadIdx.x & 15);
         const bool valid = threadIdx.x < 16 && rg < rows;
-        const int e = valid ? expo[rg] : -100000;
+        const int e = valid ? s_ex[threadIdx.x & 15] : -100000;
         int em = e;
 #pragma unroll
         for (int o = 16; o; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
         const int d = 2 * (e - em);
         const float w = (!valid || d < -126) ? 0.f : __int_as_float((127 + d) << 23);
-        float nu = w, de = valid ? w * (float)ss[rg] : 0.f;
+        float nu = w, de = valid ? w * (float)s_ss[threadIdx.x & 15] : 0.f;
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             nu += __shfl_xor_sync(0xffffffffu, nu, o);
@@ -547,13 +567,14 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
     }
     const int kblocks = Kp / 128;
     if (kblocks == 1)   // the statistics pass left this block's only tile in shared memory
-        oz_split_tile<OZ_SMALL_PER>(v, rows, K, Rp, Kp, expo, planes, X8, rblk, tile);
+        oz_split_tile<PER>(v, rows, K, Rp, Kp, expo, planes, X8, rblk, tile, s_ex);
     else
         for (int kb = 0; kb < kblocks; kb++)
-            oz_split_tile<OZ_SMALL_PER>(v, rows, K, Rp, Kp, expo, planes, X8, rblk * kblocks + kb);
+            oz_split_tile<PER>(v, rows, K, Rp, Kp, expo, planes, X8, rblk * kblocks + kb, nullptr, s_ex);
 }
 
-__global__ void __launch_bounds__(OZ_SMALL_THREADS)
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS)
 oz_prep_small(OzPrepOp a, OzPrepOp b, int planes, int *status)
 {
     // the product kernel may be scheduled now: its set-up needs none of this
@@ -561,9 +582,10 @@ oz_prep_small(OzPrepOp a, OzPrepOp b, int planes, int *status)
     asm volatile("griddepcontrol.launch_dependents;");
     const int na = a.Rp / OZ_SPLIT_ROWS;
     if ((int)blockIdx.x < na)
-        oz_prep_rows(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, a.ss, a.scale, a.X8, a.gpart, planes, blockIdx.x, status);
+        oz_prep_rows<THREADS>(a.v, a.rows, a.K, a.Rp, a.Kp, a.expo, a.ss, a.scale, a.X8, a.gpart, planes, blockIdx.x,
+                              status);
     else
-        oz_prep_rows(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, b.ss, b.scale, b.X8, b.gpart, planes, blockIdx.x - na,
+        oz_prep_rows<THREADS>(b.v, b.rows, b.K, b.Rp, b.Kp, b.expo, b.ss, b.scale, b.X8, b.gpart, planes, blockIdx.x - na,
                      status);
 }
 
@@ -597,20 +619,54 @@ struct OzParams {
 // preparation's per-block partials of both operands (the same data in the
 // same order in every CTA: one S per call) with the model oz_prep_finish
 // applies, clamped to the planes the preparation wrote; CTA 0 records it.
+// Returns 0 for a call to skip (the status word is set: a non-finite operand
+// or an earlier kernel's expired wait); every thread gets the same answer
+// before any copy or MMA is issued.  The status and up to two partials per
+// thread and operand are read in one round of loads (a round costs about a
+// microsecond at the start of a call of a few tens of microseconds).
 __device__ int oz_choose_S(const OzParams &p)
 {
+    constexpr int R = 2;   // partials per thread and operand held in registers
     __shared__ int s_e[2][32];
     __shared__ float s_v[4][32];
     __shared__ int s_S;
     const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nt = blockDim.x;
+    const int st = threadIdx.x == 0 ? *(volatile int *)p.status : 0;
     if (p.forced > 0) {
-        const int S = min(p.forced, p.smax);
-        if (blockIdx.x == 0 && threadIdx.x == 0) *p.S = S;
-        return S;
+        if (threadIdx.x == 0) {
+            s_S = st ? 0 : min(p.forced, p.smax);
+            if (blockIdx.x == 0 && s_S) *p.S = s_S;
+        }
+        __syncthreads();
+        return s_S;
     }
+    // the partial i is handled by thread i mod nt, in increasing i: the
+    // same sums in the same order whichever branch runs
+    const bool regs = p.npa <= R * nt && p.npb <= R * nt;   // uniform
+    float pa[R][3], pb[R][3];
     int ea = -100000, eb = -100000;
-    for (int i = threadIdx.x; i < p.npa; i += blockDim.x) ea = max(ea, (int)__ldcg(p.gpa + 3 * i));
-    for (int i = threadIdx.x; i < p.npb; i += blockDim.x) eb = max(eb, (int)__ldcg(p.gpb + 3 * i));
+    if (regs) {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int i = threadIdx.x + r * nt;
+            const bool va = i < p.npa, vb = i < p.npb;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                pa[r][c] = va ? __ldcg(p.gpa + 3 * i + c) : 0.f;
+                pb[r][c] = vb ? __ldcg(p.gpb + 3 * i + c) : 0.f;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int i = threadIdx.x + r * nt;
+            if (i < p.npa) ea = max(ea, (int)pa[r][0]);
+            if (i < p.npb) eb = max(eb, (int)pb[r][0]);
+        }
+    } else {
+        for (int i = threadIdx.x; i < p.npa; i += nt) ea = max(ea, (int)__ldcg(p.gpa + 3 * i));
+        for (int i = threadIdx.x; i < p.npb; i += nt) eb = max(eb, (int)__ldcg(p.gpb + 3 * i));
+    }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
         ea = max(ea, __shfl_xor_sync(0xffffffffu, ea, o));
@@ -620,17 +676,40 @@ __device__ int oz_choose_S(const OzParams &p)
     __syncthreads();
     for (int w = 0; w < nw; w++) { ea = max(ea, s_e[0][w]); eb = max(eb, s_e[1][w]); }
     float v[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int i = threadIdx.x; i < p.npa; i += blockDim.x) {
-        const int d = 2 * ((int)__ldcg(p.gpa + 3 * i) - ea);
-        const float w = d < -126 ? 0.f : __int_as_float((127 + d) << 23);
-        v[0] = fmaf(w, __ldcg(p.gpa + 3 * i + 1), v[0]);
-        v[1] = fmaf(w, __ldcg(p.gpa + 3 * i + 2), v[1]);
-    }
-    for (int i = threadIdx.x; i < p.npb; i += blockDim.x) {
-        const int d = 2 * ((int)__ldcg(p.gpb + 3 * i) - eb);
-        const float w = d < -126 ? 0.f : __int_as_float((127 + d) << 23);
-        v[2] = fmaf(w, __ldcg(p.gpb + 3 * i + 1), v[2]);
-        v[3] = fmaf(w, __ldcg(p.gpb + 3 * i + 2), v[3]);
+    auto weight = [](int e, int em) {
+        const int d = 2 * (e - em);
+        return d < -126 ? 0.f : __int_as_float((127 + d) << 23);
+    };
+    if (regs) {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int i = threadIdx.x + r * nt;
+            if (i < p.npa) {
+                const float w = weight((int)pa[r][0], ea);
+                v[0] = fmaf(w, pa[r][1], v[0]);
+                v[1] = fmaf(w, pa[r][2], v[1]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int i = threadIdx.x + r * nt;
+            if (i < p.npb) {
+                const float w = weight((int)pb[r][0], eb);
+                v[2] = fmaf(w, pb[r][1], v[2]);
+                v[3] = fmaf(w, pb[r][2], v[3]);
+            }
+        }
+    } else {
+        for (int i = threadIdx.x; i < p.npa; i += nt) {
+            const float w = weight((int)__ldcg(p.gpa + 3 * i), ea);
+            v[0] = fmaf(w, __ldcg(p.gpa + 3 * i + 1), v[0]);
+            v[1] = fmaf(w, __ldcg(p.gpa + 3 * i + 2), v[1]);
+        }
+        for (int i = threadIdx.x; i < p.npb; i += nt) {
+            const float w = weight((int)__ldcg(p.gpb + 3 * i), eb);
+            v[2] = fmaf(w, __ldcg(p.gpb + 3 * i + 1), v[2]);
+            v[3] = fmaf(w, __ldcg(p.gpb + 3 * i + 2), v[3]);
+        }
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
@@ -647,8 +726,8 @@ __device__ int oz_choose_S(const OzParams &p)
         const float gb = t[3] > 0.f ? 0.5f * __log2f(t[2] * (float)p.K / t[3]) : 0.f;
         int S = (int)ceilf((p.tol_bits + ga + gb + 1.5f) / 5.0f);
         S = max(1, min(p.smax, S));
-        s_S = S;
-        if (blockIdx.x == 0) *p.S = S;
+        s_S = st ? 0 : S;
+        if (blockIdx.x == 0 && !st) *p.S = S;
     }
     __syncthreads();
     return s_S;
@@ -727,6 +806,8 @@ template <int CH>
 __device__ __forceinline__ void tmem_ld_chunk(uint32_t taddr, uint32_t (&r)[CH]);
 template <>
 __device__ __forceinline__ void tmem_ld_chunk<8>(uint32_t taddr, uint32_t (&r)[8]) { tmem_ld_32x32b_x8(taddr, r); }
+template <>
+__device__ __forceinline__ void tmem_ld_chunk<4>(uint32_t taddr, uint32_t (&r)[4]) { tmem_ld_32x32b_x4(taddr, r); }
 
 // d * 2^sh as a signed 128-bit (lo, hi) pair, 0 <= sh <= 70 (sh is uniform
 // across the warp: every lane drains the same diagonal)
@@ -847,7 +928,7 @@ __device__ __forceinline__ OzAlpha oz_alpha_split(double alpha, double beta)
     return a;
 }
 
-// One Horner step v = 32 v + D for each of the OZS_DCOLS-wide row segment
+// One Horner step v = 32 v + D for each element of a drain thread's row segment
 // (D: FP32 accumulator values below 2^22, decoded off the FP64 pipe).
 template <int N>
 __device__ __forceinline__ void oz_horner(long long (&v)[N], const uint32_t (&r)[N])
@@ -924,6 +1005,49 @@ __device__ __forceinline__ double oz_result_split(long long vh, long long vl, in
     const unsigned long long nlo = lo + (unsigned long long)vl;
     hi = hi + (vl >> 63) + (nlo < lo ? 1 : 0);
     return oz_result(nlo, hi, e, alpha, as, beta, cold);
+}
+
+// The drain conversion of a row segment of N elements (V = vh * 2^lsh + vl
+// each, scale 2^(erow + ecol[j])): the common case of oz_result_split with
+// no control flow inside, for a given alpha form (POW2) and beta (BETA), so
+// that the FP64 chains of the N elements (addition, then beta multiply-add:
+// about 64 cycles each) overlap; with a branch in each element they ran one
+// after another, and the row took twice as long.  Returns true when some
+// part left the normal range: the caller then converts the segment again by
+// oz_result_split, whose 128-bit route handles it.
+template <bool POW2, bool BETA, int N>
+__device__ __forceinline__ bool oz_convert_segment(double *res, const long long *vh, const long long *vl, int lsh,
+                                                   int erow, const int *ecol, double alpha, const OzAlpha &as,
+                                                   double beta, const double *cold)
+{
+    bool bad = false;
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        const int e = erow + ecol[j] + (POW2 ? as.ea : 0);
+        int ebh, ebl;
+        double dh = oz_i53_ldexp(vh[j], e + lsh, ebh);
+        double dl = oz_i53_ldexp(vl[j], e, ebl);
+        bad |= (unsigned)(ebh - 1) > 2044u || (unsigned)(ebl - 1) > 2044u;
+        double r;
+        if constexpr (POW2) {
+            dh = __longlong_as_double(__double_as_longlong(dh) ^ (long long)as.sign);
+            dl = __longlong_as_double(__double_as_longlong(dl) ^ (long long)as.sign);
+            r = dh + dl;
+        } else {
+            r = alpha * (dh + dl);
+        }
+        res[j] = BETA ? fma(beta, cold[j], r) : r;
+    }
+    return bad;
+}
+
+// oz_result_split out of line, for the rare segments oz_convert_segment
+// leaves (inlined at each element of a drain thread, the 128-bit route
+// raised the register count past the small-K kernel's budget)
+__device__ __noinline__ double oz_result_split_slow(long long vh, long long vl, int lsh, int e, double alpha,
+                                                    OzAlpha as, double beta, double cold)
+{
+    return oz_result_split(vh, vl, lsh, e, alpha, as, beta, cold);
 }
 
 template <int NCOL, int CH>
@@ -1216,13 +1340,16 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 // rounds V once (oz_result_split).  Tiles are ordered column-fastest so the
 // CTAs sharing an A row block run together and its slices come from L2.
 // Warp 0: TMA; warp 1: MMA issuer; warps 2..17: drain (four per TMEM lane
-// quarter, 8 columns each: the per-element conversion work of one tile is
+// quarter, BN/4 columns each: the per-element conversion work of one tile is
 // what bounds a CTA with several tiles, so it gets most of the warps).  The
 // accumulators are released before C is written, so the next tile's MMAs
 // overlap that work.
+// Tiles are 128 x BN, BN = 32, or 16 when the 32-wide tiles would occupy at
+// most half the SMs: a call that small is one tile per CTA, and its time is
+// the tile's chain (loads, MMAs, drain); half-width tiles halve the drain
+// (the longest step: 8 conversions per thread) and double the CTAs at work.
 constexpr int OZS_BN = 32, OZS_AMAX = 8, OZS_BSTG = 2, OZS_DRAIN_WARPS = 16;
-constexpr int OZS_DCOLS = OZS_BN / (OZS_DRAIN_WARPS / 4);   // columns per drain thread
-constexpr int OZS_B_BYTES = OZS_BN * OZ_BK;                 // 4 KB: one slice's 32 rows
+constexpr int OZS_B_BYTES = OZS_BN * OZ_BK;                 // 4 KB: one slice's 32 rows (BN = 32)
 constexpr int OZS_THREADS = 64 + 32 * OZS_DRAIN_WARPS;
 // Dynamic shared memory: the two B stages (S x 4 KB each) and as many 16 KB
 // A stages as fit (8 for S <= 10, 6 for S = 14), barriers at the end.
@@ -1233,9 +1360,13 @@ constexpr int OZS_KMAX = 1024;
 static_assert((long long)OZ_SMAX * OZS_KMAX * 256 < (1LL << 22), "small-K diagonal sums must stay below 2^22");
 static_assert(OZ_SMAX * OZS_BN <= 512, "small-K accumulators must fit TMEM");
 
+template <int BN>
 __global__ void __launch_bounds__(OZS_THREADS, 1)
 oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
 {
+    static_assert(BN == 16 || BN == 32, "tile width: MMA N = BN (S - s) must be a multiple of 16");
+    constexpr int DCOLS = BN / (OZS_DRAIN_WARPS / 4);   // columns per drain thread
+    constexpr int B_BYTES = BN * OZ_BK;                 // one slice's BN rows
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + OZS_DATA);
@@ -1269,7 +1400,8 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     // above overlaps its tail; its slices, scales and S are complete and
     // visible after this wait (a no-op for an ordinary launch).
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    if (oz_skip_kernel(p)) {
+    const int S = oz_choose_S(p);   // 0: skip this call
+    if (S == 0) {
         if (warp == 1) {
             tc_fence_after();
             tmem_dealloc(tmem_base, 512);
@@ -1277,11 +1409,9 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         oz_report(p);
         return;
     }
-
-    const int S = oz_choose_S(p);
     const int nkb = p.Kp / OZ_BK;
     // B stages first (S slices of 4 KB each), then the A ring
-    const int bstage = S * OZS_B_BYTES;
+    const int bstage = S * B_BYTES;
     uint8_t *sB = smem;
     uint8_t *sA = smem + OZS_BSTG * bstage;
     const int nA = min(OZS_AMAX, (int)((OZS_DATA - (size_t)OZS_BSTG * bstage) / OZ_A_BYTES));
@@ -1295,14 +1425,14 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int tm = t / p.tiles_n, tn = t % p.tiles_n;
-                if (!tile_needed(p, tm, tn, OZ_BM, OZS_BN)) continue;
+                if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
                 for (int kb = 0; kb < nkb && ok; kb++) {
                     // the B stage: slices 0..S-1 of the tile's 32 columns, side by side
                     if (!mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
-                    mbar_arrive_expect_tx(&fullB[bs], (uint32_t)(S * OZS_B_BYTES));
+                    mbar_arrive_expect_tx(&fullB[bs], (uint32_t)(S * B_BYTES));
                     for (int tb = 0; tb < S; tb++)
-                        tma_load_2d(sB + bs * bstage + tb * OZS_B_BYTES, &tmB, &fullB[bs], kb * OZ_BK,
-                                    tb * p.Np + tn * OZS_BN);
+                        tma_load_2d(sB + bs * bstage + tb * B_BYTES, &tmB, &fullB[bs], kb * OZ_BK,
+                                    tb * p.Np + tn * BN);
                     if (++bs == OZS_BSTG) { bs = 0; bp ^= 1u; }
                     // then the A slices
                     for (int sa = 0; sa < S; sa++) {
@@ -1332,7 +1462,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int tm = t / p.tiles_n, tn = t % p.tiles_n;
-                if (!tile_needed(p, tm, tn, OZ_BM, OZS_BN)) continue;
+                if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
                 // the previous tile's sums have been read out of TMEM
                 if (!mbar_wait(tempty, tp ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
                 tc_fence_after();
@@ -1345,11 +1475,11 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                         tc_fence_after();
                         const uint32_t a_addr = a_base + as * OZ_A_BYTES;
                         // A_s against B_0..B_{S-1-s}: columns 32s.. of TMEM, N <= 256 per MMA
-                        const int ntot = OZS_BN * (S - sa);
+                        const int ntot = BN * (S - sa);
                         for (int c0 = 0; c0 < ntot; c0 += 256) {
                             const int n = min(256, ntot - c0);
                             const uint32_t idesc = idesc_e4m3_f32(OZ_BM, n);
-                            const uint32_t d_tmem = tmem_base + (uint32_t)(OZS_BN * sa + c0);
+                            const uint32_t d_tmem = tmem_base + (uint32_t)(BN * sa + c0);
 #pragma unroll
                             for (int kk = 0; kk < OZ_BK / 32; kk++)
                                 // the first k block's s = 0 products start every diagonal
@@ -1372,7 +1502,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     } else {
         // ---------------- drain (warps 2..17) ----------------
         const int quarter = warp & 3;               // TMEM lane window of this warp
-        const int cg = (warp - 2) >> 2;             // columns cg*OZS_DCOLS .. of the tile
+        const int cg = (warp - 2) >> 2;             // columns cg*DCOLS .. of the tile
         const int row = quarter * 32 + lane;
         const OzAlpha as = oz_alpha_split(p.alpha, p.beta);
         const int g = (S + 1) >> 1;                 // diagonals of the high half
@@ -1381,16 +1511,16 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         bool ok = true;
         for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
             const int tm = t / p.tiles_n, tn = t % p.tiles_n;
-            if (!tile_needed(p, tm, tn, OZ_BM, OZS_BN)) continue;
+            if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
             // this row's C values and scale exponents, loaded while the MMAs run
             const int grow = tm * OZ_BM + row;
             const bool row_ok = grow < p.M;
-            const int gc0 = tn * OZS_BN + cg * OZS_DCOLS;
+            const int gc0 = tn * BN + cg * DCOLS;
             double *cp = p.C + (size_t)gc0 * p.ldc + grow;
-            double cold[OZS_DCOLS];
-            int ecol[OZS_DCOLS];
+            double cold[DCOLS];
+            int ecol[DCOLS];
 #pragma unroll
-            for (int j = 0; j < OZS_DCOLS; j++) {
+            for (int j = 0; j < DCOLS; j++) {
                 cold[j] = (row_ok && as.beta_on && oz_c_keep(p, grow, gc0 + j)) ? cp[(size_t)j * p.ldc] : 0.0;
                 ecol[j] = __ldg(p.col_exp + gc0 + j);
             }
@@ -1400,15 +1530,15 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             if (!ok) break;
             tc_fence_after();
             tp ^= 1u;
-            long long vh[OZS_DCOLS], vl[OZS_DCOLS];
+            long long vh[DCOLS], vl[DCOLS];
 #pragma unroll
-            for (int j = 0; j < OZS_DCOLS; j++) { vh[j] = 0; vl[j] = 0; }
-            const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cg * OZS_DCOLS);
+            for (int j = 0; j < DCOLS; j++) { vh[j] = 0; vl[j] = 0; }
+            const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cg * DCOLS);
             // two diagonals per TMEM round trip; q < g folds into the high half
             for (int q = 0; q < S; q += 2) {
-                uint32_t r0[OZS_DCOLS], r1[OZS_DCOLS];
-                tmem_ld_32x32b_x8(tbase + (uint32_t)(q * OZS_BN), r0);
-                if (q + 1 < S) tmem_ld_32x32b_x8(tbase + (uint32_t)((q + 1) * OZS_BN), r1);
+                uint32_t r0[DCOLS], r1[DCOLS];
+                tmem_ld_chunk<DCOLS>(tbase + (uint32_t)(q * BN), r0);
+                if (q + 1 < S) tmem_ld_chunk<DCOLS>(tbase + (uint32_t)((q + 1) * BN), r1);
                 tmem_ld_wait();
                 if (q < g) oz_horner(vh, r0);
                 else oz_horner(vl, r0);
@@ -1418,13 +1548,33 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             tc_fence_before();
             mbar_arrive(tempty);   // TMEM free: the next tile's MMAs may start
             if (row_ok) {
-                double res[OZS_DCOLS];
+                // V = vh * 2^lsh + vl, converted and stored four elements at a
+                // time (fewer values live at once: no spills at 96 registers)
+                constexpr int SEG = DCOLS < 4 ? DCOLS : 4;
 #pragma unroll
-                for (int j = 0; j < OZS_DCOLS; j++)   // V = vh * 2^lsh + vl
-                    res[j] = oz_result_split(vh[j], vl[j], lsh, erow + ecol[j], p.alpha, as, p.beta, cold[j]);
+                for (int h = 0; h < DCOLS; h += SEG) {
+                    double res[SEG];
+                    bool bad;
+                    if (as.pow2)
+                        bad = as.beta_on ? oz_convert_segment<true, true, SEG>(res, vh + h, vl + h, lsh, erow, ecol + h,
+                                                                              p.alpha, as, p.beta, cold + h)
+                                         : oz_convert_segment<true, false, SEG>(res, vh + h, vl + h, lsh, erow, ecol + h,
+                                                                               p.alpha, as, p.beta, cold + h);
+                    else
+                        bad = as.beta_on ? oz_convert_segment<false, true, SEG>(res, vh + h, vl + h, lsh, erow, ecol + h,
+                                                                               p.alpha, as, p.beta, cold + h)
+                                         : oz_convert_segment<false, false, SEG>(res, vh + h, vl + h, lsh, erow,
+                                                                                ecol + h, p.alpha, as, p.beta, cold + h);
+                    if (bad) {   // a part outside the normal range: the 128-bit route
 #pragma unroll
-                for (int j = 0; j < OZS_DCOLS; j++)
-                    if (oz_c_keep(p, grow, gc0 + j)) cp[(size_t)j * p.ldc] = res[j];
+                        for (int j = 0; j < SEG; j++)
+                            res[j] = oz_result_split_slow(vh[h + j], vl[h + j], lsh, erow + ecol[h + j], p.alpha, as,
+                                                          p.beta, cold[h + j]);
+                    }
+#pragma unroll
+                    for (int j = 0; j < SEG; j++)
+                        if (oz_c_keep(p, grow, gc0 + h + j)) cp[(size_t)(h + j) * p.ldc] = res[j];
+                }
             }
         }
     }
@@ -1848,7 +1998,9 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     if (pr.K > 0x3fffffff) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: K too large");
     const bool pair = oz_use_pair(pr.M);
     const bool small_k = !pair && rup(std::max(pr.K, 1), OZ_BK) <= OZS_KMAX && oz_small_k(pr.K);
-    const int bn = small_k ? OZS_BN : oz_tile_n(pr.M, pr.N, gbx_ctx_sms(ctx), pair);
+    const long long sk_tiles = ((long long)pr.M + OZ_BM - 1) / OZ_BM * (((long long)pr.N + OZS_BN - 1) / OZS_BN);
+    const int bn = small_k ? (2 * sk_tiles <= gbx_ctx_sms(ctx) ? OZS_BN / 2 : OZS_BN)
+                           : oz_tile_n(pr.M, pr.N, gbx_ctx_sms(ctx), pair);
     const int Mp = (int)rup(pr.M, pair ? OZ2_BM : OZ_BM), Np = (int)rup(pr.N, bn);
     const int Kp = (int)rup(std::max(pr.K, 1), OZ_BK);
     if (tol <= 0.0) tol = 1e-14;
@@ -1897,7 +2049,10 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         if (blocks > 0x7fffffffLL) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: operands too large");
         oa.gpart = b.gpart;
         ob.gpart = b.gpart + 3 * (size_t)(Mp / OZ_SPLIT_ROWS);
-        oz_prep_small<<<(unsigned)blocks, OZ_SMALL_THREADS, 0, s>>>(oa, ob, planes, b.status);
+        if (blocks <= gbx_ctx_sms(ctx))
+            oz_prep_small<2 * OZ_SMALL_THREADS><<<(unsigned)blocks, 2 * OZ_SMALL_THREADS, 0, s>>>(oa, ob, planes, b.status);
+        else
+            oz_prep_small<OZ_SMALL_THREADS><<<(unsigned)blocks, OZ_SMALL_THREADS, 0, s>>>(oa, ob, planes, b.status);
         gbx_count_launch(ctx, 1);
         if ((st = gbx_check_launch(ctx, "ozaki prepare")) != GBX_OK) return st;
     } else if ((st = oz_prepare(ctx, oa, ob, b_stats, tol, forced, b.status, (unsigned *)(b.S + 4), b.S)) !=
@@ -1942,7 +2097,9 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         std::lock_guard<std::mutex> lk(attr_mu);
         max_pairs = (dev >= 0 && dev < 64) ? max_pairs_of[dev] : 0;
         if (max_pairs == 0) {
-            if (cudaFuncSetAttribute(oz_gemm_sk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            if (cudaFuncSetAttribute(oz_gemm_sk_kernel<OZS_BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)OZS_SMEM) != cudaSuccess ||
+                cudaFuncSetAttribute(oz_gemm_sk_kernel<OZS_BN / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OZS_SMEM) != cudaSuccess ||
                 cudaFuncSetAttribute(oz_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OzCfg<256>::SMEM) != cudaSuccess ||
@@ -1984,7 +2141,8 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
             attr[0].val.programmaticStreamSerializationAllowed = 1;
             cfg.attrs = attr;
             cfg.numAttrs = 1;
-            const cudaError_t le = cudaLaunchKernelEx(&cfg, oz_gemm_sk_kernel, tmA, tmB, p);
+            const cudaError_t le = bn == OZS_BN ? cudaLaunchKernelEx(&cfg, oz_gemm_sk_kernel<OZS_BN>, tmA, tmB, p)
+                                                : cudaLaunchKernelEx(&cfg, oz_gemm_sk_kernel<OZS_BN / 2>, tmA, tmB, p);
             if (le != cudaSuccess) {
                 cudaGetLastError();
                 return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki gemm: %s", cudaGetErrorString(le));
