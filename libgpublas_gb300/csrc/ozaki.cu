@@ -132,6 +132,21 @@ struct SsAcc {
         const float y = __int_as_float(((127 - d) << 23) | (int)((b >> 29) & 0x7FFFFFull));
         ss = fmaf(y, y, ss);
     }
+    // the same with selects instead of branches, so that a thread's elements
+    // are not separated by control flow (more instructions, more overlap:
+    // faster where a few blocks run alone, slower where the SMs are full)
+    __device__ __forceinline__ void add_sel(unsigned long long b)
+    {
+        maxb = b > maxb ? b : maxb;
+        const int E = (int)(b >> 52);   // zeros and subnormals (E = 0) do not move the estimate
+        const bool up = E > mref;       // never for E = 0 (mref >= 0)
+        ss = up ? scale(ss, mref - E) : ss;
+        mref = up ? E : mref;
+        const int d = mref - E;
+        const float y = __int_as_float(((127 - min(d, 64)) << 23) | (int)((b >> 29) & 0x7FFFFFull));
+        const float t = fmaf(y, y, ss);
+        ss = (E == 0 || d > 60) ? ss : t;
+    }
     __device__ __forceinline__ void merge(const SsAcc &o)
     {
         maxb = o.maxb > maxb ? o.maxb : maxb;
@@ -381,7 +396,7 @@ constexpr int OZ_SMALL_THREADS = 256;
 // tile already staged by the caller (one-launch path, K <= 128); expo_s: the
 // 16 rows' exponents in the caller's shared memory (one-launch path), else
 // they are read from expo
-template <int PER>
+template <int PER, bool SEL = false>
 __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K, int Rp, int Kp, const int *expo,
                                               int S, uint8_t *X8, int blk, const double (*pre)[129] = nullptr,
                                               const int *expo_s = nullptr)
@@ -414,6 +429,9 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
     const int top = 4 - e + 5 * (S - 1);
     unsigned long long lo[PER], hi[PER];
     unsigned neg = 0u;
+    // (SEL: with selects instead of branches, so that the elements of a
+    // thread are not separated by control flow and their integer chains
+    // overlap; more instructions, so only where few blocks run)
 #pragma unroll
     for (int j = 0; j < PER; j++) {
         const unsigned long long b = (unsigned long long)__double_as_longlong(T[rr][kq + j]);
@@ -421,11 +439,21 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
         const int E = (int)((b >> 52) & 0x7FF);
         const unsigned long long M = (b & 0xFFFFFFFFFFFFFull) | (E ? (1ull << 52) : 0ull);
         const int sh = (E ? E : 1) - 1075 + top;
-        if (M == 0ull || sh <= -54) { lo[j] = 0ull; hi[j] = 0ull; }
-        else if (sh < 0) { lo[j] = (M + (1ull << (-sh - 1))) >> (-sh); hi[j] = 0ull; }
-        else if (sh == 0) { lo[j] = M; hi[j] = 0ull; }
-        else if (sh < 64) { lo[j] = M << sh; hi[j] = M >> (64 - sh); }
-        else { lo[j] = 0ull; hi[j] = M << (sh - 64); }
+        if constexpr (!SEL) {
+            if (M == 0ull || sh <= -54) { lo[j] = 0ull; hi[j] = 0ull; }
+            else if (sh < 0) { lo[j] = (M + (1ull << (-sh - 1))) >> (-sh); hi[j] = 0ull; }
+            else if (sh == 0) { lo[j] = M; hi[j] = 0ull; }
+            else if (sh < 64) { lo[j] = M << sh; hi[j] = M >> (64 - sh); }
+            else { lo[j] = 0ull; hi[j] = M << (sh - 64); }
+            continue;
+        }
+        // sh < 0: M * 2^sh rounded half up (0 for sh <= -54; M = 0 gives 0);
+        // sh >= 0: M << sh in 128 bits (sh <= 69)
+        const int rs = max(1, min(-sh, 63));
+        const unsigned long long mr = sh < 0 ? (sh <= -54 ? 0ull : (M + (1ull << (rs - 1))) >> rs) : M;
+        const int ls = max(sh, 0);
+        lo[j] = ls < 64 ? mr << (ls & 63) : 0ull;
+        hi[j] = ls == 0 ? 0ull : (ls < 64 ? mr >> ((64 - ls) & 63) : mr << ((ls - 64) & 63));
     }
     // Balanced base-32 digits d_s in [-16, 16] with N = sum_s d_s 32^(S-1-s):
     // adding C = 16 * sum_{s<S} 32^s once turns every 5-bit chunk c of N + C
@@ -437,28 +465,36 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
         if (b < 64) clo |= 1ull << b;
         else chi |= 1ull << (b - 64);
     }
+    // N + C as three 32-bit words (N + C < 2^71)
+    uint32_t w0[PER], w1[PER], w2[PER];
 #pragma unroll
     for (int j = 0; j < PER; j++) {
         const unsigned long long nl = lo[j] + clo;
-        hi[j] = hi[j] + chi + (nl < clo ? 1ull : 0ull);
-        lo[j] = nl;
+        const unsigned long long nh = hi[j] + chi + (nl < clo ? 1ull : 0ull);
+        w0[j] = (uint32_t)nl;
+        w1[j] = (uint32_t)(nl >> 32);
+        w2[j] = (uint32_t)nh;
     }
-    for (int s = S - 1; s >= 0; s--) {
-        const int sh = 5 * (S - 1 - s);   // plane s holds the chunk at bit sh
-        const unsigned mask = s == 0 ? 63u : 31u;
+    // chunk t (bit 5t, from the low end) is the digit of plane S - 1 - t;
+    // unrolled over t so that its word and bit offset are constants (one
+    // funnel shift per chunk)
+#pragma unroll
+    for (int t = 0; t < OZ_SMAX; t++) {
+        if (t >= S) break;
+        const int sh = 5 * t, wk = sh >> 5, off = sh & 31;
+        const uint32_t mask = t == S - 1 ? 63u : 31u;
         uint32_t w[PER / 4] = {};
 #pragma unroll
         for (int j = 0; j < PER; j++) {
-            unsigned c;
-            if (sh == 0) c = (unsigned)lo[j];
-            else if (sh < 64) c = (unsigned)((lo[j] >> sh) | (hi[j] << (64 - sh)));
-            else c = (unsigned)(hi[j] >> (sh - 64));
-            const int d = (int)(c & mask) - 16;
-            // the digit of x = sign(x) * d, as an E4M3 byte from the table
-            const int idx = ((neg >> j) & 1u) ? 16 - d : 16 + d;
+            uint32_t c = wk == 0 ? __funnelshift_r(w0[j], w1[j], off)
+                                 : (wk == 1 ? __funnelshift_r(w1[j], w2[j], off) : w2[j] >> off);
+            c &= mask;
+            // the digit of x = sign(x) * (c - 16) as an E4M3 byte from the
+            // table, at [16 + digit]
+            const int idx = ((neg >> j) & 1u) ? 32 - (int)c : (int)c;
             w[j >> 2] |= e4m3_tbl[idx] << (8 * (j & 3));
         }
-        uint8_t *dst = X8 + ((size_t)s * Rp + r) * Kp + k0 + kq;
+        uint8_t *dst = X8 + ((size_t)(S - 1 - t) * Rp + r) * Kp + k0 + kq;
         if constexpr (PER == 8) *(uint2 *)dst = make_uint2(w[0], w[PER / 4 - 1]);
         else *(uint32_t *)dst = w[0];
     }
@@ -507,12 +543,15 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
         }
         __syncthreads();
         if (threadIdx.x < 256) {   // warp-uniform: the first eight warps
+            bool nonfinite = false;
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const unsigned long long b = abs_bits(tile[rr][lane16 + 16 * j]);
-                flag_nonfinite(b, status);
-                acc.add(b);
+                nonfinite |= (b >> 52) == 0x7FFull;
+                if constexpr (THREADS == 512) acc.add_sel(b);
+                else acc.add(b);
             }
+            if (nonfinite) atomicCAS(status, 0, OZ_NONFINITE);
         }
         __syncthreads();
     }
@@ -567,10 +606,11 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
     }
     const int kblocks = Kp / 128;
     if (kblocks == 1)   // the statistics pass left this block's only tile in shared memory
-        oz_split_tile<PER>(v, rows, K, Rp, Kp, expo, planes, X8, rblk, tile, s_ex);
+        oz_split_tile<PER, THREADS == 512>(v, rows, K, Rp, Kp, expo, planes, X8, rblk, tile, s_ex);
     else
         for (int kb = 0; kb < kblocks; kb++)
-            oz_split_tile<PER>(v, rows, K, Rp, Kp, expo, planes, X8, rblk * kblocks + kb, nullptr, s_ex);
+            oz_split_tile<PER, THREADS == 512>(v, rows, K, Rp, Kp, expo, planes, X8, rblk * kblocks + kb, nullptr,
+                                               s_ex);
 }
 
 template <int THREADS>
@@ -674,7 +714,13 @@ __device__ int oz_choose_S(const OzParams &p)
     }
     if (lane == 0) { s_e[0][warp] = ea; s_e[1][warp] = eb; }
     __syncthreads();
-    for (int w = 0; w < nw; w++) { ea = max(ea, s_e[0][w]); eb = max(eb, s_e[1][w]); }
+    ea = lane < nw ? s_e[0][lane] : -100000;   // nw <= 32
+    eb = lane < nw ? s_e[1][lane] : -100000;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        ea = max(ea, __shfl_xor_sync(0xffffffffu, ea, o));
+        eb = max(eb, __shfl_xor_sync(0xffffffffu, eb, o));
+    }
     float v[4] = {0.f, 0.f, 0.f, 0.f};
     auto weight = [](int e, int em) {
         const int d = 2 * (e - em);
@@ -718,16 +764,22 @@ __device__ int oz_choose_S(const OzParams &p)
         if (lane == 0) s_v[j][warp] = v[j];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float t[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int w = 0; w < nw; w++)
-            for (int j = 0; j < 4; j++) t[j] += s_v[j][w];
-        const float ga = t[1] > 0.f ? 0.5f * __log2f(t[0] * (float)p.K / t[1]) : 0.f;
-        const float gb = t[3] > 0.f ? 0.5f * __log2f(t[2] * (float)p.K / t[3]) : 0.f;
-        int S = (int)ceilf((p.tol_bits + ga + gb + 1.5f) / 5.0f);
-        S = max(1, min(p.smax, S));
-        s_S = st ? 0 : S;
-        if (blockIdx.x == 0 && !st) *p.S = S;
+    if (warp == 0) {
+        float t[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            t[j] = lane < nw ? s_v[j][lane] : 0.f;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) t[j] += __shfl_xor_sync(0xffffffffu, t[j], o);
+        }
+        if (lane == 0) {
+            const float ga = t[1] > 0.f ? 0.5f * __log2f(t[0] * (float)p.K / t[1]) : 0.f;
+            const float gb = t[3] > 0.f ? 0.5f * __log2f(t[2] * (float)p.K / t[3]) : 0.f;
+            int S = (int)ceilf((p.tol_bits + ga + gb + 1.5f) / 5.0f);
+            S = max(1, min(p.smax, S));
+            s_S = st ? 0 : S;
+            if (blockIdx.x == 0 && !st) *p.S = S;
+        }
     }
     __syncthreads();
     return s_S;
@@ -1534,16 +1586,33 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
             for (int j = 0; j < DCOLS; j++) { vh[j] = 0; vl[j] = 0; }
             const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cg * DCOLS);
-            // two diagonals per TMEM round trip; q < g folds into the high half
-            for (int q = 0; q < S; q += 2) {
-                uint32_t r0[DCOLS], r1[DCOLS];
-                tmem_ld_chunk<DCOLS>(tbase + (uint32_t)(q * BN), r0);
-                if (q + 1 < S) tmem_ld_chunk<DCOLS>(tbase + (uint32_t)((q + 1) * BN), r1);
-                tmem_ld_wait();
-                if (q < g) oz_horner(vh, r0);
-                else oz_horner(vl, r0);
-                if (q + 1 < g) oz_horner(vh, r1);
-                else if (q + 1 < S) oz_horner(vl, r1);
+            // G diagonals per TMEM round trip (as many as the registers allow);
+            // q < g folds into the high half
+            if constexpr (DCOLS <= 4) {
+                constexpr int G = 4;
+                for (int q = 0; q < S; q += G) {
+                    uint32_t r[G][DCOLS];
+#pragma unroll
+                    for (int i = 0; i < G; i++)
+                        if (q + i < S) tmem_ld_chunk<DCOLS>(tbase + (uint32_t)((q + i) * BN), r[i]);   // uniform
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int i = 0; i < G; i++) {
+                        if (q + i < g) oz_horner(vh, r[i]);
+                        else if (q + i < S) oz_horner(vl, r[i]);
+                    }
+                }
+            } else {
+                for (int q = 0; q < S; q += 2) {
+                    uint32_t r0[DCOLS], r1[DCOLS];
+                    tmem_ld_chunk<DCOLS>(tbase + (uint32_t)(q * BN), r0);
+                    if (q + 1 < S) tmem_ld_chunk<DCOLS>(tbase + (uint32_t)((q + 1) * BN), r1);
+                    tmem_ld_wait();
+                    if (q < g) oz_horner(vh, r0);
+                    else oz_horner(vl, r0);
+                    if (q + 1 < g) oz_horner(vh, r1);
+                    else if (q + 1 < S) oz_horner(vl, r1);
+                }
             }
             tc_fence_before();
             mbar_arrive(tempty);   // TMEM free: the next tile's MMAs may start
