@@ -534,12 +534,36 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
     SsAcc acc;
     acc.init();
     for (int k0 = 0; k0 < K; k0 += 128) {
-        for (int t = threadIdx.x; t < OZ_SPLIT_ROWS * 128; t += blockDim.x) {
-            int tr, kk;
-            if (v.row_k) { kk = t & 127; tr = t >> 7; }
-            else         { tr = t % OZ_SPLIT_ROWS; kk = t / OZ_SPLIT_ROWS; }
-            const int r = r0 + tr, k = k0 + kk;
-            tile[tr][kk] = (r < rows && k < K) ? src_get(v, r, k) : 0.0;
+        if (!v.cplx && v.Ksplit >= K && r0 + OZ_SPLIT_ROWS <= rows && k0 + 128 <= K) {
+            // a full 16 x 128 block of a real operand (uniform): strided
+            // pointers, every load issued before the first store
+            constexpr int N = OZ_SPLIT_ROWS * 128 / THREADS;
+            double x[N];
+            if (v.row_k) {   // X[r * ld + k]: 128 consecutive k per row
+                constexpr int RS = THREADS / 128;
+                const int tr = threadIdx.x >> 7, kk = threadIdx.x & 127;
+                const double *src = v.X + (long long)(r0 + tr) * v.ld + k0 + kk;
+#pragma unroll
+                for (int i = 0; i < N; i++) x[i] = src[(long long)i * RS * v.ld];
+#pragma unroll
+                for (int i = 0; i < N; i++) tile[tr + i * RS][kk] = x[i];
+            } else {         // X[k * ld + r]: 16 consecutive rows per k
+                constexpr int KS = THREADS / OZ_SPLIT_ROWS;
+                const int tr = threadIdx.x & (OZ_SPLIT_ROWS - 1), kk = threadIdx.x / OZ_SPLIT_ROWS;
+                const double *src = v.X + (long long)(k0 + kk) * v.ld + r0 + tr;
+#pragma unroll
+                for (int i = 0; i < N; i++) x[i] = src[(long long)i * KS * v.ld];
+#pragma unroll
+                for (int i = 0; i < N; i++) tile[tr][kk + i * KS] = x[i];
+            }
+        } else {
+            for (int t = threadIdx.x; t < OZ_SPLIT_ROWS * 128; t += blockDim.x) {
+                int tr, kk;
+                if (v.row_k) { kk = t & 127; tr = t >> 7; }
+                else         { tr = t % OZ_SPLIT_ROWS; kk = t / OZ_SPLIT_ROWS; }
+                const int r = r0 + tr, k = k0 + kk;
+                tile[tr][kk] = (r < rows && k < K) ? src_get(v, r, k) : 0.0;
+            }
         }
         __syncthreads();
         if (threadIdx.x < 256) {   // warp-uniform: the first eight warps
@@ -614,7 +638,7 @@ __device__ __forceinline__ void oz_prep_rows(const SrcView &v, int rows, int K, 
 }
 
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS)
+__global__ void __launch_bounds__(THREADS, THREADS == 256 ? 4 : 1)
 oz_prep_small(OzPrepOp a, OzPrepOp b, int planes, int *status)
 {
     // the product kernel may be scheduled now: its set-up needs none of this
@@ -989,6 +1013,21 @@ __device__ __forceinline__ void oz_horner(long long (&v)[N], const uint32_t (&r)
     for (int j = 0; j < N; j++)
         v[j] = (long long)(((unsigned long long)v[j] << 5) +
                            (unsigned long long)(long long)oz_f2i22(__uint_as_float(r[j])));
+}
+
+// Two Horner steps at once, v = 1024 v + (32 D_a + D_b): the pair is formed
+// in 32-bit arithmetic (|32 D_a + D_b| < 2^28; the decode's offsets cancel
+// modulo 2^32), so the 64-bit shift-add runs once per two diagonals.
+template <int N>
+__device__ __forceinline__ void oz_horner2(long long (&v)[N], const uint32_t (&ra)[N], const uint32_t (&rb)[N])
+{
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        const uint32_t ba = __float_as_uint(__fadd_rn(__uint_as_float(ra[j]), 12582912.0f));
+        const uint32_t bb = __float_as_uint(__fadd_rn(__uint_as_float(rb[j]), 12582912.0f));
+        const int g = (int)(ba * 32u + bb - 33u * 0x4B400000u);
+        v[j] = (long long)(((unsigned long long)v[j] << 10) + (unsigned long long)(long long)g);
+    }
 }
 
 // v * 2^e as a double for |v| < 2^53 (exact), built on the integer pipe;
@@ -1526,18 +1565,22 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                         if (!mbar_wait(&fullA[as], ap, status, TC_TIMEOUT_FULL)) { ok = false; break; }
                         tc_fence_after();
                         const uint32_t a_addr = a_base + as * OZ_A_BYTES;
-                        // A_s against B_0..B_{S-1-s}: columns 32s.. of TMEM, N <= 256 per MMA
+                        // A_s against B_0..B_{S-1-s}: columns BN s.. of TMEM, N <= 256 per MMA.
+                        // Descriptors are built once per stage and advanced by 32 bytes
+                        // (2 in the address field) per k step: the issuing thread shares
+                        // its SMSP with four drain warps, so its instructions are few.
+                        const uint64_t a_d = smem_desc_k128(a_addr);
+                        // the first k block's s = 0 products start every diagonal
+                        const uint32_t acc0 = (kb == 0 && sa == 0) ? 0u : 1u;
                         const int ntot = BN * (S - sa);
                         for (int c0 = 0; c0 < ntot; c0 += 256) {
                             const int n = min(256, ntot - c0);
                             const uint32_t idesc = idesc_e4m3_f32(OZ_BM, n);
                             const uint32_t d_tmem = tmem_base + (uint32_t)(BN * sa + c0);
+                            const uint64_t b_d = smem_desc_k128(b_addr + (uint32_t)c0 * OZ_BK);
 #pragma unroll
                             for (int kk = 0; kk < OZ_BK / 32; kk++)
-                                // the first k block's s = 0 products start every diagonal
-                                mma_f8f6f4(d_tmem, smem_desc_k128(a_addr + kk * 32),
-                                           smem_desc_k128(b_addr + (uint32_t)c0 * OZ_BK + kk * 32), idesc,
-                                           (kb == 0 && sa == 0 && kk == 0) ? 0u : 1u);
+                                mma_f8f6f4(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, kk == 0 ? acc0 : 1u);
                         }
                         mma_commit(&emptyA[as]);
                         if (++as == nA) { as = 0; ap ^= 1u; }
@@ -1586,6 +1629,18 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 #pragma unroll
             for (int j = 0; j < DCOLS; j++) { vh[j] = 0; vl[j] = 0; }
             const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cg * DCOLS);
+            // diagonals qa and qa + 1 into the halves (q < g: high)
+            auto fold2 = [&](int qa, const uint32_t (&ra)[DCOLS], const uint32_t (&rb)[DCOLS]) {
+                if (qa + 1 < g) {
+                    oz_horner2(vh, ra, rb);
+                } else if (qa >= g) {
+                    if (qa + 1 < S) oz_horner2(vl, ra, rb);
+                    else if (qa < S) oz_horner(vl, ra);
+                } else {   // qa = g - 1
+                    oz_horner(vh, ra);
+                    if (qa + 1 < S) oz_horner(vl, rb);
+                }
+            };
             // G diagonals per TMEM round trip (as many as the registers allow);
             // q < g folds into the high half
             if constexpr (DCOLS <= 4) {
@@ -1597,10 +1652,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                         if (q + i < S) tmem_ld_chunk<DCOLS>(tbase + (uint32_t)((q + i) * BN), r[i]);   // uniform
                     tmem_ld_wait();
 #pragma unroll
-                    for (int i = 0; i < G; i++) {
-                        if (q + i < g) oz_horner(vh, r[i]);
-                        else if (q + i < S) oz_horner(vl, r[i]);
-                    }
+                    for (int i = 0; i < G; i += 2) fold2(q + i, r[i], r[i + 1]);
                 }
             } else {
                 for (int q = 0; q < S; q += 2) {
@@ -1608,14 +1660,26 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     tmem_ld_chunk<DCOLS>(tbase + (uint32_t)(q * BN), r0);
                     if (q + 1 < S) tmem_ld_chunk<DCOLS>(tbase + (uint32_t)((q + 1) * BN), r1);
                     tmem_ld_wait();
-                    if (q < g) oz_horner(vh, r0);
-                    else oz_horner(vl, r0);
-                    if (q + 1 < g) oz_horner(vh, r1);
-                    else if (q + 1 < S) oz_horner(vl, r1);
+                    fold2(q, r0, r1);
                 }
             }
             tc_fence_before();
             mbar_arrive(tempty);   // TMEM free: the next tile's MMAs may start
+            // The next tile's C segment goes into L1 now: its MMAs overlap
+            // this tile's conversion, so at its turn the loads of C would
+            // otherwise wait on L2 with nothing to overlap them.
+            if (as.beta_on && t + (int)gridDim.x < ntiles) {
+                const int t2 = t + (int)gridDim.x;
+                const int grow2 = (t2 / p.tiles_n) * OZ_BM + row;
+                const int gc2 = (t2 % p.tiles_n) * BN + cg * DCOLS;
+                if (grow2 < p.M) {
+                    const double *cp2 = p.C + (size_t)gc2 * p.ldc + grow2;
+#pragma unroll
+                    for (int j = 0; j < DCOLS; j++)
+                        if (oz_c_keep(p, grow2, gc2 + j))
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(cp2 + (size_t)j * p.ldc));
+                }
+            }
             if (row_ok) {
                 // V = vh * 2^lsh + vl, converted and stored four elements at a
                 // time (fewer values live at once: no spills at 96 registers)
