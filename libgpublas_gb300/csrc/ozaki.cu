@@ -1336,11 +1336,13 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                                 if (!mbar_wait(&full[stage], phase, status, TC_TIMEOUT_FULL)) { ok = false; break; }
                                 tc_fence_after();
                                 const uint32_t a_addr = smem_base + stage * STAGE_BYTES;
-                                const uint32_t b_addr = a_addr + OZ_A_BYTES;
+                                // descriptors built once per stage, advanced by 32 bytes
+                                // (2 in the address field) per k step
+                                const uint64_t a_d = smem_desc_k128(a_addr);
+                                const uint64_t b_d = smem_desc_k128(a_addr + OZ_A_BYTES);
 #pragma unroll
                                 for (int kk = 0; kk < OZ_BK / 32; kk++) {
-                                    mma_f8f6f4(d_tmem, smem_desc_k128(a_addr + kk * 32),
-                                               smem_desc_k128(b_addr + kk * 32), idesc, acc);
+                                    mma_f8f6f4(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, acc);
                                     acc = 1;
                                 }
                                 mma_commit(&empty[stage]);
