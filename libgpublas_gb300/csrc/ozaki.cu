@@ -403,11 +403,16 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
 {
     static_assert(PER == 4 || PER == 8, "split width");
     __shared__ double tile[OZ_SPLIT_ROWS][129];
-    __shared__ uint32_t e4m3_tbl[33];   // E4M3 byte of the digit d at [16 + d], d in [-16, 16]
+    // E4M3 byte of the digit c - 16 at [c] and of 16 - c at [40 + c], c in
+    // [0, 32]: a negative element reads the second table (no per-digit sign)
+    __shared__ uint32_t e4m3_tbl[80];
     const int kblocks = Kp / 128;
     const int r0 = (blk / kblocks) * OZ_SPLIT_ROWS, k0 = (blk % kblocks) * 128;
     __syncthreads();   // a previous call's readers of tile are done
-    if (threadIdx.x < 33) e4m3_tbl[threadIdx.x] = e4m3_of_digit((int)threadIdx.x - 16);
+    if (threadIdx.x < 33) {
+        e4m3_tbl[threadIdx.x] = e4m3_of_digit((int)threadIdx.x - 16);
+        e4m3_tbl[40 + threadIdx.x] = e4m3_of_digit(16 - (int)threadIdx.x);
+    }
     // load: col_k -> threads along rows; row_k -> threads along k
     if (!pre)
         for (int t = threadIdx.x; t < OZ_SPLIT_ROWS * 128; t += blockDim.x) {
@@ -475,6 +480,9 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
         w1[j] = (uint32_t)(nl >> 32);
         w2[j] = (uint32_t)nh;
     }
+    const uint32_t *tb[PER];   // each element's table (by its sign)
+#pragma unroll
+    for (int j = 0; j < PER; j++) tb[j] = e4m3_tbl + (((neg >> j) & 1u) ? 40 : 0);
     // chunk t (bit 5t, from the low end) is the digit of plane S - 1 - t;
     // unrolled over t so that its word and bit offset are constants (one
     // funnel shift per chunk)
@@ -489,10 +497,8 @@ __device__ __forceinline__ void oz_split_tile(const SrcView &v, int rows, int K,
             uint32_t c = wk == 0 ? __funnelshift_r(w0[j], w1[j], off)
                                  : (wk == 1 ? __funnelshift_r(w1[j], w2[j], off) : w2[j] >> off);
             c &= mask;
-            // the digit of x = sign(x) * (c - 16) as an E4M3 byte from the
-            // table, at [16 + digit]
-            const int idx = ((neg >> j) & 1u) ? 32 - (int)c : (int)c;
-            w[j >> 2] |= e4m3_tbl[idx] << (8 * (j & 3));
+            // the digit of x = sign(x) * (c - 16) as an E4M3 byte
+            w[j >> 2] |= tb[j][c] << (8 * (j & 3));
         }
         uint8_t *dst = X8 + ((size_t)(S - 1 - t) * Rp + r) * Kp + k0 + kq;
         if constexpr (PER == 8) *(uint2 *)dst = make_uint2(w[0], w[PER / 4 - 1]);
