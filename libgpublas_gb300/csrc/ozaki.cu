@@ -683,6 +683,7 @@ struct OzParams {
     float tol_bits;            // -log2(tol)
     int forced;                // fixed slice count, or 0
     int smax;                  // digit planes prepared (upper bound of S)
+    int s_lo;                  // lower bound of S from the tolerance alone (small-K kernel)
 };
 
 // The small-K product kernel's slice count, computed by every CTA from the
@@ -806,7 +807,8 @@ __device__ int oz_choose_S(const OzParams &p)
             const float ga = t[1] > 0.f ? 0.5f * __log2f(t[0] * (float)p.K / t[1]) : 0.f;
             const float gb = t[3] > 0.f ? 0.5f * __log2f(t[2] * (float)p.K / t[3]) : 0.f;
             int S = (int)ceilf((p.tol_bits + ga + gb + 1.5f) / 5.0f);
-            S = max(1, min(p.smax, S));
+            // never below s_lo: the kernel requested that many A slices early
+            S = max(max(1, p.s_lo), min(p.smax, S));
             s_S = st ? 0 : S;
             if (blockIdx.x == 0 && !st) *p.S = S;
         }
@@ -1428,7 +1430,11 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 // of up to eight stages: an A slice whose product has a narrow N is used
 // up in a few hundred cycles, so with K > 128 the ring depth, not the tensor
 // pipe, set the pace at four stages.  The B stage is double-buffered so the
-// next k block's (or tile's) slices load under the current MMAs.
+// next k block's (or tile's) slices load under the current MMAs.  A TMA
+// request costs the issuing thread about 80 ns, so a B stage (all P
+// prepared planes, of which the MMAs read the first S) is one 3-D request,
+// and the first tile's B stage and first A slices are requested before the
+// slice count is chosen (S >= s_lo from the tolerance alone).
 //
 // The drain prefetches its row's C values and scale exponents while the
 // MMAs run, then decodes each FP32 sum on the FMA and integer pipes (oz_f2i22)
@@ -1499,22 +1505,51 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     // above overlaps its tail; its slices, scales and S are complete and
     // visible after this wait (a no-op for an ordinary launch).
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    const int S = oz_choose_S(p);   // 0: skip this call
-    if (S == 0) {
-        if (warp == 1) {
-            tc_fence_after();
-            tmem_dealloc(tmem_base, 512);
-        }
-        oz_report(p);
-        return;
-    }
+    const int P = p.smax;   // digit planes prepared: S <= P
     const int nkb = p.Kp / OZ_BK;
-    // B stages first (S slices of 4 KB each), then the A ring
-    const int bstage = S * B_BYTES;
+    // B stages first (all P slices of BN rows each: a stage can be requested
+    // before S is known; the MMAs read the first S), then the A ring
+    const int bstage = P * B_BYTES;
     uint8_t *sB = smem;
     uint8_t *sA = smem + OZS_BSTG * bstage;
     const int nA = min(OZS_AMAX, (int)((OZS_DATA - (size_t)OZS_BSTG * bstage) / OZ_A_BYTES));
     const int ntiles = p.tiles_m * p.tiles_n;
+    // The first tile's first B stage and A slices 0..spec-1 (S >= p.s_lo, a
+    // bound from the tolerance alone) are requested before the slice count
+    // is chosen, so that these loads overlap the choice.
+    int t_first = -1, spec = 0;
+    if (warp == 0 && lane == 0) {
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+            if (tile_needed(p, t / p.tiles_n, t % p.tiles_n, OZ_BM, BN)) { t_first = t; break; }
+        if (t_first >= 0) {
+            const int tm = t_first / p.tiles_n, tn = t_first % p.tiles_n;
+            spec = min(min(nA, p.s_lo), 3);   // a TMA request costs the thread ~80 ns
+            mbar_arrive_expect_tx(&fullB[0], (uint32_t)(P * B_BYTES));
+            tma_load_3d(sB, &tmB, &fullB[0], 0, tn * BN, 0);
+            for (int sa = 0; sa < spec; sa++) {
+                mbar_arrive_expect_tx(&fullA[sa], OZ_A_BYTES);
+                tma_load_2d(sA + sa * OZ_A_BYTES, &tmA, &fullA[sa], 0, sa * p.Mp + tm * OZ_BM);
+            }
+        }
+    }
+    const int S = oz_choose_S(p);   // 0: skip this call
+    if (S == 0) {
+        // the early loads land before the CTA leaves (a wait bounded by time
+        // only: the status word is set on this path)
+        if (warp == 0 && lane == 0 && t_first >= 0) {
+            const uint64_t t0 = globaltimer();
+            while (!mbar_try_wait(&fullB[0], 0u) && globaltimer() - t0 < WAIT_LIMIT_NS) {}
+            for (int sa = 0; sa < spec; sa++)
+                while (!mbar_try_wait(&fullA[sa], 0u) && globaltimer() - t0 < WAIT_LIMIT_NS) {}
+        }
+        if (warp == 1) {
+            tc_fence_after();
+            tmem_dealloc(tmem_base, 512);
+        }
+        __syncthreads();
+        oz_report(p);
+        return;
+    }
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
@@ -1526,18 +1561,22 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 const int tm = t / p.tiles_n, tn = t % p.tiles_n;
                 if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
                 for (int kb = 0; kb < nkb && ok; kb++) {
-                    // the B stage: slices 0..S-1 of the tile's 32 columns, side by side
-                    if (!mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
-                    mbar_arrive_expect_tx(&fullB[bs], (uint32_t)(S * B_BYTES));
-                    for (int tb = 0; tb < S; tb++)
-                        tma_load_2d(sB + bs * bstage + tb * B_BYTES, &tmB, &fullB[bs], kb * OZ_BK,
-                                    tb * p.Np + tn * BN);
+                    // requested before the slice count was chosen
+                    const bool early = t == t_first && kb == 0;
+                    // the B stage: slices 0..P-1 of the tile's BN columns, side by side
+                    if (!early) {
+                        if (!mbar_wait(&emptyB[bs], bp ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
+                        mbar_arrive_expect_tx(&fullB[bs], (uint32_t)(P * B_BYTES));
+                        tma_load_3d(sB + bs * bstage, &tmB, &fullB[bs], kb * OZ_BK, tn * BN, 0);   // P planes
+                    }
                     if (++bs == OZS_BSTG) { bs = 0; bp ^= 1u; }
                     // then the A slices
                     for (int sa = 0; sa < S; sa++) {
-                        if (!mbar_wait(&emptyA[as], ap ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
-                        mbar_arrive_expect_tx(&fullA[as], OZ_A_BYTES);
-                        tma_load_2d(sA + as * OZ_A_BYTES, &tmA, &fullA[as], kb * OZ_BK, sa * p.Mp + tm * OZ_BM);
+                        if (!(early && sa < spec)) {
+                            if (!mbar_wait(&emptyA[as], ap ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
+                            mbar_arrive_expect_tx(&fullA[as], OZ_A_BYTES);
+                            tma_load_2d(sA + as * OZ_A_BYTES, &tmA, &fullA[as], kb * OZ_BK, sa * p.Mp + tm * OZ_BM);
+                        }
                         if (++as == nA) { as = 0; ap ^= 1u; }
                     }
                 }
@@ -1969,6 +2008,22 @@ bool make_map_uncached(CUtensorMap *map, void *base, long long rows, long long K
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The digit planes as a 3-D tensor (k, row, plane): one load brings a
+// box_rows-row block of box_planes consecutive planes (the small-K kernel's
+// B stage in one request instead of one per plane).
+bool make_map3_uncached(CUtensorMap *map, void *base, long long rows, long long Kp, int box_rows, int box_planes)
+{
+    EncodeTiledFn enc = get_encode();
+    if (!enc) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)OZ_SMAX};
+    cuuint64_t strides[2] = {(cuuint64_t)Kp, (cuuint64_t)(rows * Kp)};
+    cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, (cuuint32_t)box_planes};
+    cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, base, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // The digit planes live in workspace slots that persist across calls, so a
 // calling thread sees the same few (base, rows, K, box) over and over: the
 // encoded maps are kept per thread (8 entries, round robin) instead of
@@ -1988,7 +2043,11 @@ bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int bo
             *map = e.map;
             return true;
         }
-    if (!make_map_uncached(map, base, rows, Kp, box_rows)) return false;
+    // box_rows < 0 asks for the 3-D form: -box_rows = rows x 256 + planes
+    const bool three = box_rows < 0;
+    if (three ? !make_map3_uncached(map, base, rows, Kp, (-box_rows) >> 8, (-box_rows) & 255)
+              : !make_map_uncached(map, base, rows, Kp, box_rows))
+        return false;
     Entry &e = cache[next];
     next = (next + 1) & 7;
     e.base = base;
@@ -2203,8 +2262,10 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     gbx_timer_end(ctx);
 
     CUtensorMap tmA, tmB;
+    // small K: op(B)^T's planes as a 3-D map, the B stage of a tile in one load
     if (!make_map(&tmA, b.A8, (long long)OZ_SMAX * Mp, Kp, OZ_BM) ||
-        !make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : bn))
+        !(small_k ? make_map(&tmB, B8, Np, Kp, -(bn * 256 + planes))
+                  : make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : bn)))
         return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
 
     OzParams p{};
@@ -2227,6 +2288,10 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     p.tol_bits = (float)(-log2(tol));
     p.forced = forced;
     p.smax = planes;
+    // S >= ceil((-log2 tol + 1.5) / 5) (gamma >= 1 per operand); one less
+    // for the FP32 arithmetic of the device's choice
+    p.s_lo = forced > 0 ? std::min(forced, planes)
+                        : std::max(1, std::min(planes, (int)ceil((-log2(tol) + 1.5) / 5.0) - 1));
 
     // kernel attributes (per device) and the resident CTA-pair count; calls
     // arrive from many host threads
