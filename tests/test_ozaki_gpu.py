@@ -143,6 +143,26 @@ def test_nonfinite_operand_is_reported_and_context_recovers(orc, dev, k, bad):
     assert rel(from_dev(C, m, n), ref) <= TOL
 
 
+@pytest.mark.parametrize("k", [64, 2048])         # small-K kernel, wide-tile kernel
+@pytest.mark.parametrize("alpha,beta", [(1.0, 0.0), (-0.75, 0.0)])
+def test_results_near_the_underflow_threshold(orc, dev, k, alpha, beta):
+    # operands scaled by 2^-512: the products are near 2^-1020, so the low
+    # part of each element's two-part conversion leaves the normal range and
+    # the 128-bit route converts it; the reference is the unscaled product
+    # scaled by the same power of two
+    m, n = 96, 80
+    a, s = orc.matrix(m, k, 77 + k)
+    b, s = orc.matrix(k, n, s)
+    c = np.zeros((m, n), order="F")
+    ref = np.ldexp(orc.dgemm_dd("N", "N", m, n, k, alpha, a, b, beta, c), -1024)
+    C = to_dev(c)
+    dev.dgemm_ozaki("N", "N", m, n, k, alpha, to_dev(np.ldexp(a, -512)), m, to_dev(np.ldexp(b, -512)), k, beta,
+                    C, m)
+    got = from_dev(C, m, n)
+    assert np.all(np.isfinite(got))
+    assert rel(got, ref) <= TOL
+
+
 @pytest.mark.parametrize("uplo", ["L", "U"])
 @pytest.mark.parametrize("trans", ["N", "T"])
 def test_dsyrk_ozaki(orc, dev, uplo, trans):
