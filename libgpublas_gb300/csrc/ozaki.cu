@@ -1477,8 +1477,8 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     uint64_t *bars = (uint64_t *)(smem + OZS_DATA);
     uint64_t *fullA = bars, *emptyA = fullA + OZS_AMAX;
     uint64_t *fullB = emptyA + OZS_AMAX, *emptyB = fullB + OZS_BSTG;
-    uint64_t *tfull = emptyB + OZS_BSTG, *tempty = tfull + 1;
-    uint32_t *tmem_slot = (uint32_t *)(tempty + 1);
+    uint64_t *tfull = emptyB + OZS_BSTG, *tempty = tfull + 2;   // two accumulator sets
+    uint32_t *tmem_slot = (uint32_t *)(tempty + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int *status = p.status;
@@ -1486,8 +1486,10 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     if (threadIdx.x == 0) {
         for (int i = 0; i < OZS_AMAX; i++) { mbar_init(&fullA[i], 1); mbar_init(&emptyA[i], 1); }
         for (int i = 0; i < OZS_BSTG; i++) { mbar_init(&fullB[i], 1); mbar_init(&emptyB[i], 1); }
-        mbar_init(tfull, 1);
-        mbar_init(tempty, 32 * OZS_DRAIN_WARPS);
+        for (int i = 0; i < 2; i++) {
+            mbar_init(&tfull[i], 1);
+            mbar_init(&tempty[i], 32 * OZS_DRAIN_WARPS);
+        }
         fence_barrier_init();
         prefetch_tmap(&tmA);
         prefetch_tmap(&tmB);
@@ -1550,6 +1552,10 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         oz_report(p);
         return;
     }
+    // Accumulator sets in TMEM: two of 256 columns when a tile's S diagonals
+    // fit (S * BN <= 256: always for BN = 16), so that a tile's MMAs run while
+    // the previous tile's sums are read out; else one
+    const int nbuf = S * BN <= 256 ? 2 : 1;
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
@@ -1594,15 +1600,15 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            int as = 0, bs = 0;
+            int as = 0, bs = 0, tbuf = 0;
             uint32_t ap = 0, bp = 0, tp = 0;
             bool ok = true;
             const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int tm = t / p.tiles_n, tn = t % p.tiles_n;
                 if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
-                // the previous tile's sums have been read out of TMEM
-                if (!mbar_wait(tempty, tp ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
+                // this accumulator set's previous sums have been read out of TMEM
+                if (!mbar_wait(&tempty[tbuf], tp ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
                 tc_fence_after();
                 for (int kb = 0; kb < nkb && ok; kb++) {
                     if (!mbar_wait(&fullB[bs], bp, status, TC_TIMEOUT_FULL)) { ok = false; break; }
@@ -1623,7 +1629,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                         for (int c0 = 0; c0 < ntot; c0 += 256) {
                             const int n = min(256, ntot - c0);
                             const uint32_t idesc = idesc_e4m3_f32(OZ_BM, n);
-                            const uint32_t d_tmem = tmem_base + (uint32_t)(BN * sa + c0);
+                            const uint32_t d_tmem = tmem_base + (uint32_t)(tbuf * 256 + BN * sa + c0);
                             const uint64_t b_d = smem_desc_k128(b_addr + (uint32_t)c0 * OZ_BK);
 #pragma unroll
                             for (int kk = 0; kk < OZ_BK / 32; kk++)
@@ -1637,8 +1643,8 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                     if (++bs == OZS_BSTG) { bs = 0; bp ^= 1u; }
                 }
                 if (!ok) break;
-                mma_commit(tfull);
-                tp ^= 1u;
+                mma_commit(&tfull[tbuf]);
+                if (++tbuf == nbuf) { tbuf = 0; tp ^= 1u; }
             }
         }
     } else {
@@ -1650,6 +1656,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const int g = (S + 1) >> 1;                 // diagonals of the high half
         const int lsh = 5 * (S - g);                // weight of the high half over the low one
         uint32_t tp = 0;
+        int tbuf = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
             const int tm = t / p.tiles_n, tn = t % p.tiles_n;
@@ -1668,14 +1675,16 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             }
             const int erow = row_ok ? p.row_exp[grow] - 5 * (S - 1) : 0;
 
-            ok = __all_sync(0xffffffffu, mbar_wait(tfull, tp, status, TC_TIMEOUT_TMEM_FULL));
+            ok = __all_sync(0xffffffffu, mbar_wait(&tfull[tbuf], tp, status, TC_TIMEOUT_TMEM_FULL));
             if (!ok) break;
             tc_fence_after();
-            tp ^= 1u;
+            const int cur = tbuf;
+            if (++tbuf == nbuf) { tbuf = 0; tp ^= 1u; }
             long long vh[DCOLS], vl[DCOLS];
 #pragma unroll
             for (int j = 0; j < DCOLS; j++) { vh[j] = 0; vl[j] = 0; }
-            const uint32_t tbase = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cg * DCOLS);
+            const uint32_t tbase =
+                tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cur * 256 + cg * DCOLS);
             // diagonals qa and qa + 1 into the halves (q < g: high)
             auto fold2 = [&](int qa, const uint32_t (&ra)[DCOLS], const uint32_t (&rb)[DCOLS]) {
                 if (qa + 1 < g) {
@@ -1711,7 +1720,7 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                 }
             }
             tc_fence_before();
-            mbar_arrive(tempty);   // TMEM free: the next tile's MMAs may start
+            mbar_arrive(&tempty[cur]);   // this set free: a later tile's MMAs may use it
             // The next tile's C segment goes into L1 now: its MMAs overlap
             // this tile's conversion, so at its turn the loads of C would
             // otherwise wait on L2 with nothing to overlap them.
