@@ -50,8 +50,8 @@ void gbx_timer_end(gbx_ctx *ctx);
  * mapped host mirror, which such kernels set to the status when it is
  * nonzero as they finish.  gbx_ctx_sync reports a nonzero mirror (5: a
  * non-finite Ozaki operand, GBX_ERR_ARG; else GBX_ERR_TIMEOUT) and clears
- * both.  Word 0 is the status; words 8 (Ozaki one-launch preparation) and
- * 12 (DPOTRF step) are last-CTA counters that their kernels reset. */
+ * both.  Word 0 is the status; word 12 is the DPOTRF step's last-CTA
+ * counter, which its kernel resets. */
 gbx_status gbx_ctx_status(gbx_ctx *ctx, int **dev_status, int **host_mirror);
 /* Check cudaGetLastError after a launch, record and map it. */
 gbx_status gbx_check_launch(gbx_ctx *ctx, const char *what);

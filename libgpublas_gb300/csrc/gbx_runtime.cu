@@ -40,7 +40,7 @@ struct gbx_ctx {
     void  *pinned;
     size_t pinned_bytes;
     uint64_t launches;
-    int *status_dev;     // device status words of kernels with bounded waits ([0]; [8] a counter)
+    int *status_dev;     // device status words of kernels with bounded waits ([0]; [12] a counter)
     int *status_host;    // mapped pinned mirror of status_dev[0], written by the kernels on failure
     int *status_mirror;  // the mirror's device address
     int status_armed;    // a kernel that reports through the mirror ran since the last sync
@@ -250,8 +250,8 @@ extern "C" gbx_status gbx_ctx_sync(gbx_ctx *c)
     c->status_armed = 0;
     const int bad = *(volatile int *)c->status_host;
     if (!bad) return GBX_OK;
-    // clear the words for the next call (the prep counter at [8] is reset by
-    // the kernel that uses it, but a failed call may have left it behind)
+    // clear the words for the next call (the DPOTRF counter at [12] is reset
+    // by the kernel that uses it, but a failed call may have left it behind)
     cudaMemsetAsync(c->status_dev, 0, 64, c->stream);
     e = cudaStreamSynchronize(c->stream);
     *(volatile int *)c->status_host = 0;
