@@ -507,6 +507,8 @@ def run_ours(args):
                            "d2h_bytes_per_step": (s1["bytes_d2h"] - s0["bytes_d2h"]) // args.steps,
                            "api": "Fortran ABI symbol, pinned host operands"}
 
+    if w == "dgemm":
+        line["accuracy"] = plain_accuracy(dev, work)
     if w == "dgemm" and not args.no_ozaki:
         try:
             line["ozaki"] = bench_ozaki(args, dev, work, stream)
@@ -527,6 +529,35 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     dev.close()
+
+
+def sample_indices(m, n, count, seed):
+    """count random (row, col) pairs plus 64 on the last row and 64 on the
+    last column (the edge tiles)."""
+    rng = np.random.default_rng(seed)
+    rows = np.concatenate([rng.integers(0, m, count), np.full(64, m - 1), rng.integers(0, m, 64)])
+    cols = np.concatenate([rng.integers(0, n, count), rng.integers(0, n, 64), np.full(64, n - 1)])
+    return rows, cols
+
+
+def plain_accuracy(dev, work, ta="N"):
+    """The benchmarked kernel checks its own result: one fresh FP64 DGEMM
+    of the workload (same operands, C restored), sampled entries against the
+    double-double oracle.  Tolerance of the FP64 routines: 1e-13."""
+    import torch
+    m, n, k = work.m, work.n, work.k
+    dc = torch.from_numpy(work.c.ravel(order="F")).cuda()
+    lda = m if ta == "N" else k
+    dev.dgemm_checked(ta, "N", m, n, k, 1.0, work.d["a"], lda, work.d["b"], k, 0.5, dc, m)
+    dev.sync()
+    got = dc.view(n, m)   # column j is row j of this view
+    rows, cols = sample_indices(m, n, 2048, 1)
+    vals = got[torch.from_numpy(cols).cuda(), torch.from_numpy(rows).cuda()].cpu().numpy()
+    ref = work.orc.dgemm_dd_sample(ta, "N", k, 1.0, work.a, work.b, 0.5, work.c, rows, cols)
+    err = float(np.linalg.norm(vals - ref) / np.linalg.norm(ref))
+    del dc
+    return {"rel_err_fro_sampled": err, "samples": int(len(rows)), "tol": 1e-13,
+            "ok": bool(err <= 1e-13), "oracle": "double-double dot products of the sampled entries"}
 
 
 def ozaki_accuracy(dev, work):

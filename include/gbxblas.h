@@ -75,9 +75,6 @@ enum {
 };
 gbx_status gbx_ctx_enable_timing(gbx_ctx *ctx, int on);
 gbx_status gbx_ctx_kernel_time(gbx_ctx *ctx, int tag, double *ms, uint64_t *count);
-/* Measured FP64 FMA throughput of the device (TFLOP/s) from a ~50 ms DFMA
- * loop on the context's stream; the denominator of the FP64 roofline. */
-gbx_status gbx_diag_fp64_peak(gbx_ctx *ctx, double *tflops);
 /* Last status / CUDA error text recorded on the context. */
 const char *gbx_ctx_last_error(const gbx_ctx *ctx);
 const char *gbx_status_string(gbx_status s);
@@ -335,29 +332,6 @@ gbx_status gbx_server_stats(gbx_server *srv, uint64_t *completed, uint64_t *batc
                             uint64_t *admission_waits);
 gbx_status gbx_server_reset_stats(gbx_server *srv);
 gbx_status gbx_server_destroy(gbx_server *srv);
-
-/* Native driver of the serving workload (diagnostic; no reference
- * counterpart): nthreads host threads, thread t running the calls of a
- * blocked right-looking Cholesky of the n[t] x n[t] matrix A[t] (leading
- * dimension lda[t], block nb[t] <= 256, lower triangle, info[t] its INFO)
- * through server (or plain per-call dispatch on one context per thread when
- * server is NULL); ozaki selects the Ozaki forms of dtrsm/dsyrk/dgemm.  The
- * threads start together; per-call latency is taken on the calling thread.
- * Op kinds index kind_calls / kind_sum_us. */
-#define GBX_TRACE_MAX_THREADS 64
-#define GBX_TRACE_KINDS 16
-typedef struct {
-    uint64_t calls;
-    double wall_s;
-    double p50_us, p99_us;
-    uint64_t kind_calls[GBX_TRACE_KINDS];
-    double kind_sum_us[GBX_TRACE_KINDS];
-    double thread_finish_s[GBX_TRACE_MAX_THREADS];
-    int first_error;   /* status of the first failed call (0: none) */
-} gbx_trace_stats;
-gbx_status gbx_diag_cholesky_trace(gbx_server *server, int device, int nthreads, const int *n, const int *nb,
-                                   double *const *A, const int *lda, int *info, int ozaki,
-                                   gbx_trace_stats *out);
 
 #ifdef __cplusplus
 }

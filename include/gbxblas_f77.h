@@ -39,7 +39,7 @@ void dtrmm_(const char *side, const char *uplo, const char *transa, const char *
             const int *m, const int *n, const double *alpha, const double *a, const int *lda,
             double *b, const int *ldb);
 /* The other precisions and Level-3 routines the reference exports
- * (prototypes blas.h:202-314, bodies blas_level3/*.cc).  Complex scalars and
+ * (prototypes blas.h:202-314, bodies blas_level3/<routine>.cc).  Complex scalars and
  * matrices are (re, im) pairs; Hermitian routines take the real alpha/beta
  * netlib gives them. */
 /* F77_gemm(s|c)  gemm.cc:143-160, 181-198 */

@@ -1,0 +1,55 @@
+/*
+ * gbxdiag.h — diagnostics of libgbxblas, in a library of their own
+ * (libgbxdiag.so, linked against libgbxblas.so).  They measure the device
+ * and drive benchmark and failure-path workloads; an application linking the
+ * BLAS library needs none of them.  None has a counterpart in the reference
+ * (its statistics are hit/miss counts only, blas2cuda.c:266-273).
+ */
+#ifndef GBXDIAG_H
+#define GBXDIAG_H
+
+#include "gbxblas.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Measured FP64 FMA throughput of the device (TFLOP/s) from a ~50 ms DFMA
+ * loop on the context's stream; the denominator of the FP64 roofline. */
+gbx_status gbx_diag_fp64_peak(gbx_ctx *ctx, double *tflops);
+
+/* Failure-path check of the bounded device waits: launches, on the context's
+ * stream, one CTA that waits on an mbarrier nothing will ever arrive on,
+ * through the same bounded wait the tensor-core kernels use (2 s limit).  The
+ * wait gives up, records its code in the context's status word and mirror,
+ * and the kernel returns; nothing is left in flight.  The next
+ * gbx_ctx_sync returns GBX_ERR_TIMEOUT and clears the status, after which
+ * the context is usable again.  Returns the launch status. */
+gbx_status gbx_diag_expire_wait(gbx_ctx *ctx);
+
+/* Native driver of the serving workload: nthreads host threads, thread t
+ * running the calls of a blocked right-looking Cholesky of the n[t] x n[t]
+ * matrix A[t] (leading dimension lda[t], block nb[t] <= 256, lower triangle,
+ * info[t] its INFO) through server (or plain per-call dispatch on one
+ * context per thread when server is NULL); ozaki selects the Ozaki forms of
+ * dtrsm/dsyrk/dgemm.  The threads start together; per-call latency is taken
+ * on the calling thread.  Op kinds index kind_calls / kind_sum_us. */
+#define GBX_TRACE_MAX_THREADS 64
+#define GBX_TRACE_KINDS 16
+typedef struct {
+    uint64_t calls;
+    double wall_s;
+    double p50_us, p99_us;
+    uint64_t kind_calls[GBX_TRACE_KINDS];
+    double kind_sum_us[GBX_TRACE_KINDS];
+    double thread_finish_s[GBX_TRACE_MAX_THREADS];
+    int first_error;   /* status of the first failed call (0: none) */
+} gbx_trace_stats;
+gbx_status gbx_diag_cholesky_trace(gbx_server *server, int device, int nthreads, const int *n, const int *nb,
+                                   double *const *A, const int *lda, int *info, int ozaki,
+                                   gbx_trace_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

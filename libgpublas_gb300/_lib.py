@@ -19,8 +19,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgbxblas.so")
+DIAG_LIB_PATH = os.path.join(HERE, "libgbxdiag.so")
 HEADERS = [os.path.join(os.path.dirname(HERE), "include", h)
            for h in ("gbxblas.h", "gbxblas_f77.h")]
+DIAG_HEADERS = [os.path.join(os.path.dirname(HERE), "include", "gbxdiag.h")]
 
 _P = C.c_void_p
 _I = C.c_int
@@ -28,6 +30,7 @@ _D = C.c_double
 _CH = C.c_char
 
 _lib = None
+_diag = None
 
 
 def load(path=None):
@@ -45,10 +48,29 @@ def load(path=None):
     return lib
 
 
-def declared_symbols():
-    """Function names declared in the public headers."""
+def load_diag():
+    """Load libgbxdiag.so (benchmark and failure-path diagnostics; it
+    resolves its calls into libgbxblas.so, loaded first)."""
+    global _diag
+    if _diag is not None:
+        return _diag
+    load()
+    if not os.path.exists(DIAG_LIB_PATH):
+        raise OSError(f"{DIAG_LIB_PATH} is missing: build it with __graft_entry__.build()")
+    d = C.CDLL(DIAG_LIB_PATH)
+    d.gbx_diag_fp64_peak.argtypes = [_P, C.POINTER(_D)]
+    d.gbx_diag_expire_wait.argtypes = [_P]
+    d.gbx_diag_cholesky_trace.argtypes = [_P, _I, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_P),
+                                          C.POINTER(_I), _P, _I, C.POINTER(TraceStats)]
+    _diag = d
+    return d
+
+
+def declared_symbols(headers=None):
+    """Function names declared in the public headers (default: those of
+    libgbxblas.so; DIAG_HEADERS for libgbxdiag.so)."""
     names = []
-    for h in HEADERS:
+    for h in headers or HEADERS:
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         for m in re.finditer(r"^\s*[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", text, flags=re.M):
@@ -145,9 +167,6 @@ def _declare(L):
     L.gbx_server_destroy.argtypes = [_P]
     L.gbx_ctx_enable_timing.argtypes = [_P, _I]
     L.gbx_ctx_kernel_time.argtypes = [_P, _I, C.POINTER(_D), C.POINTER(C.c_uint64)]
-    L.gbx_diag_fp64_peak.argtypes = [_P, C.POINTER(_D)]
-    L.gbx_diag_cholesky_trace.argtypes = [_P, _I, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_P),
-                                          C.POINTER(_I), _P, _I, C.POINTER(TraceStats)]
 
 
 class GbxOp(C.Structure):
@@ -166,7 +185,7 @@ TRACE_MAX_THREADS, TRACE_KINDS = 64, 16
 
 
 class TraceStats(C.Structure):
-    """gbx_trace_stats of include/gbxblas.h."""
+    """gbx_trace_stats of include/gbxdiag.h."""
     _fields_ = [("calls", C.c_uint64), ("wall_s", C.c_double), ("p50_us", C.c_double),
                 ("p99_us", C.c_double), ("kind_calls", C.c_uint64 * TRACE_KINDS),
                 ("kind_sum_us", C.c_double * TRACE_KINDS),
@@ -179,7 +198,7 @@ def cholesky_trace(server, device, n, nb, mats, info_ptr, ozaki):
     is mats[t] (n[t] x n[t], leading dimension n[t], block nb[t]); server is
     a Server or None (plain per-call dispatch).  Returns gbx_trace_stats as a
     dict."""
-    L = load()
+    L = load_diag()
     k = len(n)
     ni = (_I * k)(*n)
     nbi = (_I * k)(*nb)
@@ -483,8 +502,13 @@ class Device:
 
     def fp64_peak(self):
         t = C.c_double(0.0)
-        self._ok(self.L.gbx_diag_fp64_peak(self.ctx, C.byref(t)), "fp64_peak")
+        self._ok(load_diag().gbx_diag_fp64_peak(self.ctx, C.byref(t)), "fp64_peak")
         return t.value
+
+    def expire_wait(self):
+        """Launch the diagnostic whose bounded device wait runs out (about
+        2 s); the next sync reports GBX_ERR_TIMEOUT."""
+        self._ok(load_diag().gbx_diag_expire_wait(self.ctx), "expire_wait")
 
     # Level 1
     def daxpy(self, n, alpha, x, incx, y, incy):

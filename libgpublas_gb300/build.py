@@ -3,7 +3,12 @@
 Compiles every CUDA translation unit with nvcc and every C file with gcc,
 in parallel, and links one shared library in-tree:
 
-    libgpublas_gb300/libgbxblas.so
+    libgpublas_gb300/libgbxblas.so           the BLAS library (csrc/)
+    libgpublas_gb300/libgbxblas_preload.so   the same plus the allocation
+                                             interposer (csrc/preload_*.c)
+    libgpublas_gb300/libgbxdiag.so           diagnostics for benchmarks and
+                                             failure-path tests (csrc_diag/),
+                                             linked against libgbxblas.so
 
 The build is skipped when a stamp of all sources, headers and flags matches
 the last successful build.  No cmake, no torch extension machinery: the
@@ -19,9 +24,11 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
+CSRC_DIAG = os.path.join(HERE, "csrc_diag")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbxblas.so")
 PRELOAD_LIB = os.path.join(HERE, "libgbxblas_preload.so")
+DIAG_LIB = os.path.join(HERE, "libgbxdiag.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
@@ -44,6 +51,10 @@ def _sources():
     return cu, c, hdr
 
 
+def _diag_sources():
+    return sorted(glob.glob(os.path.join(CSRC_DIAG, "*.cu")))
+
+
 def _stamp(files, extra):
     h = hashlib.sha256()
     for f in files:
@@ -63,11 +74,12 @@ def _run(cmd):
 
 def build_library(force: bool = False, verbose: bool = False) -> str:
     cu, c, hdr = _sources()
+    dcu = _diag_sources()
     nvcc = _nvcc()
-    stamp = _stamp(cu + c + hdr, NVCC_FLAGS + CC_FLAGS + [nvcc])
+    stamp = _stamp(cu + c + hdr + dcu, NVCC_FLAGS + CC_FLAGS + [nvcc])
     stamp_file = os.path.join(BUILD, "stamp")
-    if (not force and os.path.exists(LIB) and os.path.exists(stamp_file)
-            and open(stamp_file).read() == stamp):
+    if (not force and all(os.path.exists(p) for p in (LIB, PRELOAD_LIB, DIAG_LIB))
+            and os.path.exists(stamp_file) and open(stamp_file).read() == stamp):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     jobs = []
@@ -77,6 +89,11 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     for src in c:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         jobs.append((["gcc"] + CC_FLAGS + ["-c", src, "-o", obj], obj))
+    diag_objs = []
+    for src in dcu:
+        obj = os.path.join(BUILD, "diag_" + os.path.basename(src) + ".o")
+        jobs.append(([nvcc] + NVCC_FLAGS + ["-I" + CSRC, "-c", src, "-o", obj], obj))
+        diag_objs.append(obj)
     workers = max(1, min(len(jobs), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(workers) as ex:
         outs = list(ex.map(lambda j: _run(j[0]), jobs))
@@ -84,7 +101,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         for o in outs:
             if o.strip():
                 print(o)
-    objs = [j[1] for j in jobs]
+    objs = [j[1] for j in jobs if j[1] not in diag_objs]
     # libgbxblas.so: the BLAS library; libgbxblas_preload.so: the same plus
     # the malloc/free interposer (preload_*.c), for LD_PRELOAD use.
     core = [o for o in objs if not os.path.basename(o).startswith("preload_")]
@@ -92,6 +109,12 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         tmp = out + ".tmp%d" % os.getpid()
         _run([nvcc] + ARCH + ["-shared", "-o", tmp] + parts + ["-lpthread", "-ldl"])
         os.replace(tmp, out)
+    # libgbxdiag.so: benchmark and failure-path diagnostics, resolved against
+    # libgbxblas.so next to it
+    tmp = DIAG_LIB + ".tmp%d" % os.getpid()
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + diag_objs +
+         ["-L" + HERE, "-lgbxblas", "-Xlinker", "-rpath=$ORIGIN", "-lpthread"])
+    os.replace(tmp, DIAG_LIB)
     with open(stamp_file, "w") as fh:
         fh.write(stamp)
     return LIB

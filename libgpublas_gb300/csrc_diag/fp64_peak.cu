@@ -1,10 +1,11 @@
-// diag.cu — device capability measurement used as the FP64 roofline
+// fp64_peak.cu — device capability measurement used as the FP64 roofline
 // denominator: sustained DFMA throughput of the whole GPU.
 //
 // Each thread runs 8 independent FMA chains (enough to cover the DFMA
 // latency), 8 blocks of 256 threads per SM; the result is written so the
 // chains cannot be eliminated.
 #include "gbx_internal.h"
+#include "gbxdiag.h"
 
 #include <cuda_runtime.h>
 

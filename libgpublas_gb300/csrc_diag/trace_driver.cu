@@ -11,6 +11,7 @@
 // The threads start together; each call's latency is taken around the call
 // on the calling thread.  Statistics come back in gbx_trace_stats.
 #include "gbx_internal.h"
+#include "gbxdiag.h"
 
 #include <cuda_runtime.h>
 #include <algorithm>

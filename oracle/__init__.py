@@ -83,6 +83,8 @@ class Oracle:
         L.orc_dtrsm_residual.restype = _c_dbl
         L.orc_dtrsm_residual.argtypes = [_c_char] * 4 + [_c_int, _c_int, _c_dbl, _P, _c_int,
                                                          _P, _c_int, _P, _c_int]
+        L.orc_dtrsm_residual_cw.restype = _c_dbl
+        L.orc_dtrsm_residual_cw.argtypes = L.orc_dtrsm_residual.argtypes
         L.orc_zsymm.argtypes = [_c_char, _c_char, _c_int, _c_int, _P, _P, _c_int, _P, _c_int, _P, _P,
                                 _c_int, _c_int]
         L.orc_zsyrk.argtypes = [_c_char, _c_char, _c_int, _c_int, _c_int, _P, _P, _c_int, _P, _P, _c_int,
@@ -268,6 +270,11 @@ class Oracle:
         return self.lib.orc_dtrsm_residual(_ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n,
                                            alpha, _ptr(a), a.shape[0], _ptr(b0), b0.shape[0],
                                            _ptr(x), x.shape[0])
+
+    def dtrsm_residual_cw(self, side, uplo, ta, diag, m, n, alpha, a, b0, x):
+        return self.lib.orc_dtrsm_residual_cw(_ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n,
+                                              alpha, _ptr(a), a.shape[0], _ptr(b0), b0.shape[0],
+                                              _ptr(x), x.shape[0])
 
     def rel_fro(self, m, n, x, ref):
         return self.lib.orc_rel_fro(m, n, _ptr(x), x.shape[0], _ptr(ref), ref.shape[0])

@@ -946,6 +946,47 @@ double orc_dtrsm_residual(char side, char uplo, char ta, char diag, int m, int n
     return den > 0.0 ? sqrt(dd_to_d(rn)) / den : sqrt(dd_to_d(rn));
 }
 
+/* Componentwise backward error of a triangular solve (Oettli-Prager):
+ * max over entries of |op(A) X - alpha B0| / (|op(A)| |X| + |alpha| |B0|),
+ * side L (op(A) X) or R (X op(A)), residual and denominators in
+ * double-double.  A substitution solve keeps it near n*u whatever the
+ * conditioning; it is the measure under which inverse-based solves can lose. */
+double orc_dtrsm_residual_cw(char side, char uplo, char ta, char diag, int m, int n,
+                             double alpha, const double *a, int lda,
+                             const double *b0, int ldb0, const double *x, int ldx)
+{
+    int lside = same(side, 'L');
+    int na = lside ? m : n;
+    double *t = (double *)malloc(sizeof(double) * (size_t)na * na);
+    explicit_tri(uplo, ta, diag, na, a, lda, t);
+    double worst = 0.0;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            double bv = b0[(size_t)j * ldb0 + i];
+            dd s = {0.0, 0.0}, w = {0.0, 0.0};
+            if (lside)
+                for (int l = 0; l < m; l++) {
+                    double tv = t[(size_t)l * na + i], xv = x[(size_t)j * ldx + l];
+                    s = dd_fma(s, tv, xv);
+                    w = dd_fma(w, fabs(tv), fabs(xv));
+                }
+            else
+                for (int l = 0; l < n; l++) {
+                    double tv = t[(size_t)j * na + l], xv = x[(size_t)l * ldx + i];
+                    s = dd_fma(s, xv, tv);
+                    w = dd_fma(w, fabs(xv), fabs(tv));
+                }
+            double p, pe; two_prod(-alpha, bv, &p, &pe);
+            dd q = {p, pe};
+            double r = fabs(dd_to_d(dd_add(s, q)));
+            double den = dd_to_d(w) + fabs(alpha) * fabs(bv);
+            double ratio = den > 0.0 ? r / den : (r > 0.0 ? INFINITY : 0.0);
+            if (ratio > worst || ratio != ratio) worst = ratio;
+        }
+    free(t);
+    return worst;
+}
+
 double orc_rel_fro(int m, int n, const double *x, int ldx, const double *ref, int ldr)
 {
     dd num = {0.0, 0.0}, den = {0.0, 0.0};

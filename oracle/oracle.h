@@ -117,6 +117,11 @@ void orc_zgemm_dd_sample(char ta, char tb, int k, const double *alpha,
 double orc_dtrsm_residual(char side, char uplo, char transa, char diag, int m, int n,
                           double alpha, const double *a, int lda,
                           const double *b0, int ldb0, const double *x, int ldx);
+/* max |op(A)*X - alpha*B0| / (|op(A)|*|X| + |alpha|*|B0|) entrywise, dd
+ * (componentwise backward error of a triangular solve). */
+double orc_dtrsm_residual_cw(char side, char uplo, char transa, char diag, int m, int n,
+                             double alpha, const double *a, int lda,
+                             const double *b0, int ldb0, const double *x, int ldx);
 /* dd dot product rounded to double */
 double orc_ddot_dd(int n, const double *x, int incx, const double *y, int incy);
 

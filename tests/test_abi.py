@@ -25,6 +25,21 @@ def test_exports_every_declared_symbol(lib):
     assert not missing, missing
 
 
+def test_diag_library_exports_its_symbols(lib):
+    # benchmark and failure-path diagnostics live in libgbxdiag.so, not in
+    # the BLAS library an application loads
+    import libgpublas_gb300 as g
+    names = g.declared_symbols(g.DIAG_HEADERS)
+    assert "gbx_diag_fp64_peak" in names and "gbx_diag_expire_wait" in names
+    nm = lambda p: {ln.split()[-1] for ln in subprocess.run(  # noqa: E731
+        ["nm", "-D", "--defined-only", p], capture_output=True, text=True, check=True).stdout.splitlines()
+        if ln.strip()}
+    diag, blas = nm(g.DIAG_LIB_PATH), nm(g.LIB_PATH)
+    assert not [n for n in names if n not in diag]
+    assert not [n for n in blas if n.startswith("gbx_diag")]
+    g.load_diag()
+
+
 def test_library_is_sm103a_only(lib):
     import libgpublas_gb300 as g
     out = subprocess.run(["cuobjdump", "--list-elf", g.LIB_PATH], capture_output=True, text=True)

@@ -1,0 +1,278 @@
+"""Parity at the shapes that select the large tiles, i.e. the kernels the
+benchmarks time.
+
+The GEMM core picks its block tile from the number of output tiles (the
+largest tile that still gives every SM two of them): the 128 x 128 FP64 tile
+(8 x 8 per thread) needs about 2200 rows and columns, the 64 x 64 complex tile
+about 1100, and the Ozaki product takes its 128 x 256 tile once 152 such tiles
+exist (about 2560 x 2560) with K > 1024.  The small shapes of the other test
+files never reach those instantiations, so each case here is sized past the
+threshold, with ragged edges (sizes that are not multiples of the tile), odd
+leading dimensions whose padding rows hold a sentinel, and beta != 0.
+
+Checks, each with the tolerance stated:
+  * sampled entries (random plus the last rows and columns, where the edge
+    tiles are) against the double-double oracle: relative error <= 1e-13 for
+    the FP64 routines, <= 1e-14 for the Ozaki products (their default target);
+  * every entry against an FP64 host product (numpy): relative Frobenius
+    difference <= 1e-13, so a wrong tile anywhere is caught;
+  * padding rows and the untouched triangle are bit-identical afterwards.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-13
+TOL_OZ = 1e-14
+SENT = 12345.678
+
+
+def rel(x, ref):
+    d = np.linalg.norm(ref)
+    return float(np.linalg.norm(x - ref) / (d if d > 0 else 1.0))
+
+
+def padded(orc, rows, cols, seed, pad=3):
+    a, s = orc.matrix(rows, cols, seed, ld=rows + pad)
+    a[rows:, :] = SENT
+    return a, s
+
+
+def to_dev(a):
+    import torch
+    return torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+
+
+def from_dev(t, rows, cols):
+    return t.cpu().numpy().reshape(rows, cols, order="F")
+
+
+def samples(m, n, count, seed, lower=None):
+    """Random (row, col) pairs plus the last rows and columns (edge tiles);
+    lower=True/False keeps only the lower/upper triangle."""
+    rng = np.random.default_rng(seed)
+    r = np.concatenate([rng.integers(0, m, count), np.full(64, m - 1), rng.integers(0, m, 64),
+                        m - 1 - np.arange(64) % m])
+    c = np.concatenate([rng.integers(0, n, count), rng.integers(0, n, 64), np.full(64, n - 1),
+                        n - 1 - np.arange(64) % n])
+    if lower is not None:
+        keep = (r >= c) if lower else (r <= c)
+        r, c = r[keep], c[keep]
+    return r.astype(np.int32), c.astype(np.int32)
+
+
+def op(x, t):
+    return x if t == "N" else x.T
+
+
+# ------------------------------------------------------------ FP64 DGEMM, 128 x 128 tile
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+@pytest.mark.parametrize("m,n,k", [(2311, 2305, 129), (2304, 2304, 512)])
+def test_dgemm_128_tile(orc, dev, ta, tb, m, n, k):
+    if (m, n, k) == (2304, 2304, 512) and tb == "T":
+        pytest.skip("the square case runs NN and TN (the benchmarked forms)")
+    ra, ca = (m, k) if ta == "N" else (k, m)
+    rb, cb = (k, n) if tb == "N" else (n, k)
+    a, s = padded(orc, ra, ca, 7000 + m + k)
+    b, s = padded(orc, rb, cb, s)
+    c, s = padded(orc, m, n, s)
+    A, B = to_dev(a), to_dev(b)
+    rows, cols = samples(m, n, 2048, m + n + k)
+    for alpha, beta in [(1.5, 0.5), (1.0, 0.0)]:
+        cin = c.copy(order="F")
+        if beta == 0.0:
+            cin[:m] = np.nan          # beta = 0 must overwrite, not scale
+        C = to_dev(cin)
+        dev.dgemm_checked(ta, tb, m, n, k, alpha, A, a.shape[0], B, b.shape[0], beta, C, c.shape[0])
+        got = from_dev(C, c.shape[0], n)
+        assert np.all(got[m:] == SENT)
+        ref = orc.dgemm_dd_sample(ta, tb, k, alpha, a, b, beta, c, rows, cols)
+        assert rel(got[rows, cols], ref) <= TOL
+        full = alpha * (op(a[:ra], ta) @ op(b[:rb], tb)) + (beta * c[:m] if beta else 0.0)
+        assert rel(got[:m], full) <= TOL
+
+
+def test_dgemm_128_tile_through_fortran_symbol(orc, f77):
+    # the drop-in path: host operands with an odd leading dimension, staged
+    m, n, k = 2400, 2333, 300
+    a, s = padded(orc, m, k, 71)
+    b, s = padded(orc, k, n, s)
+    c, s = padded(orc, m, n, s)
+    got = c.copy(order="F")
+    f77.dgemm("N", "N", m, n, k, -0.5, a, a.shape[0], b, b.shape[0], 0.25, got, got.shape[0])
+    assert np.all(got[m:] == SENT)
+    rows, cols = samples(m, n, 2048, 72)
+    ref = orc.dgemm_dd_sample("N", "N", k, -0.5, a, b, 0.25, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL
+    assert rel(got[:m], -0.5 * (a[:m] @ b[:k]) + 0.25 * c[:m]) <= TOL
+
+
+# ------------------------------------------------------------ FP64 DSYRK, 128 x 128 tile
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_dsyrk_128_tile(orc, dev, uplo, trans):
+    # 26 x 27 / 2 = 351 triangular tiles of 128 (>= 2 per SM)
+    n, k = 3201, 300
+    ra, ca = (n, k) if trans == "N" else (k, n)
+    a, s = padded(orc, ra, ca, 7100 + ord(uplo) + ord(trans))
+    c, _ = padded(orc, n, n, s)
+    C = to_dev(c)
+    dev.dsyrk(uplo, trans, n, k, -0.75, to_dev(a), a.shape[0], 0.5, C, c.shape[0])
+    got = from_dev(C, c.shape[0], n)
+    assert np.all(got[n:] == SENT)
+    lower = uplo == "L"
+    rows, cols = samples(n, n, 2048, 7101, lower=lower)
+    ta, tb = ("N", "T") if trans == "N" else ("T", "N")
+    ref = orc.dgemm_dd_sample(ta, tb, k, -0.75, a, a, 0.5, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL
+    x = a[:ra]
+    full = -0.75 * (x @ x.T if trans == "N" else x.T @ x) + 0.5 * c[:n]
+    tri = np.tril if lower else np.triu
+    assert rel(tri(got[:n]), tri(full)) <= TOL
+    untouched = np.triu(np.ones((n, n), bool), 1) if lower else np.tril(np.ones((n, n), bool), -1)
+    assert np.array_equal(got[:n][untouched], c[:n][untouched])
+
+
+# ------------------------------------------------------------ FP64 DTRMM on the 128 tile
+@pytest.mark.parametrize("side,uplo,ta", [("L", "L", "N"), ("R", "U", "T")])
+def test_dtrmm_128_tile(orc, dev, side, uplo, ta):
+    m, n = 2311, 2305
+    na = m if side == "L" else n
+    a, s = orc.trsm_matrix(na, 7200 + ord(side))
+    b, _ = padded(orc, m, n, s)
+    B = to_dev(b)
+    dev.dtrmm(side, uplo, ta, "N", m, n, 0.5, to_dev(a), na, B, b.shape[0])
+    got = from_dev(B, b.shape[0], n)
+    assert np.all(got[m:] == SENT)
+    t = np.tril(a) if uplo == "L" else np.triu(a)
+    t = t if ta == "N" else t.T
+    full = 0.5 * (t @ b[:m] if side == "L" else b[:m] @ t)
+    assert rel(got[:m], full) <= TOL
+
+
+# ------------------------------------------------------------ FP64 ZGEMM, 64 x 64 complex tile
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("C", "N"), ("N", "T")])
+def test_zgemm_64_tile(orc, dev, ta, tb):
+    # 19 x 19 = 361 complex tiles of 64
+    m, n, k = 1201, 1153, 200
+    rng = np.random.default_rng(7300 + ord(ta))
+    ra, ca = (m, k) if ta == "N" else (k, m)
+    rb, cb = (k, n) if tb == "N" else (n, k)
+    a = np.asfortranarray(rng.uniform(-1, 1, (ra, ca)) + 1j * rng.uniform(-1, 1, (ra, ca)))
+    b = np.asfortranarray(rng.uniform(-1, 1, (rb, cb)) + 1j * rng.uniform(-1, 1, (rb, cb)))
+    c = np.asfortranarray(rng.uniform(-1, 1, (m, n)) + 1j * rng.uniform(-1, 1, (m, n)))
+    alpha, beta = 0.5 - 1.25j, 0.25 + 0.5j
+    A = to_dev(a.ravel(order="F").view(np.float64))
+    B = to_dev(b.ravel(order="F").view(np.float64))
+    C = to_dev(c.ravel(order="F").view(np.float64))
+    dev.zgemm(ta, tb, m, n, k, alpha, A, ra, B, rb, beta, C, m)
+    got = C.cpu().numpy().view(np.complex128).reshape(m, n, order="F")
+    rows, cols = samples(m, n, 1024, 7301)
+    ref = orc.zgemm_dd_sample(ta, tb, k, alpha, a, b, beta, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL
+
+    def zop(x, t):
+        return x if t == "N" else (x.T if t == "T" else x.conj().T)
+    assert rel(got, alpha * (zop(a, ta) @ zop(b, tb)) + beta * c) <= TOL
+
+
+# ------------------------------------------------------------ Ozaki, 128 x 256 tile (K > 1024)
+@pytest.mark.parametrize("spread", [0, 8, 24])
+def test_dgemm_ozaki_wide_256_tile(orc, dev, spread):
+    # 20 x 10 = 200 tiles of 128 x 256 (>= one per SM), K = 2048
+    m = n = 2560
+    k = 2048
+    a, s = orc.spread((m, k), spread, 7400 + spread)
+    b, s = orc.spread((k, n), spread, s)
+    c, _ = orc.matrix(m, n, s)
+    C = to_dev(c)
+    used = dev.dgemm_ozaki("N", "N", m, n, k, 1.0, to_dev(a), m, to_dev(b), k, 0.5, C, m)
+    assert 1 <= used <= 14
+    got = from_dev(C, m, n)
+    rows, cols = samples(m, n, 2048, 7401 + spread)
+    ref = orc.dgemm_dd_sample("N", "N", k, 1.0, a, b, 0.5, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL_OZ, (spread, used)
+
+
+@pytest.mark.parametrize("ta,tb", [("T", "N"), ("N", "T")])
+def test_dgemm_ozaki_wide_256_tile_ragged(orc, dev, ta, tb):
+    # ragged edges in every dimension: 21 x 11 = 231 tiles, K = 2100
+    m, n, k = 2600, 2590, 2100
+    ra, ca = (m, k) if ta == "N" else (k, m)
+    rb, cb = (k, n) if tb == "N" else (n, k)
+    a, s = padded(orc, ra, ca, 7500)
+    b, s = padded(orc, rb, cb, s)
+    c, _ = padded(orc, m, n, s)
+    C = to_dev(c)
+    dev.dgemm_ozaki(ta, tb, m, n, k, -1.25, to_dev(a), a.shape[0], to_dev(b), b.shape[0], 0.75, C,
+                    c.shape[0])
+    got = from_dev(C, c.shape[0], n)
+    assert np.all(got[m:] == SENT)
+    rows, cols = samples(m, n, 2048, 7501)
+    ref = orc.dgemm_dd_sample(ta, tb, k, -1.25, a, b, 0.75, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL_OZ
+    full = -1.25 * (op(a[:ra], ta) @ op(b[:rb], tb)) + 0.75 * c[:m]
+    assert rel(got[:m], full) <= TOL
+
+
+@pytest.mark.parametrize("spread", [0, 8])
+def test_zgemm_ozaki_wide_256_tile(orc, dev, spread):
+    # complex K = 1024 is a real product of K = 2048 on the wide tile
+    m = n = 2560
+    k = 1024
+    ar, s = orc.spread((m, k), spread, 7600 + spread)
+    ai, s = orc.spread((m, k), spread, s)
+    br, s = orc.spread((k, n), spread, s)
+    bi, s = orc.spread((k, n), spread, s)
+    a = np.asfortranarray(ar + 1j * ai)
+    b = np.asfortranarray(br + 1j * bi)
+    c = np.zeros((m, n), dtype=np.complex128, order="F")
+    alpha = 0.75 + 0.5j
+    A = to_dev(a.ravel(order="F").view(np.float64))
+    B = to_dev(b.ravel(order="F").view(np.float64))
+    C = to_dev(c.ravel(order="F").view(np.float64))
+    dev.zgemm_ozaki("N", "N", m, n, k, alpha, A, m, B, k, 0.0, C, m)
+    got = C.cpu().numpy().view(np.complex128).reshape(m, n, order="F")
+    rows, cols = samples(m, n, 1024, 7601)
+    ref = orc.zgemm_dd_sample("N", "N", k, alpha, a, b, 0.0, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL_OZ
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_dsyrk_ozaki_wide(orc, dev, uplo):
+    n, k = 2600, 2048
+    a, s = orc.matrix(n, k, 7700 + ord(uplo))
+    c, _ = orc.matrix(n, n, s)
+    C = to_dev(c)
+    dev.dsyrk_ozaki(uplo, "N", n, k, -1.0, to_dev(a), n, 1.0, C, n)
+    got = from_dev(C, n, n)
+    lower = uplo == "L"
+    rows, cols = samples(n, n, 2048, 7701, lower=lower)
+    ref = orc.dgemm_dd_sample("N", "T", k, -1.0, a, a, 1.0, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL_OZ
+    untouched = np.triu(np.ones((n, n), bool), 1) if lower else np.tril(np.ones((n, n), bool), -1)
+    assert np.array_equal(got[untouched], c[untouched])
+
+
+# ------------------------------------------------------------ DTRSM with 128-tile updates
+def test_dtrsm_large_left_lower(orc, dev):
+    # config-2 distribution (diagonal uniform[1,2], off-diagonal
+    # uniform[-1,1]/m); the recursive updates run on the 128 x 128 tile.
+    # Backward residual of 16 sampled right-hand sides against the
+    # double-double oracle, forward error of the same columns against the
+    # oracle's substitution.
+    m, n = 4096, 512
+    a, s = orc.trsm_matrix(m, 7800)
+    b, _ = orc.matrix(m, n, s)
+    B = to_dev(b)
+    dev.dtrsm("L", "L", "N", "N", m, n, 1.0, to_dev(a), m, B, m)
+    got = from_dev(B, m, n)
+    cols = np.sort(np.random.default_rng(7801).choice(n, 16, replace=False))
+    cols[-1] = n - 1
+    xs = np.asfortranarray(got[:, cols])
+    bs = np.asfortranarray(b[:, cols])
+    assert orc.dtrsm_residual("L", "L", "N", "N", m, len(cols), 1.0, a, bs, xs) <= 1e-14
+    want = bs.copy(order="F")
+    orc.dtrsm("L", "L", "N", "N", m, len(cols), 1.0, a, want)
+    assert rel(xs, want) <= TOL

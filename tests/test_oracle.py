@@ -140,3 +140,26 @@ def test_argument_checks_follow_netlib(orc):
     assert orc.check_dtrsm("R", "L", "N", "N", 5, 3, 3, 4) == 11
     assert orc.check_dsyrk("L", "T", 5, 7, 6, 5) == 7
     assert orc.check_dgemv("N", 5, 3, 5, 0, 1) == 8
+
+
+def test_componentwise_trsm_residual(orc):
+    # The oracle's substitution solve has a componentwise backward error near
+    # n*u even on a triangle with condition number ~1e9; a solution perturbed
+    # by 1e-12 relative (a planted mistake, on the CPU) is flagged.
+    rng = np.random.default_rng(4)
+    n, nrhs = 200, 8
+    t = np.asfortranarray(np.tril(rng.uniform(-1, 1, (n, n)), -1) + np.diag(rng.uniform(1, 2, n)))
+    assert np.linalg.cond(np.tril(t)) > 1e6
+    b = np.asfortranarray(rng.uniform(-1, 1, (n, nrhs)))
+    x = b.copy(order="F")
+    orc.dtrsm("L", "L", "N", "N", n, nrhs, 1.0, t, x)
+    cw = orc.dtrsm_residual_cw("L", "L", "N", "N", n, nrhs, 1.0, t, b, x)
+    assert cw <= 1e-15
+    bad = np.asfortranarray(x * (1.0 + 1e-12 * rng.choice([-1.0, 1.0], x.shape)))
+    assert orc.dtrsm_residual_cw("L", "L", "N", "N", n, nrhs, 1.0, t, b, bad) > 1e-13
+    # side R, upper, transposed: X op(A) = alpha B
+    xr = np.asfortranarray(rng.uniform(-1, 1, (nrhs, n)))
+    br = xr.copy(order="F")
+    orc.dtrsm("R", "U", "T", "N", nrhs, n, 2.0, np.asfortranarray(t.T), br)
+    # br now holds the solution of X op(A) = 2 xr
+    assert orc.dtrsm_residual_cw("R", "U", "T", "N", nrhs, n, 2.0, np.asfortranarray(t.T), xr, br) <= 1e-15
