@@ -71,6 +71,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ozaki", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-sweep", action="store_true",
+                   help="dgemm: skip the rest of the FP64 sweep and the Ozaki spreads")
     p.add_argument("--no-open-loop", action="store_true", help="serving: skip the Poisson-arrival sweep")
     return p.parse_args()
 
@@ -495,17 +497,30 @@ def run_ours(args):
                                           "BLAS2CUDA_OPTIONS=precision=ozaki at load time"}
         else:
             work.f77_step(f)
+            # the Fortran symbols run on this thread's own context: its
+            # event timers split each step into copies in, kernel, copy out
+            tctx = g.Device.of_thread()
+            tctx.enable_timing(True)
             s0 = g.stats()
             barrier(ws)
-            t0 = time.perf_counter()
-            for _ in range(args.steps):
-                work.f77_step(f)
-            te = max_over_ranks(ws, time.perf_counter() - t0, device="cuda")
+            with ClockSampler(local) as eclk:
+                t0 = time.perf_counter()
+                for _ in range(args.steps):
+                    work.f77_step(f)
+                te = max_over_ranks(ws, time.perf_counter() - t0, device="cuda")
             s1 = g.stats()
+            phases = {}
+            for name, tag in (("h2d_ms", tctx.TIMER_H2D), ("kernel_ms", work.timer_tag(tctx)),
+                              ("d2h_ms", tctx.TIMER_D2H)):
+                ms, cnt = tctx.kernel_time(tag)
+                phases[name] = ms / args.steps if cnt else None
+            tctx.enable_timing(False)
+            phases["wall_ms"] = te / args.steps * 1e3
             line["e2e"] = {"value": work.units * args.steps * ws / te, "unit": work.unit,
                            "h2d_bytes_per_step": (s1["bytes_h2d"] - s0["bytes_h2d"]) // args.steps,
                            "d2h_bytes_per_step": (s1["bytes_d2h"] - s0["bytes_d2h"]) // args.steps,
-                           "api": "Fortran ABI symbol, pinned host operands"}
+                           "api": "Fortran ABI symbol, pinned host operands",
+                           "per_step": phases, "clocks": eclk.summary()}
 
     if w == "dgemm":
         line["accuracy"] = plain_accuracy(dev, work)
@@ -516,6 +531,16 @@ def run_ours(args):
             line["ozaki"] = {"unavailable": str(e)}
     if w == "ozaki":
         line["ozaki_accuracy"] = ozaki_accuracy(dev, work)
+    if w == "dgemm" and not args.no_sweep and ws == 1:
+        del work.d
+        import torch
+        torch.cuda.empty_cache()
+        fp64_peak = line["roofline"]["peak"]
+        line["sweep"] = run_sweep(dev, stream, work.orc, fp64_peak, peaks.get("hbm_gbs", 6800.0),
+                                  2.0 * peaks.get("bf16_tflops", 1900.0), log=sys.stderr)
+        line["sweep_peaks"] = {"fp64_tflops": fp64_peak, "hbm_gbs": peaks.get("hbm_gbs"),
+                               "tensor_fp8_tflops": 2.0 * peaks.get("bf16_tflops", 1900.0),
+                               "source": f"FP64: measured in this run; HBM and bf16: {peak_src}"}
 
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         from oracle import cpublas
@@ -558,6 +583,199 @@ def plain_accuracy(dev, work, ta="N"):
     del dc
     return {"rel_err_fro_sampled": err, "samples": int(len(rows)), "tol": 1e-13,
             "ok": bool(err <= 1e-13), "oracle": "double-double dot products of the sampled entries"}
+
+
+# --------------------------------------------------------------------------
+# the rest of the plain FP64 sweep and of the Ozaki configuration, reported
+# beside the headline: DGEMM n in {1024, 4096, 8192, 16384} NN and TN, DSYRK
+# lower n = 8192 k = 2048, DTRSM LLNN 8192 with 1024 right-hand sides, DGEMV
+# 16384^2 N and T, DAXPY / DDOT / DNRM2 / IDAMAX at n = 2^28, Ozaki DGEMM 8192
+# at spreads 8 and 24.  Every entry is device-resident, timed with CUDA
+# events on the library's stream, carries its roofline fraction and checks
+# its own output against the oracle.
+# --------------------------------------------------------------------------
+def _timed(stream, fn, steps):
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        fn()
+    ev1.record(stream)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3 / steps
+
+
+def _measure(dev, stream, call, est_s, budget_s=0.6, hi=20):
+    """Time call(): one warm-up call unless a call is estimated to take more
+    than 2 s (the kernel is warm from earlier entries then), then enough
+    calls for about budget_s.  Returns (seconds per call, timed calls,
+    calls made in all)."""
+    warm = est_s <= 2.0
+    if warm:
+        call()
+        dev.sync()
+    steps = int(max(1, min(hi, budget_s / max(est_s, 1e-6))))
+    return _timed(stream, call, steps), steps, steps + int(warm)
+
+
+def run_sweep(dev, stream, orc, fp64_peak, hbm_peak, tc_peak, seed=1, log=None):
+    import torch
+    out = []
+
+    def dd(a):
+        return torch.from_numpy(np.asarray(a).ravel(order="F")).cuda()
+
+    def note(e):
+        out.append(e)
+        if log:
+            print(json.dumps(e), file=log, flush=True)
+
+    def rel(x, r):
+        return float(np.linalg.norm(np.asarray(x) - r) / np.linalg.norm(r))
+
+    # ---- DGEMM, both transposition forms, C := A op(B) + 0.5 C repeated:
+    # after s calls C = (2 - 2^(1-s)) op(A) B + 2^-s C0, checked on samples
+    for n in (1024, 4096, 8192, 16384):
+        a, st = orc.matrix(n, n, seed)
+        b, st = orc.matrix(n, n, st)
+        c, st = orc.matrix(n, n, st)
+        A, B = dd(a), dd(b)
+        for ta in ("N", "T"):
+            if n == 8192 and ta == "N":
+                continue                      # the headline line itself
+            C = dd(c)
+            call = lambda: dev.dgemm_checked(ta, "N", n, n, n, 1.0, A, n, B, n, 0.5, C, n)  # noqa: E731
+            t, steps, s_total = _measure(dev, stream, call, 2.0 * n ** 3 / (fp64_peak * 1e12))
+            rows, cols = sample_indices(n, n, 512, n)
+            got = C.view(n, n)[torch.from_numpy(cols).cuda(), torch.from_numpy(rows).cuda()].cpu().numpy()
+            ref = orc.dgemm_dd_sample(ta, "N", n, 2.0 - 2.0 ** (1 - s_total), a, b, 0.5 ** s_total, c, rows, cols)
+            tf = 2.0 * n ** 3 / t / 1e12
+            note({"routine": "dgemm", "trans": ta + "N", "m": n, "n": n, "k": n, "tflops": tf, "ms": t * 1e3,
+                  "steps": steps, "frac_fp64": tf / fp64_peak, "rel_err_sampled": rel(got, ref)})
+            del C
+        del A, B, a, b, c
+        torch.cuda.empty_cache()
+
+    # ---- DSYRK lower, n = 8192, k = 2048 (alpha 1, beta 0.5, repeated)
+    n, k = 8192, 2048
+    a, st = orc.matrix(n, k, seed)
+    c, st = orc.matrix(n, n, st)
+    A, C = dd(a), dd(c)
+    call = lambda: dev.dsyrk("L", "N", n, k, 1.0, A, n, 0.5, C, n)  # noqa: E731
+    t, steps, s_total = _measure(dev, stream, call, float(n) * (n + 1) * k / (fp64_peak * 1e12))
+    rows, cols = sample_indices(n, n, 1024, 5)
+    keep = rows >= cols
+    rows, cols = rows[keep], cols[keep]
+    got = C.view(n, n)[torch.from_numpy(cols).cuda(), torch.from_numpy(rows).cuda()].cpu().numpy()
+    ref = orc.dgemm_dd_sample("N", "T", k, 2.0 - 2.0 ** (1 - s_total), a, a, 0.5 ** s_total, c, rows, cols)
+    tf = float(n) * (n + 1) * k / t / 1e12
+    note({"routine": "dsyrk", "uplo": "L", "trans": "N", "n": n, "k": k, "tflops": tf, "ms": t * 1e3,
+          "steps": steps, "frac_fp64": tf / fp64_peak, "rel_err_sampled": rel(got, ref)})
+    del A, C, a, c
+
+    # ---- DTRSM LLNN, 8192 x 8192 triangle, 1024 right-hand sides
+    m, nrhs = 8192, 1024
+    a, st = orc.trsm_matrix(m, seed)
+    b, st = orc.matrix(m, nrhs, st)
+    A, B0 = dd(a), dd(b)
+    B = B0.clone()
+    call = lambda: dev.dtrsm("L", "L", "N", "N", m, nrhs, 1.0, A, m, B, m)  # noqa: E731
+    t, steps, _ = _measure(dev, stream, call, float(m) * m * nrhs / (fp64_peak * 1e12), hi=10)
+    B.copy_(B0)
+    torch.cuda.synchronize()      # torch's stream does not order with the library's
+    call()
+    dev.sync()
+    cols = np.array([0, 377, 801, nrhs - 1])
+    xs = B.view(nrhs, m)[torch.from_numpy(cols).cuda()].cpu().numpy().T.copy(order="F")
+    want = np.asfortranarray(b[:, cols])
+    orc.dtrsm("L", "L", "N", "N", m, len(cols), 1.0, a, want)
+    tf = float(m) * m * nrhs / t / 1e12
+    note({"routine": "dtrsm", "side": "L", "uplo": "L", "trans": "N", "diag": "N", "m": m, "n": nrhs,
+          "tflops": tf, "ms": t * 1e3, "steps": steps, "frac_fp64": tf / fp64_peak,
+          "rel_err_sampled": rel(xs, want), "checked": "4 solution columns against the oracle's substitution"})
+    del A, B, B0, a, b
+    torch.cuda.empty_cache()
+
+    # ---- DGEMV 16384^2, N and T (y := A x + 0.5 y repeated)
+    n = 16384
+    a, st = orc.matrix(n, n, seed)
+    x, st = orc.uniform(n, st)
+    y, st = orc.uniform(n, st)
+    A, X = dd(a), dd(x)
+    for tr in ("N", "T"):
+        Y = dd(y)
+        call = lambda: dev.dgemv(tr, n, n, 1.0, A, n, X, 1, 0.5, Y, 1)  # noqa: E731
+        t, steps, s_total = _measure(dev, stream, call, 8.0 * n * n / (hbm_peak * 1e9), budget_s=0.3)
+        rows = np.random.default_rng(7).integers(0, n, 256)
+        got = Y.cpu().numpy()[rows]
+        ref = orc.dgemm_dd_sample(tr, "N", n, 2.0 - 2.0 ** (1 - s_total), a, x.reshape(n, 1, order="F"),
+                                  0.5 ** s_total, y.reshape(n, 1, order="F"), rows, np.zeros_like(rows))
+        gbs = 8.0 * (n * n + n + 2 * n) / t / 1e9
+        note({"routine": "dgemv", "trans": tr, "m": n, "n": n, "gbs": gbs, "ms": t * 1e3, "steps": steps,
+              "frac_hbm": gbs / hbm_peak, "rel_err_sampled": rel(got, ref)})
+        del Y
+    del A, X, a
+
+    # ---- Level 1 at n = 2^28
+    n = 1 << 28
+    x, st = orc.uniform(n, seed)
+    y, st = orc.uniform(n, st)
+    X, Y = dd(x), dd(y)
+    res = torch.zeros(2, dtype=torch.float64, device="cuda")
+    for r, nbytes in (("daxpy", 24), ("ddot", 16), ("dnrm2", 8), ("idamax", 8)):
+        if r == "daxpy":
+            Yw = Y.clone()
+            call = lambda: dev.daxpy(n, 0.5, X, 1, Yw, 1)  # noqa: E731
+        elif r == "ddot":
+            call = lambda: dev.ddot(n, X, 1, Y, 1, res)  # noqa: E731
+        elif r == "dnrm2":
+            call = lambda: dev.dnrm2(n, X, 1, res)  # noqa: E731
+        else:
+            call = lambda: dev.idamax(n, X, 1, res)  # noqa: E731
+        t, steps, s_total = _measure(dev, stream, call, float(nbytes) * n / (hbm_peak * 1e9), budget_s=0.2)
+        dev.sync()
+        if r == "daxpy":
+            idx = np.random.default_rng(3).integers(0, n, 4096)
+            got = Yw[torch.from_numpy(idx).cuda()].cpu().numpy()
+            err = rel(got, y[idx] + 0.5 * s_total * x[idx])
+            del Yw
+        elif r == "ddot":
+            err = abs(float(res[0].item()) - orc.ddot_dd(n, x, 1, y, 1)) / float(np.abs(x) @ np.abs(y))
+        elif r == "dnrm2":
+            ref = orc.dnrm2(n, x, 1)
+            err = abs(float(res[0].item()) - ref) / ref
+        else:
+            got = int(res.view(torch.int32)[0].item())
+            err = 0.0 if got == orc.idamax(n, x, 1) else 1.0
+        gbs = float(nbytes) * n / t / 1e9
+        note({"routine": r, "n": n, "gbs": gbs, "ms": t * 1e3, "steps": steps, "frac_hbm": gbs / hbm_peak,
+              ("index_mismatch" if r == "idamax" else "rel_err"): err})
+    del X, Y, x, y, res
+    torch.cuda.empty_cache()
+
+    # ---- Ozaki DGEMM n = 8192 at exponent spreads 8 and 24 (tol 1e-14)
+    n = 8192
+    for spread in (8, 24):
+        st = 1000 + n + spread
+        a, st = orc.spread((n, n), spread, st)
+        b, st = orc.spread((n, n), spread, st)
+        A, B = dd(a), dd(b)
+        C = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+        used = dev.dgemm_ozaki("N", "N", n, n, n, 1.0, A, n, B, n, 0.0, C, n)
+        call = lambda: dev.dgemm_ozaki("N", "N", n, n, n, 1.0, A, n, B, n, 0.0, C, n,  # noqa: E731
+                                       want_slices=False)
+        t, steps, _ = _measure(dev, stream, call, 0.03, budget_s=0.3)
+        rows, cols = sample_indices(n, n, 512, spread)
+        got = C.view(n, n)[torch.from_numpy(cols).cuda(), torch.from_numpy(rows).cuda()].cpu().numpy()
+        ref = orc.dgemm_dd_sample("N", "N", n, 1.0, a, b, 0.0, np.zeros((1, 1), order="F"), rows, cols)
+        tf = 2.0 * n ** 3 / t / 1e12
+        raw = used * (used + 1) / 2 * 2.0 * n ** 3 / t / 1e12
+        note({"routine": "dgemm_ozaki", "spread": spread, "m": n, "n": n, "k": n, "slices": used,
+              "tflops": tf, "ms": t * 1e3, "steps": steps, "vs_plain_fp64": tf / fp64_peak,
+              "frac_tensor": raw / tc_peak, "rel_err_sampled": rel(got, ref)})
+        del A, B, C, a, b
+        torch.cuda.empty_cache()
+    return out
 
 
 def ozaki_accuracy(dev, work):

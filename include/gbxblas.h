@@ -71,7 +71,9 @@ enum {
     GBX_TIMER_OZAKI_SPLIT = 3, /* slicing of the FP64 operands                   */
     GBX_TIMER_LEVEL1 = 4,      /* Level-1 streaming kernels                      */
     GBX_TIMER_GEMV = 5,        /* DGEMV streaming kernel                         */
-    GBX_TIMER_BATCH = 6        /* grouped / batched kernels                      */
+    GBX_TIMER_BATCH = 6,       /* grouped / batched kernels                      */
+    GBX_TIMER_H2D = 7,         /* staging copies of host operands into the GPU   */
+    GBX_TIMER_D2H = 8          /* copies of staged results back to the host      */
 };
 gbx_status gbx_ctx_enable_timing(gbx_ctx *ctx, int on);
 gbx_status gbx_ctx_kernel_time(gbx_ctx *ctx, int tag, double *ms, uint64_t *count);

@@ -428,9 +428,24 @@ class Device:
         if stream is not None:
             self.L.gbx_ctx_set_stream(self.ctx, C.c_void_p(stream))
 
+    @classmethod
+    def of_thread(cls):
+        """The calling thread's own context (the one the Fortran-ABI symbols
+        use), wrapped without taking ownership: close() leaves it alive."""
+        self = cls.__new__(cls)
+        self.L = load()
+        self.L.gbx_thread_ctx.restype = _P
+        h = self.L.gbx_thread_ctx()
+        if not h:
+            raise GbxError("gbx_thread_ctx failed")
+        self.ctx = _P(h)
+        self._borrowed = True
+        return self
+
     def close(self):
         if self.ctx:
-            self.L.gbx_ctx_destroy(self.ctx)
+            if not getattr(self, "_borrowed", False):
+                self.L.gbx_ctx_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):
@@ -464,6 +479,7 @@ class Device:
 
     TIMER_GEMM_FP64, TIMER_OZAKI_MMA, TIMER_OZAKI_SPLIT = 1, 2, 3
     TIMER_LEVEL1, TIMER_GEMV, TIMER_BATCH = 4, 5, 6
+    TIMER_H2D, TIMER_D2H = 7, 8
 
     def enable_timing(self, on=True):
         self._ok(self.L.gbx_ctx_enable_timing(self.ctx, 1 if on else 0), "enable_timing")

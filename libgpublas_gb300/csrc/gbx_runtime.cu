@@ -407,10 +407,12 @@ extern "C" gbx_status gbx_place_in(gbx_ctx *c, int slot, const void *host, int r
     if (copy_in && rows > 0 && cols > 0) {
         // one linear copy when the columns are contiguous on both sides (a
         // pitched copy of many short rows runs well below the link rate)
+        gbx_timer_begin(c, GBX_TIMER_H2D);
         cudaError_t e = (dld == ld && dld == rows)
                             ? cudaMemcpyAsync(d, host, (size_t)rows * cols * elem, cudaMemcpyHostToDevice, c->stream)
                             : cudaMemcpy2DAsync(d, (size_t)dld * elem, host, (size_t)ld * elem, (size_t)rows * elem,
                                                 (size_t)cols, cudaMemcpyHostToDevice, c->stream);
+        gbx_timer_end(c);
         if (e != cudaSuccess)
             return gbx_fail(c, GBX_ERR_CUDA, "stage in: %s", cudaGetErrorString(e));
         g_h2d += (uint64_t)rows * cols * elem;
@@ -422,12 +424,14 @@ extern "C" gbx_status gbx_place_out(gbx_ctx *c, const gbx_operand *op, int rows,
                                     size_t elem)
 {
     if (!op->staged || rows <= 0 || cols <= 0) return GBX_OK;
+    gbx_timer_begin(c, GBX_TIMER_D2H);
     cudaError_t e = (op->ld == op->host_ld && op->ld == rows)
                         ? cudaMemcpyAsync((void *)op->host, op->dev, (size_t)rows * cols * elem,
                                           cudaMemcpyDeviceToHost, c->stream)
                         : cudaMemcpy2DAsync((void *)op->host, (size_t)op->host_ld * elem, op->dev,
                                             (size_t)op->ld * elem, (size_t)rows * elem, (size_t)cols,
                                             cudaMemcpyDeviceToHost, c->stream);
+    gbx_timer_end(c);
     if (e != cudaSuccess) return gbx_fail(c, GBX_ERR_CUDA, "stage out: %s", cudaGetErrorString(e));
     g_d2h += (uint64_t)rows * cols * elem;
     return GBX_OK;

@@ -29,8 +29,12 @@ GBX_ERR_TIMEOUT = 4
 
 
 def to_dev(a):
+    # the library's context stream does not order with torch's stream: the
+    # copy is complete before the call is issued
     import torch
-    return torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+    t = torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+    torch.cuda.synchronize()
+    return t
 
 
 def test_expired_wait_reports_timeout_and_context_recovers(orc, lib):

@@ -40,8 +40,12 @@ def padded(orc, rows, cols, seed, pad=3):
 
 
 def to_dev(a):
+    # the library's context stream does not order with torch's stream: the
+    # copy is complete before the call is issued
     import torch
-    return torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+    t = torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+    torch.cuda.synchronize()
+    return t
 
 
 def from_dev(t, rows, cols):
@@ -85,6 +89,7 @@ def test_dgemm_128_tile(orc, dev, ta, tb, m, n, k):
             cin[:m] = np.nan          # beta = 0 must overwrite, not scale
         C = to_dev(cin)
         dev.dgemm_checked(ta, tb, m, n, k, alpha, A, a.shape[0], B, b.shape[0], beta, C, c.shape[0])
+        dev.sync()
         got = from_dev(C, c.shape[0], n)
         assert np.all(got[m:] == SENT)
         ref = orc.dgemm_dd_sample(ta, tb, k, alpha, a, b, beta, c, rows, cols)
@@ -119,6 +124,7 @@ def test_dsyrk_128_tile(orc, dev, uplo, trans):
     c, _ = padded(orc, n, n, s)
     C = to_dev(c)
     dev.dsyrk(uplo, trans, n, k, -0.75, to_dev(a), a.shape[0], 0.5, C, c.shape[0])
+    dev.sync()
     got = from_dev(C, c.shape[0], n)
     assert np.all(got[n:] == SENT)
     lower = uplo == "L"
@@ -143,6 +149,7 @@ def test_dtrmm_128_tile(orc, dev, side, uplo, ta):
     b, _ = padded(orc, m, n, s)
     B = to_dev(b)
     dev.dtrmm(side, uplo, ta, "N", m, n, 0.5, to_dev(a), na, B, b.shape[0])
+    dev.sync()
     got = from_dev(B, b.shape[0], n)
     assert np.all(got[m:] == SENT)
     t = np.tril(a) if uplo == "L" else np.triu(a)
@@ -167,6 +174,7 @@ def test_zgemm_64_tile(orc, dev, ta, tb):
     B = to_dev(b.ravel(order="F").view(np.float64))
     C = to_dev(c.ravel(order="F").view(np.float64))
     dev.zgemm(ta, tb, m, n, k, alpha, A, ra, B, rb, beta, C, m)
+    dev.sync()
     got = C.cpu().numpy().view(np.complex128).reshape(m, n, order="F")
     rows, cols = samples(m, n, 1024, 7301)
     ref = orc.zgemm_dd_sample(ta, tb, k, alpha, a, b, beta, c, rows, cols)
@@ -267,6 +275,7 @@ def test_dtrsm_large_left_lower(orc, dev):
     b, _ = orc.matrix(m, n, s)
     B = to_dev(b)
     dev.dtrsm("L", "L", "N", "N", m, n, 1.0, to_dev(a), m, B, m)
+    dev.sync()
     got = from_dev(B, m, n)
     cols = np.sort(np.random.default_rng(7801).choice(n, 16, replace=False))
     cols[-1] = n - 1

@@ -31,8 +31,12 @@ CASES = [(s, u, t) for s, u, t in [("L", "L", "N"), ("L", "U", "T"), ("R", "L", 
 
 
 def to_dev(a):
+    # the library's context stream does not order with torch's stream: the
+    # copy is complete before the call is issued
     import torch
-    return torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+    t = torch.from_numpy(np.asfortranarray(a).ravel(order="F").copy()).cuda()
+    torch.cuda.synchronize()
+    return t
 
 
 def from_dev(t, rows, cols):
@@ -53,13 +57,14 @@ def triangle(kind, n, seed, uplo):
     return np.asfortranarray(a)
 
 
-def solve_and_measure(orc, run, kind, na, side, uplo, ta, nrhs=48):
+def solve_and_measure(orc, dev, run, kind, na, side, uplo, ta, nrhs=48):
     a = triangle(kind, na, 8000 + na + ord(side) + ord(uplo), uplo)
     m, n = (na, nrhs) if side == "L" else (nrhs, na)
     b = np.asfortranarray(np.random.default_rng(8100 + na).uniform(-1, 1, (m, n)))
     alpha = 1.5
     B = to_dev(b)
     run(side, uplo, ta, m, n, alpha, to_dev(a), na, B, m)
+    dev.sync()
     x = np.asfortranarray(from_dev(B, m, n))
     assert np.all(np.isfinite(x))
     nw = orc.dtrsm_residual(side, uplo, ta, "N", m, n, alpha, a, b, x)
@@ -75,7 +80,7 @@ def solve_and_measure(orc, run, kind, na, side, uplo, ta, nrhs=48):
 def test_plain_dtrsm_ill_conditioned(orc, dev, kind, na, side, uplo, ta):
     def run(side, uplo, ta, m, n, alpha, A, lda, B, ldb):
         dev.dtrsm(side, uplo, ta, "N", m, n, alpha, A, lda, B, ldb)
-    nw, cw, cw_subst, cond = solve_and_measure(orc, run, kind, na, side, uplo, ta)
+    nw, cw, cw_subst, cond = solve_and_measure(orc, dev, run, kind, na, side, uplo, ta)
     print(f"plain {kind} n={na} {side}{uplo}{ta}: cond {cond:.1e} normwise {nw:.2e} "
           f"componentwise {cw:.2e} (substitution {cw_subst:.2e})")
     assert cond > 1e7
@@ -88,7 +93,7 @@ def test_plain_dtrsm_ill_conditioned(orc, dev, kind, na, side, uplo, ta):
 def test_ozaki_dtrsm_ill_conditioned(orc, dev, kind, na, side, uplo, ta):
     def run(side, uplo, ta, m, n, alpha, A, lda, B, ldb):
         dev.dtrsm_ozaki(side, uplo, ta, "N", m, n, alpha, A, lda, B, ldb)
-    nw, cw, cw_subst, cond = solve_and_measure(orc, run, kind, na, side, uplo, ta)
+    nw, cw, cw_subst, cond = solve_and_measure(orc, dev, run, kind, na, side, uplo, ta)
     print(f"ozaki {kind} n={na} {side}{uplo}{ta}: cond {cond:.1e} normwise {nw:.2e} "
           f"componentwise {cw:.2e} (substitution {cw_subst:.2e})")
     assert nw <= 1e-14
