@@ -18,6 +18,9 @@ Trace lines (written by the interposer):
   T #<nth> [<ptr>] fun=[malloc|calloc|realloc] reqsize=[<n>] tid=[..] time=[<s>s+<ns>ns] uid=[<uid>]
   U #<nth> ... fun=[free] ...
   C #<nth> ... fun=[<blas routine>] ...
+(with OBJTRACKER_OPTIONS=only_print_calls only the C lines are written; the
+decision file then lists the called objects alone, and the rest stay on the
+host by default).
 Decision lines:
   D #<nth> U<uid> fun=[malloc] reqsize=[<n>] calls=[<k>]
 """
@@ -37,8 +40,11 @@ def analyze(lines):
         kind, nth, fun, reqsize, uid = m.group(1), int(m.group(2)), m.group(3), int(m.group(4)), int(m.group(5))
         if kind == "T":
             objs[uid] = {"nth": nth, "fun": fun, "reqsize": reqsize, "calls": 0}
-        elif kind == "C" and uid in objs:
-            objs[uid]["calls"] += 1
+        elif kind == "C":
+            # a trace written with OBJTRACKER_OPTIONS=only_print_calls has no
+            # T lines: the call line carries the object's index and size
+            o = objs.setdefault(uid, {"nth": nth, "fun": "alloc", "reqsize": reqsize, "calls": 0})
+            o["calls"] += 1
     return objs
 
 

@@ -107,7 +107,9 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     core = [o for o in objs if not os.path.basename(o).startswith("preload_")]
     for out, parts in ((LIB, core), (PRELOAD_LIB, objs)):
         tmp = out + ".tmp%d" % os.getpid()
-        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + parts + ["-lpthread", "-ldl"])
+        # executing the library prints its options (csrc/so_entry.c)
+        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + parts +
+             ["-Xlinker", "-e", "-Xlinker", "gbx_so_entry", "-lpthread", "-ldl"])
         os.replace(tmp, out)
     # libgbxdiag.so: benchmark and failure-path diagnostics, resolved against
     # libgbxblas.so next to it

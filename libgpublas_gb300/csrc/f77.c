@@ -125,6 +125,7 @@ void dgemm_(const char *transa, const char *transb, const int *m, const int *n, 
     int info = gbx_check_gemm_args(*transa, *transb, *m, *n, *k, *lda, *ldb, *ldc);
     if (info) { xerbla_("DGEMM ", &info, 6); return; }
     NOTE("dgemm_", a); NOTE("dgemm_", b); NOTE("dgemm_", c);
+    GBX_FORWARD(dgemm_, (transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc));
     if (*m == 0 || *n == 0 || ((*alpha == 0.0 || *k == 0) && *beta == 1.0)) return;
     gbx_ctx *ctx = ctx_or_report("DGEMM");
     if (!ctx) return;
@@ -173,6 +174,7 @@ void zgemm_(const char *transa, const char *transb, const int *m, const int *n, 
     int info = gbx_check_gemm_args(*transa, *transb, *m, *n, *k, *lda, *ldb, *ldc);
     if (info) { xerbla_("ZGEMM ", &info, 6); return; }
     NOTE("zgemm_", a); NOTE("zgemm_", b); NOTE("zgemm_", c);
+    GBX_FORWARD(zgemm_, (transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc));
     const int alpha0 = alpha[0] == 0.0 && alpha[1] == 0.0;
     const int beta0 = beta[0] == 0.0 && beta[1] == 0.0;
     const int beta1 = beta[0] == 1.0 && beta[1] == 0.0;
@@ -210,6 +212,7 @@ void dsyrk_(const char *uplo, const char *trans, const int *n, const int *k, con
     int info = gbx_check_syrk_args(*uplo, *trans, *n, *k, *lda, *ldc);
     if (info) { xerbla_("DSYRK ", &info, 6); return; }
     NOTE("dsyrk_", a); NOTE("dsyrk_", c);
+    GBX_FORWARD(dsyrk_, (uplo, trans, n, k, alpha, a, lda, beta, c, ldc));
     if (*n == 0 || ((*alpha == 0.0 || *k == 0) && *beta == 1.0)) return;
     gbx_ctx *ctx = ctx_or_report("DSYRK");
     if (!ctx) return;
@@ -258,6 +261,8 @@ static void trxm(const char *name, trxm_fn fn, const char *side, const char *upl
     if (info) { xerbla_(name, &info, 6); return; }
     NOTE(fn == gbx_dtrsm ? "dtrsm_" : "dtrmm_", a);
     NOTE(fn == gbx_dtrsm ? "dtrsm_" : "dtrmm_", b);
+    if (fn == gbx_dtrsm) GBX_FORWARD(dtrsm_, (side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb));
+    else GBX_FORWARD(dtrmm_, (side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb));
     if (*m == 0 || *n == 0) return;
     gbx_ctx *ctx = ctx_or_report(name);
     if (!ctx) return;
@@ -314,6 +319,7 @@ void dgemv_(const char *trans, const int *m, const int *n, const double *alpha, 
     int info = gbx_check_gemv_args(*trans, *m, *n, *lda, *incx, *incy);
     if (info) { xerbla_("DGEMV ", &info, 6); return; }
     NOTE("dgemv_", a); NOTE("dgemv_", x); NOTE("dgemv_", y);
+    GBX_FORWARD(dgemv_, (trans, m, n, alpha, a, lda, x, incx, beta, y, incy));
     if (*m == 0 || *n == 0 || (*alpha == 0.0 && *beta == 1.0)) return;
     gbx_ctx *ctx = ctx_or_report("DGEMV");
     if (!ctx) return;
@@ -347,6 +353,7 @@ void dger_(const int *m, const int *n, const double *alpha, const double *x, con
     int info = gbx_check_ger_args(*m, *n, *incx, *incy, *lda);
     if (info) { xerbla_("DGER  ", &info, 6); return; }
     NOTE("dger_", x); NOTE("dger_", y); NOTE("dger_", a);
+    GBX_FORWARD(dger_, (m, n, alpha, x, incx, y, incy, a, lda));
     if (*m == 0 || *n == 0 || *alpha == 0.0) return;
     gbx_ctx *ctx = ctx_or_report("DGER");
     if (!ctx) return;
@@ -369,6 +376,7 @@ void dsymv_(const char *uplo, const int *n, const double *alpha, const double *a
     int info = gbx_check_symv_args(*uplo, *n, *lda, *incx, *incy);
     if (info) { xerbla_("DSYMV ", &info, 6); return; }
     NOTE("dsymv_", a); NOTE("dsymv_", x); NOTE("dsymv_", y);
+    GBX_FORWARD(dsymv_, (uplo, n, alpha, a, lda, x, incx, beta, y, incy));
     if (*n == 0 || (*alpha == 0.0 && *beta == 1.0)) return;
     gbx_ctx *ctx = ctx_or_report("DSYMV");
     if (!ctx) return;
@@ -394,6 +402,7 @@ void dtrsv_(const char *uplo, const char *trans, const char *diag, const int *n,
     int info = gbx_check_trsv_args(*uplo, *trans, *diag, *n, *lda, *incx);
     if (info) { xerbla_("DTRSV ", &info, 6); return; }
     NOTE("dtrsv_", a); NOTE("dtrsv_", x);
+    GBX_FORWARD(dtrsv_, (uplo, trans, diag, n, a, lda, x, incx));
     if (*n == 0) return;
     gbx_ctx *ctx = ctx_or_report("DTRSV");
     if (!ctx) return;
@@ -415,6 +424,7 @@ void daxpy_(const int *n, const double *alpha, const double *x, const int *incx,
 {
     if (*n <= 0 || *alpha == 0.0) return;
     NOTE("daxpy_", x); NOTE("daxpy_", y);
+    GBX_FORWARD(daxpy_, (n, alpha, x, incx, y, incy));
     gbx_ctx *ctx = ctx_or_report("DAXPY");
     if (!ctx) return;
     gbx_status st;
@@ -433,6 +443,7 @@ double ddot_(const int *n, const double *x, const int *incx, const double *y, co
 {
     if (*n <= 0) return 0.0;
     NOTE("ddot_", x); NOTE("ddot_", y);
+    GBX_FORWARD_RET(ddot_, (n, x, incx, y, incy));
     gbx_ctx *ctx = ctx_or_report("DDOT");
     if (!ctx) return 0.0;
     gbx_status st;
@@ -453,6 +464,7 @@ double dnrm2_(const int *n, const double *x, const int *incx)
 {
     if (*n < 1 || *incx < 1) return 0.0;
     NOTE("dnrm2_", x);
+    GBX_FORWARD_RET(dnrm2_, (n, x, incx));
     gbx_ctx *ctx = ctx_or_report("DNRM2");
     if (!ctx) return 0.0;
     gbx_status st;
@@ -472,6 +484,8 @@ static int iamx(const char *name, int is_min, const int *n, const double *x, con
 {
     if (*n < 1 || *incx <= 0) return 0;
     NOTE(is_min ? "idamin_" : "idamax_", x);
+    if (is_min) GBX_FORWARD_RET(idamin_, (n, x, incx));
+    else GBX_FORWARD_RET(idamax_, (n, x, incx));
     if (*n == 1) return 1;
     gbx_ctx *ctx = ctx_or_report(name);
     if (!ctx) return 0;

@@ -2,7 +2,7 @@
  * f77_level3.c — Fortran-ABI and CBLAS entry points of the Level-3 routines
  * beyond the D/Z set of f77.c: xGEMM for S and C, xSYMM, xHEMM, xSYRK (S, C,
  * Z), xHERK, xSYR2K, xHER2K, xTRMM (S, C, Z) and xTRSM (S, C, Z).  These are
- * the symbols the reference exports from blas_level3/*.cc (F77_gemm,
+ * the symbols the reference exports from blas_level3/<routine>.cc (F77_gemm,
  * F77_symm, ... prototypes at blas.h:202-314); the reference hands each to
  * cuBLAS after its argument check.
  *
@@ -89,10 +89,11 @@ static gbx_status run_cgemm(gbx_ctx *ctx, const gbx_operand *a, const gbx_operan
                      c->ld);
 }
 
-#define GEMM_BODY(LABEL, NAME, ESZ, RUN, ALPHA0, BETA0, BETA1)                                                  \
+#define GEMM_BODY(LABEL, NAME, SYM, ESZ, RUN, ALPHA0, BETA0, BETA1)                                                  \
     int info = gbx_check_gemm_args(*transa, *transb, *m, *n, *k, *lda, *ldb, *ldc);                             \
     if (info) { xerbla_(LABEL, &info, 6); return; }                                                             \
     NOTE(NAME, a); NOTE(NAME, b); NOTE(NAME, c);                                                                \
+    GBX_FORWARD(SYM, (transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc));                           \
     if (*m == 0 || *n == 0 || (((ALPHA0) || *k == 0) && (BETA1))) return;                                       \
     const int nota = gbx_lsame(*transa, 'N'), notb = gbx_lsame(*transb, 'N');                                  \
     struct gemm_args g = {*transa, *transb, *m, *n, *k, alpha, beta};                                           \
@@ -103,14 +104,14 @@ void sgemm_(const char *transa, const char *transb, const int *m, const int *n, 
             const float *a, const int *lda, const float *b, const int *ldb, const float *beta, float *c,
             const int *ldc)
 {
-    GEMM_BODY("SGEMM ", "sgemm_", 4, run_sgemm, *alpha == 0.0f, *beta == 0.0f, *beta == 1.0f)
+    GEMM_BODY("SGEMM ", "sgemm_", sgemm_, 4, run_sgemm, *alpha == 0.0f, *beta == 0.0f, *beta == 1.0f)
 }
 
 void cgemm_(const char *transa, const char *transb, const int *m, const int *n, const int *k, const float *alpha,
             const float *a, const int *lda, const float *b, const int *ldb, const float *beta, float *c,
             const int *ldc)
 {
-    GEMM_BODY("CGEMM ", "cgemm_", 8, run_cgemm, z2(alpha), z2(beta), o2(beta))
+    GEMM_BODY("CGEMM ", "cgemm_", cgemm_, 8, run_cgemm, z2(alpha), z2(beta), o2(beta))
 }
 
 /* -------------------------------------------------------- xSYMM / xHEMM */
@@ -143,10 +144,11 @@ RUN_SYMM_CPLX(zsymm)
 RUN_SYMM_CPLX(chemm)
 RUN_SYMM_CPLX(zhemm)
 
-#define SYMM_BODY(LABEL, NAME, ESZ, RUN, ALPHA0, BETA0, BETA1)                                                  \
+#define SYMM_BODY(LABEL, NAME, SYM, ESZ, RUN, ALPHA0, BETA0, BETA1)                                                  \
     int info = gbx_check_symm_args(*side, *uplo, *m, *n, *lda, *ldb, *ldc);                                     \
     if (info) { xerbla_(LABEL, &info, 6); return; }                                                             \
     NOTE(NAME, a); NOTE(NAME, b); NOTE(NAME, c);                                                                \
+    GBX_FORWARD(SYM, (side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc));                                  \
     if (*m == 0 || *n == 0 || ((ALPHA0) && (BETA1))) return;                                                    \
     const int na = gbx_lsame(*side, 'L') ? *m : *n;                                                             \
     struct symm_args s = {*side, *uplo, *m, *n, alpha, beta};                                                   \
@@ -157,12 +159,12 @@ RUN_SYMM_CPLX(zhemm)
     void FN##_(const char *side, const char *uplo, const int *m, const int *n, const T *alpha, const T *a,      \
                const int *lda, const T *b, const int *ldb, const T *beta, T *c, const int *ldc)
 
-SYMM_PROTO(ssymm, float) { SYMM_BODY("SSYMM ", "ssymm_", 4, run_ssymm, *alpha == 0.0f, *beta == 0.0f, *beta == 1.0f) }
-SYMM_PROTO(dsymm, double) { SYMM_BODY("DSYMM ", "dsymm_", 8, run_dsymm, *alpha == 0.0, *beta == 0.0, *beta == 1.0) }
-SYMM_PROTO(csymm, float) { SYMM_BODY("CSYMM ", "csymm_", 8, run_csymm, z2(alpha), z2(beta), o2(beta)) }
-SYMM_PROTO(zsymm, double) { SYMM_BODY("ZSYMM ", "zsymm_", 16, run_zsymm, zz(alpha), zz(beta), oz(beta)) }
-SYMM_PROTO(chemm, float) { SYMM_BODY("CHEMM ", "chemm_", 8, run_chemm, z2(alpha), z2(beta), o2(beta)) }
-SYMM_PROTO(zhemm, double) { SYMM_BODY("ZHEMM ", "zhemm_", 16, run_zhemm, zz(alpha), zz(beta), oz(beta)) }
+SYMM_PROTO(ssymm, float) { SYMM_BODY("SSYMM ", "ssymm_", ssymm_, 4, run_ssymm, *alpha == 0.0f, *beta == 0.0f, *beta == 1.0f) }
+SYMM_PROTO(dsymm, double) { SYMM_BODY("DSYMM ", "dsymm_", dsymm_, 8, run_dsymm, *alpha == 0.0, *beta == 0.0, *beta == 1.0) }
+SYMM_PROTO(csymm, float) { SYMM_BODY("CSYMM ", "csymm_", csymm_, 8, run_csymm, z2(alpha), z2(beta), o2(beta)) }
+SYMM_PROTO(zsymm, double) { SYMM_BODY("ZSYMM ", "zsymm_", zsymm_, 16, run_zsymm, zz(alpha), zz(beta), oz(beta)) }
+SYMM_PROTO(chemm, float) { SYMM_BODY("CHEMM ", "chemm_", chemm_, 8, run_chemm, z2(alpha), z2(beta), o2(beta)) }
+SYMM_PROTO(zhemm, double) { SYMM_BODY("ZHEMM ", "zhemm_", zhemm_, 16, run_zhemm, zz(alpha), zz(beta), oz(beta)) }
 
 /* -------------------------------------------------------- xSYRK / xHERK */
 struct rk_args {
@@ -195,10 +197,11 @@ RUN_SYRK_CPLX(zsyrk)
 RUN_SYRK_SCALAR(cherk, float)
 RUN_SYRK_SCALAR(zherk, double)
 
-#define RK_BODY(LABEL, NAME, ESZ, RUN, ALLOWED, ALPHA0, BETA1)                                                  \
+#define RK_BODY(LABEL, NAME, SYM, ESZ, RUN, ALLOWED, ALPHA0, BETA1)                                                  \
     int info = gbx_check_rank_k_args(*uplo, *trans, ALLOWED, *n, *k, *lda, *ldc);                               \
     if (info) { xerbla_(LABEL, &info, 6); return; }                                                             \
     NOTE(NAME, a); NOTE(NAME, c);                                                                               \
+    GBX_FORWARD(SYM, (uplo, trans, n, k, alpha, a, lda, beta, c, ldc));                                         \
     if (*n == 0 || (((ALPHA0) || *k == 0) && (BETA1))) return;                                                  \
     const int notr = gbx_lsame(*trans, 'N');                                                                    \
     struct rk_args r = {*uplo, *trans, *n, *k, alpha, beta, NULL};                                              \
@@ -212,17 +215,17 @@ RUN_SYRK_SCALAR(zherk, double)
 
 RK_PROTO(ssyrk, float, float)
 {
-    RK_BODY("SSYRK ", "ssyrk_", 4, run_ssyrk, GBX_TR_N | GBX_TR_T | GBX_TR_C, *alpha == 0.0f, *beta == 1.0f)
+    RK_BODY("SSYRK ", "ssyrk_", ssyrk_, 4, run_ssyrk, GBX_TR_N | GBX_TR_T | GBX_TR_C, *alpha == 0.0f, *beta == 1.0f)
 }
-RK_PROTO(csyrk, float, float) { RK_BODY("CSYRK ", "csyrk_", 8, run_csyrk, GBX_TR_N | GBX_TR_T, z2(alpha), o2(beta)) }
-RK_PROTO(zsyrk, double, double) { RK_BODY("ZSYRK ", "zsyrk_", 16, run_zsyrk, GBX_TR_N | GBX_TR_T, zz(alpha), oz(beta)) }
+RK_PROTO(csyrk, float, float) { RK_BODY("CSYRK ", "csyrk_", csyrk_, 8, run_csyrk, GBX_TR_N | GBX_TR_T, z2(alpha), o2(beta)) }
+RK_PROTO(zsyrk, double, double) { RK_BODY("ZSYRK ", "zsyrk_", zsyrk_, 16, run_zsyrk, GBX_TR_N | GBX_TR_T, zz(alpha), oz(beta)) }
 RK_PROTO(cherk, float, float)
 {
-    RK_BODY("CHERK ", "cherk_", 8, run_cherk, GBX_TR_N | GBX_TR_C, *alpha == 0.0f, *beta == 1.0f)
+    RK_BODY("CHERK ", "cherk_", cherk_, 8, run_cherk, GBX_TR_N | GBX_TR_C, *alpha == 0.0f, *beta == 1.0f)
 }
 RK_PROTO(zherk, double, double)
 {
-    RK_BODY("ZHERK ", "zherk_", 16, run_zherk, GBX_TR_N | GBX_TR_C, *alpha == 0.0, *beta == 1.0)
+    RK_BODY("ZHERK ", "zherk_", zherk_, 16, run_zherk, GBX_TR_N | GBX_TR_C, *alpha == 0.0, *beta == 1.0)
 }
 
 /* ------------------------------------------------------ xSYR2K / xHER2K */
@@ -257,10 +260,11 @@ RUN_R2K_CPLX(zsyr2k)
 RUN_R2K_HERM(cher2k, float)
 RUN_R2K_HERM(zher2k, double)
 
-#define R2K_BODY(LABEL, NAME, ESZ, RUN, ALLOWED, ALPHA0, BETA1)                                                 \
+#define R2K_BODY(LABEL, NAME, SYM, ESZ, RUN, ALLOWED, ALPHA0, BETA1)                                                 \
     int info = gbx_check_rank_2k_args(*uplo, *trans, ALLOWED, *n, *k, *lda, *ldb, *ldc);                        \
     if (info) { xerbla_(LABEL, &info, 6); return; }                                                             \
     NOTE(NAME, a); NOTE(NAME, b); NOTE(NAME, c);                                                                \
+    GBX_FORWARD(SYM, (uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc));                                 \
     if (*n == 0 || (((ALPHA0) || *k == 0) && (BETA1))) return;                                                  \
     const int notr = gbx_lsame(*trans, 'N');                                                                    \
     struct rk_args r = {*uplo, *trans, *n, *k, alpha, beta, NULL};                                              \
@@ -273,27 +277,27 @@ RUN_R2K_HERM(zher2k, double)
 
 R2K_PROTO(ssyr2k, float, float)
 {
-    R2K_BODY("SSYR2K", "ssyr2k_", 4, run_ssyr2k, GBX_TR_N | GBX_TR_T | GBX_TR_C, *alpha == 0.0f, *beta == 1.0f)
+    R2K_BODY("SSYR2K", "ssyr2k_", ssyr2k_, 4, run_ssyr2k, GBX_TR_N | GBX_TR_T | GBX_TR_C, *alpha == 0.0f, *beta == 1.0f)
 }
 R2K_PROTO(dsyr2k, double, double)
 {
-    R2K_BODY("DSYR2K", "dsyr2k_", 8, run_dsyr2k, GBX_TR_N | GBX_TR_T | GBX_TR_C, *alpha == 0.0, *beta == 1.0)
+    R2K_BODY("DSYR2K", "dsyr2k_", dsyr2k_, 8, run_dsyr2k, GBX_TR_N | GBX_TR_T | GBX_TR_C, *alpha == 0.0, *beta == 1.0)
 }
 R2K_PROTO(csyr2k, float, float)
 {
-    R2K_BODY("CSYR2K", "csyr2k_", 8, run_csyr2k, GBX_TR_N | GBX_TR_T, z2(alpha), o2(beta))
+    R2K_BODY("CSYR2K", "csyr2k_", csyr2k_, 8, run_csyr2k, GBX_TR_N | GBX_TR_T, z2(alpha), o2(beta))
 }
 R2K_PROTO(zsyr2k, double, double)
 {
-    R2K_BODY("ZSYR2K", "zsyr2k_", 16, run_zsyr2k, GBX_TR_N | GBX_TR_T, zz(alpha), oz(beta))
+    R2K_BODY("ZSYR2K", "zsyr2k_", zsyr2k_, 16, run_zsyr2k, GBX_TR_N | GBX_TR_T, zz(alpha), oz(beta))
 }
 R2K_PROTO(cher2k, float, float)
 {
-    R2K_BODY("CHER2K", "cher2k_", 8, run_cher2k, GBX_TR_N | GBX_TR_C, z2(alpha), *beta == 1.0f)
+    R2K_BODY("CHER2K", "cher2k_", cher2k_, 8, run_cher2k, GBX_TR_N | GBX_TR_C, z2(alpha), *beta == 1.0f)
 }
 R2K_PROTO(zher2k, double, double)
 {
-    R2K_BODY("ZHER2K", "zher2k_", 16, run_zher2k, GBX_TR_N | GBX_TR_C, zz(alpha), *beta == 1.0)
+    R2K_BODY("ZHER2K", "zher2k_", zher2k_, 16, run_zher2k, GBX_TR_N | GBX_TR_C, zz(alpha), *beta == 1.0)
 }
 
 /* -------------------------------------------------------- xTRMM / xTRSM */
@@ -328,10 +332,11 @@ RUN_TR_REAL(strsm, float)
 RUN_TR_CPLX(ctrsm)
 RUN_TR_CPLX(ztrsm)
 
-#define TR_BODY(LABEL, NAME, ESZ, RUN, ALPHA0)                                                                  \
+#define TR_BODY(LABEL, NAME, SYM, ESZ, RUN, ALPHA0)                                                                  \
     int info = gbx_check_trxm_args(*side, *uplo, *transa, *diag, *m, *n, *lda, *ldb);                           \
     if (info) { xerbla_(LABEL, &info, 6); return; }                                                             \
     NOTE(NAME, a); NOTE(NAME, b);                                                                               \
+    GBX_FORWARD(SYM, (side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb));                                  \
     if (*m == 0 || *n == 0) return;                                                                             \
     const int na = gbx_lsame(*side, 'L') ? *m : *n;                                                             \
     struct tr_args t = {*side, *uplo, *transa, *diag, *m, *n, alpha};                                           \
@@ -342,12 +347,12 @@ RUN_TR_CPLX(ztrsm)
     void FN##_(const char *side, const char *uplo, const char *transa, const char *diag, const int *m,          \
                const int *n, const T *alpha, const T *a, const int *lda, T *b, const int *ldb)
 
-TR_PROTO(strmm, float) { TR_BODY("STRMM ", "strmm_", 4, run_strmm, *alpha == 0.0f) }
-TR_PROTO(ctrmm, float) { TR_BODY("CTRMM ", "ctrmm_", 8, run_ctrmm, z2(alpha)) }
-TR_PROTO(ztrmm, double) { TR_BODY("ZTRMM ", "ztrmm_", 16, run_ztrmm, zz(alpha)) }
-TR_PROTO(strsm, float) { TR_BODY("STRSM ", "strsm_", 4, run_strsm, *alpha == 0.0f) }
-TR_PROTO(ctrsm, float) { TR_BODY("CTRSM ", "ctrsm_", 8, run_ctrsm, z2(alpha)) }
-TR_PROTO(ztrsm, double) { TR_BODY("ZTRSM ", "ztrsm_", 16, run_ztrsm, zz(alpha)) }
+TR_PROTO(strmm, float) { TR_BODY("STRMM ", "strmm_", strmm_, 4, run_strmm, *alpha == 0.0f) }
+TR_PROTO(ctrmm, float) { TR_BODY("CTRMM ", "ctrmm_", ctrmm_, 8, run_ctrmm, z2(alpha)) }
+TR_PROTO(ztrmm, double) { TR_BODY("ZTRMM ", "ztrmm_", ztrmm_, 16, run_ztrmm, zz(alpha)) }
+TR_PROTO(strsm, float) { TR_BODY("STRSM ", "strsm_", strsm_, 4, run_strsm, *alpha == 0.0f) }
+TR_PROTO(ctrsm, float) { TR_BODY("CTRSM ", "ctrsm_", ctrsm_, 8, run_ctrsm, z2(alpha)) }
+TR_PROTO(ztrsm, double) { TR_BODY("ZTRSM ", "ztrsm_", ztrsm_, 16, run_ztrsm, zz(alpha)) }
 
 /* ------------------------------------------------------------------ CBLAS */
 static char tch(int t) { return t == GbxNoTrans ? 'N' : t == GbxTrans ? 'T' : t == GbxConjTrans ? 'C' : '?'; }

@@ -19,13 +19,13 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 static gbx_config g_cfg = {0, 1e-14, 1, 1, 0, 0, 0, {0}, {0}, 0, {0}};
 static pthread_once_t g_once = PTHREAD_ONCE_INIT;
 
-static void print_help(void)
-{
-    fputs("gbxblas options (set BLAS2CUDA_OPTIONS, chain with ';'):\n"
+static const char help_text[] =
+          "gbxblas options (set BLAS2CUDA_OPTIONS, chain with ';'):\n"
           "   help                      -- print help\n"
           "   debug_execfail            -- accepted for compatibility\n"
           "   debug_exec                -- accepted for compatibility\n"
@@ -38,8 +38,14 @@ static void print_help(void)
           "   serve=on|off              -- route Level-3 calls through the serving loop\n"
           "   managed_min=<bytes>       -- smaller allocations stay on the host\n"
           "   statistics[=<file>]       -- write call/placement counters at exit\n"
-          "   trace=<file>              -- (preload library) write the allocation/call trace\n",
-          stderr);
+          "   trace=<file>              -- (preload library) write the allocation/call trace\n";
+
+static void print_help(void) { fputs(help_text, stderr); }
+
+/* The option help without stdio (usable from the program entry point). */
+void gbx_print_options(int fd)
+{
+    if (write(fd, help_text, sizeof help_text - 1) < 0) { /* nothing to do */ }
 }
 
 static void parse(void)

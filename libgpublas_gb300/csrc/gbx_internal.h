@@ -104,6 +104,31 @@ typedef struct {
 void gbx_tracker_note(const char *fun, const void *ptr) __attribute__((weak));
 const gbx_config *gbx_get_config(void);
 
+/* Forwarding hook (defined by libgbxblas_preload.so when
+ * OBJTRACKER_OPTIONS=blas_libs=... names CPU BLAS libraries): the function
+ * the Fortran routine `sym` is forwarded to, or NULL to run it here.
+ * GBX_FORWARD(sym, (args)) returns from the calling routine after the
+ * forwarded call; GBX_FORWARD_RET does the same for routines with a result.
+ * The target's type is the routine's own prototype (gbxblas_f77.h). */
+void *gbx_tracker_forward(const char *sym) __attribute__((weak));
+#define GBX_FORWARD(sym, args)                                                  \
+    do {                                                                        \
+        if (gbx_tracker_forward) {                                              \
+            __typeof__(&sym) fwd_ = (__typeof__(&sym))gbx_tracker_forward(#sym); \
+            if (fwd_) {                                                         \
+                fwd_ args;                                                      \
+                return;                                                         \
+            }                                                                   \
+        }                                                                       \
+    } while (0)
+#define GBX_FORWARD_RET(sym, args)                                              \
+    do {                                                                        \
+        if (gbx_tracker_forward) {                                              \
+            __typeof__(&sym) fwd_ = (__typeof__(&sym))gbx_tracker_forward(#sym); \
+            if (fwd_) return fwd_ args;                                         \
+        }                                                                       \
+    } while (0)
+
 /* Fortran-layer helpers (f77.c): the calling thread's context (counting
  * the call; reports when no context can be made) and the failure report
  * (prints, and aborts under errors=abort). */

@@ -76,8 +76,15 @@ static int in_boot(const void *p)
     return (const char *)p >= g_boot && (const char *)p < g_boot + sizeof g_boot;
 }
 
+/* sizes of the first bootstrap allocations (OBJTRACKER_OPTIONS=debug_uninit) */
+#define BOOT_LOG 64
+static size_t g_boot_log[BOOT_LOG];
+static atomic_int g_boot_calls;
+
 static void *boot_alloc(size_t n)
 {
+    const int k = atomic_fetch_add(&g_boot_calls, 1);
+    if (k < BOOT_LOG) g_boot_log[k] = n;
     n = (n + 63) & ~(size_t)63;
     size_t off = atomic_fetch_add(&g_boot_used, n);
     if (off + n > sizeof g_boot) return NULL;
@@ -228,7 +235,6 @@ int gbx_tracker_load_oracle(const char *path)
 #define LARGE_ALIGN ((size_t)2 << 20)
 #define TAB_BITS 20
 #define TAB_SIZE ((size_t)1 << TAB_BITS)
-#define TAB_TOMB ((uintptr_t)1)
 
 struct cls {
     char *cur, *end;
@@ -261,13 +267,35 @@ static int tab_insert(uintptr_t p, size_t size, int cls)
 {
     if (g_tab_used >= TAB_SIZE - TAB_SIZE / 8) return 0;
     for (size_t i = slot(p);; i = (i + 1) & (TAB_SIZE - 1)) {
-        if (g_tab[i].p == 0 || g_tab[i].p == TAB_TOMB) {
+        if (g_tab[i].p == 0) {
             g_tab[i].p = p;
             g_tab[i].size = size;
             g_tab[i].cls = cls;
             g_tab_used++;
             return 1;
         }
+    }
+}
+
+/* Removes e by backward-shift deletion (Knuth, TAOCP vol. 3, 6.4,
+ * Algorithm R): later entries of the same probe run move into the hole
+ * unless their home slot lies cyclically in (hole, their slot].  No
+ * tombstones are left, so lookups stay short under any allocate/free churn
+ * and every run still ends at an empty slot. */
+static void tab_erase(struct ent *e)
+{
+    const size_t mask = TAB_SIZE - 1;
+    size_t hole = (size_t)(e - g_tab);
+    g_tab[hole].p = 0;
+    g_tab_used--;
+    for (size_t j = (hole + 1) & mask; g_tab[j].p != 0; j = (j + 1) & mask) {
+        const size_t home = slot(g_tab[j].p);
+        /* the entry may stay iff home is in the cyclic interval (hole, j] */
+        const int stays = hole <= j ? (home > hole && home <= j) : (home > hole || home <= j);
+        if (stays) continue;
+        g_tab[hole] = g_tab[j];
+        g_tab[j].p = 0;
+        hole = j;
     }
 }
 
@@ -335,8 +363,7 @@ static void pool_free(struct ent *e)
     const int c = e->cls;
     atomic_fetch_sub(&g_managed_objects, 1);
     atomic_fetch_sub(&g_managed_bytes, e->size);
-    e->p = TAB_TOMB;
-    g_tab_used--;
+    tab_erase(e);
     if (c < 0) {
         gbx_tracker_slab_free(p, r_free);
         return;
@@ -389,6 +416,110 @@ static int managed_release(void *p)
     return e != NULL;
 }
 
+/* ---- OBJTRACKER_OPTIONS --------------------------------------------------------
+ * The reference's standalone tracker options (lib/obj_tracker.c:246-321),
+ * same variable and syntax (chained with ';'), for the trace mode here:
+ *   help              print these options
+ *   only_print_calls  write only the BLAS-call lines ("C"): each names the
+ *                     object's allocation index, size and address, which is
+ *                     all the decision file needs
+ *   debug_uninit      report the allocations served before the interposer
+ *                     was ready (from its bootstrap arena)
+ *   blas_libs=a,b,... load these libraries, in order; every Fortran BLAS
+ *                     call is then forwarded to the first of them that
+ *                     defines the routine, so the traced program computes on
+ *                     the CPU BLAS as it would without this library
+ *                     (lib/blas_tracker.c:65-93, 100-116) */
+static int g_only_calls, g_debug_uninit;
+#define MAX_BLAS_LIBS 16
+static void *g_blas_handles[MAX_BLAS_LIBS];
+static int g_nblas;
+
+static const char objtracker_help[] =
+    "object tracker options (set OBJTRACKER_OPTIONS, chain with ';'):\n"
+    "   help               -- print this help\n"
+    "   only_print_calls   -- trace only the BLAS calls that use objects\n"
+    "   blas_libs=<a,b,..> -- comma-separated libraries to load, in order; the\n"
+    "                         BLAS calls are forwarded to the first that defines\n"
+    "                         each routine (the traced program runs on that BLAS)\n"
+    "   debug_uninit       -- report allocations made before the tracker was ready\n";
+
+void gbx_tracker_print_options(void)
+{
+    if (write(STDERR_FILENO, objtracker_help, sizeof objtracker_help - 1) < 0) { /* nothing to do */ }
+}
+
+/* caller has t_in set (allocations pass through) */
+static void parse_objtracker_options(void)
+{
+    const char *env = getenv("OBJTRACKER_OPTIONS");
+    if (!env || !*env) return;
+    char *copy = strdup(env);
+    if (!copy) return;
+    char *save = NULL;
+    int helped = 0;
+    for (char *opt = strtok_r(copy, ";", &save); opt; opt = strtok_r(NULL, ";", &save)) {
+        if (strcmp(opt, "help") == 0) {
+            if (!helped) gbx_tracker_print_options();
+            helped = 1;
+        } else if (strcmp(opt, "only_print_calls") == 0) {
+            g_only_calls = 1;
+        } else if (strcmp(opt, "debug_uninit") == 0) {
+            g_debug_uninit = 1;
+        } else if (strncmp(opt, "blas_libs=", 10) == 0) {
+            char *save2 = NULL;
+            for (char *lib = strtok_r(opt + 10, ",", &save2); lib; lib = strtok_r(NULL, ",", &save2)) {
+                if (g_nblas == MAX_BLAS_LIBS) {
+                    fprintf(stderr, "objtracker: at most %d BLAS libraries; '%s' ignored\n", MAX_BLAS_LIBS, lib);
+                    continue;
+                }
+                void *h = dlopen(lib, RTLD_NOW | RTLD_LOCAL);
+                if (!h) {
+                    fprintf(stderr, "objtracker: dlopen(%s): %s\n", lib, dlerror());
+                    abort();   /* the reference aborts too: the run would not be the one asked for */
+                }
+                g_blas_handles[g_nblas++] = h;
+            }
+            if (!g_nblas) fprintf(stderr, "objtracker: blas_libs= names no library. Set OBJTRACKER_OPTIONS=help.\n");
+        } else {
+            fprintf(stderr, "objtracker: unknown option '%s'. Set OBJTRACKER_OPTIONS=help.\n", opt);
+        }
+    }
+    free(copy);
+}
+
+/* Forwarding target of a Fortran BLAS routine (NULL: run it here).  Looked
+ * up once per name in the blas_libs= libraries, in order. */
+#define FWD_CACHE 256
+static struct { const char *name; void *fn; } g_fwd[FWD_CACHE];
+static atomic_int g_nfwd;
+static pthread_mutex_t g_fwd_mu = PTHREAD_MUTEX_INITIALIZER;
+
+void *gbx_tracker_forward(const char *sym)
+{
+    if (!g_nblas) return NULL;
+    int n = atomic_load_explicit(&g_nfwd, memory_order_acquire);
+    for (int i = 0; i < n; i++)
+        if (g_fwd[i].name == sym || strcmp(g_fwd[i].name, sym) == 0) return g_fwd[i].fn;
+    const int saved = t_in;
+    t_in = 1;
+    pthread_mutex_lock(&g_fwd_mu);
+    void *fn = NULL;
+    n = atomic_load(&g_nfwd);
+    for (int i = 0; i < n && !fn; i++)
+        if (strcmp(g_fwd[i].name, sym) == 0) fn = g_fwd[i].fn;
+    for (int i = 0; i < g_nblas && !fn; i++) fn = dlsym(g_blas_handles[i], sym);
+    if (!fn) fprintf(stderr, "objtracker: no library in blas_libs= defines '%s'; it runs on the GPU\n", sym);
+    if (n < FWD_CACHE) {
+        g_fwd[n].name = sym;
+        g_fwd[n].fn = fn;
+        atomic_store_explicit(&g_nfwd, n + 1, memory_order_release);
+    }
+    pthread_mutex_unlock(&g_fwd_mu);
+    t_in = saved;
+    return fn;
+}
+
 /* ---- trace mode (trace=<file>): the producer side of the allocation-file
  * workflow.  Same line grammar as the reference's standalone tracker
  * (obj_tracker.c:426-483, blas_tracker.c:24-31):
@@ -424,6 +555,7 @@ static int tcmp(const void *a, const void *b)
 
 static void trace_line(char c, const struct tobj *o, const char *fun)
 {
+    if (g_only_calls && c != 'C') return;
     char buf[256];
     struct timespec ts;
     clock_gettime(CLOCK_MONOTONIC_RAW, &ts);
@@ -585,6 +717,8 @@ void *realloc(void *p, size_t n)
 
 int posix_memalign(void **out, size_t align, size_t n)
 {
+    /* POSIX: the alignment must be a power of two multiple of sizeof(void *) */
+    if (align < sizeof(void *) || (align & (align - 1)) != 0) return EINVAL;
     if (!ready()) {
         void *p = boot_alloc(n + align);
         if (!p) return ENOMEM;
@@ -610,7 +744,13 @@ void *aligned_alloc(size_t align, size_t n)
     return posix_memalign(&p, align < sizeof(void *) ? sizeof(void *) : align, n) == 0 ? p : NULL;
 }
 
-void *memalign(size_t align, size_t n) { return aligned_alloc(align, n); }
+void *memalign(size_t align, size_t n)
+{
+    /* like glibc: an alignment that is not a power of two is rounded up */
+    size_t a = sizeof(void *);
+    while (a < align) a <<= 1;
+    return aligned_alloc(a, n);
+}
 
 size_t malloc_usable_size(void *p)
 {
@@ -622,6 +762,23 @@ size_t malloc_usable_size(void *p)
 
 /* ---- introspection (tests, statistics) ------------------------------------- */
 int gbx_tracker_is_managed(const void *p) { return managed_size(p) != 0; }
+
+/* Entries in the side table and the longest run of occupied slots (the
+ * worst lookup length). */
+void gbx_tracker_table_stats(uint64_t *used, uint64_t *longest_run)
+{
+    pthread_mutex_lock(&g_mu);
+    size_t run = 0, best = 0, first = 0;
+    while (first < TAB_SIZE && g_tab[first].p != 0) first++;   /* start after an empty slot */
+    for (size_t k = 1; k <= TAB_SIZE; k++) {
+        const size_t i = (first + k) & (TAB_SIZE - 1);
+        run = g_tab[i].p ? run + 1 : 0;
+        if (run > best) best = run;
+    }
+    if (used) *used = g_tab_used;
+    if (longest_run) *longest_run = best;
+    pthread_mutex_unlock(&g_mu);
+}
 
 void gbx_tracker_counters(uint64_t *nth, uint64_t *objects, uint64_t *bytes, uint64_t *failures)
 {
@@ -636,6 +793,14 @@ __attribute__((constructor(101))) static void tracker_init(void)
     t_in = 1;
     ready();
     gbx_tracker_refresh();
+    parse_objtracker_options();
+    if (g_debug_uninit) {
+        const int calls = atomic_load(&g_boot_calls);
+        fprintf(stderr, "objtracker: %d allocation(s) before initialisation, %zu bytes of the bootstrap arena\n",
+                calls, atomic_load(&g_boot_used));
+        for (int i = 0; i < calls && i < BOOT_LOG; i++)
+            fprintf(stderr, "objtracker:   before initialisation: allocation of %zu bytes\n", g_boot_log[i]);
+    }
     const gbx_config *cfg = gbx_get_config();
     g_min_bytes = cfg->managed_min;
     if (cfg->heuristic == 3 && !gbx_tracker_load_oracle(cfg->oracle_file)) {

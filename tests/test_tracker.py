@@ -152,3 +152,90 @@ def test_managed_operands_are_used_in_place(prog):
     assert d["blas managed"] == [0, 0, 1]
     hits, misses, moved = d["blas stats"]
     assert hits == 0 and misses == 3 and moved > 0
+
+
+# ---- OBJTRACKER_OPTIONS and the runnable library (lib/obj_tracker.c:246-321,
+# entry.c:4-11); all on the CPU: forwarded calls never reach the GPU path
+@pytest.fixture(scope="module")
+def fake_blas(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("fakeblas") / "libfakecpublas.so")
+    subprocess.check_call(["gcc", "-O1", "-shared", "-fPIC", "-o", so,
+                           os.path.join(ROOT, "tests", "fake_cpublas.c"), "-lm"])
+    return so
+
+
+def run_env(prog, args, options="", objtracker=None):
+    env = dict(os.environ, LD_PRELOAD=PRELOAD, BLAS2CUDA_OPTIONS=options, GBX_TRACKER_FAKE_MANAGED="1")
+    if objtracker is not None:
+        env["OBJTRACKER_OPTIONS"] = objtracker
+    return subprocess.run([prog] + args, capture_output=True, text=True, env=env, timeout=300)
+
+
+def test_blas_libs_forwards_calls_to_the_named_library(prog, fake_blas, tmp_path):
+    trace = tmp_path / "fwd.trace"
+    r = run_env(prog, ["fwd"], f"heuristic=false;errors=return;trace={trace}", f"blas_libs={fake_blas}")
+    assert r.returncode == 0, r.stderr
+    res = {ln.split()[0]: int(ln.split()[1]) for ln in r.stdout.splitlines()}
+    assert res == {"dgemm": 1, "dsymm": 1, "ddot": 30, "idamax": 3}, r.stdout
+    for name in ("dgemm_", "dsymm_", "ddot_", "idamax_"):
+        assert f"fake {name}" in r.stderr
+    assert "gbxblas:" not in r.stderr          # nothing ran (or failed) on the GPU path
+    text = trace.read_text()
+    # the traced program's objects and the calls naming them are all recorded
+    assert text.count("\nC #") + text.startswith("C #") == 3 + 3 + 2 + 1
+    assert "T #" in text
+
+
+def test_only_print_calls_keeps_the_call_lines(prog, fake_blas, tmp_path):
+    import sys
+    trace = tmp_path / "calls.trace"
+    r = run_env(prog, ["fwd"], f"heuristic=false;trace={trace}", f"only_print_calls;blas_libs={fake_blas}")
+    assert r.returncode == 0, r.stderr
+    lines = trace.read_text().splitlines()
+    assert lines and all(ln.startswith("C #") for ln in lines)
+    dec = tmp_path / "dec.txt"
+    a = subprocess.run([sys.executable, "-m", "libgpublas_gb300.analyze_trace", str(trace), str(dec)],
+                       capture_output=True, text=True, cwd=ROOT, timeout=60)
+    assert a.returncode == 0, a.stderr
+    d = [ln for ln in dec.read_text().splitlines() if ln.startswith("D #")]
+    assert len(d) == 3                          # a, b, c: every object a call named
+
+
+def test_objtracker_help_debug_uninit_and_unknown_option(prog):
+    r = run_env(prog, ["seq"], "heuristic=false", "help;debug_uninit;no_such_option")
+    assert r.returncode == 0, r.stderr
+    assert "object tracker options" in r.stderr and "blas_libs" in r.stderr
+    assert "before initialisation" in r.stderr
+    assert "unknown option 'no_such_option'" in r.stderr
+
+
+def test_missing_blas_library_aborts(prog, tmp_path):
+    r = run_env(prog, ["seq"], "heuristic=false", f"blas_libs={tmp_path / 'nope.so'}")
+    assert r.returncode != 0 and "dlopen" in r.stderr
+
+
+def test_running_the_library_prints_its_options(lib):
+    blas = os.path.join(ROOT, "libgpublas_gb300", "libgbxblas.so")
+    r = subprocess.run([blas], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "BLAS2CUDA_OPTIONS" in r.stdout, (r.returncode, r.stdout, r.stderr)
+    r = subprocess.run([PRELOAD], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "BLAS2CUDA_OPTIONS" in r.stdout and "OBJTRACKER_OPTIONS" in r.stderr
+
+
+def test_side_table_under_churn(prog):
+    # freed entries leave no tombstones: after 300k allocate/free pairs the
+    # table holds exactly the live objects, probe runs stay short, and
+    # interior pointers are never mistaken for objects
+    lines = run(prog, ["churn"], "heuristic=true")
+    d = {ln.split()[0]: [int(v) for v in ln.split()[1:]] for ln in lines}
+    live, used, bad = d["live"]
+    assert used == live and bad == 0
+    assert d["after"][0] == 0 and d["after"][1] == 0
+
+
+def test_posix_memalign_rejects_bad_alignment(prog):
+    import errno
+    for options in ("heuristic=true", "heuristic=false"):
+        d = {ln.split()[0]: [int(v) for v in ln.split()[1:]] for ln in run(prog, ["align"], options)}
+        assert d["posix_memalign"] == [errno.EINVAL, errno.EINVAL, 1]
+        assert d["memalign"][:2] == [1, 1]

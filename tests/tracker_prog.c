@@ -8,11 +8,19 @@
  *   tracker_prog threads    8 threads x 20000 malloc/free of random sizes
  *   tracker_prog blas <n>   (GPU) dgemm_ on managed operands; prints the
  *                           placement counters
+ *   tracker_prog fwd        dgemm_, dsymm_, ddot_, idamax_ on host arrays
+ *                           (run with OBJTRACKER_OPTIONS=blas_libs=...: the
+ *                           calls go to that library); prints the results
+ *   tracker_prog churn      300000 managed malloc/free pairs with up to 1000
+ *                           live objects; prints the side table's use and
+ *                           longest probe run
+ *   tracker_prog align      posix_memalign / memalign alignment rules
  * Output uses write(2) on a stack buffer so the program itself makes no
  * hidden allocations between the counted ones.
  */
 #define _GNU_SOURCE
 #include <dlfcn.h>
+#include <malloc.h>
 #include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -195,6 +203,86 @@ static int blas_note(void)
     return 0;
 }
 
+typedef void (*dsymm_fn)(const char *, const char *, const int *, const int *, const double *, const double *,
+                         const int *, const double *, const int *, const double *, double *, const int *);
+
+static int fwd(void)
+{
+    dgemm_fn dgemm = (dgemm_fn)dlsym(RTLD_DEFAULT, "dgemm_");
+    dsymm_fn dsymm = (dsymm_fn)dlsym(RTLD_DEFAULT, "dsymm_");
+    double (*ddot)(const int *, const double *, const int *, const double *, const int *) =
+        (double (*)(const int *, const double *, const int *, const double *, const int *))dlsym(RTLD_DEFAULT, "ddot_");
+    int (*idamax)(const int *, const double *, const int *) =
+        (int (*)(const int *, const double *, const int *))dlsym(RTLD_DEFAULT, "idamax_");
+    const int n = 4, one_i = 1;
+    double *a = (double *)malloc(sizeof(double) * 16), *b = (double *)malloc(sizeof(double) * 16);
+    double *c = (double *)malloc(sizeof(double) * 16);
+    for (int i = 0; i < 16; i++) { a[i] = i + 1; b[i] = (i % 3) - 1; c[i] = 1; }
+    const double one = 1.0, half = 0.5;
+    dgemm("N", "N", &n, &n, &n, &one, a, &n, b, &n, &half, c, &n);
+    double want = 0.5;
+    for (int l = 0; l < n; l++) want += a[l * n + 2] * b[3 * n + l];   /* C(2,3) */
+    out("dgemm %llu %llu %llu\n", (unsigned long long)(c[3 * n + 2] == want), 0, 0);
+    for (int i = 0; i < 16; i++) c[i] = 0;
+    dsymm("L", "U", &n, &n, &one, a, &n, b, &n, &one, c, &n);
+    want = 0;   /* C(1,0) with A symmetric from its upper triangle */
+    for (int l = 0; l < n; l++) want += (l >= 1 ? a[l * n + 1] : a[1 * n + l]) * b[0 * n + l];
+    out("dsymm %llu %llu %llu\n", (unsigned long long)(c[1] == want), 0, 0);
+    const double d = ddot(&n, a, &one_i, a, &one_i);
+    out("ddot %llu %llu %llu\n", (unsigned long long)d, 0, 0);     /* 1+4+9+16 = 30 */
+    a[2] = -99;
+    out("idamax %llu %llu %llu\n", (unsigned long long)idamax(&n, a, &one_i), 0, 0);
+    free(a);
+    free(b);
+    free(c);
+    return 0;
+}
+
+static int churn(void)
+{
+    void (*table)(uint64_t *, uint64_t *) = (void (*)(uint64_t *, uint64_t *))dlsym(RTLD_DEFAULT,
+                                                                                   "gbx_tracker_table_stats");
+    if (!table) return 7;
+    enum { LIVE = 1000, ROUNDS = 300000 };
+    void *live[LIVE] = {0};
+    uint64_t x = 88172645463325252ull, bad = 0;
+    for (int r = 0; r < ROUNDS; r++) {
+        x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+        const int i = (int)(x % LIVE);
+        if (live[i]) {
+            if (!is_managed(live[i])) bad++;
+            free(live[i]);
+        }
+        live[i] = malloc(64 + (x >> 40) % 4000);
+        /* a pointer that is in the managed range but is not an object start */
+        if (live[i] && is_managed((char *)live[i] + 8)) bad++;
+    }
+    uint64_t used, longest;
+    table(&used, &longest);
+    int count = 0;
+    for (int i = 0; i < LIVE; i++) count += live[i] != NULL;
+    out("live %llu %llu %llu\n", (unsigned long long)count, (unsigned long long)used, (unsigned long long)bad);
+    for (int i = 0; i < LIVE; i++) free(live[i]);
+    table(&used, &longest);
+    out("after %llu %llu %llu\n", (unsigned long long)used, (unsigned long long)longest, 0);
+    return 0;
+}
+
+static int align_case(void)
+{
+    void *p = NULL;
+    const int e24 = posix_memalign(&p, 24, 100), e4 = posix_memalign(&p, 4, 100);
+    void *q = NULL;
+    const int ok = posix_memalign(&q, 64, 100);
+    out("posix_memalign %llu %llu %llu\n", (unsigned long long)e24, (unsigned long long)e4,
+        (unsigned long long)(ok == 0 && ((uintptr_t)q & 63) == 0));
+    void *m = memalign(48, 100);   /* rounded up to 64 */
+    out("memalign %llu %llu %llu\n", (unsigned long long)(m != NULL), (unsigned long long)(((uintptr_t)m & 63) == 0), 0);
+    free(q);
+    free(m);
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     is_managed = (int (*)(const void *))dlsym(RTLD_DEFAULT, "gbx_tracker_is_managed");
@@ -211,5 +299,8 @@ int main(int argc, char **argv)
     if (!strcmp(argv[1], "many")) return many();
     if (!strcmp(argv[1], "blas_note")) return blas_note();
     if (!strcmp(argv[1], "blas")) return blas(argc > 2 ? atoi(argv[2]) : 512);
+    if (!strcmp(argv[1], "fwd")) return fwd();
+    if (!strcmp(argv[1], "churn")) return churn();
+    if (!strcmp(argv[1], "align")) return align_case();
     return 8;
 }
