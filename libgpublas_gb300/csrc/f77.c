@@ -135,6 +135,13 @@ void dgemm_(const char *transa, const char *transb, const int *m, const int *n, 
     gbx_server *srv = server();
     const size_t bytes = 8 * ((size_t)*m * *k + (size_t)*k * *n + (size_t)*m * *n);
     if (srv && (st = gbx_server_admit(srv, bytes)) != GBX_OK) { report("DGEMM", ctx, st); return; }
+    const gbx_config *cfg = gbx_get_config();
+    if (!srv && work && !cfg->precision_ozaki && gbx_dgemm_pipeline_eligible(ctx, *m, *n, *k, a, b, c)) {
+        /* large call on host operands: copies overlap the block products */
+        TRY(gbx_dgemm_host_pipelined(ctx, *transa, *transb, *m, *n, *k, *alpha, a, *lda, b, *ldb, *beta, c, *ldc));
+        TRY(gbx_ctx_sync(ctx));
+        return;
+    }
     /* operands left unplaced on quick paths keep the caller's (valid) ld */
     gbx_operand oa = {.ld = *lda}, ob = {.ld = *ldb}, oc = {0};
     if (work) {
@@ -142,7 +149,6 @@ void dgemm_(const char *transa, const char *transb, const int *m, const int *n, 
         TRY(gbx_place_in(ctx, GBX_WS_STAGE_B, b, notb ? *k : *n, notb ? *n : *k, *ldb, 8, 1, &ob));
     }
     TRY(gbx_place_in(ctx, GBX_WS_STAGE_C, c, *m, *n, *ldc, 8, *beta != 0.0, &oc));
-    const gbx_config *cfg = gbx_get_config();
     if (srv) {
         gbx_op op = {0};
         op.kind = (work && cfg->precision_ozaki) ? GBX_OP_GEMM_OZAKI : GBX_OP_GEMM;

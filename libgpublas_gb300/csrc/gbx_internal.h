@@ -83,6 +83,14 @@ gbx_status gbx_place_vec(gbx_ctx *ctx, int slot, const void *host, int n, int in
 gbx_status gbx_place_vec_out(gbx_ctx *ctx, const gbx_operand *op, int n, int inc, size_t elem);
 void gbx_placement_counters(uint64_t *hits, uint64_t *misses, uint64_t *bytes_h2d,
                             uint64_t *bytes_d2h);
+/* DGEMM on host operands with the copies pipelined against block products
+ * (gbx_runtime.cu): eligible when op(A), op(B) and C are all host memory and
+ * C splits into blocks of two 128 x 128 tiles per SM; the call returns after
+ * the result is back in C (the context's stream may still be finishing). */
+int gbx_dgemm_pipeline_eligible(gbx_ctx *ctx, int m, int n, int k, const void *A, const void *B, const void *C);
+gbx_status gbx_dgemm_host_pipelined(gbx_ctx *ctx, char ta, char tb, int m, int n, int k, double alpha,
+                                    const double *A, int lda, const double *B, int ldb, double beta,
+                                    double *C, int ldc);
 
 /* ---- library configuration (gbx_config.c) ---------------------------------- */
 typedef struct {

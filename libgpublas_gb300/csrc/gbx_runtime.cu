@@ -13,6 +13,7 @@
 #include "gbx_internal.h"
 
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -23,7 +24,8 @@
 // Kernel timing: when enabled, the main kernel of each routine is bracketed by
 // a pair of CUDA events on the context's stream; gbx_ctx_kernel_time() sums
 // the elapsed times per tag after a synchronisation.
-#define GBX_TIMER_PAIRS 256
+#define GBX_TIMER_PAIRS 1024
+#define GBX_AUX_EVENTS 160
 struct gbx_timer_rec {
     cudaEvent_t start, stop;
     int tag;
@@ -48,6 +50,8 @@ struct gbx_ctx {
     int timer_next;
     int timer_open;
     gbx_timer_rec timers[GBX_TIMER_PAIRS];
+    cudaStream_t aux[2];           // copy-in and copy-out streams of the pipelined DGEMM (lazy)
+    cudaEvent_t aux_ev[GBX_AUX_EVENTS];
     char err[512];
 };
 
@@ -81,6 +85,24 @@ extern "C" void gbx_timer_end(gbx_ctx *c)
 {
     if (!c || !c->timing) return;
     cudaEventRecord(c->timers[c->timer_open].stop, c->stream);
+    c->timer_next++;
+}
+
+// The same bracket on another stream of the context (the pipelined copies).
+static void timer_begin_on(gbx_ctx *c, int tag, cudaStream_t s)
+{
+    if (!c || !c->timing) return;
+    gbx_timer_rec *r = &c->timers[c->timer_next % GBX_TIMER_PAIRS];
+    r->tag = tag;
+    r->used = 1;
+    c->timer_open = c->timer_next % GBX_TIMER_PAIRS;
+    cudaEventRecord(r->start, s);
+}
+
+static void timer_end_on(gbx_ctx *c, cudaStream_t s)
+{
+    if (!c || !c->timing) return;
+    cudaEventRecord(c->timers[c->timer_open].stop, s);
     c->timer_next++;
 }
 
@@ -175,6 +197,10 @@ extern "C" gbx_status gbx_ctx_destroy(gbx_ctx *c)
         if (c->timers[i].start) cudaEventDestroy(c->timers[i].start);
         if (c->timers[i].stop) cudaEventDestroy(c->timers[i].stop);
     }
+    for (int i = 0; i < 2; i++)
+        if (c->aux[i]) cudaStreamDestroy(c->aux[i]);
+    for (int i = 0; i < GBX_AUX_EVENTS; i++)
+        if (c->aux_ev[i]) cudaEventDestroy(c->aux_ev[i]);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     free(c);
     return GBX_OK;
@@ -476,5 +502,173 @@ extern "C" gbx_status gbx_place_vec_out(gbx_ctx *c, const gbx_operand *op, int n
                                     c->stream);
     if (e != cudaSuccess) return gbx_fail(c, GBX_ERR_CUDA, "stage vec out: %s", cudaGetErrorString(e));
     g_d2h += span * elem;
+    return GBX_OK;
+}
+
+// --------------------------------------------------------------------------
+// DGEMM on host operands with the copies pipelined against the products
+// --------------------------------------------------------------------------
+// The reference stages every operand with blocking copies before cuBLAS runs
+// (gemm.cc:46-83, runtime-mem.hpp:84-155), so a large call pays all of its
+// host transfers on top of the product.  Here, when op(A), op(B) and C all
+// live in host memory and C is large, C is cut into R x P blocks, each still
+// at least two 128 x 128 tiles per SM: the copy-in stream brings row block r
+// of op(A), column panel c of op(B) and block C(r, c) (when beta != 0), the
+// context's stream multiplies each block as soon as its operands are in, and
+// the copy-out stream returns each finished block.  Only the first block's
+// operands and the last block's result are exposed.  Every block runs the
+// same kernel instantiation over the same K order as the whole call would,
+// so the result is bit-identical to the undivided product.
+static gbx_status aux_ready(gbx_ctx *c)
+{
+    for (int i = 0; i < 2; i++)
+        if (!c->aux[i] && cudaStreamCreateWithFlags(&c->aux[i], cudaStreamNonBlocking) != cudaSuccess) {
+            c->aux[i] = nullptr;
+            cudaGetLastError();
+            return gbx_fail(c, GBX_ERR_CUDA, "copy streams");
+        }
+    for (int i = 0; i < GBX_AUX_EVENTS; i++)
+        if (!c->aux_ev[i] && cudaEventCreateWithFlags(&c->aux_ev[i], cudaEventDisableTiming) != cudaSuccess) {
+            c->aux_ev[i] = nullptr;
+            cudaGetLastError();
+            return gbx_fail(c, GBX_ERR_CUDA, "copy events");
+        }
+    return GBX_OK;
+}
+
+// Block grid for an m x n product: row blocks of op(A) of >= 4096 rows (at
+// most 4) and column panels of >= 2048 columns (at most 8), reduced until
+// every block holds two 128 x 128 tiles per SM.  Returns 0 when the call is
+// too small to split.
+static int pipeline_plan(int m, int n, int sms, int *rb, int *cb)
+{
+    int R = std::max(1, std::min(4, m / 4096)), P = std::max(1, std::min(8, n / 2048));
+    while (R * P > 1) {
+        const int r = ((m + R - 1) / R + 127) / 128 * 128, q = ((n + P - 1) / P + 127) / 128 * 128;
+        if ((long long)(r / 128) * (q / 128) >= 2LL * sms) {
+            *rb = r;
+            *cb = q;
+            return 1;
+        }
+        if (P >= R) P--;
+        else R--;
+    }
+    return 0;
+}
+
+extern "C" int gbx_dgemm_pipeline_eligible(gbx_ctx *c, int m, int n, int k, const void *A, const void *B,
+                                           const void *C)
+{
+    int managed, rb, cb;
+    if (!c || m <= 0 || n <= 0 || k <= 0) return 0;
+    if (!pipeline_plan(m, n, gbx_ctx_sms(c), &rb, &cb)) return 0;
+    return !resident_kind(c, A, &managed) && !resident_kind(c, B, &managed) && !resident_kind(c, C, &managed);
+}
+
+static cudaError_t copy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
+                          cudaMemcpyKind kind, cudaStream_t s)
+{
+    if (width == 0 || height == 0) return cudaSuccess;
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, s);
+}
+
+extern "C" gbx_status gbx_dgemm_host_pipelined(gbx_ctx *c, char ta, char tb, int m, int n, int k, double alpha,
+                                               const double *A, int lda, const double *B, int ldb, double beta,
+                                               double *C, int ldc)
+{
+    int rb, cb;
+    if (!pipeline_plan(m, n, gbx_ctx_sms(c), &rb, &cb)) return GBX_ERR_UNSUPPORTED;
+    gbx_status st = aux_ready(c);
+    if (st != GBX_OK) return st;
+    const bool nota = gbx_lsame(ta, 'N'), notb = gbx_lsame(tb, 'N');
+    const bool cin = beta != 0.0;
+    // staged copies keep the stored shape: A is (nota ? m x k : k x m), B is (notb ? k x n : n x k)
+    const int ar = nota ? m : k, ac = nota ? k : m, br = notb ? k : n, bc = notb ? n : k;
+    const int dla = round_ld(ar), dlb = round_ld(br), dlc = round_ld(m);
+    double *dA, *dB, *dC;
+    if ((st = gbx_ws(c, GBX_WS_STAGE_A, sizeof(double) * (size_t)dla * ac, (void **)&dA)) != GBX_OK) return st;
+    if ((st = gbx_ws(c, GBX_WS_STAGE_B, sizeof(double) * (size_t)dlb * bc, (void **)&dB)) != GBX_OK) return st;
+    if ((st = gbx_ws(c, GBX_WS_STAGE_C, sizeof(double) * (size_t)dlc * n, (void **)&dC)) != GBX_OK) return st;
+    const int R = (m + rb - 1) / rb, P = (n + cb - 1) / cb;
+    if (R + P + 2 * R * P > GBX_AUX_EVENTS) return GBX_ERR_UNSUPPORTED;
+    cudaEvent_t *evA = c->aux_ev, *evB = evA + R, *evC = evB + P, *evK = evC + R * P;
+    cudaStream_t cin_s = c->aux[0], cout_s = c->aux[1], ks = c->stream;
+    const size_t e8 = sizeof(double);
+    cudaError_t e = cudaSuccess;
+    uint64_t h2d = 0, d2h = 0;
+    g_misses += 3;
+    // the copy-in stream must not start before earlier work on the context's
+    // stream (which may still read these staging buffers) is done
+    e = cudaEventRecord(evK[0], ks);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cin_s, evK[0], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cout_s, evK[0], 0);
+    for (int r = 0; r < R && e == cudaSuccess; r++) {
+        const int r0 = r * rb, rn = std::min(rb, m - r0);
+        // row block r of op(A): rows r0.. of A (nota) or columns r0.. of A
+        timer_begin_on(c, GBX_TIMER_H2D, cin_s);
+        if (nota)
+            e = copy2d(dA + r0, dla * e8, A + r0, (size_t)lda * e8, rn * e8, (size_t)k, cudaMemcpyHostToDevice, cin_s);
+        else
+            e = copy2d(dA + (size_t)r0 * dla, dla * e8, A + (size_t)r0 * lda, (size_t)lda * e8, (size_t)k * e8,
+                       (size_t)rn, cudaMemcpyHostToDevice, cin_s);
+        timer_end_on(c, cin_s);
+        h2d += (uint64_t)rn * k * e8;
+        if (e == cudaSuccess) e = cudaEventRecord(evA[r], cin_s);
+        for (int q = 0; q < P && e == cudaSuccess; q++) {
+            const int c0 = q * cb, cn = std::min(cb, n - c0);
+            if (r == 0) {
+                // column panel q of op(B): columns c0.. of B (notb) or rows c0.. of B
+                timer_begin_on(c, GBX_TIMER_H2D, cin_s);
+                if (notb)
+                    e = copy2d(dB + (size_t)c0 * dlb, dlb * e8, B + (size_t)c0 * ldb, (size_t)ldb * e8, (size_t)k * e8,
+                               (size_t)cn, cudaMemcpyHostToDevice, cin_s);
+                else
+                    e = copy2d(dB + c0, dlb * e8, B + c0, (size_t)ldb * e8, cn * e8, (size_t)k, cudaMemcpyHostToDevice,
+                               cin_s);
+                timer_end_on(c, cin_s);
+                h2d += (uint64_t)cn * k * e8;
+                if (e == cudaSuccess) e = cudaEventRecord(evB[q], cin_s);
+            }
+            if (cin && e == cudaSuccess) {
+                timer_begin_on(c, GBX_TIMER_H2D, cin_s);
+                e = copy2d(dC + (size_t)c0 * dlc + r0, dlc * e8, C + (size_t)c0 * ldc + r0, (size_t)ldc * e8, rn * e8,
+                           (size_t)cn, cudaMemcpyHostToDevice, cin_s);
+                timer_end_on(c, cin_s);
+                h2d += (uint64_t)rn * cn * e8;
+                if (e == cudaSuccess) e = cudaEventRecord(evC[r * P + q], cin_s);
+            }
+            if (e != cudaSuccess) break;
+            // the block's product on the context's stream, once its operands are in
+            e = cudaStreamWaitEvent(ks, evA[r], 0);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(ks, evB[q], 0);
+            if (e == cudaSuccess && cin) e = cudaStreamWaitEvent(ks, evC[r * P + q], 0);
+            if (e != cudaSuccess) break;
+            const double *ab = nota ? dA + r0 : dA + (size_t)r0 * dla;
+            const double *bb = notb ? dB + (size_t)c0 * dlb : dB + c0;
+            st = gbx_dgemm(c, ta, tb, rn, cn, k, alpha, ab, dla, bb, dlb, beta, dC + (size_t)c0 * dlc + r0, dlc);
+            if (st != GBX_OK) return st;
+            e = cudaEventRecord(evK[r * P + q], ks);
+        }
+    }
+    // results back, block by block, as each product finishes
+    for (int r = 0; r < R && e == cudaSuccess; r++)
+        for (int q = 0; q < P && e == cudaSuccess; q++) {
+            const int r0 = r * rb, rn = std::min(rb, m - r0), c0 = q * cb, cn = std::min(cb, n - c0);
+            e = cudaStreamWaitEvent(cout_s, evK[r * P + q], 0);
+            timer_begin_on(c, GBX_TIMER_D2H, cout_s);
+            if (e == cudaSuccess)
+                e = copy2d(C + (size_t)c0 * ldc + r0, (size_t)ldc * e8, dC + (size_t)c0 * dlc + r0, dlc * e8, rn * e8,
+                           (size_t)cn, cudaMemcpyDeviceToHost, cout_s);
+            timer_end_on(c, cout_s);
+            d2h += (uint64_t)rn * cn * e8;
+        }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cout_s);
+    g_h2d += h2d;
+    g_d2h += d2h;
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(cin_s);
+        cudaStreamSynchronize(ks);
+        return gbx_fail(c, GBX_ERR_CUDA, "pipelined dgemm: %s", cudaGetErrorString(e));
+    }
     return GBX_OK;
 }

@@ -285,3 +285,38 @@ def test_dtrsm_large_left_lower(orc, dev):
     want = bs.copy(order="F")
     orc.dtrsm("L", "L", "N", "N", m, len(cols), 1.0, a, want)
     assert rel(xs, want) <= TOL
+
+
+# ------------------------------------------------------------ dgemm_ on host operands, pipelined copies
+@pytest.mark.parametrize("ta,tb,beta", [("N", "N", 0.5), ("T", "N", 0.0), ("N", "T", -1.0)])
+def test_fortran_dgemm_pipelined_copies_match_device_path(orc, f77, dev, ta, tb, beta):
+    # large enough for the Fortran symbol to cut C into blocks whose copies
+    # overlap the block products (2 x 3 blocks here); the result must be
+    # bit-identical to the same product on device operands (same kernel,
+    # same K order), padding rows untouched
+    import libgpublas_gb300 as g
+    m, n, k = 8300, 6200, 300
+    ra, ca = (m, k) if ta == "N" else (k, m)
+    rb, cb = (k, n) if tb == "N" else (n, k)
+    a, s = padded(orc, ra, ca, 7900)
+    b, s = padded(orc, rb, cb, s)
+    c, _ = padded(orc, m, n, s)
+    cin = c.copy(order="F")
+    if beta == 0.0:
+        cin[:m] = np.nan
+    C = to_dev(cin)
+    dev.dgemm_checked(ta, tb, m, n, k, 1.25, to_dev(a), a.shape[0], to_dev(b), b.shape[0], beta, C, c.shape[0])
+    dev.sync()
+    want = from_dev(C, c.shape[0], n)
+    s0 = g.stats()
+    got = cin.copy(order="F")
+    f77.dgemm(ta, tb, m, n, k, 1.25, a, a.shape[0], b, b.shape[0], beta, got, got.shape[0])
+    s1 = g.stats()
+    moved = (ra * ca + rb * cb + (m * n if beta != 0.0 else 0)) * 8
+    assert s1["bytes_h2d"] - s0["bytes_h2d"] == moved
+    assert s1["bytes_d2h"] - s0["bytes_d2h"] == m * n * 8
+    assert np.all(got[m:] == SENT)
+    assert np.array_equal(got, want)
+    rows, cols = samples(m, n, 1024, 7901)
+    ref = orc.dgemm_dd_sample(ta, tb, k, 1.25, a, b, beta, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL
