@@ -546,6 +546,17 @@ def run_ours(args):
                                "tensor_fp8_tflops": 2.0 * peaks.get("bf16_tflops", 1900.0),
                                "source": f"FP64: measured in this run; HBM and bf16: {peak_src}"}
 
+    if w == "dgemm" and not args.no_sweep and ws == 1:
+        # the serving trace, shortened (16 threads, n in [1024, 4096]): the
+        # loop against plain per-call dispatch in the same precision
+        sizes, nbs, modes = serving_trace(g, 16, 1024, 4096)
+        line["serving"] = {
+            "workload": "cholesky_trace_16threads_n1024-4096",
+            "n": sizes, "nb": nbs,
+            "modes": {m: {k: v[k] for k in ("calls", "calls_per_s", "p50_us", "p99_us", "tflops",
+                                            "residual_sampled", "wall_s", "first_error")}
+                      for m, v in modes.items()},
+            "ratios": serving_ratios(modes)}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         from oracle import cpublas
         cb = cpublas.get()
@@ -983,51 +994,60 @@ def cholesky_calls(n, nb, base, lda, info_ptr, ozaki=False):
     return calls
 
 
-def run_serving(args):
+MODES = {
+    # name: (through the serving loop, Ozaki forms of dtrsm/dsyrk/dgemm)
+    "plain": (False, False),         # FP64, plain per-call dispatch
+    "served": (True, False),         # FP64, serving loop
+    "ozaki_plain": (False, True),    # Ozaki, plain per-call dispatch
+    "ozaki": (True, True),           # Ozaki, serving loop
+}
+
+
+def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES)):
+    """Closed-loop Cholesky trace: nthreads native caller threads, thread t
+    factorising A = G G^T + n I (G uniform[-1,1], n log-uniform in
+    [nmin, nmax], nb in {128, 256}) through the library, once per mode.
+    Returns (sizes, nbs, {mode: stats}); each mode reports calls/s, p50/p99
+    per-call latency, the sampled residual |A - L L^T| / |A| and the time of
+    each thread's chain."""
     import torch
-    import libgpublas_gb300 as g
-    from libgpublas_gb300 import build
-    build.build_library()
-    nthreads = 16
-    rng = np.random.default_rng(5)
-    nmax = args.n or 16384
-    sizes = [int(v) for v in loguni(rng, 1024, nmax, nthreads)]
+    rng = np.random.default_rng(seed)
+    sizes = [int(v) for v in loguni(rng, nmin, nmax, nthreads)]
     nbs = [int(v) for v in rng.choice([128, 256], nthreads)]
     dev = g.Device(0)
-    mats, origs = [], []
+    origs = []
     gen = torch.Generator(device="cuda")
-    gen.manual_seed(5)
+    gen.manual_seed(seed)
     for n in sizes:
         G = torch.empty(n * n, dtype=torch.float64, device="cuda").uniform_(-1.0, 1.0, generator=gen)
         A = torch.empty(n * n, dtype=torch.float64, device="cuda")
-        # A = G G^T + n I, both triangles (setup, on the Ozaki path)
-        dev.dgemm_ozaki("N", "T", n, n, n, 1.0, G, n, G, n, 0.0, A, n)
-        A.view(n, n).diagonal().add_(float(n))
+        torch.cuda.synchronize()
+        # A = G G^T + n I, both triangles (setup, FP64)
+        dev.dgemm_checked("N", "T", n, n, n, 1.0, G, n, G, n, 0.0, A, n)
         dev.sync()
+        A.view(n, n).diagonal().add_(float(n))
+        torch.cuda.synchronize()
         del G
         origs.append(A)
     info = torch.zeros(nthreads, dtype=torch.int32, device="cuda")
     results = {}
-
-    def run_mode(mode):
-        # the 16 caller threads are native (gbx_diag_cholesky_trace): C++
+    for mode in modes:
+        use_server, ozaki = MODES[mode]
+        info.zero_()
+        # the caller threads are native (gbx_diag_cholesky_trace): C++
         # threads calling the library as a C or Fortran application would,
         # without interpreter time or lock contention on every call
-        server = g.Server(0, slots=nthreads) if mode != "plain" else None
+        server = g.Server(0, slots=nthreads) if use_server else None
         work = [o.clone() for o in origs]
         torch.cuda.synchronize()
-        r = g.cholesky_trace(server, 0, sizes, nbs, [w.data_ptr() for w in work], info.data_ptr(),
-                             mode == "ozaki")
+        r = g.cholesky_trace(server, 0, sizes, nbs, [w.data_ptr() for w in work], info.data_ptr(), ozaki)
         wall = r["wall_s"]
-        errs = [r["first_error"]] if r["first_error"] else []
         by_kind = {k: (c, r["kind_sum_us"][k]) for k, c in enumerate(r["kind_calls"]) if c}
-        thread_s = r["thread_finish_s"]
         srv_stats = server.stats() if server else None
         if server:
             server.close()
         # residual on sampled entries: (L L^T)_ij through ddot on rows of L
         res_num = res_den = 0.0
-        d = g.Device(0)
         out = torch.zeros(1, dtype=torch.float64, device="cuda")
         srng = np.random.default_rng(9)
         for t in range(nthreads):
@@ -1035,32 +1055,47 @@ def run_serving(args):
             L = work[t]
             for _ in range(8):
                 i, j = sorted(int(v) for v in srng.integers(0, n, 2))[::-1]   # i >= j
-                d.ddot(j + 1, L.data_ptr() + 8 * i, n, L.data_ptr() + 8 * j, n, out)
-                d.sync()
+                dev.ddot(j + 1, L.data_ptr() + 8 * i, n, L.data_ptr() + 8 * j, n, out)
+                dev.sync()
                 aij = float(origs[t][j * n + i].item())
                 res_num += (out.item() - aij) ** 2
                 res_den += aij ** 2
-        d.close()
         flops = sum(float(n) ** 3 / 3 for n in sizes)
         results[mode] = {"calls": r["calls"], "wall_s": wall, "calls_per_s": r["calls"] / wall,
                          "p50_us": r["p50_us"], "p99_us": r["p99_us"],
                          "tflops": flops / wall / 1e12,
                          "residual_sampled": (res_num / res_den) ** 0.5 if res_den else None,
-                         "info_nonzero": int((info != 0).sum().item()), "errors": errs[:4],
-                         "server": srv_stats,
+                         "info_nonzero": int((info != 0).sum().item()),
+                         "first_error": r["first_error"], "server": srv_stats,
                          # per operation kind: calls, mean and summed latency
                          "by_kind": {OP_NAMES.get(k, str(k)): {"calls": c, "mean_us": tot / c, "sum_s": tot / 1e6}
                                      for k, (c, tot) in sorted(by_kind.items())},
                          # each thread's finish time: the slowest thread's call chain bounds the wall
-                         "thread_finish_s": [round(x, 3) for x in thread_s]}
+                         "thread_finish_s": [round(x, 3) for x in r["thread_finish_s"]]}
         del work
         torch.cuda.synchronize()
-
-    for mode in ("plain", "served", "ozaki"):
-        info.zero_()
-        run_mode(mode)
     origs.clear()
-    torch.cuda.synchronize()
+    dev.close()
+    torch.cuda.empty_cache()
+    return sizes, nbs, results
+
+
+def serving_ratios(results):
+    """Same-precision ratios (the loop's own effect) and the precision's."""
+    def ratio(a, b):
+        return results[a]["calls_per_s"] / results[b]["calls_per_s"] if a in results and b in results else None
+    return {"served_vs_plain_fp64": ratio("served", "plain"),
+            "served_vs_plain_ozaki": ratio("ozaki", "ozaki_plain"),
+            "ozaki_plain_vs_fp64_plain": ratio("ozaki_plain", "plain"),
+            "ozaki_served_vs_fp64_plain": ratio("ozaki", "plain")}
+
+
+def run_serving(args):
+    import libgpublas_gb300 as g
+    from libgpublas_gb300 import build
+    build.build_library()
+    nthreads = 16
+    sizes, nbs, results = serving_trace(g, nthreads, 1024, args.n or 16384)
     open_loop = None if args.no_open_loop else run_serving_open_loop(g, results)
     head = results["ozaki"]
     line = {"metric": "serving_calls_per_s", "value": head["calls_per_s"],
@@ -1074,14 +1109,11 @@ def run_serving(args):
                        "headline_mode": "ozaki: serving loop, dgemm/dsyrk/dtrsm through the Ozaki path "
                                         "(tolerance 1e-14, FP64 results), dpotrf in FP64"},
             "modes": results,
-            "speedup_vs_plain_dispatch": {
-                "ozaki": head["calls_per_s"] / results["plain"]["calls_per_s"],
-                "served_fp64": results["served"]["calls_per_s"] / results["plain"]["calls_per_s"]},
+            "ratios": serving_ratios(results),
             "residual_sampled": {m: results[m]["residual_sampled"] for m in results},
             "open_loop": open_loop,
             "e2e": {"unavailable": "operands are device-resident by design of this workload"}}
     print(json.dumps(line), flush=True)
-    dev.close()
 
 
 def run_serving_open_loop(g, closed, njobs=48, nmax=4096, workers=16, seed=11):
@@ -1104,6 +1136,7 @@ def run_serving_open_loop(g, closed, njobs=48, nmax=4096, workers=16, seed=11):
     for n in sizes:
         G = torch.empty(n * n, dtype=torch.float64, device="cuda").uniform_(-1.0, 1.0, generator=gen)
         A = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
         dev.dgemm_ozaki("N", "T", n, n, n, 1.0, G, n, G, n, 0.0, A, n)
         A.view(n, n).diagonal().add_(float(n))
         dev.sync()
@@ -1112,7 +1145,8 @@ def run_serving_open_loop(g, closed, njobs=48, nmax=4096, workers=16, seed=11):
     info = torch.zeros(njobs, dtype=torch.int32, device="cuda")
     ncalls = [len(cholesky_calls(n, nb, 0, n, 0)) for n, nb in zip(sizes, nbs)]
     out = {}
-    for mode in ("plain", "served", "ozaki"):
+    for mode in ("plain", "served", "ozaki_plain", "ozaki"):
+        use_server, ozaki = MODES[mode]
         cap = closed[mode]["calls_per_s"] / (sum(ncalls) / njobs)   # jobs/s at closed-loop throughput
         rows = []
         for frac in (0.25, 0.5, 0.75, 1.0):
@@ -1121,7 +1155,7 @@ def run_serving_open_loop(g, closed, njobs=48, nmax=4096, workers=16, seed=11):
             work = [o.clone() for o in origs]
             info.zero_()
             torch.cuda.synchronize()
-            server = g.Server(0, slots=workers) if mode != "plain" else None
+            server = g.Server(0, slots=workers) if use_server else None
             lat, job_lat, errs = [], [0.0] * njobs, []
             lock = threading.Lock()
             nxt = [0]
@@ -1140,7 +1174,7 @@ def run_serving_open_loop(g, closed, njobs=48, nmax=4096, workers=16, seed=11):
                     if wait > 0:
                         time.sleep(wait)
                     calls = cholesky_calls(sizes[j], nbs[j], work[j].data_ptr(), sizes[j],
-                                           info.data_ptr() + 4 * j, ozaki=(mode == "ozaki"))
+                                           info.data_ptr() + 4 * j, ozaki=ozaki)
                     for op in calls:
                         if server is None:
                             c0 = time.perf_counter()

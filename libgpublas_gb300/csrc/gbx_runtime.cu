@@ -50,7 +50,7 @@ struct gbx_ctx {
     int timer_next;
     int timer_open;
     gbx_timer_rec timers[GBX_TIMER_PAIRS];
-    cudaStream_t aux[2];           // copy-in and copy-out streams of the pipelined DGEMM (lazy)
+    cudaStream_t aux[3];           // copy-in, copy-out and second compute stream of the pipelined DGEMM (lazy)
     cudaEvent_t aux_ev[GBX_AUX_EVENTS];
     char err[512];
 };
@@ -197,7 +197,7 @@ extern "C" gbx_status gbx_ctx_destroy(gbx_ctx *c)
         if (c->timers[i].start) cudaEventDestroy(c->timers[i].start);
         if (c->timers[i].stop) cudaEventDestroy(c->timers[i].stop);
     }
-    for (int i = 0; i < 2; i++)
+    for (int i = 0; i < 3; i++)
         if (c->aux[i]) cudaStreamDestroy(c->aux[i]);
     for (int i = 0; i < GBX_AUX_EVENTS; i++)
         if (c->aux_ev[i]) cudaEventDestroy(c->aux_ev[i]);
@@ -514,14 +514,16 @@ extern "C" gbx_status gbx_place_vec_out(gbx_ctx *c, const gbx_operand *op, int n
 // live in host memory and C is large, C is cut into R x P blocks, each still
 // at least two 128 x 128 tiles per SM: the copy-in stream brings row block r
 // of op(A), column panel c of op(B) and block C(r, c) (when beta != 0), the
-// context's stream multiplies each block as soon as its operands are in, and
+// context's stream and a second compute stream take the blocks in turn, each
+// as soon as its operands are in (two streams, so that the last wave of one
+// block's tiles overlaps the next block instead of leaving SMs idle), and
 // the copy-out stream returns each finished block.  Only the first block's
-// operands and the last block's result are exposed.  Every block runs the
-// same kernel instantiation over the same K order as the whole call would,
-// so the result is bit-identical to the undivided product.
+// operands and the last block's result are exposed.  Every output element
+// is one FMA chain over K in the same order as in the undivided product, so
+// the result is bit-identical to it.
 static gbx_status aux_ready(gbx_ctx *c)
 {
-    for (int i = 0; i < 2; i++)
+    for (int i = 0; i < 3; i++)
         if (!c->aux[i] && cudaStreamCreateWithFlags(&c->aux[i], cudaStreamNonBlocking) != cudaSuccess) {
             c->aux[i] = nullptr;
             cudaGetLastError();
@@ -590,18 +592,19 @@ extern "C" gbx_status gbx_dgemm_host_pipelined(gbx_ctx *c, char ta, char tb, int
     if ((st = gbx_ws(c, GBX_WS_STAGE_B, sizeof(double) * (size_t)dlb * bc, (void **)&dB)) != GBX_OK) return st;
     if ((st = gbx_ws(c, GBX_WS_STAGE_C, sizeof(double) * (size_t)dlc * n, (void **)&dC)) != GBX_OK) return st;
     const int R = (m + rb - 1) / rb, P = (n + cb - 1) / cb;
-    if (R + P + 2 * R * P > GBX_AUX_EVENTS) return GBX_ERR_UNSUPPORTED;
-    cudaEvent_t *evA = c->aux_ev, *evB = evA + R, *evC = evB + P, *evK = evC + R * P;
-    cudaStream_t cin_s = c->aux[0], cout_s = c->aux[1], ks = c->stream;
+    if (R + P + 2 * R * P + 1 > GBX_AUX_EVENTS) return GBX_ERR_UNSUPPORTED;
+    cudaEvent_t *evA = c->aux_ev, *evB = evA + R, *evC = evB + P, *evK = evC + R * P, evJoin = evK[R * P];
+    cudaStream_t cin_s = c->aux[0], cout_s = c->aux[1], ks0 = c->stream, ks1 = c->aux[2];
     const size_t e8 = sizeof(double);
     cudaError_t e = cudaSuccess;
     uint64_t h2d = 0, d2h = 0;
     g_misses += 3;
     // the copy-in stream must not start before earlier work on the context's
     // stream (which may still read these staging buffers) is done
-    e = cudaEventRecord(evK[0], ks);
+    e = cudaEventRecord(evK[0], ks0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cin_s, evK[0], 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cout_s, evK[0], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ks1, evK[0], 0);
     for (int r = 0; r < R && e == cudaSuccess; r++) {
         const int r0 = r * rb, rn = std::min(rb, m - r0);
         // row block r of op(A): rows r0.. of A (nota) or columns r0.. of A
@@ -638,14 +641,17 @@ extern "C" gbx_status gbx_dgemm_host_pipelined(gbx_ctx *c, char ta, char tb, int
                 if (e == cudaSuccess) e = cudaEventRecord(evC[r * P + q], cin_s);
             }
             if (e != cudaSuccess) break;
-            // the block's product on the context's stream, once its operands are in
+            // the block's product on one of the two compute streams, once its operands are in
+            const cudaStream_t ks = ((r * P + q) & 1) ? ks1 : ks0;
             e = cudaStreamWaitEvent(ks, evA[r], 0);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(ks, evB[q], 0);
             if (e == cudaSuccess && cin) e = cudaStreamWaitEvent(ks, evC[r * P + q], 0);
             if (e != cudaSuccess) break;
             const double *ab = nota ? dA + r0 : dA + (size_t)r0 * dla;
             const double *bb = notb ? dB + (size_t)c0 * dlb : dB + c0;
+            c->stream = ks;
             st = gbx_dgemm(c, ta, tb, rn, cn, k, alpha, ab, dla, bb, dlb, beta, dC + (size_t)c0 * dlc + r0, dlc);
+            c->stream = ks0;
             if (st != GBX_OK) return st;
             e = cudaEventRecord(evK[r * P + q], ks);
         }
@@ -662,12 +668,16 @@ extern "C" gbx_status gbx_dgemm_host_pipelined(gbx_ctx *c, char ta, char tb, int
             timer_end_on(c, cout_s);
             d2h += (uint64_t)rn * cn * e8;
         }
+    // the context's stream orders after the second compute stream's blocks
+    if (e == cudaSuccess) e = cudaEventRecord(evJoin, ks1);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ks0, evJoin, 0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(cout_s);
     g_h2d += h2d;
     g_d2h += d2h;
     if (e != cudaSuccess) {
         cudaStreamSynchronize(cin_s);
-        cudaStreamSynchronize(ks);
+        cudaStreamSynchronize(ks1);
+        cudaStreamSynchronize(ks0);
         return gbx_fail(c, GBX_ERR_CUDA, "pipelined dgemm: %s", cudaGetErrorString(e));
     }
     return GBX_OK;

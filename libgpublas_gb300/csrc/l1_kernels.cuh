@@ -195,6 +195,66 @@ __device__ __forceinline__ void blue_acc(double v, double &asml, double &amed, d
     else amed = fma(v, v, amed);
 }
 
+// Exact sum of squares on the integer pipe, for one element in four of the
+// warps whose elements all lie in the medium range.  One DFMA per element
+// would cap the kernel at the FP64 pipe's 2 lanes per clock per SM (about
+// 5 TB/s of operands); moving a quarter of the squares to the integer pipe
+// lifts that cap above the HBM rate.  A medium-range x is m 2^(e - 1075)
+// with the 53-bit significand m, so x^2 = m^2 2^(2e - 2150); the
+// accumulator is the unsigned 128-bit integer sum of m^2 2^(2(e - eref) -
+// 12), eref the largest exponent seen so far: an element at eref adds
+// m^2 >> 12 < 2^94 (2^34 of them fit), a smaller one drops only its bits
+// below 2^-94 of the largest square, and a larger exponent shifts the sum
+// down first.  The truncation is far below the FP64 rounding of the DFMA
+// partials it is added to.
+struct SqFix {
+    unsigned long long lo, hi;
+    int eref;
+    __device__ __forceinline__ void init() { lo = 0ull; hi = 0ull; eref = 0; }
+    __device__ __forceinline__ void shift_down(int d)
+    {
+        if (d >= 128) { lo = 0ull; hi = 0ull; }
+        else if (d >= 64) { lo = hi >> (d - 64); hi = 0ull; }
+        else if (d > 0) { lo = (lo >> d) | (hi << (64 - d)); hi >>= d; }
+    }
+    // v: a finite normal double (the medium range guarantees it)
+    __device__ __forceinline__ void add(double v)
+    {
+        const unsigned long long b = abs_bits(v);
+        const int e = (int)(b >> 52);
+        const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+        if (e > eref) {
+            shift_down(2 * (e - eref));
+            eref = e;
+        }
+        const int sh = 12 + 2 * (eref - e);   // >= 12
+        const unsigned long long plo = m * m, phi = __umul64hi(m, m);   // m^2 < 2^106
+        const int s1 = min(sh, 63), s2 = min(max(sh - 64, 0), 63);
+        unsigned long long clo = sh < 64 ? (plo >> s1) | (phi << (64 - s1)) : (phi >> s2);
+        unsigned long long chi = sh < 64 ? (phi >> s1) : 0ull;
+        if (sh >= 106) { clo = 0ull; chi = 0ull; }
+        lo += clo;
+        hi += chi + (lo < clo ? 1ull : 0ull);
+    }
+    // the sum as a double: acc * 2^(2 eref - 2150 + 12)
+    __device__ __forceinline__ double value() const
+    {
+        if ((lo | hi) == 0ull) return 0.0;
+        return ldexp(fma((double)hi, 0x1p64, (double)lo), 2 * eref - 2138);
+    }
+};
+
+// True when every active lane's four elements lie in the medium range
+// (integer tests on the high words, as in blue_acc).
+__device__ __forceinline__ bool all_medium4(double a, double b, double c, double d)
+{
+    constexpr unsigned kBigHi = (unsigned)(486 + 1023) << 20;
+    constexpr unsigned kSmlHi = (unsigned)(1023 - 511) << 20;
+    const bool out = (abs_hi_word(a) - kSmlHi > kBigHi - kSmlHi) | (abs_hi_word(b) - kSmlHi > kBigHi - kSmlHi) |
+                     (abs_hi_word(c) - kSmlHi > kBigHi - kSmlHi) | (abs_hi_word(d) - kSmlHi > kBigHi - kSmlHi);
+    return !__any_sync(__activemask(), out);
+}
+
 static __global__ void __launch_bounds__(L1_THREADS)
 nrm2_partial(int n, const double *__restrict__ x, int incx, double *__restrict__ part)
 {
@@ -208,13 +268,23 @@ nrm2_partial(int n, const double *__restrict__ x, int incx, double *__restrict__
         // four independent accumulator chains per thread (the DFMA latency
         // would otherwise serialise the loop)
         double s1 = 0.0, m1 = 0.0, b1 = 0.0, s2 = 0.0, m2 = 0.0, b2 = 0.0, s3 = 0.0, m3 = 0.0, b3 = 0.0;
+        SqFix fx;
+        fx.init();
         for (; i + stride < n2; i += 2 * stride) {
             double2 a = ldg2(x2 + i), b = ldg2(x2 + i + stride);
-            blue_acc(a.x, asml, amed, abig); blue_acc(a.y, s1, m1, b1);
-            blue_acc(b.x, s2, m2, b2); blue_acc(b.y, s3, m3, b3);
+            if (all_medium4(a.x, a.y, b.x, b.y)) {
+                // three squares on the FP64 pipe, the fourth on the integer pipe
+                amed = fma(a.x, a.x, amed);
+                m1 = fma(a.y, a.y, m1);
+                m2 = fma(b.x, b.x, m2);
+                fx.add(b.y);
+            } else {
+                blue_acc(a.x, asml, amed, abig); blue_acc(a.y, s1, m1, b1);
+                blue_acc(b.x, s2, m2, b2); blue_acc(b.y, s3, m3, b3);
+            }
         }
         asml += (s1 + s2) + s3;
-        amed += (m1 + m2) + m3;
+        amed += ((m1 + m2) + m3) + fx.value();
         abig += (b1 + b2) + b3;
         for (; i < n2; i += stride) {
             double2 a = ldg2(x2 + i);
