@@ -538,16 +538,19 @@ static gbx_status aux_ready(gbx_ctx *c)
     return GBX_OK;
 }
 
-// Block grid for an m x n product: row blocks of op(A) of >= 4096 rows (at
-// most 4) and column panels of >= 2048 columns (at most 8), reduced until
-// every block holds two 128 x 128 tiles per SM.  Returns 0 when the call is
-// too small to split.
+// Block grid for an m x n product: row blocks of op(A) of >= 2048 rows (at
+// most 8) and column panels of >= 1024 columns (at most 8), reduced until
+// every block holds at least 128 tiles of 128 x 128.  Small first blocks keep
+// the exposed copy-in short (the host link runs at a few tens of GB/s on
+// some boxes); the two compute streams keep the SMs busy across blocks.
+// Returns 0 when the call is too small to split.
 static int pipeline_plan(int m, int n, int sms, int *rb, int *cb)
 {
-    int R = std::max(1, std::min(4, m / 4096)), P = std::max(1, std::min(8, n / 2048));
+    (void)sms;
+    int R = std::max(1, std::min(8, m / 2048)), P = std::max(1, std::min(8, n / 1024));
     while (R * P > 1) {
         const int r = ((m + R - 1) / R + 127) / 128 * 128, q = ((n + P - 1) / P + 127) / 128 * 128;
-        if ((long long)(r / 128) * (q / 128) >= 2LL * sms) {
+        if ((long long)(r / 128) * (q / 128) >= 128) {
             *rb = r;
             *cb = q;
             return 1;

@@ -25,73 +25,6 @@ constexpr int ROWS_PER_BLOCK = 2 * GEMV_THREADS;
 inline cudaStream_t S(gbx_ctx *ctx) { return (cudaStream_t)gbx_ctx_get_stream(ctx); }
 inline long long base_off(int n, int inc) { return inc >= 0 ? 0 : (long long)(n - 1) * (-inc); }
 
-// Exact signed sum of products on the integer pipe, for a quarter of the
-// products of the streaming DGEMV kernels.  Each matrix element is used once
-// with one DFMA, and the FP64 pipe (2 lanes per clock per SM) caps that at
-// about 5 TB/s of matrix; products moved to the integer pipe lift the cap
-// above the HBM rate.  For finite a = ma 2^(ea - 1075) and x = mx 2^(ex -
-// 1075) (53-bit significands, subnormals with exponent 1 and no hidden bit)
-// the product is ma mx 2^(ea + ex - 2150); the accumulator is the signed
-// 128-bit sum of ma mx 2^((ea + ex) - eref - 12), eref the largest exponent
-// sum seen: a product at eref adds |ma mx| >> 12 < 2^94 (2^33 of them fit),
-// a smaller one drops only its bits below 2^-94 of the largest product, and
-// a larger exponent shifts the sum down first.
-struct ProdFix {
-    unsigned long long lo;
-    long long hi;
-    int eref;
-    __device__ __forceinline__ void init() { lo = 0ull; hi = 0; eref = 0; }
-    __device__ __forceinline__ void shift_down(int d)   // arithmetic
-    {
-        if (d >= 127) { hi = hi >> 63; lo = (unsigned long long)hi; }
-        else if (d >= 64) { lo = (unsigned long long)(hi >> (d - 64)); hi >>= 63; }
-        else if (d > 0) { lo = (lo >> d) | ((unsigned long long)hi << (64 - d)); hi >>= d; }
-    }
-    __device__ __forceinline__ void add(double a, double x)
-    {
-        const unsigned long long ba = (unsigned long long)__double_as_longlong(a);
-        const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
-        const int ea = (int)((ba >> 52) & 0x7FF), ex = (int)((bx >> 52) & 0x7FF);
-        const unsigned long long ma = (ba & 0xFFFFFFFFFFFFFull) | (ea ? 0x10000000000000ull : 0ull);
-        const unsigned long long mx = (bx & 0xFFFFFFFFFFFFFull) | (ex ? 0x10000000000000ull : 0ull);
-        const int e = max(ea, 1) + max(ex, 1);
-        if (e > eref) {
-            shift_down(e - eref);
-            eref = e;
-        }
-        const int sh = 12 + (eref - e);
-        const unsigned long long plo = ma * mx, phi = __umul64hi(ma, mx);   // < 2^106
-        const int s1 = min(sh, 63), s2 = min(max(sh - 64, 0), 63);
-        unsigned long long clo = sh < 64 ? (plo >> s1) | (phi << (64 - s1)) : (phi >> s2);
-        unsigned long long chi = sh < 64 ? (phi >> s1) : 0ull;
-        if (sh >= 106) { clo = 0ull; chi = 0ull; }
-        // two's complement negation when the signs differ
-        const unsigned long long neg = 0ull - ((ba ^ bx) >> 63);
-        clo ^= neg;
-        chi ^= neg;
-        const unsigned long long c1 = clo + (neg & 1ull);
-        chi += (c1 < clo) ? 1ull : 0ull;
-        lo += c1;
-        hi += (long long)chi + (lo < c1 ? 1 : 0);
-    }
-    // the sum as a double: acc * 2^(eref - 2150 + 12)
-    __device__ __forceinline__ double value() const
-    {
-        if ((lo | (unsigned long long)hi) == 0ull) return 0.0;
-        const double d = (hi == ((long long)lo >> 63)) ? (double)(long long)lo : fma((double)hi, 0x1p64, (double)lo);
-        return ldexp(d, eref - 2138);
-    }
-};
-
-// True when every active lane's operands are finite (integer tests on the
-// high words): the integer products then stand in for the DFMAs exactly.
-__device__ __forceinline__ bool all_finite3(double a, double b, double c)
-{
-    const auto hi = [](double v) { return (unsigned)(__double_as_longlong(v) >> 32) & 0x7FF00000u; };
-    const bool bad = (hi(a) == 0x7FF00000u) | (hi(b) == 0x7FF00000u) | (hi(c) == 0x7FF00000u);
-    return !__any_sync(__activemask(), bad);
-}
-
 __global__ void __launch_bounds__(GEMV_THREADS)
 gemv_n_partial(int m, int n, int chunk, const double *__restrict__ A, long long lda,
                const double *__restrict__ x, int incx, double *__restrict__ part, int vec)
@@ -103,9 +36,6 @@ gemv_n_partial(int m, int n, int chunk, const double *__restrict__ A, long long 
     if (vec && r + 1 < m) {
         const double *ap = A + (long long)c0 * lda + r;
         int c = c0;
-        ProdFix f0, f1;
-        f0.init();
-        f1.init();
         for (; c + 4 <= c1; c += 4) {
             const double2 a0 = __ldg((const double2 *)(ap));
             const double2 a1 = __ldg((const double2 *)(ap + lda));
@@ -116,17 +46,9 @@ gemv_n_partial(int m, int n, int chunk, const double *__restrict__ A, long long 
             s0 = fma(a0.x, x0, s0); s1 = fma(a0.y, x0, s1);
             s0 = fma(a1.x, x1, s0); s1 = fma(a1.y, x1, s1);
             s0 = fma(a2.x, x2, s0); s1 = fma(a2.y, x2, s1);
-            if (all_finite3(a3.x, a3.y, x3)) {
-                // a quarter of the products on the integer pipe
-                f0.add(a3.x, x3);
-                f1.add(a3.y, x3);
-            } else {
-                s0 = fma(a3.x, x3, s0); s1 = fma(a3.y, x3, s1);
-            }
+            s0 = fma(a3.x, x3, s0); s1 = fma(a3.y, x3, s1);
             ap += 4 * lda;
         }
-        s0 += f0.value();
-        s1 += f1.value();
         for (; c < c1; c++) {
             const double2 a0 = __ldg((const double2 *)(ap));
             const double xv = __ldg(x + (long long)c * incx);
@@ -176,25 +98,12 @@ gemv_t_warp(int m, int n, const double *__restrict__ A, long long lda, const dou
     double s0 = 0.0, s1 = 0.0;
     if (vec) {
         const int m2 = m >> 1;
-        ProdFix f;
-        f.init();
-        int i = lane;
-        for (; i + 32 < m2; i += 64) {
-            const double2 a = __ldg((const double2 *)col + i), b = __ldg((const double2 *)col + i + 32);
-            const double2 xv = __ldg((const double2 *)x + i), xw = __ldg((const double2 *)x + i + 32);
-            s0 = fma(a.x, xv.x, s0);
-            s1 = fma(a.y, xv.y, s1);
-            s0 = fma(b.x, xw.x, s0);
-            if (all_finite3(b.y, xw.y, 0.0)) f.add(b.y, xw.y);   // a quarter on the integer pipe
-            else s1 = fma(b.y, xw.y, s1);
-        }
-        for (; i < m2; i += 32) {
+        for (int i = lane; i < m2; i += 32) {
             const double2 a = __ldg((const double2 *)col + i);
             const double2 xv = __ldg((const double2 *)x + i);
             s0 = fma(a.x, xv.x, s0);
             s1 = fma(a.y, xv.y, s1);
         }
-        s1 += f.value();
         if ((m & 1) && lane == 0) s0 = fma(col[m - 1], x[m - 1], s0);
     } else {
         for (int i = lane; i < m; i += 32) s0 = fma(__ldg(col + i), __ldg(x + (long long)i * incx), s0);

@@ -14,10 +14,11 @@
 //     slices is exact;
 //   * products with the same s + t = q share one TMEM accumulator (and one
 //     power-of-two weight 2^-5q); only q <= S-1 are formed (S(S+1)/2 slice
-//     products); the drain adds each diagonal sum exactly into a 128-bit
-//     integer running sum (smallest q first), and the last group converts
-//     it once to FP64, scales it by 2^(e_i+f_j-8-5(S-1)) and writes
-//     C = alpha*sum + beta*C;
+//     products); the diagonal sums are combined by Horner's rule, largest
+//     weight first: in the wide-tile kernel as one FP64 value per element
+//     (rounded once per step, relative to the partial value), in the
+//     small-K kernel exactly in two 64-bit integers; the result is scaled by
+//     2^(e_i+f_j-8-5(S-1)) and written as C = alpha*sum + beta*C;
 //   * S is chosen on the device from the operands' exponent statistics for a
 //     target relative Frobenius error (or forced by the caller).
 // The scaling, the final recombination and alpha/beta are FP64.
@@ -668,7 +669,8 @@ struct OzParams {
     int *S;                    // slice count (written by the small-K kernel, read by the others)
     const int *row_exp;        // Mp: e_i - 4
     const int *col_exp;        // Np: f_j - 4
-    long long *W;              // Mp x Np running sums, two words per element, column-major
+    long long *W;              // Mp x Np running sums, column-major: two 64-bit words per element
+                               // (exact drain) or one double (Horner drain)
     double *C;
     long long ldc;
     double alpha, beta;
@@ -862,10 +864,11 @@ __device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, i
     return p.c_part == 1 ? (r1 >= c0) : (r0 <= c1);
 }
 
-// The drain: per output element, the diagonal sums D_q (integers, |D_q| <
-// 2^24 per accumulation group, exact in the FP32 TMEM accumulator) are
-// summed exactly as one signed 128-bit integer in units of the last
-// diagonal's weight,
+// The exact drain (the CTA-pair kernel; the wide-tile kernel uses the
+// Horner drain oz_drain_row_h below): per output element, the diagonal sums
+// D_q (integers, |D_q| < 2^24 per accumulation group, exact in the FP32 TMEM
+// accumulator) are summed exactly as one signed 128-bit integer in units of
+// the last diagonal's weight,
 //     V = sum_q D_q 2^(5(S-1-q)),     C_ij = V 2^(e_i + f_j - 8 - 5(S-1)),
 // held in W (two 64-bit words per element, column-major Mp x Np) between
 // diagonals.  Each diagonal costs a decode of the FP32 value and a 128-bit
@@ -1226,6 +1229,103 @@ __device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, 
     }
 }
 
+// Tile order of the wide-tile kernel: groups of OZ_GROUP_M row tiles, the
+// row tile fastest within a group, so the 152 tiles resident at once form an
+// 8 x 19 block (at 8192^2) instead of all 64 row tiles of two or three
+// column tiles.  The slice tiles that block streams per K step are about a
+// third fewer, and each A tile is shared by 19 CTAs instead of two or three
+// (the CTAs progress through K at about the same pace, so shared tiles are
+// read from L2).
+constexpr int OZ_GROUP_M = 8;
+__device__ __forceinline__ void oz_tile_coords(int t, int tiles_m, int tiles_n, int &tm, int &tn)
+{
+    const int per_group = OZ_GROUP_M * tiles_n;
+    const int g = t / per_group, r = t - g * per_group;
+    const int rows = min(OZ_GROUP_M, tiles_m - g * OZ_GROUP_M);   // the last group may be shorter
+    tm = g * OZ_GROUP_M + r % rows;
+    tn = r / rows;
+}
+
+// Drain of the wide-tile kernel: diagonals arrive in ascending q (largest
+// weight first) and each element's running value is one double, combined by
+// Horner's rule: v = 32 v + D_q at the first accumulation group of diagonal
+// q, v += D for that diagonal's further groups (D: the group's FP32 sum, an
+// integer below 2^24, exact in a double).  The last group scales v by
+// 2^(e_i + f_j - 8 - 5(S-1)) and writes C = alpha v 2^e + beta C.  Keeping v
+// in 8 bytes instead of the exact 128-bit integer halves the running-sum
+// traffic between diagonals, the kernel's largest DRAM stream (the sums of
+// 152 resident 128 x 256 tiles do not stay in L2 next to the slices); each
+// Horner step rounds once, relative to the partial value, so the result
+// carries about S units of roundoff of |C| -- far below the target error of
+// the slice truncation.
+template <int NCOL, int CH>
+__device__ __forceinline__ void oz_drain_row_h(const OzParams &p, uint32_t taddr, int grow, int gcol0, int S,
+                                               int rexp, bool first, bool new_diag, bool last)
+{
+    constexpr int NCH = NCOL / CH;
+    const int erow = rexp - 5 * (S - 1);   // scale of v without the column part
+    const bool row_ok = grow < p.M;
+    const bool need_c = last && row_ok && p.beta != 0.0;
+    const double *wrow = (const double *)p.W + (size_t)gcol0 * p.Mp + grow;
+    double *crow = p.C + (size_t)gcol0 * p.ldc + grow;
+    double wn[CH], cn[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) { wn[j] = 0.0; cn[j] = 0.0; }
+    if (!first) {
+#pragma unroll
+        for (int j = 0; j < CH; j++) wn[j] = __ldcg(wrow + (size_t)j * p.Mp);
+    }
+    if (need_c) {
+#pragma unroll
+        for (int j = 0; j < CH; j++) cn[j] = oz_c_keep(p, grow, gcol0 + j) ? crow[(size_t)j * p.ldc] : 0.0;
+    }
+#pragma unroll 1
+    for (int c = 0; c < NCH; c++) {
+        double wc[CH], cc[CH];
+#pragma unroll
+        for (int j = 0; j < CH; j++) { wc[j] = wn[j]; cc[j] = cn[j]; }
+        const int nc = (c + 1) * CH;
+        if (c + 1 < NCH) {
+            if (!first) {
+#pragma unroll
+                for (int j = 0; j < CH; j++) wn[j] = __ldcg(wrow + (size_t)(nc + j) * p.Mp);
+            }
+            if (need_c) {
+#pragma unroll
+                for (int j = 0; j < CH; j++)
+                    cn[j] = oz_c_keep(p, grow, gcol0 + nc + j) ? crow[(size_t)(nc + j) * p.ldc] : 0.0;
+            }
+        }
+        uint32_t r[CH];
+        tmem_ld_chunk<CH>(taddr + (uint32_t)(c * CH), r);
+        tmem_ld_wait();
+        const int cb = c * CH;
+#pragma unroll
+        for (int j = 0; j < CH; j++) {
+            const double d = (double)__uint_as_float(r[j]);
+            wc[j] = first ? d : (new_diag ? fma(wc[j], 32.0, d) : wc[j] + d);
+        }
+        if (!last) {
+            double *wdst = (double *)p.W + (size_t)(gcol0 + cb) * p.Mp + grow;
+#pragma unroll
+            for (int j = 0; j < CH; j++) __stcg(wdst + (size_t)j * p.Mp, wc[j]);
+        } else if (row_ok) {
+            const bool beta_on = p.beta != 0.0;
+#pragma unroll
+            for (int j = 0; j < CH; j++) {
+                const int gcol = gcol0 + cb + j;
+                if (!oz_c_keep(p, grow, gcol)) continue;
+                const int e = erow + __ldg(p.col_exp + gcol);
+                // alpha 2^e exactly (an exponent-field add) when it stays normal,
+                // else scale v itself first (results near the underflow threshold)
+                const double r0 = (e >= -1000 && e <= 1000) ? oz_alpha_pow2(p.alpha, e) * wc[j]
+                                                             : p.alpha * ldexp(wc[j], e);
+                crow[(size_t)(cb + j) * p.ldc] = beta_on ? fma(p.beta, cc[j], r0) : r0;
+            }
+        }
+    }
+}
+
 // 1-CTA kernel, BM = 128 rows by BN = 256 or 128 columns.  Warp 0 issues the
 // TMA loads, warp 1 the MMAs, warps 2..9 drain: two warps per TMEM lane
 // quarter (a warp may only read the 32 TMEM lanes of its rank within its
@@ -1292,9 +1392,10 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             uint32_t phase = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+                int tm, tn;
+                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
                 if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
-                for (int q = gp.S - 1; q >= 0 && ok; q--) {
+                for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
                     for (int it = 0; it < nitems && ok; it++) {
@@ -1326,9 +1427,10 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             bool ok = true;
             const uint32_t smem_base = smem_u32(smem);
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+                int tm, tn;
+                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
                 if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
-                for (int q = gp.S - 1; q >= 0 && ok; q--) {
+                for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
                     for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
@@ -1372,24 +1474,25 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         uint32_t tphase = 0;
         bool ok = true;
         for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-            const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+            int tm, tn;
+                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
             if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
             const int grow = tm * OZ_BM + row;
             const int rexp = p.row_exp[grow];
             bool first = true;
-            for (int q = gp.S - 1; q >= 0 && ok; q--) {
+            for (int q = 0; q < gp.S && ok; q++) {
                 const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                 const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
                 for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
-                    const bool last = (q == 0) && (g0 + gp.items_per_group >= nitems);
+                    const bool last = (q == gp.S - 1) && (g0 + gp.items_per_group >= nitems);
                     // warp-uniform outcome: tcgen05.ld below is .sync.aligned
                     ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tphase, status, TC_TIMEOUT_TMEM_FULL));
                     if (!ok) break;
                     tc_fence_after();
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) +
                                            (uint32_t)(buf * BN + half * Cfg::DRAIN_COLS);
-                    oz_drain_row<Cfg::DRAIN_COLS, Cfg::DRAIN_CH>(p, taddr, grow, tn * BN + half * Cfg::DRAIN_COLS,
-                                                                 q, gp.S, rexp, first, last);
+                    oz_drain_row_h<Cfg::DRAIN_COLS, Cfg::DRAIN_CH>(p, taddr, grow, tn * BN + half * Cfg::DRAIN_COLS,
+                                                                   gp.S, rexp, first, g0 == 0, last);
                     tc_fence_before();
                     mbar_arrive(&tempty[buf]);
                     first = false;
