@@ -554,9 +554,9 @@ def run_ours(args):
             "workload": "cholesky_trace_16threads_n1024-4096",
             "n": sizes, "nb": nbs,
             "modes": {m: {k: v[k] for k in ("calls", "calls_per_s", "p50_us", "p99_us", "tflops",
-                                            "residual_sampled", "wall_s", "first_error")}
+                                            "residual_sampled", "wall_s", "first_error", "chains")}
                       for m, v in modes.items()},
-            "ratios": serving_ratios(modes)}
+            "ratios": serving_ratios(modes, line["roofline"]["peak"])}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         from oracle import cpublas
         cb = cpublas.get()
@@ -1003,7 +1003,7 @@ MODES = {
 }
 
 
-def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES)):
+def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES), chains=True):
     """Closed-loop Cholesky trace: nthreads native caller threads, thread t
     factorising A = G G^T + n I (G uniform[-1,1], n log-uniform in
     [nmin, nmax], nb in {128, 256}) through the library, once per mode.
@@ -1061,9 +1061,25 @@ def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES)):
                 res_num += (out.item() - aij) ** 2
                 res_den += aij ** 2
         flops = sum(float(n) ** 3 / 3 for n in sizes)
+        # each thread's chain alone on the GPU (plain per-call dispatch, one
+        # caller thread): a caller's calls are synchronous and dependent, so
+        # no scheduler can finish the trace before its slowest lone chain
+        chain = None
+        if chains and not use_server:
+            alone = []
+            for t in range(nthreads):
+                wt = origs[t].clone()
+                torch.cuda.synchronize()
+                ra = g.cholesky_trace(None, 0, [sizes[t]], [nbs[t]], [wt.data_ptr()], info.data_ptr() + 4 * t,
+                                      ozaki)
+                alone.append(ra["wall_s"])
+                del wt
+            chain = {"alone_s": [round(x, 5) for x in alone], "longest_alone_s": max(alone),
+                     "sum_alone_s": sum(alone)}
         results[mode] = {"calls": r["calls"], "wall_s": wall, "calls_per_s": r["calls"] / wall,
+                         "chains": chain,
                          "p50_us": r["p50_us"], "p99_us": r["p99_us"],
-                         "tflops": flops / wall / 1e12,
+                         "tflops": flops / wall / 1e12, "flops": flops,
                          "residual_sampled": (res_num / res_den) ** 0.5 if res_den else None,
                          "info_nonzero": int((info != 0).sum().item()),
                          "first_error": r["first_error"], "server": srv_stats,
@@ -1080,14 +1096,29 @@ def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES)):
     return sizes, nbs, results
 
 
-def serving_ratios(results):
-    """Same-precision ratios (the loop's own effect) and the precision's."""
+def serving_ratios(results, fp64_peak_tflops=None):
+    """Same-precision ratios (the loop's own effect) and the precision's,
+    and the bounds on what any scheduler could gain over plain dispatch."""
     def ratio(a, b):
         return results[a]["calls_per_s"] / results[b]["calls_per_s"] if a in results and b in results else None
-    return {"served_vs_plain_fp64": ratio("served", "plain"),
-            "served_vs_plain_ozaki": ratio("ozaki", "ozaki_plain"),
-            "ozaki_plain_vs_fp64_plain": ratio("ozaki_plain", "plain"),
-            "ozaki_served_vs_fp64_plain": ratio("ozaki", "plain")}
+    out = {"served_vs_plain_fp64": ratio("served", "plain"),
+           "served_vs_plain_ozaki": ratio("ozaki", "ozaki_plain"),
+           "ozaki_plain_vs_fp64_plain": ratio("ozaki_plain", "plain"),
+           "ozaki_served_vs_fp64_plain": ratio("ozaki", "plain")}
+    # the most any scheduler could gain over plain dispatch in the same
+    # precision: the plain wall over the slowest caller's chain run alone
+    for prec, plain in (("fp64", "plain"), ("ozaki", "ozaki_plain")):
+        ch = results.get(plain, {}).get("chains")
+        if ch:
+            out[f"plain_wall_over_longest_chain_{prec}"] = results[plain]["wall_s"] / ch["longest_alone_s"]
+    if fp64_peak_tflops and "plain" in results:
+        # FP64: the trace's n^3/3 flops at the measured DFMA rate
+        fb = results["plain"]["flops"] / (fp64_peak_tflops * 1e12)
+        out["fp64_pipe_bound_s"] = fb
+        ch = results["plain"].get("chains")
+        if ch:
+            out["max_gain_fp64_any_scheduler"] = results["plain"]["wall_s"] / max(fb, ch["longest_alone_s"])
+    return out
 
 
 def run_serving(args):
@@ -1109,7 +1140,7 @@ def run_serving(args):
                        "headline_mode": "ozaki: serving loop, dgemm/dsyrk/dtrsm through the Ozaki path "
                                         "(tolerance 1e-14, FP64 results), dpotrf in FP64"},
             "modes": results,
-            "ratios": serving_ratios(results),
+            "ratios": serving_ratios(results, g.Device(0).fp64_peak()),
             "residual_sampled": {m: results[m]["residual_sampled"] for m in results},
             "open_loop": open_loop,
             "e2e": {"unavailable": "operands are device-resident by design of this workload"}}

@@ -110,6 +110,9 @@ gbx_status gbx_idamin(gbx_ctx *ctx, int n, const double *x, int incx, int *res);
  * (4096 partials of 65536 elements) and larger n returns GBX_ERR_ARG.
  * Calls that overlap on the GPU race on that array.  The first call on a
  * device looks up the array's address; make it before any stream capture.
+ * The looked-up address is kept for the life of the process: after a
+ * cudaDeviceReset of that device it is stale, so do not call this entry
+ * point on a device that was reset. 
  * Results agree with gbx_ddot within rounding (different partition). */
 gbx_status gbx_ddot_noalloc(void *stream, int n, const double *x, int incx,
                             const double *y, int incy, double *res);

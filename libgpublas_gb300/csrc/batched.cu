@@ -18,6 +18,7 @@
 // $HOME/.cache/gbxblas/autotune.json), so later plans skip the timing.
 #include "gbx_internal.h"
 #include "gemm_host.h"
+#include "grouped_dev.cuh"
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -33,25 +34,14 @@
 
 namespace {
 
+using gbx_grouped::DevOp;
+using gbx_grouped::trsm_item;
+
 constexpr int BT_THREADS = 256;
 constexpr int BT_BK = 16;
 constexpr int TRSM_MAX_ORDER = 256;
 constexpr int TRSM_SYS = 16;      // right-hand sides solved together
 constexpr int NBUCKET = 6;        // max(M,N) <= 32, 64, 128, 256, 512, larger
-
-struct DevOp {
-    int kind;                     // GBX_OP_GEMM / GBX_OP_TRSM
-    int ta, tb;                   // GEMM transpositions; TRSM: ta = op(A) transposed
-    int lower, unit, left;        // TRSM: effective triangle of the solved matrix, diag, side
-    int m, n, k;
-    double alpha, beta;
-    const double *A;
-    long long lda;
-    const double *B;
-    long long ldb;
-    double *C;
-    long long ldc;
-};
 
 struct Item {
     int op;
@@ -120,53 +110,6 @@ __device__ void gemm_tile(const DevOp &o, int tm, int tn, double *smem)
     }
 }
 
-// ---------------------------------------------------------------- TRSM item
-// Solves T y = alpha*b for up to TRSM_SYS systems of order n (<= 256), where
-// for side 'L' T = op(A) and the systems are columns of B (m x nrhs), and for
-// side 'R' T = op(A)^T and the systems are rows of B.  Substitution order is
-// chosen by the effective triangle of T.
-__device__ void trsm_item(const DevOp &o, int sys0, double *smem)
-{
-    const int n = o.left ? o.m : o.n;                 // order of T
-    const int nsys_total = o.left ? o.n : o.m;
-    const int nsys = min(TRSM_SYS, nsys_total - sys0);
-    double *X = smem;                                  // X[i * TRSM_SYS + s]
-    // element (i, s) of system vector s
-    auto bidx = [&](int i, int s) -> long long {
-        return o.left ? (long long)(sys0 + s) * o.ldc + i : (long long)i * o.ldc + (sys0 + s);
-    };
-    // T(i, j): side L: op(A)(i,j); side R: op(A)(j,i)
-    auto T = [&](int i, int j) -> double {
-        int r = i, c = j;
-        if (!o.left) { r = j; c = i; }
-        return o.ta ? o.A[(long long)r * o.lda + c] : o.A[(long long)c * o.lda + r];
-    };
-    for (int t = threadIdx.x; t < n * TRSM_SYS; t += BT_THREADS) {
-        const int i = t / TRSM_SYS, s = t % TRSM_SYS;
-        X[t] = s < nsys ? o.alpha * o.C[bidx(i, s)] : 0.0;
-    }
-    __syncthreads();
-    for (int step = 0; step < n; step++) {
-        const int kk = o.lower ? step : n - 1 - step;
-        if (!o.unit) {
-            const double d = T(kk, kk);
-            if (threadIdx.x < TRSM_SYS) X[kk * TRSM_SYS + threadIdx.x] /= d;
-            __syncthreads();
-        }
-        // update the rows still to be solved
-        const int r0 = o.lower ? kk + 1 : 0, r1 = o.lower ? n : kk;
-        for (int t = threadIdx.x; t < (r1 - r0) * TRSM_SYS; t += BT_THREADS) {
-            const int i = r0 + t / TRSM_SYS, s = t % TRSM_SYS;
-            X[i * TRSM_SYS + s] = fma(-T(i, kk), X[kk * TRSM_SYS + s], X[i * TRSM_SYS + s]);
-        }
-        __syncthreads();
-    }
-    for (int t = threadIdx.x; t < n * TRSM_SYS; t += BT_THREADS) {
-        const int i = t / TRSM_SYS, s = t % TRSM_SYS;
-        if (s < nsys) o.C[bidx(i, s)] = X[t];
-    }
-}
-
 __global__ void __launch_bounds__(BT_THREADS, 2)
 grouped_kernel(const DevOp *__restrict__ ops, const Item *__restrict__ items, int nitems, int *counter)
 {
@@ -181,7 +124,7 @@ grouped_kernel(const DevOp *__restrict__ ops, const Item *__restrict__ items, in
         if (it >= nitems) break;
         const Item w = items[it];
         const DevOp o = ops[w.op];
-        if (o.kind == GBX_OP_TRSM) trsm_item(o, w.variant * TRSM_SYS, smem);
+        if (o.kind == GBX_OP_TRSM) trsm_item<TRSM_SYS, BT_THREADS>(o, w.variant * TRSM_SYS, smem);
         else if (w.variant == 0) gemm_tile<32>(o, w.tm, w.tn, smem);
         else gemm_tile<64>(o, w.tm, w.tn, smem);
         __syncthreads();

@@ -200,9 +200,14 @@ __device__ __forceinline__ void tri_decode(int t, int &bi, int &bj)
     bj = t - i * (i + 1) / 2;
 }
 
+// One BM x BN tile of C (tile index: column-major over the tile grid, or the
+// triangular enumeration for C_LOWER / C_UPPER), computed by the whole CTA
+// of GEMM_THREADS threads.  The launch kernel below runs one tile per CTA;
+// the serving loop's persistent kernel calls it for the tiles it takes.
+// Every output element is one FMA chain over K in increasing order,
+// whatever the tile size.
 template <typename T, int TM, int TN, int BK>
-__global__ void __launch_bounds__(GEMM_THREADS)
-gemm_simt_kernel(GemmArgs<T> p)
+__device__ __forceinline__ void gemm_simt_tile(const GemmArgs<T> &p, int tile)
 {
     constexpr int BM = 16 * TM, BN = 16 * TN;
     __shared__ __align__(16) T As[2][BK][BM];
@@ -210,11 +215,11 @@ gemm_simt_kernel(GemmArgs<T> p)
 
     int bi, bj;
     if (p.c_part == C_FULL) {
-        bi = blockIdx.x % p.tiles_m;
-        bj = blockIdx.x / p.tiles_m;
+        bi = tile % p.tiles_m;
+        bj = tile / p.tiles_m;
     } else {
         int r, c;
-        tri_decode(blockIdx.x, r, c);
+        tri_decode(tile, r, c);
         if (p.c_part == C_LOWER) { bi = r; bj = c; } else { bi = c; bj = r; }
     }
     const int m0 = bi * BM, n0 = bj * BN;
@@ -299,6 +304,13 @@ gemm_simt_kernel(GemmArgs<T> p)
             *cp = v;
         }
     }
+}
+
+template <typename T, int TM, int TN, int BK>
+__global__ void __launch_bounds__(GEMM_THREADS)
+gemm_simt_kernel(GemmArgs<T> p)
+{
+    gemm_simt_tile<T, TM, TN, BK>(p, blockIdx.x);
 }
 
 }  // namespace gbx_gemm

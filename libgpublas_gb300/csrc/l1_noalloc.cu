@@ -21,7 +21,9 @@
 //     array and may return wrong sums;
 //   * set-up: the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current and caches it; make
-//     that first call before any stream capture.
+//     that first call before any stream capture.  The cached address does
+//     not survive a cudaDeviceReset of that device: after a reset, this entry
+//     point must not be called on it.
 // It calls no cudaMalloc, cudaFree or allocating library routine.
 #include "gbx_internal.h"
 #include "l1_kernels.cuh"

@@ -32,7 +32,7 @@ gemv_n_partial(int m, int n, int chunk, const double *__restrict__ A, long long 
     const int r = blockIdx.x * ROWS_PER_BLOCK + 2 * threadIdx.x;
     const int c0 = blockIdx.y * chunk;
     const int c1 = min(n, c0 + chunk);
-    double s0 = 0.0, s1 = 0.0;
+    double s0 = 0.0, s1 = 0.0, t0 = 0.0, t1 = 0.0;
     if (vec && r + 1 < m) {
         const double *ap = A + (long long)c0 * lda + r;
         int c = c0;
@@ -43,12 +43,16 @@ gemv_n_partial(int m, int n, int chunk, const double *__restrict__ A, long long 
             const double2 a3 = __ldg((const double2 *)(ap + 3 * lda));
             const double x0 = __ldg(x + (long long)c * incx), x1 = __ldg(x + (long long)(c + 1) * incx);
             const double x2 = __ldg(x + (long long)(c + 2) * incx), x3 = __ldg(x + (long long)(c + 3) * incx);
+            // two chains per row: the FP64 pipe is the bound, so its
+            // dependent-latency gaps must be covered within the warp
             s0 = fma(a0.x, x0, s0); s1 = fma(a0.y, x0, s1);
-            s0 = fma(a1.x, x1, s0); s1 = fma(a1.y, x1, s1);
+            t0 = fma(a1.x, x1, t0); t1 = fma(a1.y, x1, t1);
             s0 = fma(a2.x, x2, s0); s1 = fma(a2.y, x2, s1);
-            s0 = fma(a3.x, x3, s0); s1 = fma(a3.y, x3, s1);
+            t0 = fma(a3.x, x3, t0); t1 = fma(a3.y, x3, t1);
             ap += 4 * lda;
         }
+        s0 += t0;
+        s1 += t1;
         for (; c < c1; c++) {
             const double2 a0 = __ldg((const double2 *)(ap));
             const double xv = __ldg(x + (long long)c * incx);
@@ -98,12 +102,24 @@ gemv_t_warp(int m, int n, const double *__restrict__ A, long long lda, const dou
     double s0 = 0.0, s1 = 0.0;
     if (vec) {
         const int m2 = m >> 1;
-        for (int i = lane; i < m2; i += 32) {
+        double s2 = 0.0, s3 = 0.0;
+        int i = lane;
+        for (; i + 32 < m2; i += 64) {
+            const double2 a = __ldg((const double2 *)col + i), b = __ldg((const double2 *)col + i + 32);
+            const double2 xv = __ldg((const double2 *)x + i), xw = __ldg((const double2 *)x + i + 32);
+            s0 = fma(a.x, xv.x, s0);
+            s1 = fma(a.y, xv.y, s1);
+            s2 = fma(b.x, xw.x, s2);
+            s3 = fma(b.y, xw.y, s3);
+        }
+        for (; i < m2; i += 32) {
             const double2 a = __ldg((const double2 *)col + i);
             const double2 xv = __ldg((const double2 *)x + i);
             s0 = fma(a.x, xv.x, s0);
             s1 = fma(a.y, xv.y, s1);
         }
+        s0 += s2;
+        s1 += s3;
         if ((m & 1) && lane == 0) s0 = fma(col[m - 1], x[m - 1], s0);
     } else {
         for (int i = lane; i < m; i += 32) s0 = fma(__ldg(col + i), __ldg(x + (long long)i * incx), s0);
