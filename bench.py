@@ -995,12 +995,27 @@ def cholesky_calls(n, nb, base, lda, info_ptr, ozaki=False):
 
 
 MODES = {
-    # name: (through the serving loop, Ozaki forms of dtrsm/dsyrk/dgemm)
-    "plain": (False, False),         # FP64, plain per-call dispatch
-    "served": (True, False),         # FP64, serving loop
-    "ozaki_plain": (False, True),    # Ozaki, plain per-call dispatch
-    "ozaki": (True, True),           # Ozaki, serving loop
+    # name: (through the serving layer, Ozaki forms of dtrsm/dsyrk/dgemm,
+    # device-side request loop on)
+    "plain": (False, False, False),         # FP64, plain per-call dispatch
+    "served": (True, False, True),          # FP64, serving layer with its device-side loop
+    "served_host": (True, False, False),    # FP64, serving layer on host worker threads only
+    "ozaki_plain": (False, True, False),    # Ozaki, plain per-call dispatch
+    "ozaki": (True, True, True),            # Ozaki, serving layer
 }
+
+
+def make_server(g, slots, loop):
+    """A Server with its device-side request loop on or off (read at creation)."""
+    old = os.environ.get("GBX_SERVE_LOOP")
+    os.environ["GBX_SERVE_LOOP"] = "1" if loop else "0"
+    try:
+        return g.Server(0, slots=slots)
+    finally:
+        if old is None:
+            del os.environ["GBX_SERVE_LOOP"]
+        else:
+            os.environ["GBX_SERVE_LOOP"] = old
 
 
 def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES), chains=True):
@@ -1032,18 +1047,21 @@ def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES), chains=Tr
     info = torch.zeros(nthreads, dtype=torch.int32, device="cuda")
     results = {}
     for mode in modes:
-        use_server, ozaki = MODES[mode]
+        use_server, ozaki, loop = MODES[mode]
         info.zero_()
         # the caller threads are native (gbx_diag_cholesky_trace): C++
         # threads calling the library as a C or Fortran application would,
         # without interpreter time or lock contention on every call
-        server = g.Server(0, slots=nthreads) if use_server else None
+        server = make_server(g, nthreads, loop) if use_server else None
         work = [o.clone() for o in origs]
         torch.cuda.synchronize()
         r = g.cholesky_trace(server, 0, sizes, nbs, [w.data_ptr() for w in work], info.data_ptr(), ozaki)
         wall = r["wall_s"]
         by_kind = {k: (c, r["kind_sum_us"][k]) for k, c in enumerate(r["kind_calls"]) if c}
         srv_stats = server.stats() if server else None
+        if server:
+            on, lcalls, llaunch = server.loop_stats()
+            srv_stats.update(loop_enabled=on, loop_calls=lcalls, loop_launches=llaunch)
         if server:
             server.close()
         # residual on sampled entries: (L L^T)_ij through ddot on rows of L
@@ -1102,6 +1120,7 @@ def serving_ratios(results, fp64_peak_tflops=None):
     def ratio(a, b):
         return results[a]["calls_per_s"] / results[b]["calls_per_s"] if a in results and b in results else None
     out = {"served_vs_plain_fp64": ratio("served", "plain"),
+           "served_loop_vs_host_workers_fp64": ratio("served", "served_host"),
            "served_vs_plain_ozaki": ratio("ozaki", "ozaki_plain"),
            "ozaki_plain_vs_fp64_plain": ratio("ozaki_plain", "plain"),
            "ozaki_served_vs_fp64_plain": ratio("ozaki", "plain")}
@@ -1177,7 +1196,7 @@ def run_serving_open_loop(g, closed, njobs=48, nmax=4096, workers=16, seed=11):
     ncalls = [len(cholesky_calls(n, nb, 0, n, 0)) for n, nb in zip(sizes, nbs)]
     out = {}
     for mode in ("plain", "served", "ozaki_plain", "ozaki"):
-        use_server, ozaki = MODES[mode]
+        use_server, ozaki, loop = MODES[mode]
         cap = closed[mode]["calls_per_s"] / (sum(ncalls) / njobs)   # jobs/s at closed-loop throughput
         rows = []
         for frac in (0.25, 0.5, 0.75, 1.0):
@@ -1186,7 +1205,7 @@ def run_serving_open_loop(g, closed, njobs=48, nmax=4096, workers=16, seed=11):
             work = [o.clone() for o in origs]
             info.zero_()
             torch.cuda.synchronize()
-            server = g.Server(0, slots=workers) if use_server else None
+            server = make_server(g, workers, loop) if use_server else None
             lat, job_lat, errs = [], [0.0] * njobs, []
             lock = threading.Lock()
             nxt = [0]

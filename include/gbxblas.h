@@ -317,11 +317,15 @@ gbx_status gbx_ops_run(gbx_ctx *ctx, const gbx_op *ops, int count);
 /* ---- serving loop (no reference counterpart: the reference serves one call
  * at a time on one cuBLAS handle, runtime-blas.c:14-23) -------------------
  * Continuous batching of calls from many host threads on device-resident
- * operands: a dispatcher thread takes everything queued, groups the small
- * DGEMM (m, n <= 512, k <= 4096) and DTRSM (order <= 256) requests into one
- * grouped kernel and runs the others with the regular routines, each batch
- * on the stream of a free slot, so new requests overlap with work already on
- * the GPU.  Routing depends only on the operation, so results are identical
+ * operands.  gbx_server_call hands FP64 DGEMM, DSYRK and DTRSM (order <= 256)
+ * requests to a device-side request loop: a resident kernel that takes them
+ * from a ring in pinned host memory and shares the SMs among them tile by
+ * tile, with no launch or synchronisation per call.  Other requests (and
+ * gbx_server_submit) go to worker threads that group the small DGEMM
+ * (m, n <= 512, k <= 4096) and DTRSM (order <= 256) requests queued at that
+ * moment into one grouped kernel and run the others with the regular
+ * routines, each batch on the stream of a free slot, so new requests overlap
+ * with work already on the GPU.  Routing depends only on the operation, so results are identical
  * served alone or in a mix.  gbx_server_admit / gbx_server_release reserve
  * staging memory against a budget (mem_budget, or 80% of the HBM free at
  * creation when 0) and block while it is exhausted. */
@@ -335,6 +339,10 @@ gbx_status gbx_server_release(gbx_server *srv, size_t bytes);
 gbx_status gbx_server_stats(gbx_server *srv, uint64_t *completed, uint64_t *batches,
                             uint64_t *grouped_calls, double *p50_us, double *p99_us,
                             uint64_t *admission_waits);
+/* The device-side request loop behind gbx_server_call: whether the server
+ * has one (GBX_SERVE_LOOP=0 at creation turns it off), the calls it ran and
+ * how often its resident kernel was (re)started. */
+gbx_status gbx_server_loop_stats(gbx_server *srv, int *enabled, uint64_t *calls, uint64_t *launches);
 gbx_status gbx_server_reset_stats(gbx_server *srv);
 gbx_status gbx_server_destroy(gbx_server *srv);
 

@@ -164,6 +164,7 @@ def _declare(L):
                                    C.POINTER(C.c_uint64), C.POINTER(_D), C.POINTER(_D),
                                    C.POINTER(C.c_uint64)]
     L.gbx_server_reset_stats.argtypes = [_P]
+    L.gbx_server_loop_stats.argtypes = [_P, C.POINTER(_I), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     L.gbx_server_destroy.argtypes = [_P]
     L.gbx_ctx_enable_timing.argtypes = [_P, _I]
     L.gbx_ctx_kernel_time.argtypes = [_P, _I, C.POINTER(_D), C.POINTER(C.c_uint64)]
@@ -256,6 +257,12 @@ class Server:
                                 C.byref(p99), C.byref(w))
         return dict(completed=c.value, batches=b.value, grouped_calls=g.value, p50_us=p50.value,
                     p99_us=p99.value, admission_waits=w.value)
+
+    def loop_stats(self):
+        """(enabled, calls run on the device-side request loop, kernel launches)."""
+        e, c, l = C.c_int(), C.c_uint64(), C.c_uint64()
+        self.L.gbx_server_loop_stats(self.h, C.byref(e), C.byref(c), C.byref(l))
+        return bool(e.value), c.value, l.value
 
     def reset_stats(self):
         self.L.gbx_server_reset_stats(self.h)

@@ -137,6 +137,18 @@ void *gbx_tracker_forward(const char *sym) __attribute__((weak));
         }                                                                       \
     } while (0)
 
+/* The serving layer's device-side request loop (serve_loop.cu): a resident
+ * kernel fed through a ring in pinned host memory.  gbx_loop_accepts tells
+ * whether an operation can run there (FP64 GEMM, SYRK, TRSM of order <= 256
+ * with work to do); gbx_loop_call submits it from the calling thread and
+ * waits for its completion word. */
+typedef struct gbx_loop gbx_loop;
+gbx_status gbx_loop_create(int device, int ctas, gbx_loop **out);
+int gbx_loop_accepts(const gbx_op *op);
+gbx_status gbx_loop_call(gbx_loop *l, const gbx_op *op);
+uint64_t gbx_loop_launches(const gbx_loop *l);
+gbx_status gbx_loop_destroy(gbx_loop *l);
+
 /* Fortran-layer helpers (f77.c): the calling thread's context (counting
  * the call; reports when no context can be made) and the failure report
  * (prints, and aborts under errors=abort). */

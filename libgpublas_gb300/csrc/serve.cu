@@ -19,6 +19,14 @@
 // Critical-path requests (DPOTRF of a diagonal block, DTRSM of a panel) run
 // on a high-priority stream of their slot.
 //
+// FP64 DGEMM, DSYRK and DTRSM requests (triangle order <= 256) made through
+// gbx_server_call run on the device-side request loop (serve_loop.cu): a
+// resident kernel fed through a ring in pinned host memory, so such a call
+// costs no launch, stream synchronisation or worker-thread hand-off.  The
+// loop is started on the first such call and leaves the GPU after 20 ms
+// without work; GBX_SERVE_LOOP=0 at server creation keeps every request on
+// the slot streams.
+//
 // Admission by memory: callers that stage host operands reserve their bytes
 // with gbx_server_admit (blocks while the reserved total would exceed the
 // budget: a fraction of the free HBM when the server started, or an explicit
@@ -27,6 +35,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -81,6 +90,9 @@ struct gbx_server {
     // memory admission
     size_t budget = 0, reserved = 0;
     uint64_t admission_waits = 0;
+    // device-side request loop (null when disabled)
+    gbx_loop *loop = nullptr;
+    std::atomic<uint64_t> loop_calls{0};
 };
 
 namespace {
@@ -250,6 +262,12 @@ extern "C" gbx_status gbx_server_create(int device, int nslots, size_t mem_budge
     cudaMemGetInfo(&free_b, &total_b);
     const size_t auto_budget = free_b / 10 * 8;   // 80% of what is free now
     s->budget = mem_budget ? std::min(mem_budget, auto_budget) : auto_budget;
+    const char *lp = getenv("GBX_SERVE_LOOP");
+    if (!(lp && atoi(lp) == 0)) {
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        if (gbx_loop_create(device, sms, &s->loop) != GBX_OK) s->loop = nullptr;   // the slot streams serve alone
+    }
     for (auto &sl : s->slots) s->workers.emplace_back(worker_loop, s, &sl);
     *out = s;
     return GBX_OK;
@@ -307,6 +325,18 @@ extern "C" gbx_status gbx_server_wait(gbx_server *s, uint64_t ticket, double *la
 extern "C" gbx_status gbx_server_call(gbx_server *s, const gbx_op *op, double *latency_us)
 {
     if (!s || !op) return GBX_ERR_ARG;
+    if (s->loop && gbx_loop_accepts(op)) {
+        const auto t0 = clk::now();
+        const gbx_status st = gbx_loop_call(s->loop, op);
+        const auto t1 = clk::now();
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            record(s, t0, t1);
+        }
+        s->loop_calls++;
+        if (latency_us) *latency_us = std::chrono::duration<double, std::micro>(t1 - t0).count();
+        return st;
+    }
     if (!is_small(*op)) {
         Slot *sl = nullptr;
         const auto t0 = clk::now();
@@ -393,6 +423,15 @@ extern "C" gbx_status gbx_server_stats(gbx_server *s, uint64_t *completed, uint6
     return GBX_OK;
 }
 
+extern "C" gbx_status gbx_server_loop_stats(gbx_server *s, int *enabled, uint64_t *calls, uint64_t *launches)
+{
+    if (!s) return GBX_ERR_ARG;
+    if (enabled) *enabled = s->loop != nullptr;
+    if (calls) *calls = s->loop_calls.load();
+    if (launches) *launches = gbx_loop_launches(s->loop);
+    return GBX_OK;
+}
+
 extern "C" gbx_status gbx_server_reset_stats(gbx_server *s)
 {
     if (!s) return GBX_ERR_ARG;
@@ -415,6 +454,7 @@ extern "C" gbx_status gbx_server_destroy(gbx_server *s)
     s->cv_done.notify_all();
     for (auto &w : s->workers)
         if (w.joinable()) w.join();
+    if (s->loop) gbx_loop_destroy(s->loop);
     for (auto *r : s->finished) delete r;
     for (auto &sl : s->slots) {
         if (sl.ctx) gbx_ctx_destroy(sl.ctx);

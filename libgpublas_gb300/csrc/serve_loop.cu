@@ -1,0 +1,430 @@
+// serve_loop.cu — the device-side request loop of the serving layer.
+//
+// A persistent kernel executes the FP64 Level-3 requests (DGEMM, DSYRK, and
+// DTRSM with a triangle of order <= 256) that host threads hand it through a
+// ring in pinned, mapped host memory.  No reference counterpart: the
+// reference runs one cuBLAS call at a time on one handle and the legacy
+// stream (runtime-blas.c:14-23), and every call pays a launch and a
+// synchronisation.  Here a caller thread converts its request, writes it
+// into a ring slot and publishes it; a CTA of the resident kernel claims
+// the ticket, copies the request to device memory and cuts it into work
+// items (64 x 64 tiles of C on the SIMT GEMM core, or chunks of 16
+// right-hand sides of a triangular solve) appended to one of two device
+// queues; every CTA takes items from the critical-path queue (the panel
+// solves) before the other; the CTA that finishes a request's last item
+// writes its completion word, which the caller polls.  Requests from any
+// number of threads and of any size share the SMs tile by tile: no launch,
+// no stream synchronisation and no host thread hand-off per call.
+//
+// Bounded waits: a CTA waits at most LOOP_WAIT_NS for a queue item its
+// producer has reserved, and leaves the loop after LOOP_IDLE_NS without
+// work; the host relaunches the kernel when a request finds it gone.  A wait
+// that gives up marks the requests it touches as failed (GBX_ERR_TIMEOUT)
+// and the kernel exits; nothing is left in flight.
+//
+// Results: each output element is one FMA chain over K in increasing order
+// on the same GEMM core as the stream path, so a request served here gives
+// the same bits as the same call on its own; the triangular solves use the
+// substitution of the grouped kernel.
+#include "gbx_internal.h"
+#include "gemm_simt.cuh"
+#include "grouped_dev.cuh"
+#include "tc_ptx.cuh"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <cstring>
+#include <thread>
+
+using namespace gbx_gemm;
+using gbx_grouped::DevOp;
+using gbx_grouped::trsm_item;
+
+namespace {
+
+constexpr int LOOP_RING = 1024;                 // requests in flight
+constexpr int LOOP_QCAP = 1 << 15;              // items per queue
+constexpr int LOOP_THREADS = GEMM_THREADS;      // 256
+constexpr int LOOP_TM = 4;                      // 64 x 64 tiles of C
+constexpr int LOOP_TILE = 16 * LOOP_TM;
+constexpr int LOOP_TRSM_SYS = 16;
+constexpr int LOOP_TRSM_ORDER = 256;
+constexpr size_t LOOP_DSMEM = sizeof(double) * LOOP_TRSM_ORDER * LOOP_TRSM_SYS;   // 32 KB
+constexpr int LOOP_POLLERS = 8;                 // CTAs that watch the ring for new requests
+constexpr unsigned long long LOOP_IDLE_NS = 20000000ull;    // 20 ms without work: the CTA leaves
+constexpr unsigned long long LOOP_WAIT_NS = 1000000000ull;  // 1 s for a reserved queue item
+
+enum { LOOP_GEMM = 1, LOOP_TRSM = 2 };
+
+struct LoopReq {
+    int kind;         // LOOP_GEMM (GEMM core: DGEMM or DSYRK) or LOOP_TRSM
+    int nitems;       // tiles of C, or chunks of LOOP_TRSM_SYS systems
+    int critical;     // items go to the critical-path queue
+    int pad;
+    GemmArgs<double> g;
+    DevOp t;
+};
+
+// One ring slot in pinned, mapped host memory.
+struct RingSlot {
+    LoopReq req;
+    unsigned long long pub;    // ticket + 1 once req is complete (host)
+    unsigned long long done;   // ticket + 1 once the result is in place (device)
+    int status;                // 0, or a TC_* code of a wait that gave up
+    int pad;
+};
+
+// Host-written control words (pinned, mapped).
+struct LoopCtl {
+    int stop;
+};
+
+struct LoopQueue {
+    unsigned long long head, tail;
+    unsigned long long seq[LOOP_QCAP];     // item i is written when seq[i % CAP] == i + 1
+    unsigned long long ticket[LOOP_QCAP];
+    int item[LOOP_QCAP];
+};
+
+// Device memory of the loop.
+struct LoopState {
+    unsigned long long claim;              // next ticket to expand
+    int err;                               // first wait that gave up (0: none)
+    int pad;
+    int left[LOOP_RING];                   // items not yet finished, per ring slot
+    LoopReq req[LOOP_RING];                // device copy of each request in flight
+    LoopQueue q[2];                        // [0] critical path, [1] the rest
+};
+
+__device__ __forceinline__ unsigned long long vload(const unsigned long long *p)
+{
+    return *(const volatile unsigned long long *)p;
+}
+
+// Thread 0: take the next item of queue qi, if any.  Returns 1 with the
+// ticket and item, 0 when the queue is empty, -1 when a reserved item never
+// appeared (a producer that died: the loop stops).
+__device__ int take_item(LoopState *st, int qi, unsigned long long &ticket, int &item)
+{
+    LoopQueue &q = st->q[qi];
+    const unsigned long long h = vload(&q.head);
+    if (h >= vload(&q.tail)) return 0;
+    if (atomicCAS(&q.head, h, h + 1) != h) return 0;   // another CTA took it; look again next round
+    const unsigned long long t0 = gbx_tc::globaltimer();
+    while (vload(&q.seq[h % LOOP_QCAP]) != h + 1)
+        if (gbx_tc::globaltimer() - t0 > LOOP_WAIT_NS) return -1;
+    __threadfence();
+    ticket = *(volatile unsigned long long *)&q.ticket[h % LOOP_QCAP];
+    item = *(volatile int *)&q.item[h % LOOP_QCAP];
+    return 1;
+}
+
+__device__ void finish(RingSlot *ring, unsigned long long ticket, int status)
+{
+    RingSlot &rs = ring[ticket % LOOP_RING];
+    *(volatile int *)&rs.status = status;
+    __threadfence_system();
+    *(volatile unsigned long long *)&rs.done = ticket + 1;
+}
+
+__global__ void __launch_bounds__(LOOP_THREADS, 1)
+serve_loop_kernel(LoopState *st, RingSlot *ring, const LoopCtl *ctl)
+{
+    extern __shared__ __align__(16) double tsm[];   // triangular solves: LOOP_TRSM_ORDER x LOOP_TRSM_SYS
+    __shared__ unsigned long long s_ticket, s_base;
+    __shared__ int s_action, s_item, s_n, s_qi;
+    unsigned long long idle0 = gbx_tc::globaltimer();
+    while (true) {
+        if (threadIdx.x == 0) {
+            s_action = 0;
+            unsigned long long tk = 0;
+            int it = 0, r = 0;
+            // 1. an item, critical-path queue first
+            for (int qi = 0; qi < 2 && r == 0; qi++) r = take_item(st, qi, tk, it);
+            if (r == 1) {
+                s_action = 1;
+                s_ticket = tk;
+                s_item = it;
+            } else if (r < 0) {
+                atomicCAS(&st->err, 0, gbx_tc::TC_TIMEOUT_FULL);
+                s_action = 3;
+            } else {
+                // 2. a published request to expand (the first LOOP_POLLERS CTAs
+                // watch the ring in host memory; the others only take items)
+                const unsigned long long c = vload(&st->claim);
+                RingSlot &rs = ring[c % LOOP_RING];
+                if (blockIdx.x < LOOP_POLLERS && vload(&rs.pub) == c + 1 && atomicCAS(&st->claim, c, c + 1) == c) {
+                    __threadfence_system();
+                    LoopReq &dr = st->req[c % LOOP_RING];
+                    const int *src = (const int *)&rs.req;
+                    int *dst = (int *)&dr;
+                    for (int w = 0; w < (int)(sizeof(LoopReq) / sizeof(int)); w++) dst[w] = ((const volatile int *)src)[w];
+                    const int n = dr.nitems, qi = dr.critical ? 0 : 1;
+                    if (n <= 0) {
+                        finish(ring, c, 0);
+                    } else {
+                        st->left[c % LOOP_RING] = n;
+                        // reserve n items (the queue holds LOOP_QCAP; requests are
+                        // cut so that one never needs more)
+                        LoopQueue &q = st->q[qi];
+                        const unsigned long long t0 = gbx_tc::globaltimer();
+                        unsigned long long base = 0;
+                        bool ok = false;
+                        while (gbx_tc::globaltimer() - t0 <= LOOP_WAIT_NS) {
+                            const unsigned long long t = vload(&q.tail);
+                            if (t + n - vload(&q.head) > LOOP_QCAP) continue;
+                            if (atomicCAS(&q.tail, t, t + n) == t) {
+                                base = t;
+                                ok = true;
+                                break;
+                            }
+                        }
+                        if (!ok) {
+                            atomicCAS(&st->err, 0, gbx_tc::TC_TIMEOUT_EMPTY);
+                            finish(ring, c, gbx_tc::TC_TIMEOUT_EMPTY);
+                            s_action = 3;
+                        } else {
+                            // the request copy and its item count are visible
+                            // device-wide before any of its items is published
+                            __threadfence();
+                            s_action = 2;
+                            s_ticket = c;
+                            s_base = base;
+                            s_n = n;
+                            s_qi = qi;
+                        }
+                    }
+                    if (s_action != 3) idle0 = gbx_tc::globaltimer();
+                } else if (*(const volatile int *)&ctl->stop || vload((const unsigned long long *)&st->err) != 0 ||
+                           gbx_tc::globaltimer() - idle0 > LOOP_IDLE_NS) {
+                    s_action = 3;
+                }
+            }
+            if (s_action == 1) idle0 = gbx_tc::globaltimer();
+        }
+        __syncthreads();
+        const int action = s_action;
+        if (action == 3) break;
+        if (action == 1) {
+            const unsigned long long tk = s_ticket;
+            const LoopReq &r = st->req[tk % LOOP_RING];
+            if (r.kind == LOOP_GEMM) {
+                const GemmArgs<double> g = r.g;
+                gemm_simt_tile<double, LOOP_TM, LOOP_TM, 8>(g, s_item);
+            } else {
+                const DevOp t = r.t;
+                trsm_item<LOOP_TRSM_SYS, LOOP_THREADS>(t, s_item * LOOP_TRSM_SYS, tsm);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();
+                if (atomicSub(&st->left[tk % LOOP_RING], 1) == 1) finish(ring, tk, 0);
+            }
+        } else if (action == 2) {
+            // the whole CTA writes the new request's items
+            LoopQueue &q = st->q[s_qi];
+            const unsigned long long base = s_base, tk = s_ticket;
+            for (int i = threadIdx.x; i < s_n; i += LOOP_THREADS) {
+                const unsigned long long idx = base + i;
+                q.ticket[idx % LOOP_QCAP] = tk;
+                q.item[idx % LOOP_QCAP] = i;
+                __threadfence();
+                *(volatile unsigned long long *)&q.seq[idx % LOOP_QCAP] = idx + 1;
+            }
+        } else {
+            __nanosleep(500);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- host side --------------------------------------------------------------
+// Converts an operation to its loop form; 0 when the loop does not take it.
+int to_loop_req(const gbx_op &o, LoopReq &r)
+{
+    r = LoopReq{};
+    if (o.kind == GBX_OP_GEMM) {
+        if (gbx_check_gemm_args(o.transa, o.transb, o.m, o.n, o.k, o.lda, o.ldb, o.ldc)) return 0;
+        if (o.m <= 0 || o.n <= 0 || o.k <= 0 || o.alpha == 0.0) return 0;   // quick paths stay on the streams
+        GemmArgs<double> &g = r.g;
+        g.m = o.m; g.n = o.n; g.k = o.k;
+        g.A = o.A; g.lda = o.lda; g.ta = !gbx_lsame(o.transa, 'N');
+        g.B = o.B; g.ldb = o.ldb; g.tb = !gbx_lsame(o.transb, 'N');
+        g.alpha = o.alpha; g.beta = o.beta;
+        g.C = o.C; g.ldc = o.ldc;
+        g.c_part = C_FULL;
+        g.tiles_m = (o.m + LOOP_TILE - 1) / LOOP_TILE;
+        g.tiles_n = (o.n + LOOP_TILE - 1) / LOOP_TILE;
+        r.kind = LOOP_GEMM;
+        r.nitems = g.tiles_m * g.tiles_n;
+        return r.nitems <= LOOP_QCAP;
+    }
+    if (o.kind == GBX_OP_SYRK) {
+        if (gbx_check_syrk_args(o.uplo, o.transa, o.n, o.k, o.lda, o.ldc)) return 0;
+        if (o.n <= 0 || o.k <= 0 || o.alpha == 0.0) return 0;
+        const bool notr = gbx_lsame(o.transa, 'N');
+        GemmArgs<double> &g = r.g;
+        g.m = o.n; g.n = o.n; g.k = o.k;
+        g.A = o.A; g.lda = o.lda; g.ta = !notr;
+        g.B = o.A; g.ldb = o.lda; g.tb = notr;
+        g.alpha = o.alpha; g.beta = o.beta;
+        g.C = o.C; g.ldc = o.ldc;
+        g.c_part = gbx_lsame(o.uplo, 'U') ? C_UPPER : C_LOWER;
+        g.tiles_m = g.tiles_n = (o.n + LOOP_TILE - 1) / LOOP_TILE;
+        r.kind = LOOP_GEMM;
+        r.nitems = g.tiles_m * (g.tiles_m + 1) / 2;
+        return r.nitems <= LOOP_QCAP;
+    }
+    if (o.kind == GBX_OP_TRSM) {
+        if (gbx_check_trxm_args(o.side, o.uplo, o.transa, o.diag, o.m, o.n, o.lda, o.ldc)) return 0;
+        if (o.m <= 0 || o.n <= 0 || o.alpha == 0.0) return 0;
+        DevOp &d = r.t;
+        d.kind = GBX_OP_TRSM;
+        d.m = o.m; d.n = o.n;
+        d.alpha = o.alpha;
+        d.A = o.A; d.lda = o.lda; d.C = o.C; d.ldc = o.ldc;
+        d.left = gbx_lsame(o.side, 'L');
+        const int order = d.left ? o.m : o.n;
+        if (order > LOOP_TRSM_ORDER) return 0;
+        d.ta = !gbx_lsame(o.transa, 'N');
+        const bool op_lower = (gbx_op_tri(o.uplo, o.transa, o.diag) & 1) != 0;
+        d.lower = d.left ? op_lower : !op_lower;
+        d.unit = gbx_lsame(o.diag, 'U');
+        const int nsys = d.left ? o.n : o.m;
+        r.kind = LOOP_TRSM;
+        r.nitems = (nsys + LOOP_TRSM_SYS - 1) / LOOP_TRSM_SYS;
+        r.critical = 1;
+        return r.nitems <= LOOP_QCAP;
+    }
+    return 0;
+}
+
+}  // namespace
+
+struct gbx_loop {
+    int device = 0, ctas = 0;
+    RingSlot *ring_h = nullptr, *ring_d = nullptr;
+    LoopCtl *ctl_h = nullptr, *ctl_d = nullptr;
+    LoopState *st = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ended = nullptr;
+    std::atomic<unsigned long long> head{0};
+    std::mutex launch_mu;
+    bool launched = false;
+    std::atomic<unsigned long long> launches{0};
+};
+
+namespace {
+
+// (Re)launches the resident kernel when it is not running.
+gbx_status loop_ensure_running(gbx_loop *l)
+{
+    std::lock_guard<std::mutex> lk(l->launch_mu);
+    if (l->launched) {
+        const cudaError_t q = cudaEventQuery(l->ended);
+        if (q == cudaErrorNotReady) return GBX_OK;
+        if (q != cudaSuccess) return GBX_ERR_CUDA;
+    }
+    int err = 0;
+    if (cudaMemcpy(&err, &l->st->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return GBX_ERR_CUDA;
+    if (err) return GBX_ERR_TIMEOUT;   // the loop stopped on a wait that gave up
+    serve_loop_kernel<<<l->ctas, LOOP_THREADS, LOOP_DSMEM, l->stream>>>(l->st, l->ring_d, l->ctl_d);
+    if (cudaGetLastError() != cudaSuccess || cudaEventRecord(l->ended, l->stream) != cudaSuccess)
+        return GBX_ERR_CUDA;
+    l->launched = true;
+    l->launches++;
+    return GBX_OK;
+}
+
+}  // namespace
+
+extern "C" int gbx_loop_accepts(const gbx_op *op)
+{
+    LoopReq r;
+    return op && to_loop_req(*op, r);
+}
+
+extern "C" gbx_status gbx_loop_create(int device, int ctas, gbx_loop **out)
+{
+    if (!out || ctas < 1) return GBX_ERR_ARG;
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return GBX_ERR_CUDA;
+    gbx_loop *l = new gbx_loop();
+    l->device = device;
+    l->ctas = ctas;
+    bool ok = cudaHostAlloc((void **)&l->ring_h, sizeof(RingSlot) * LOOP_RING, cudaHostAllocMapped) == cudaSuccess &&
+              cudaHostGetDevicePointer((void **)&l->ring_d, l->ring_h, 0) == cudaSuccess &&
+              cudaHostAlloc((void **)&l->ctl_h, sizeof(LoopCtl), cudaHostAllocMapped) == cudaSuccess &&
+              cudaHostGetDevicePointer((void **)&l->ctl_d, l->ctl_h, 0) == cudaSuccess &&
+              cudaMalloc((void **)&l->st, sizeof(LoopState)) == cudaSuccess &&
+              cudaMemset(l->st, 0, sizeof(LoopState)) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&l->ended, cudaEventDisableTiming) == cudaSuccess &&
+              cudaFuncSetAttribute(serve_loop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)LOOP_DSMEM) == cudaSuccess &&
+              cudaDeviceSynchronize() == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        gbx_loop_destroy(l);
+        return GBX_ERR_ALLOC;
+    }
+    memset(l->ring_h, 0, sizeof(RingSlot) * LOOP_RING);
+    l->ctl_h->stop = 0;
+    *out = l;
+    return GBX_OK;
+}
+
+// Submits one operation and waits for it: the caller's thread writes the
+// request into its ring slot and polls the completion word.
+extern "C" gbx_status gbx_loop_call(gbx_loop *l, const gbx_op *op)
+{
+    LoopReq r;
+    if (!l || !op || !to_loop_req(*op, r)) return GBX_ERR_ARG;
+    cudaSetDevice(l->device);
+    const unsigned long long t = l->head.fetch_add(1);
+    RingSlot *rs = &l->ring_h[t % LOOP_RING];
+    volatile unsigned long long *done = &rs->done;
+    // the slot's previous request (t - LOOP_RING) must have completed
+    for (unsigned spins = 0; t >= LOOP_RING && *done != t - LOOP_RING + 1; spins++) {
+        if ((spins & 1023u) == 1023u) {
+            const gbx_status st = loop_ensure_running(l);
+            if (st != GBX_OK) return st;
+            std::this_thread::yield();
+        }
+    }
+    rs->req = r;
+    rs->status = 0;
+    std::atomic_thread_fence(std::memory_order_release);
+    *(volatile unsigned long long *)&rs->pub = t + 1;
+    gbx_status st = loop_ensure_running(l);
+    if (st != GBX_OK) return st;
+    for (unsigned spins = 0; *done != t + 1; spins++) {
+        if ((spins & 4095u) == 4095u) {
+            // the kernel may have left (idle) just before this request was
+            // published; relaunch it then
+            if ((st = loop_ensure_running(l)) != GBX_OK) return st;
+            std::this_thread::yield();
+        }
+    }
+    std::atomic_thread_fence(std::memory_order_acquire);
+    return rs->status ? GBX_ERR_TIMEOUT : GBX_OK;
+}
+
+extern "C" uint64_t gbx_loop_launches(const gbx_loop *l) { return l ? l->launches.load() : 0; }
+
+extern "C" gbx_status gbx_loop_destroy(gbx_loop *l)
+{
+    if (!l) return GBX_OK;
+    if (l->ctl_h) *(volatile int *)&l->ctl_h->stop = 1;
+    if (l->stream) cudaStreamSynchronize(l->stream);
+    if (l->ended) cudaEventDestroy(l->ended);
+    if (l->stream) cudaStreamDestroy(l->stream);
+    if (l->st) cudaFree(l->st);
+    if (l->ring_h) cudaFreeHost(l->ring_h);
+    if (l->ctl_h) cudaFreeHost(l->ctl_h);
+    delete l;
+    return GBX_OK;
+}
