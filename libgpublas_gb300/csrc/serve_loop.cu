@@ -199,7 +199,9 @@ serve_loop_kernel(LoopState *st, RingSlot *ring, const LoopCtl *ctl)
                     }
                     if (s_action != 3) idle0 = gbx_tc::globaltimer();
                 } else if (*(const volatile int *)&ctl->stop || vload((const unsigned long long *)&st->err) != 0 ||
-                           gbx_tc::globaltimer() - idle0 > LOOP_IDLE_NS) {
+                           gbx_tc::globaltimer() - idle0 > (blockIdx.x < LOOP_POLLERS ? 4 : 1) * LOOP_IDLE_NS) {
+                    // the ring watchers stay longest, so that requests published
+                    // while long tiles still run elsewhere get picked up
                     s_action = 3;
                 }
             }
