@@ -53,7 +53,7 @@ CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.a
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 WORKLOADS = ("dgemm", "ozaki", "daxpy", "ddot", "dnrm2", "idamax", "dgemv", "dtrsm", "dsyrk",
-             "batched", "serving", "ozaki_sweep")
+             "batched", "serving", "ozaki_sweep", "pipes")
 
 
 def parse_args():
@@ -1351,6 +1351,38 @@ def run_ozaki_sweep(args):
     dev.close()
 
 
+# --------------------------------------------------------------------------
+# arithmetic pipes of the GPU (the measurements behind the kernel choices):
+# SIMT DFMA and the legacy mma.sync paths, dependent-chain latencies, and
+# the issue cost of tcgen05.mma for the Ozaki tile widths
+# --------------------------------------------------------------------------
+def run_pipes(args):
+    import libgpublas_gb300 as g
+    from libgpublas_gb300 import build
+    build.build_library()
+    dev = g.Device(0)
+    with ClockSampler(0) as clk:
+        rates = dev.pipe_rates()
+        sms = 152
+        try:
+            import torch
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+        except Exception:
+            pass
+        issue = []
+        for n in (16, 32, 64, 128, 256):
+            for grid in (1, sms):
+                i_cyc, d_cyc = dev.mma_issue(n, 1024, grid)
+                issue.append({"n": n, "count": 1024, "ctas": grid, "issue_cycles": i_cyc, "done_cycles": d_cyc})
+    line = {"metric": "dfma_tflops", "value": rates["dfma_tflops"], "unit": "TFLOP/s", "n_gpus": 1,
+            "steps": 3, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "pipe_throughput_and_tcgen05_issue"},
+            "pipes": rates, "tcgen05_mma_issue": issue, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    dev.close()
+
+
 def ctypes_ref(op):
     import ctypes
     return ctypes.byref(op)
@@ -1365,6 +1397,9 @@ def main():
     if args.workload == "serving":
         return run_serving(args) if args.impl == "ours" else print(json.dumps(
             {"impl": "reference", "unavailable": "the reference has no serving loop"}))
+    if args.workload == "pipes":
+        return run_pipes(args) if args.impl == "ours" else print(json.dumps(
+            {"impl": "reference", "unavailable": "a measurement of the GPU, not of a BLAS path"}))
     if args.workload == "ozaki_sweep":
         return run_ozaki_sweep(args) if args.impl == "ours" else print(json.dumps(
             {"impl": "reference", "unavailable": "the reference has no Ozaki path"}))

@@ -317,8 +317,9 @@ gbx_status gbx_ops_run(gbx_ctx *ctx, const gbx_op *ops, int count);
 /* ---- serving loop (no reference counterpart: the reference serves one call
  * at a time on one cuBLAS handle, runtime-blas.c:14-23) -------------------
  * Continuous batching of calls from many host threads on device-resident
- * operands.  gbx_server_call hands FP64 DGEMM, DSYRK and DTRSM (order <= 256)
- * requests to a device-side request loop: a resident kernel that takes them
+ * operands.  gbx_server_call hands FP64 DGEMM, DSYRK and DTRSM
+ * requests (DTRSM: order <= 256, at most 256 right-hand sides) to a
+ * device-side request loop: a resident kernel that takes them
  * from a ring in pinned host memory and shares the SMs among them tile by
  * tile, with no launch or synchronisation per call.  Other requests (and
  * gbx_server_submit) go to worker threads that group the small DGEMM

@@ -18,6 +18,29 @@ extern "C" {
  * loop on the context's stream; the denominator of the FP64 roofline. */
 gbx_status gbx_diag_fp64_peak(gbx_ctx *ctx, double *tflops);
 
+/* Throughput of the arithmetic pipes (best over 1-8 CTAs of 256 threads per
+ * SM, best of three launches on the context's stream): SIMT DFMA, FP64
+ * mma.sync m8n8k4, s8 mma.sync m16n8k32 (TOP/s), bf16 m16n8k16 and E4M3
+ * m16n8k32 mma.sync; the same kernel's warps on DFMA only, on the FP64
+ * mma.sync only, and half and half (TFLOP/s); and dependent-chain latency
+ * in clock64 cycles per operation for 1, 32 and 256 threads of one CTA:
+ * FP64 FMA, FP32 FMA, FP64 multiply, shared load + FP64 FMA, shuffle + FP64
+ * multiply. */
+typedef struct {
+    double dfma_tflops, dmma_tflops, imma_tops, hmma_bf16_tflops, qmma_e4m3_tflops;
+    double mix_tflops[3];
+    double latency_cycles[3][5];
+} gbx_pipe_rates;
+gbx_status gbx_diag_pipe_rates(gbx_ctx *ctx, gbx_pipe_rates *rates);
+
+/* Issue and completion cost of tcgen05.mma kind::f8f6f4 (E4M3 x E4M3 ->
+ * FP32, M = 128, K = 32, both operands in shared memory) for a given N: one
+ * thread per CTA (grid CTAs, one per SM) issues count MMAs back to back into
+ * accumulators that rotate every four, commits and waits (bounded, 2 s).
+ * Best of three launches of the slowest CTA, in SM cycles per MMA. */
+gbx_status gbx_diag_mma_issue(gbx_ctx *ctx, int n, int count, int grid, double *issue_cycles,
+                              double *done_cycles);
+
 /* Failure-path check of the bounded device waits: launches, on the context's
  * stream, one CTA that waits on an mbarrier nothing will ever arrive on,
  * through the same bounded wait the tensor-core kernels use (2 s limit).  The

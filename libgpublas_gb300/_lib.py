@@ -60,6 +60,8 @@ def load_diag():
     d = C.CDLL(DIAG_LIB_PATH)
     d.gbx_diag_fp64_peak.argtypes = [_P, C.POINTER(_D)]
     d.gbx_diag_expire_wait.argtypes = [_P]
+    d.gbx_diag_pipe_rates.argtypes = [_P, _P]
+    d.gbx_diag_mma_issue.argtypes = [_P, _I, _I, _I, C.POINTER(_D), C.POINTER(_D)]
     d.gbx_diag_cholesky_trace.argtypes = [_P, _I, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_P),
                                           C.POINTER(_I), _P, _I, C.POINTER(TraceStats)]
     _diag = d
@@ -527,6 +529,27 @@ class Device:
         t = C.c_double(0.0)
         self._ok(load_diag().gbx_diag_fp64_peak(self.ctx, C.byref(t)), "fp64_peak")
         return t.value
+
+    def pipe_rates(self):
+        """gbx_diag_pipe_rates as a dict (TFLOP/s, TOP/s, cycles)."""
+        class Rates(C.Structure):
+            _fields_ = [("dfma", _D), ("dmma", _D), ("imma", _D), ("hmma_bf16", _D), ("qmma_e4m3", _D),
+                        ("mix", _D * 3), ("lat", (_D * 5) * 3)]
+        r = Rates()
+        self._ok(load_diag().gbx_diag_pipe_rates(self.ctx, C.byref(r)), "pipe_rates")
+        names = ("dfma", "ffma", "dmul", "lds_dfma", "shfl_dmul")
+        return {"dfma_tflops": r.dfma, "dmma_tflops": r.dmma, "imma_s8_tops": r.imma,
+                "hmma_bf16_tflops": r.hmma_bf16, "qmma_e4m3_tflops": r.qmma_e4m3,
+                "mix_dfma_only_tflops": r.mix[0], "mix_dmma_only_tflops": r.mix[1],
+                "mix_half_half_tflops": r.mix[2],
+                "latency_cycles": {str(t): dict(zip(names, list(r.lat[i])))
+                                   for i, t in enumerate((1, 32, 256))}}
+
+    def mma_issue(self, n, count, grid):
+        """(issue, completion) SM cycles per tcgen05.mma of width n."""
+        a, b = C.c_double(), C.c_double()
+        self._ok(load_diag().gbx_diag_mma_issue(self.ctx, n, count, grid, C.byref(a), C.byref(b)), "mma_issue")
+        return a.value, b.value
 
     def expire_wait(self):
         """Launch the diagnostic whose bounded device wait runs out (about

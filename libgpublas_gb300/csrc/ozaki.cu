@@ -1526,7 +1526,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 // N = 32(S - s) columns multiplies A_s by B_0..B_{S-1-s} at once and writes
 // A_s B_t into columns 32(s + t): exactly diagonal s + t's accumulator.  A
 // tcgen05.mma costs the issuing thread about 70 cycles whatever its N up to
-// 128 (N = 256: 128 cycles; diag/utc_probe.cu), so S(S+1)/2 products of
+// 128 (N = 256: 128 cycles; measured by gbx_diag_mma_issue), so S(S+1)/2 products of
 // N = 32 would leave the tensor pipe three quarters idle; concatenated, a
 // 128-wide k block of a tile is sum_s ceil(32(S - s) / 256) * 4 MMAs (48 for
 // S = 10 instead of 220).  The A slices (16 KB each) stream through a ring

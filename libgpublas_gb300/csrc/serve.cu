@@ -19,7 +19,8 @@
 // Critical-path requests (DPOTRF of a diagonal block, DTRSM of a panel) run
 // on a high-priority stream of their slot.
 //
-// FP64 DGEMM, DSYRK and DTRSM requests (triangle order <= 256) made through
+// FP64 DGEMM, DSYRK and DTRSM requests (triangle order <= 256, at most 256
+// right-hand sides) made through
 // gbx_server_call run on the device-side request loop (serve_loop.cu): a
 // resident kernel fed through a ring in pinned host memory, so such a call
 // costs no launch, stream synchronisation or worker-thread hand-off.  The

@@ -1,14 +1,15 @@
 // serve_loop.cu — the device-side request loop of the serving layer.
 //
 // A persistent kernel executes the FP64 Level-3 requests (DGEMM, DSYRK, and
-// DTRSM with a triangle of order <= 256) that host threads hand it through a
+// DTRSM with a triangle of order <= 256 and at most 256 right-hand sides)
+// that host threads hand it through a
 // ring in pinned, mapped host memory.  No reference counterpart: the
 // reference runs one cuBLAS call at a time on one handle and the legacy
 // stream (runtime-blas.c:14-23), and every call pays a launch and a
 // synchronisation.  Here a caller thread converts its request, writes it
 // into a ring slot and publishes it; a CTA of the resident kernel claims
 // the ticket, copies the request to device memory and cuts it into work
-// items (64 x 64 tiles of C on the SIMT GEMM core, or chunks of 16
+// items (32 x 32 tiles of C on the SIMT GEMM core, or chunks of 16
 // right-hand sides of a triangular solve) appended to one of two device
 // queues; every CTA takes items from the critical-path queue (the panel
 // solves) before the other; the CTA that finishes a request's last item
@@ -48,7 +49,11 @@ namespace {
 constexpr int LOOP_RING = 1024;                 // requests in flight
 constexpr int LOOP_QCAP = 1 << 15;              // items per queue
 constexpr int LOOP_THREADS = GEMM_THREADS;      // 256
-constexpr int LOOP_TM = 4;                      // 64 x 64 tiles of C
+constexpr int LOOP_TM = 2;                      // 32 x 32 tiles of C: an SM retires 2 DFMA per clock,
+                                                // so the rank-nb updates of the Cholesky trace need
+                                                // fine tiles to spread over the SMs
+constexpr int LOOP_TRSM_MAX_SYS = 256;          // larger solves (Cholesky panels) stay on the slot
+                                                // streams, where the inverted-block solve uses every SM
 constexpr int LOOP_TILE = 16 * LOOP_TM;
 constexpr int LOOP_TRSM_SYS = 16;
 constexpr int LOOP_TRSM_ORDER = 256;
@@ -296,6 +301,7 @@ int to_loop_req(const gbx_op &o, LoopReq &r)
         d.lower = d.left ? op_lower : !op_lower;
         d.unit = gbx_lsame(o.diag, 'U');
         const int nsys = d.left ? o.n : o.m;
+        if (nsys > LOOP_TRSM_MAX_SYS) return 0;
         r.kind = LOOP_TRSM;
         r.nitems = (nsys + LOOP_TRSM_SYS - 1) / LOOP_TRSM_SYS;
         r.critical = 1;

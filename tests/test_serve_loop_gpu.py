@@ -1,7 +1,7 @@
 """The serving layer's device-side request loop.
 
-FP64 DGEMM, DSYRK and DTRSM (triangle order <= 256) made through
-gbx_server_call run on a resident kernel fed through a ring in pinned host
+FP64 DGEMM, DSYRK and DTRSM (triangle order <= 256, at most 256 right-hand
+sides) made through gbx_server_call run on a resident kernel fed through a ring in pinned host
 memory.  Checked here:
   * results: DGEMM and DSYRK bit-identical to the same call on the stream
     path (the same GEMM core, one FMA chain per element over K in order);
@@ -63,7 +63,7 @@ def ops_for(g, orc, seed):
         else:
             order = int(rng.integers(8, 257))
             side, uplo, ta = rng.choice(["L", "R"]), rng.choice(["L", "U"]), rng.choice(["N", "T"])
-            nrhs = int(rng.integers(1, 400))
+            nrhs = int(rng.integers(1, 257))       # the loop takes solves of <= 256 right-hand sides
             m, n = (order, nrhs) if side == "L" else (nrhs, order)
             a, s = orc.trsm_matrix(order, s)
             b, s = orc.matrix(m, n, s)
