@@ -139,8 +139,9 @@ void *gbx_tracker_forward(const char *sym) __attribute__((weak));
 
 /* The serving layer's device-side request loop (serve_loop.cu): a resident
  * kernel fed through a ring in pinned host memory.  gbx_loop_accepts tells
- * whether an operation can run there (FP64 GEMM, SYRK, TRSM of order <= 256
- * with at most 256 right-hand sides, each with work to do); gbx_loop_call submits it from the calling thread and
+ * whether an operation can run there (FP64 GEMM and SYRK with m, n <= 512
+ * and k <= 4096, TRSM of order <= 256 with at most 256 right-hand sides,
+ * each with work to do); gbx_loop_call submits it from the calling thread and
  * waits for its completion word. */
 typedef struct gbx_loop gbx_loop;
 gbx_status gbx_loop_create(int device, int ctas, gbx_loop **out);

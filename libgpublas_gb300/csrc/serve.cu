@@ -19,8 +19,8 @@
 // Critical-path requests (DPOTRF of a diagonal block, DTRSM of a panel) run
 // on a high-priority stream of their slot.
 //
-// FP64 DGEMM, DSYRK and DTRSM requests (triangle order <= 256, at most 256
-// right-hand sides) made through
+// Small FP64 DGEMM, DSYRK and DTRSM requests (m, n <= 512, k <= 4096;
+// triangle order <= 256, at most 256 right-hand sides) made through
 // gbx_server_call run on the device-side request loop (serve_loop.cu): a
 // resident kernel fed through a ring in pinned host memory, so such a call
 // costs no launch, stream synchronisation or worker-thread hand-off.  The
@@ -265,9 +265,11 @@ extern "C" gbx_status gbx_server_create(int device, int nslots, size_t mem_budge
     s->budget = mem_budget ? std::min(mem_budget, auto_budget) : auto_budget;
     const char *lp = getenv("GBX_SERVE_LOOP");
     if (!(lp && atoi(lp) == 0)) {
+        // a quarter of the SMs: the loop takes the small requests, and the SMs it
+        // leaves free run the large ones and the factorisation steps on the slot streams
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        if (gbx_loop_create(device, sms, &s->loop) != GBX_OK) s->loop = nullptr;   // the slot streams serve alone
+        if (gbx_loop_create(device, std::max(8, sms / 4), &s->loop) != GBX_OK) s->loop = nullptr;
     }
     for (auto &sl : s->slots) s->workers.emplace_back(worker_loop, s, &sl);
     *out = s;

@@ -1,8 +1,8 @@
 // serve_loop.cu — the device-side request loop of the serving layer.
 //
-// A persistent kernel executes the FP64 Level-3 requests (DGEMM, DSYRK, and
-// DTRSM with a triangle of order <= 256 and at most 256 right-hand sides)
-// that host threads hand it through a
+// A persistent kernel executes the small FP64 Level-3 requests (DGEMM and
+// DSYRK with m, n <= 512 and k <= 4096, DTRSM with a triangle of order <= 256
+// and at most 256 right-hand sides) that host threads hand it through a
 // ring in pinned, mapped host memory.  No reference counterpart: the
 // reference runs one cuBLAS call at a time on one handle and the legacy
 // stream (runtime-blas.c:14-23), and every call pays a launch and a
@@ -54,6 +54,8 @@ constexpr int LOOP_TM = 2;                      // 32 x 32 tiles of C: an SM ret
                                                 // fine tiles to spread over the SMs
 constexpr int LOOP_TRSM_MAX_SYS = 256;          // larger solves (Cholesky panels) stay on the slot
                                                 // streams, where the inverted-block solve uses every SM
+constexpr int LOOP_MAX_MN = 512, LOOP_MAX_K = 4096;   // larger products run as their own launches on
+                                                      // the slot streams, with every SM at their disposal
 constexpr int LOOP_TILE = 16 * LOOP_TM;
 constexpr int LOOP_TRSM_SYS = 16;
 constexpr int LOOP_TRSM_ORDER = 256;
@@ -267,7 +269,7 @@ int to_loop_req(const gbx_op &o, LoopReq &r)
         g.tiles_n = (o.n + LOOP_TILE - 1) / LOOP_TILE;
         r.kind = LOOP_GEMM;
         r.nitems = g.tiles_m * g.tiles_n;
-        return r.nitems <= LOOP_QCAP;
+        return o.m <= LOOP_MAX_MN && o.n <= LOOP_MAX_MN && o.k <= LOOP_MAX_K;
     }
     if (o.kind == GBX_OP_SYRK) {
         if (gbx_check_syrk_args(o.uplo, o.transa, o.n, o.k, o.lda, o.ldc)) return 0;
@@ -283,7 +285,7 @@ int to_loop_req(const gbx_op &o, LoopReq &r)
         g.tiles_m = g.tiles_n = (o.n + LOOP_TILE - 1) / LOOP_TILE;
         r.kind = LOOP_GEMM;
         r.nitems = g.tiles_m * (g.tiles_m + 1) / 2;
-        return r.nitems <= LOOP_QCAP;
+        return o.n <= LOOP_MAX_MN && o.k <= LOOP_MAX_K;
     }
     if (o.kind == GBX_OP_TRSM) {
         if (gbx_check_trxm_args(o.side, o.uplo, o.transa, o.diag, o.m, o.n, o.lda, o.ldc)) return 0;

@@ -1,7 +1,8 @@
 """The serving layer's device-side request loop.
 
-FP64 DGEMM, DSYRK and DTRSM (triangle order <= 256, at most 256 right-hand
-sides) made through gbx_server_call run on a resident kernel fed through a ring in pinned host
+FP64 DGEMM and DSYRK with m, n <= 512 and k <= 4096, and DTRSM with a
+triangle of order <= 256 and at most 256 right-hand sides, made through
+gbx_server_call run on a resident kernel fed through a ring in pinned host
 memory.  Checked here:
   * results: DGEMM and DSYRK bit-identical to the same call on the stream
     path (the same GEMM core, one FMA chain per element over K in order);
@@ -39,7 +40,7 @@ def ops_for(g, orc, seed):
     for i in range(24):
         kind = (1, 3, 2)[i % 3]
         if kind == 1:
-            m, n, k = (int(v) for v in rng.integers(8, 700, 3))
+            m, n, k = (int(v) for v in rng.integers(8, 513, 3))   # the loop takes m, n <= 512
             ta, tb = rng.choice(["N", "T"], 2)
             ra, ca = (m, k) if ta == "N" else (k, m)
             rb, cb = (k, n) if tb == "N" else (n, k)
@@ -51,7 +52,7 @@ def ops_for(g, orc, seed):
             ops.append(g.GbxOp(kind=1, transa=ta.encode(), transb=tb.encode(), m=m, n=n, k=k, alpha=1.25, beta=-0.5,
                                A=A.data_ptr(), lda=ra, B=B.data_ptr(), ldb=rb, C=Cd.data_ptr(), ldc=m))
         elif kind == 3:
-            n, k = (int(v) for v in rng.integers(16, 600, 2))
+            n, k = (int(v) for v in rng.integers(16, 513, 2))
             uplo, tr = rng.choice(["L", "U"]), rng.choice(["N", "T"])
             ra, ca = (n, k) if tr == "N" else (k, n)
             a, s = orc.matrix(ra, ca, s)
