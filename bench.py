@@ -556,7 +556,10 @@ def run_ours(args):
             "modes": {m: {k: v[k] for k in ("calls", "calls_per_s", "p50_us", "p99_us", "tflops",
                                             "residual_sampled", "wall_s", "first_error", "chains")}
                       for m, v in modes.items()},
-            "ratios": serving_ratios(modes, line["roofline"]["peak"])}
+            "ratios": serving_ratios(modes, line["roofline"]["peak"]),
+            # latency-bound FP64 calls (DGEMM 64^3), 1 and 16 caller threads
+            "small_calls": {"dgemm_64_threads1": small_call_trace(g, 1, 2000),
+                            "dgemm_64_threads16": small_call_trace(g, 16, 500)}}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         from oracle import cpublas
         cb = cpublas.get()
@@ -1114,6 +1117,44 @@ def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES), chains=Tr
     return sizes, nbs, results
 
 
+def small_call_trace(g, nthreads, ncalls, size=64, modes=("plain", "served", "served_host")):
+    """Latency-bound calls: nthreads native threads each issue ncalls FP64
+    DGEMMs of size^3 (C += A B on the thread's own operands), one at a time,
+    per mode: plain per-call dispatch, the serving layer with its device-side
+    loop, and the serving layer on host worker threads.  Returns calls/s,
+    p50/p99 per mode and the loop's gain over plain dispatch."""
+    import torch
+    n = size
+    bufs = []
+    for t in range(nthreads):
+        a = torch.rand(n * n, dtype=torch.float64, device="cuda") * 2 - 1
+        b = torch.rand(n * n, dtype=torch.float64, device="cuda") * 2 - 1
+        c = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+        bufs.append((a, b, c))
+    torch.cuda.synchronize()
+    ops = [[g.GbxOp(kind=1, transa=b"N", transb=b"N", m=n, n=n, k=n, alpha=1.0, beta=1.0, A=a.data_ptr(), lda=n,
+                    B=b.data_ptr(), ldb=n, C=c.data_ptr(), ldc=n)] * ncalls for a, b, c in bufs]
+    out = {}
+    for mode in modes:
+        use_server, _, loop = MODES[mode]
+        for _, _, c in bufs:
+            c.zero_()
+        torch.cuda.synchronize()
+        server = make_server(g, max(2, min(16, nthreads)), loop) if use_server else None
+        r = g.ops_trace(server, 0, ops)
+        if server:
+            server.close()
+        a, b, c = bufs[0]
+        want = ncalls * (a.view(n, n).T @ b.view(n, n).T)       # column-major: A = a.view(n, n).T
+        got = c.view(n, n).T
+        err = float((got - want).norm() / want.norm())
+        out[mode] = {"calls": r["calls"], "calls_per_s": r["calls"] / r["wall_s"], "p50_us": r["p50_us"],
+                     "p99_us": r["p99_us"], "rel_err_thread0": err, "first_error": r["first_error"]}
+    if "plain" in out and "served" in out:
+        out["loop_vs_plain"] = out["served"]["calls_per_s"] / out["plain"]["calls_per_s"]
+    return out
+
+
 def serving_ratios(results, fp64_peak_tflops=None):
     """Same-precision ratios (the loop's own effect) and the precision's,
     and the bounds on what any scheduler could gain over plain dispatch."""
@@ -1160,6 +1201,8 @@ def run_serving(args):
                                         "(tolerance 1e-14, FP64 results), dpotrf in FP64"},
             "modes": results,
             "ratios": serving_ratios(results, g.Device(0).fp64_peak()),
+            "small_calls": {"dgemm_64_threads1": small_call_trace(g, 1, 2000),
+                            "dgemm_64_threads16": small_call_trace(g, 16, 500)},
             "residual_sampled": {m: results[m]["residual_sampled"] for m in results},
             "open_loop": open_loop,
             "e2e": {"unavailable": "operands are device-resident by design of this workload"}}

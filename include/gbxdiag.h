@@ -71,6 +71,10 @@ typedef struct {
 gbx_status gbx_diag_cholesky_trace(gbx_server *server, int device, int nthreads, const int *n, const int *nb,
                                    double *const *A, const int *lda, int *info, int ozaki,
                                    gbx_trace_stats *out);
+/* The same driver on given operation lists: thread t issues ops[t][0 ..
+ * count[t]) one call at a time, through server or plain per-call dispatch. */
+gbx_status gbx_diag_ops_trace(gbx_server *server, int device, int nthreads, const gbx_op *const *ops,
+                              const int *count, gbx_trace_stats *out);
 
 #ifdef __cplusplus
 }

@@ -10,4 +10,4 @@ benchmarks and failure-path tests use; the BLAS library does not need it.
 """
 from ._lib import (F77, OP_DOT, OP_GEMM, OP_NRM2, OP_SYRK, OP_TRSM, Device, GbxError, GbxOp,  # noqa: F401
                    DIAG_HEADERS, DIAG_LIB_PATH, LIB_PATH, Server, cholesky_trace, declared_symbols, load,
-                   load_diag, stats)
+                   load_diag, ops_trace, stats)

@@ -61,6 +61,7 @@ def load_diag():
     d.gbx_diag_fp64_peak.argtypes = [_P, C.POINTER(_D)]
     d.gbx_diag_expire_wait.argtypes = [_P]
     d.gbx_diag_pipe_rates.argtypes = [_P, _P]
+    d.gbx_diag_ops_trace.argtypes = [_P, _I, _I, C.POINTER(_P), C.POINTER(_I), C.POINTER(TraceStats)]
     d.gbx_diag_mma_issue.argtypes = [_P, _I, _I, _I, C.POINTER(_D), C.POINTER(_D)]
     d.gbx_diag_cholesky_trace.argtypes = [_P, _I, _I, C.POINTER(_I), C.POINTER(_I), C.POINTER(_P),
                                           C.POINTER(_I), _P, _I, C.POINTER(TraceStats)]
@@ -215,6 +216,22 @@ def cholesky_trace(server, device, n, nb, mats, info_ptr, ozaki):
     return {"calls": out.calls, "wall_s": out.wall_s, "p50_us": out.p50_us, "p99_us": out.p99_us,
             "kind_calls": list(out.kind_calls), "kind_sum_us": list(out.kind_sum_us),
             "thread_finish_s": list(out.thread_finish_s)[:k], "first_error": out.first_error}
+
+
+def ops_trace(server, device, per_thread_ops):
+    """Runs gbx_diag_ops_trace: thread t issues per_thread_ops[t] (a list of
+    GbxOp) one call at a time; returns gbx_trace_stats as a dict."""
+    L = load_diag()
+    k = len(per_thread_ops)
+    arrays = [(GbxOp * len(o))(*o) for o in per_thread_ops]
+    ptrs = (_P * k)(*[C.cast(a, _P) for a in arrays])
+    cnt = (_I * k)(*[len(o) for o in per_thread_ops])
+    out = TraceStats()
+    st = L.gbx_diag_ops_trace(server.h if server else None, device, k, ptrs, cnt, C.byref(out))
+    if st != 0:
+        raise GbxError(f"gbx_diag_ops_trace failed with status {st}")
+    return {"calls": out.calls, "wall_s": out.wall_s, "p50_us": out.p50_us, "p99_us": out.p99_us,
+            "first_error": out.first_error}
 
 
 class Server:

@@ -95,20 +95,13 @@ std::vector<gbx_op> cholesky_ops(int n, int nb, double *A, int lda, int *info, b
     return ops;
 }
 
-}  // namespace
 
-extern "C" gbx_status gbx_diag_cholesky_trace(gbx_server *server, int device, int nthreads, const int *n,
-                                              const int *nb, double *const *A, const int *lda, int *info,
-                                              int ozaki, gbx_trace_stats *out)
+// Runs plan[t] on thread t (all threads start together), through server or
+// as plain per-call dispatch, and fills out.
+gbx_status run_trace(gbx_server *server, int device, const std::vector<std::vector<gbx_op>> &plan,
+                     gbx_trace_stats *out)
 {
-    if (!out || nthreads < 1 || nthreads > GBX_TRACE_MAX_THREADS || !n || !nb || !A || !lda || !info)
-        return GBX_ERR_ARG;
-    *out = gbx_trace_stats{};
-    std::vector<std::vector<gbx_op>> plan(nthreads);
-    for (int t = 0; t < nthreads; t++) {
-        if (n[t] < 1 || nb[t] < 1 || nb[t] > 256 || lda[t] < n[t] || !A[t]) return GBX_ERR_ARG;
-        plan[t] = cholesky_ops(n[t], nb[t], A[t], lda[t], info + t, ozaki != 0);
-    }
+    const int nthreads = (int)plan.size();
     std::vector<std::vector<float>> lat(nthreads);
     std::vector<double> finish(nthreads, 0.0);
     std::vector<std::array<double, GBX_TRACE_KINDS>> ksum(nthreads);
@@ -181,4 +174,34 @@ extern "C" gbx_status gbx_diag_cholesky_trace(gbx_server *server, int device, in
     }
     out->first_error = first_error.load();
     return GBX_OK;
+}
+
+}  // namespace
+
+extern "C" gbx_status gbx_diag_cholesky_trace(gbx_server *server, int device, int nthreads, const int *n,
+                                              const int *nb, double *const *A, const int *lda, int *info,
+                                              int ozaki, gbx_trace_stats *out)
+{
+    if (!out || nthreads < 1 || nthreads > GBX_TRACE_MAX_THREADS || !n || !nb || !A || !lda || !info)
+        return GBX_ERR_ARG;
+    *out = gbx_trace_stats{};
+    std::vector<std::vector<gbx_op>> plan(nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        if (n[t] < 1 || nb[t] < 1 || nb[t] > 256 || lda[t] < n[t] || !A[t]) return GBX_ERR_ARG;
+        plan[t] = cholesky_ops(n[t], nb[t], A[t], lda[t], info + t, ozaki != 0);
+    }
+    return run_trace(server, device, plan, out);
+}
+
+extern "C" gbx_status gbx_diag_ops_trace(gbx_server *server, int device, int nthreads, const gbx_op *const *ops,
+                                         const int *count, gbx_trace_stats *out)
+{
+    if (!out || nthreads < 1 || nthreads > GBX_TRACE_MAX_THREADS || !ops || !count) return GBX_ERR_ARG;
+    *out = gbx_trace_stats{};
+    std::vector<std::vector<gbx_op>> plan(nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        if (count[t] < 0 || (count[t] > 0 && !ops[t])) return GBX_ERR_ARG;
+        plan[t].assign(ops[t], ops[t] + count[t]);
+    }
+    return run_trace(server, device, plan, out);
 }
