@@ -317,13 +317,13 @@ gbx_status gbx_ops_run(gbx_ctx *ctx, const gbx_op *ops, int count);
 /* ---- serving loop (no reference counterpart: the reference serves one call
  * at a time on one cuBLAS handle, runtime-blas.c:14-23) -------------------
  * Continuous batching of calls from many host threads on device-resident
- * operands.  gbx_server_call hands the small FP64 requests (DGEMM and
- * DSYRK with m, n <= 512 and k <= 4096; DTRSM of order <= 256 with at most
- * 256 right-hand sides) to a device-side request loop: a resident kernel on
- * a quarter of the SMs that takes them from a ring in pinned host memory and
- * shares its CTAs among them tile by tile, with no launch or
- * synchronisation per call; larger calls from the calling thread run on a
- * free slot's stream with the whole GPU.  Other requests (and
+ * operands.  With GBX_SERVE_LOOP=1 at creation, gbx_server_call hands the
+ * small FP64 requests (DGEMM and DSYRK with m, n <= 512 and k <= 4096; DTRSM
+ * of order <= 256 with at most 256 right-hand sides) to a device-side request
+ * loop: a resident kernel on a quarter of the SMs that takes them from a
+ * ring in pinned host memory and shares its CTAs among them tile by tile,
+ * with no launch or synchronisation per call.  Larger calls from the calling
+ * thread run on a free slot's stream with the whole GPU.  Other requests (and
  * gbx_server_submit) go to worker threads that group the small DGEMM
  * (m, n <= 512, k <= 4096) and DTRSM (order <= 256) requests queued at that
  * moment into one grouped kernel and run the others with the regular
@@ -343,7 +343,7 @@ gbx_status gbx_server_stats(gbx_server *srv, uint64_t *completed, uint64_t *batc
                             uint64_t *grouped_calls, double *p50_us, double *p99_us,
                             uint64_t *admission_waits);
 /* The device-side request loop behind gbx_server_call: whether the server
- * has one (GBX_SERVE_LOOP=0 at creation turns it off), the calls it ran and
+ * has one (GBX_SERVE_LOOP=1 at creation turns it on), the calls it ran and
  * how often its resident kernel was (re)started. */
 gbx_status gbx_server_loop_stats(gbx_server *srv, int *enabled, uint64_t *calls, uint64_t *launches);
 gbx_status gbx_server_reset_stats(gbx_server *srv);

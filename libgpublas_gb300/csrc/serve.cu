@@ -21,12 +21,13 @@
 //
 // Small FP64 DGEMM, DSYRK and DTRSM requests (m, n <= 512, k <= 4096;
 // triangle order <= 256, at most 256 right-hand sides) made through
-// gbx_server_call run on the device-side request loop (serve_loop.cu): a
+// gbx_server_call can run on the device-side request loop (serve_loop.cu): a
 // resident kernel fed through a ring in pinned host memory, so such a call
 // costs no launch, stream synchronisation or worker-thread hand-off.  The
-// loop is started on the first such call and leaves the GPU after 20 ms
-// without work; GBX_SERVE_LOOP=0 at server creation keeps every request on
-// the slot streams.
+// loop holds a quarter of the SMs while it is resident (it leaves the GPU
+// after 20 ms without work), which pays off for latency-bound callers and
+// loses on FP64-bound traces, so it is opt-in: GBX_SERVE_LOOP=1 at server
+// creation.
 //
 // Admission by memory: callers that stage host operands reserve their bytes
 // with gbx_server_admit (blocks while the reserved total would exceed the
@@ -264,7 +265,7 @@ extern "C" gbx_status gbx_server_create(int device, int nslots, size_t mem_budge
     const size_t auto_budget = free_b / 10 * 8;   // 80% of what is free now
     s->budget = mem_budget ? std::min(mem_budget, auto_budget) : auto_budget;
     const char *lp = getenv("GBX_SERVE_LOOP");
-    if (!(lp && atoi(lp) == 0)) {
+    if (lp && atoi(lp) != 0) {
         // a quarter of the SMs: the loop takes the small requests, and the SMs it
         // leaves free run the large ones and the factorisation steps on the slot streams
         int sms = 152;

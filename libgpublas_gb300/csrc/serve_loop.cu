@@ -36,6 +36,7 @@
 #include <stdint.h>
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <mutex>
 #include <cstring>
 #include <thread>
@@ -63,6 +64,7 @@ constexpr size_t LOOP_DSMEM = sizeof(double) * LOOP_TRSM_ORDER * LOOP_TRSM_SYS; 
 constexpr int LOOP_POLLERS = 8;                 // CTAs that watch the ring for new requests
 constexpr unsigned long long LOOP_IDLE_NS = 20000000ull;    // 20 ms without work: the CTA leaves
 constexpr unsigned long long LOOP_WAIT_NS = 1000000000ull;  // 1 s for a reserved queue item
+constexpr long long LOOP_ALIVE_NS = 3 * (long long)LOOP_IDLE_NS;  // host side: margin under the watchers' 4 * LOOP_IDLE_NS
 
 enum { LOOP_GEMM = 1, LOOP_TRSM = 2 };
 
@@ -164,47 +166,11 @@ serve_loop_kernel(LoopState *st, RingSlot *ring, const LoopCtl *ctl)
                 const unsigned long long c = vload(&st->claim);
                 RingSlot &rs = ring[c % LOOP_RING];
                 if (blockIdx.x < LOOP_POLLERS && vload(&rs.pub) == c + 1 && atomicCAS(&st->claim, c, c + 1) == c) {
+                    // the request in host memory is complete once pub is seen
                     __threadfence_system();
-                    LoopReq &dr = st->req[c % LOOP_RING];
-                    const int *src = (const int *)&rs.req;
-                    int *dst = (int *)&dr;
-                    for (int w = 0; w < (int)(sizeof(LoopReq) / sizeof(int)); w++) dst[w] = ((const volatile int *)src)[w];
-                    const int n = dr.nitems, qi = dr.critical ? 0 : 1;
-                    if (n <= 0) {
-                        finish(ring, c, 0);
-                    } else {
-                        st->left[c % LOOP_RING] = n;
-                        // reserve n items (the queue holds LOOP_QCAP; requests are
-                        // cut so that one never needs more)
-                        LoopQueue &q = st->q[qi];
-                        const unsigned long long t0 = gbx_tc::globaltimer();
-                        unsigned long long base = 0;
-                        bool ok = false;
-                        while (gbx_tc::globaltimer() - t0 <= LOOP_WAIT_NS) {
-                            const unsigned long long t = vload(&q.tail);
-                            if (t + n - vload(&q.head) > LOOP_QCAP) continue;
-                            if (atomicCAS(&q.tail, t, t + n) == t) {
-                                base = t;
-                                ok = true;
-                                break;
-                            }
-                        }
-                        if (!ok) {
-                            atomicCAS(&st->err, 0, gbx_tc::TC_TIMEOUT_EMPTY);
-                            finish(ring, c, gbx_tc::TC_TIMEOUT_EMPTY);
-                            s_action = 3;
-                        } else {
-                            // the request copy and its item count are visible
-                            // device-wide before any of its items is published
-                            __threadfence();
-                            s_action = 2;
-                            s_ticket = c;
-                            s_base = base;
-                            s_n = n;
-                            s_qi = qi;
-                        }
-                    }
-                    if (s_action != 3) idle0 = gbx_tc::globaltimer();
+                    s_action = 2;
+                    s_ticket = c;
+                    idle0 = gbx_tc::globaltimer();
                 } else if (*(const volatile int *)&ctl->stop || vload((const unsigned long long *)&st->err) != 0 ||
                            gbx_tc::globaltimer() - idle0 > (blockIdx.x < LOOP_POLLERS ? 4 : 1) * LOOP_IDLE_NS) {
                     // the ring watchers stay longest, so that requests published
@@ -233,12 +199,62 @@ serve_loop_kernel(LoopState *st, RingSlot *ring, const LoopCtl *ctl)
                 if (atomicSub(&st->left[tk % LOOP_RING], 1) == 1) finish(ring, tk, 0);
             }
         } else if (action == 2) {
+            const unsigned long long c = s_ticket;
+            // the whole CTA copies the request out of host memory, one word
+            // per thread, so the copy costs one host round trip, not one per word
+            {
+                const volatile int *src = (const volatile int *)&ring[c % LOOP_RING].req;
+                int *dst = (int *)&st->req[c % LOOP_RING];
+                for (int w = threadIdx.x; w < (int)(sizeof(LoopReq) / sizeof(int)); w += LOOP_THREADS)
+                    dst[w] = src[w];
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const LoopReq &dr = st->req[c % LOOP_RING];
+                const int n = dr.nitems, qi = dr.critical ? 0 : 1;
+                s_n = 0;
+                if (n <= 0) {
+                    finish(ring, c, 0);
+                } else {
+                    st->left[c % LOOP_RING] = n;
+                    // reserve n items (the queue holds LOOP_QCAP; requests are
+                    // cut so that one never needs more)
+                    LoopQueue &q = st->q[qi];
+                    const unsigned long long t0 = gbx_tc::globaltimer();
+                    unsigned long long base = 0;
+                    bool ok = false;
+                    while (gbx_tc::globaltimer() - t0 <= LOOP_WAIT_NS) {
+                        const unsigned long long t = vload(&q.tail);
+                        if (t + n - vload(&q.head) > LOOP_QCAP) continue;
+                        if (atomicCAS(&q.tail, t, t + n) == t) {
+                            base = t;
+                            ok = true;
+                            break;
+                        }
+                    }
+                    if (!ok) {
+                        atomicCAS(&st->err, 0, gbx_tc::TC_TIMEOUT_EMPTY);
+                        finish(ring, c, gbx_tc::TC_TIMEOUT_EMPTY);
+                        s_action = 3;
+                    } else {
+                        // the request copy (written by the whole CTA, ordered by
+                        // the barrier above) and its item count are visible
+                        // device-wide before any of its items is published
+                        __threadfence();
+                        s_base = base;
+                        s_n = n;
+                        s_qi = qi;
+                    }
+                }
+            }
+            __syncthreads();
+            if (s_action == 3) break;
             // the whole CTA writes the new request's items
             LoopQueue &q = st->q[s_qi];
-            const unsigned long long base = s_base, tk = s_ticket;
+            const unsigned long long base = s_base;
             for (int i = threadIdx.x; i < s_n; i += LOOP_THREADS) {
                 const unsigned long long idx = base + i;
-                q.ticket[idx % LOOP_QCAP] = tk;
+                q.ticket[idx % LOOP_QCAP] = c;
                 q.item[idx % LOOP_QCAP] = i;
                 __threadfence();
                 *(volatile unsigned long long *)&q.seq[idx % LOOP_QCAP] = idx + 1;
@@ -325,6 +341,10 @@ struct gbx_loop {
     std::mutex launch_mu;
     bool launched = false;
     std::atomic<unsigned long long> launches{0};
+    // steady-clock time (ns) before which a ring watcher is known to be
+    // resident: a watcher expanded a request published at t, and watchers
+    // leave only after 4 * LOOP_IDLE_NS without work
+    std::atomic<long long> alive_until_ns{0};
 };
 
 namespace {
@@ -407,10 +427,15 @@ extern "C" gbx_status gbx_loop_call(gbx_loop *l, const gbx_op *op)
     }
     rs->req = r;
     rs->status = 0;
+    const long long t_pub = std::chrono::duration_cast<std::chrono::nanoseconds>(
+                                std::chrono::steady_clock::now().time_since_epoch()).count();
     std::atomic_thread_fence(std::memory_order_release);
     *(volatile unsigned long long *)&rs->pub = t + 1;
-    gbx_status st = loop_ensure_running(l);
-    if (st != GBX_OK) return st;
+    gbx_status st = GBX_OK;
+    // while a ring watcher is known to be resident, no launch check (a mutex
+    // and a driver query) is needed on the call path
+    if (t_pub >= l->alive_until_ns.load(std::memory_order_relaxed) && (st = loop_ensure_running(l)) != GBX_OK)
+        return st;
     for (unsigned spins = 0; *done != t + 1; spins++) {
         if ((spins & 4095u) == 4095u) {
             // the kernel may have left (idle) just before this request was
@@ -420,7 +445,11 @@ extern "C" gbx_status gbx_loop_call(gbx_loop *l, const gbx_op *op)
         }
     }
     std::atomic_thread_fence(std::memory_order_acquire);
-    return rs->status ? GBX_ERR_TIMEOUT : GBX_OK;
+    if (rs->status) return GBX_ERR_TIMEOUT;
+    // a watcher expanded this request after t_pub and stays at least
+    // 4 * LOOP_IDLE_NS after that
+    l->alive_until_ns.store(t_pub + LOOP_ALIVE_NS, std::memory_order_relaxed);
+    return GBX_OK;
 }
 
 extern "C" uint64_t gbx_loop_launches(const gbx_loop *l) { return l ? l->launches.load() : 0; }

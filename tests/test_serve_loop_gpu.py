@@ -2,16 +2,16 @@
 
 FP64 DGEMM and DSYRK with m, n <= 512 and k <= 4096, and DTRSM with a
 triangle of order <= 256 and at most 256 right-hand sides, made through
-gbx_server_call run on a resident kernel fed through a ring in pinned host
-memory.  Checked here:
+gbx_server_call run, on a server created with GBX_SERVE_LOOP=1, on a
+resident kernel fed through a ring in pinned host memory.  Checked here:
   * results: DGEMM and DSYRK bit-identical to the same call on the stream
     path (the same GEMM core, one FMA chain per element over K in order);
     DTRSM within a backward residual of 1e-14 of the double-double oracle;
   * the calls really ran on the loop (its counters), and the resident kernel
     comes back after it left the GPU for lack of work;
   * 16 host threads at once: every result equal to the one served alone;
-  * with the loop turned off (GBX_SERVE_LOOP=0) the same calls run on the
-    slot streams.
+  * without GBX_SERVE_LOOP=1 (the default) the same calls run on the slot
+    streams.
 """
 import os
 import threading
@@ -21,6 +21,20 @@ import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+
+def loop_server(g, slots):
+    """A server with its device-side request loop on (GBX_SERVE_LOOP=1 is
+    read at creation)."""
+    old = os.environ.get("GBX_SERVE_LOOP")
+    os.environ["GBX_SERVE_LOOP"] = "1"
+    try:
+        return g.Server(0, slots=slots)
+    finally:
+        if old is None:
+            del os.environ["GBX_SERVE_LOOP"]
+        else:
+            os.environ["GBX_SERVE_LOOP"] = old
 
 
 def to_dev(a):
@@ -87,7 +101,7 @@ def ops_for(g, orc, seed):
 def test_loop_results_and_counters(orc, dev, lib):
     import libgpublas_gb300 as g
     specs, ops, reset, outputs = ops_for(g, orc, 41)
-    srv = g.Server(0, slots=4)
+    srv = loop_server(g, 4)
     try:
         enabled, calls0, _ = srv.loop_stats()
         assert enabled
@@ -123,7 +137,7 @@ def test_loop_results_and_counters(orc, dev, lib):
 def test_loop_restarts_after_leaving_idle(orc, lib):
     import libgpublas_gb300 as g
     specs, ops, reset, outputs = ops_for(g, orc, 42)
-    srv = g.Server(0, slots=2)
+    srv = loop_server(g, 2)
     try:
         reset()
         assert srv.call(ops[0])[0] == 0
@@ -142,7 +156,7 @@ def test_loop_restarts_after_leaving_idle(orc, lib):
 def test_loop_sixteen_threads_equal_alone(orc, lib):
     import libgpublas_gb300 as g
     specs, ops, reset, outputs = ops_for(g, orc, 43)
-    srv = g.Server(0, slots=8)
+    srv = loop_server(g, 8)
     try:
         reset()
         for op in ops:
@@ -171,14 +185,11 @@ def test_loop_sixteen_threads_equal_alone(orc, lib):
 def test_loop_off_runs_on_slot_streams(orc, lib):
     import libgpublas_gb300 as g
     specs, ops, reset, outputs = ops_for(g, orc, 44)
-    old = os.environ.get("GBX_SERVE_LOOP")
-    os.environ["GBX_SERVE_LOOP"] = "0"
+    old = os.environ.pop("GBX_SERVE_LOOP", None)
     try:
         srv = g.Server(0, slots=4)
     finally:
-        if old is None:
-            del os.environ["GBX_SERVE_LOOP"]
-        else:
+        if old is not None:
             os.environ["GBX_SERVE_LOOP"] = old
     try:
         enabled, calls, _ = srv.loop_stats()
