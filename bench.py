@@ -1002,6 +1002,7 @@ MODES = {
     # device-side request loop on)
     "plain": (False, False, False),         # FP64, plain per-call dispatch
     "served": (True, False, True),          # FP64, serving layer with its device-side loop
+    "served_all": (True, False, "all"),     # FP64, the same with the loop on every SM
     "served_host": (True, False, False),    # FP64, serving layer on host worker threads only
     "ozaki_plain": (False, True, False),    # Ozaki, plain per-call dispatch
     "ozaki": (True, True, True),            # Ozaki, serving layer
@@ -1009,19 +1010,30 @@ MODES = {
 
 
 def make_server(g, slots, loop):
-    """A Server with its device-side request loop on or off (read at creation)."""
-    old = os.environ.get("GBX_SERVE_LOOP")
-    os.environ["GBX_SERVE_LOOP"] = "1" if loop else "0"
+    """A Server with its device-side request loop off, on (a quarter of the
+    SMs) or on every SM ("all"); both variables are read at creation."""
+    import torch
+    env = {"GBX_SERVE_LOOP": "1" if loop else "0",
+           "GBX_SERVE_LOOP_CTAS": str(torch.cuda.get_device_properties(0).multi_processor_count)
+           if loop == "all" else None}
+    old = {k: os.environ.get(k) for k in env}
+    for k, v in env.items():
+        if v is None:
+            os.environ.pop(k, None)
+        else:
+            os.environ[k] = v
     try:
         return g.Server(0, slots=slots)
     finally:
-        if old is None:
-            del os.environ["GBX_SERVE_LOOP"]
-        else:
-            os.environ["GBX_SERVE_LOOP"] = old
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
-def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES), chains=True):
+def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=("plain", "served", "served_host", "ozaki_plain", "ozaki"),
+                  chains=True):
     """Closed-loop Cholesky trace: nthreads native caller threads, thread t
     factorising A = G G^T + n I (G uniform[-1,1], n log-uniform in
     [nmin, nmax], nb in {128, 256}) through the library, once per mode.
@@ -1117,12 +1129,13 @@ def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=tuple(MODES), chains=Tr
     return sizes, nbs, results
 
 
-def small_call_trace(g, nthreads, ncalls, size=64, modes=("plain", "served", "served_host")):
+def small_call_trace(g, nthreads, ncalls, size=64, modes=("plain", "served", "served_all", "served_host")):
     """Latency-bound calls: nthreads native threads each issue ncalls FP64
     DGEMMs of size^3 (C += A B on the thread's own operands), one at a time,
     per mode: plain per-call dispatch, the serving layer with its device-side
-    loop, and the serving layer on host worker threads.  Returns calls/s,
-    p50/p99 per mode and the loop's gain over plain dispatch."""
+    loop (on a quarter of the SMs, and on every SM), and the serving layer on
+    host worker threads.  Returns calls/s, p50/p99 per mode and the loop's
+    gain over plain dispatch."""
     import torch
     n = size
     bufs = []
@@ -1152,6 +1165,8 @@ def small_call_trace(g, nthreads, ncalls, size=64, modes=("plain", "served", "se
                      "p99_us": r["p99_us"], "rel_err_thread0": err, "first_error": r["first_error"]}
     if "plain" in out and "served" in out:
         out["loop_vs_plain"] = out["served"]["calls_per_s"] / out["plain"]["calls_per_s"]
+    if "plain" in out and "served_all" in out:
+        out["loop_all_sms_vs_plain"] = out["served_all"]["calls_per_s"] / out["plain"]["calls_per_s"]
     return out
 
 
@@ -1161,6 +1176,7 @@ def serving_ratios(results, fp64_peak_tflops=None):
     def ratio(a, b):
         return results[a]["calls_per_s"] / results[b]["calls_per_s"] if a in results and b in results else None
     out = {"served_vs_plain_fp64": ratio("served", "plain"),
+           "served_all_sms_vs_plain_fp64": ratio("served_all", "plain"),
            "served_loop_vs_host_workers_fp64": ratio("served", "served_host"),
            "served_vs_plain_ozaki": ratio("ozaki", "ozaki_plain"),
            "ozaki_plain_vs_fp64_plain": ratio("ozaki_plain", "plain"),

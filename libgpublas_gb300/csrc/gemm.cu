@@ -57,7 +57,7 @@ template gbx_status scale_matrix<dcplx>(gbx_ctx *, int, int, dcplx, dcplx *, lon
 template <typename T, int TM>
 gbx_status launch_gemm_tile(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
 {
-    constexpr int TN = TM, BK = 8;
+    constexpr int TN = TM, BK = TM == 1 ? 16 : 8;
     constexpr int BM = 16 * TM, BN = 16 * TN;
     p.tiles_m = (p.m + BM - 1) / BM;
     p.tiles_n = (p.n + BN - 1) / BN;
@@ -78,8 +78,11 @@ gbx_status launch_gemm_tile(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
 // Tile choice: the largest block tile that still gives every SM two tiles;
 // 128x128 (8x8 per thread) for large problems, 64x64 and 32x32 for the
 // skinny and small products that DTRSM's recursion and small calls produce
-// (with few large tiles most SMs would idle).  Complex double uses 64x64 /
-// 32x32 (its 8x8 register tile would not fit).
+// (with few large tiles most SMs would idle), and 16x16 (one element per
+// thread) below that: at 2 FP64 lanes per clock per SM a small product's
+// latency is its FMAs per SM, so spreading it over four times the SMs cuts
+// it almost fourfold.  Complex double uses 64x64 / 32x32 (its 8x8 register
+// tile would not fit).
 template <typename T>
 gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
 {
@@ -92,7 +95,8 @@ gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
     if constexpr (sizeof(T) <= 8) {
         if (tiles(128) >= want) return launch_gemm_tile<T, 8>(ctx, p, what);
         if (tiles(64) >= want) return launch_gemm_tile<T, 4>(ctx, p, what);
-        return launch_gemm_tile<T, 2>(ctx, p, what);
+        if (tiles(32) >= want) return launch_gemm_tile<T, 2>(ctx, p, what);
+        return launch_gemm_tile<T, 1>(ctx, p, what);
     } else {
         if (tiles(64) >= want) return launch_gemm_tile<T, 4>(ctx, p, what);
         return launch_gemm_tile<T, 2>(ctx, p, what);

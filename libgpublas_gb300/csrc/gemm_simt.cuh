@@ -44,6 +44,13 @@ template <> struct Ops<double> {
     static __device__ __forceinline__ double conj(double a) { return a; }
     static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
     static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+    // a x + b y with the rounding spelled out (x a rounded, then one FMA), so
+    // that every instantiation of the GEMM core gives the same bits whatever
+    // the compiler would contract
+    static __device__ __forceinline__ double axpby(double a, double x, double b, double y)
+    {
+        return __fma_rn(b, y, __dmul_rn(a, x));
+    }
     static __device__ __forceinline__ double div(double a, double b) { return a / b; }
     static __device__ __forceinline__ double neg(double a) { return -a; }
     static __device__ __forceinline__ double real_only(double a) { return a; }
@@ -56,6 +63,10 @@ template <> struct Ops<float> {
     static __device__ __forceinline__ float conj(float a) { return a; }
     static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
     static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float axpby(float a, float x, float b, float y)
+    {
+        return __fmaf_rn(b, y, __fmul_rn(a, x));
+    }
     static __device__ __forceinline__ float div(float a, float b) { return a / b; }
     static __device__ __forceinline__ float neg(float a) { return -a; }
     static __device__ __forceinline__ float real_only(float a) { return a; }
@@ -74,9 +85,16 @@ template <> struct Ops<fcplx> {
     static __device__ __forceinline__ fcplx conj(fcplx a) { return {a.x, -a.y}; }
     static __device__ __forceinline__ fcplx mul(fcplx a, fcplx b)
     {
-        return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+        // rounding spelled out (one product rounded, one FMA), so that the
+        // result does not depend on what the compiler contracts
+        return {__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)), __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x))};
     }
     static __device__ __forceinline__ fcplx add(fcplx a, fcplx b) { return {a.x + b.x, a.y + b.y}; }
+    static __device__ __forceinline__ fcplx axpby(fcplx a, fcplx x, fcplx b, fcplx y)
+    {
+        const fcplx u = mul(a, x), v = mul(b, y);
+        return {__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y)};
+    }
     static __device__ __forceinline__ fcplx div(fcplx a, fcplx b) { return smith_div<fcplx, float>(a, b); }
     static __device__ __forceinline__ fcplx neg(fcplx a) { return {-a.x, -a.y}; }
     static __device__ __forceinline__ fcplx real_only(fcplx a) { return {a.x, 0.0f}; }
@@ -95,9 +113,16 @@ template <> struct Ops<dcplx> {
     static __device__ __forceinline__ dcplx conj(dcplx a) { return {a.x, -a.y}; }
     static __device__ __forceinline__ dcplx mul(dcplx a, dcplx b)
     {
-        return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+        // rounding spelled out (one product rounded, one FMA), so that the
+        // result does not depend on what the compiler contracts
+        return {__fma_rn(a.x, b.x, -__dmul_rn(a.y, b.y)), __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x))};
     }
     static __device__ __forceinline__ dcplx add(dcplx a, dcplx b) { return {a.x + b.x, a.y + b.y}; }
+    static __device__ __forceinline__ dcplx axpby(dcplx a, dcplx x, dcplx b, dcplx y)
+    {
+        const dcplx u = mul(a, x), v = mul(b, y);
+        return {__dadd_rn(u.x, v.x), __dadd_rn(u.y, v.y)};
+    }
     static __device__ __forceinline__ dcplx div(dcplx a, dcplx b) { return smith_div<dcplx, double>(a, b); }
     static __device__ __forceinline__ dcplx neg(dcplx a) { return {-a.x, -a.y}; }
     static __device__ __forceinline__ dcplx real_only(dcplx a) { return {a.x, 0.0}; }
@@ -200,16 +225,29 @@ __device__ __forceinline__ void tri_decode(int t, int &bi, int &bj)
     bj = t - i * (i + 1) / 2;
 }
 
+// Row (col) of a thread's i-th register-tile entry within the block tile:
+// with TM >= 2 a thread holds TM/2 adjacent rows in each half of the tile
+// (conflict-free shared-memory reads); with TM == 1 one row.
+template <int TM>
+__device__ __forceinline__ int frag_pos(int t, int i)
+{
+    if constexpr (TM == 1) return t;
+    else return i < TM / 2 ? t * (TM / 2) + i : 8 * TM + t * (TM / 2) + (i - TM / 2);
+}
+
 // One BM x BN tile of C (tile index: column-major over the tile grid, or the
 // triangular enumeration for C_LOWER / C_UPPER), computed by the whole CTA
 // of GEMM_THREADS threads.  The launch kernel below runs one tile per CTA;
 // the serving loop's persistent kernel calls it for the tiles it takes.
 // Every output element is one FMA chain over K in increasing order,
-// whatever the tile size.
+// whatever the tile size (TM = TN = 1, a 16 x 16 tile with one element per
+// thread, needs BK = 16 so that a panel has one element per thread).
 template <typename T, int TM, int TN, int BK>
 __device__ __forceinline__ void gemm_simt_tile(const GemmArgs<T> &p, int tile)
 {
     constexpr int BM = 16 * TM, BN = 16 * TN;
+    static_assert((TM == 1 || TM % 2 == 0) && (TN == 1 || TN % 2 == 0), "register tile");
+    static_assert(BM * BK % GEMM_THREADS == 0 && BN * BK % GEMM_THREADS == 0, "panel per thread");
     __shared__ __align__(16) T As[2][BK][BM];
     __shared__ __align__(16) T Bs[2][BK][BN];
 
@@ -263,15 +301,9 @@ __device__ __forceinline__ void gemm_simt_tile(const GemmArgs<T> &p, int tile)
         for (int kk = 0; kk < BK; kk++) {
             T a[TM], b[TN];
 #pragma unroll
-            for (int i = 0; i < TM / 2; i++) {
-                a[i] = As[cur][kk][ty * (TM / 2) + i];
-                a[i + TM / 2] = As[cur][kk][BM / 2 + ty * (TM / 2) + i];
-            }
+            for (int i = 0; i < TM; i++) a[i] = As[cur][kk][frag_pos<TM>(ty, i)];
 #pragma unroll
-            for (int j = 0; j < TN / 2; j++) {
-                b[j] = Bs[cur][kk][tx * (TN / 2) + j];
-                b[j + TN / 2] = Bs[cur][kk][BN / 2 + tx * (TN / 2) + j];
-            }
+            for (int j = 0; j < TN; j++) b[j] = Bs[cur][kk][frag_pos<TN>(tx, j)];
 #pragma unroll
             for (int i = 0; i < TM; i++)
 #pragma unroll
@@ -289,17 +321,16 @@ __device__ __forceinline__ void gemm_simt_tile(const GemmArgs<T> &p, int tile)
     const bool beta0 = Ops<T>::is_zero(p.beta);
 #pragma unroll
     for (int j = 0; j < TN; j++) {
-        const int col = n0 + (j < TN / 2 ? tx * (TN / 2) + j : BN / 2 + tx * (TN / 2) + (j - TN / 2));
+        const int col = n0 + frag_pos<TN>(tx, j);
         if (col >= p.n) continue;
 #pragma unroll
         for (int i = 0; i < TM; i++) {
-            const int row = m0 + (i < TM / 2 ? ty * (TM / 2) + i : BM / 2 + ty * (TM / 2) + (i - TM / 2));
+            const int row = m0 + frag_pos<TM>(ty, i);
             if (row >= p.m) continue;
             if (p.c_part == C_LOWER && row < col) continue;
             if (p.c_part == C_UPPER && row > col) continue;
             T *cp = p.C + (long long)col * p.ldc + row;
-            T v = Ops<T>::mul(p.alpha, acc[i][j]);
-            if (!beta0) v = Ops<T>::add(v, Ops<T>::mul(p.beta, *cp));
+            T v = beta0 ? Ops<T>::mul(p.alpha, acc[i][j]) : Ops<T>::axpby(p.alpha, acc[i][j], p.beta, *cp);
             if (p.c_herm && row == col) v = Ops<T>::real_only(v);
             *cp = v;
         }

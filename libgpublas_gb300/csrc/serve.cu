@@ -270,7 +270,12 @@ extern "C" gbx_status gbx_server_create(int device, int nslots, size_t mem_budge
         // leaves free run the large ones and the factorisation steps on the slot streams
         int sms = 152;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        if (gbx_loop_create(device, std::max(8, sms / 4), &s->loop) != GBX_OK) s->loop = nullptr;
+        int ctas = std::max(8, sms / 4);
+        // GBX_SERVE_LOOP_CTAS: another size (at most one CTA per SM), e.g. every
+        // SM for callers whose requests are all small
+        if (const char *lc = getenv("GBX_SERVE_LOOP_CTAS"))
+            if (atoi(lc) > 0) ctas = std::min(atoi(lc), sms);
+        if (gbx_loop_create(device, ctas, &s->loop) != GBX_OK) s->loop = nullptr;
     }
     for (auto &sl : s->slots) s->workers.emplace_back(worker_loop, s, &sl);
     *out = s;

@@ -50,14 +50,14 @@ namespace {
 constexpr int LOOP_RING = 1024;                 // requests in flight
 constexpr int LOOP_QCAP = 1 << 15;              // items per queue
 constexpr int LOOP_THREADS = GEMM_THREADS;      // 256
-constexpr int LOOP_TM = 2;                      // 32 x 32 tiles of C: an SM retires 2 DFMA per clock,
-                                                // so the rank-nb updates of the Cholesky trace need
-                                                // fine tiles to spread over the SMs
+constexpr int LOOP_TILE = 32, LOOP_TILE_SMALL = 16;   // tiles of C: an SM retires 2 DFMA per clock,
+                                                      // so small products need fine tiles to spread
+                                                      // over the SMs; 16 x 16 when 32 x 32 would give
+                                                      // the loop's CTAs fewer than two tiles each
 constexpr int LOOP_TRSM_MAX_SYS = 256;          // larger solves (Cholesky panels) stay on the slot
                                                 // streams, where the inverted-block solve uses every SM
 constexpr int LOOP_MAX_MN = 512, LOOP_MAX_K = 4096;   // larger products run as their own launches on
                                                       // the slot streams, with every SM at their disposal
-constexpr int LOOP_TILE = 16 * LOOP_TM;
 constexpr int LOOP_TRSM_SYS = 16;
 constexpr int LOOP_TRSM_ORDER = 256;
 constexpr size_t LOOP_DSMEM = sizeof(double) * LOOP_TRSM_ORDER * LOOP_TRSM_SYS;   // 32 KB
@@ -72,7 +72,7 @@ struct LoopReq {
     int kind;         // LOOP_GEMM (GEMM core: DGEMM or DSYRK) or LOOP_TRSM
     int nitems;       // tiles of C, or chunks of LOOP_TRSM_SYS systems
     int critical;     // items go to the critical-path queue
-    int pad;
+    int small;        // GEMM core with 16 x 16 tiles (else 32 x 32)
     GemmArgs<double> g;
     DevOp t;
 };
@@ -188,7 +188,8 @@ serve_loop_kernel(LoopState *st, RingSlot *ring, const LoopCtl *ctl)
             const LoopReq &r = st->req[tk % LOOP_RING];
             if (r.kind == LOOP_GEMM) {
                 const GemmArgs<double> g = r.g;
-                gemm_simt_tile<double, LOOP_TM, LOOP_TM, 8>(g, s_item);
+                if (r.small) gemm_simt_tile<double, 1, 1, 16>(g, s_item);
+                else gemm_simt_tile<double, 2, 2, 8>(g, s_item);
             } else {
                 const DevOp t = r.t;
                 trsm_item<LOOP_TRSM_SYS, LOOP_THREADS>(t, s_item * LOOP_TRSM_SYS, tsm);
@@ -267,8 +268,16 @@ serve_loop_kernel(LoopState *st, RingSlot *ring, const LoopCtl *ctl)
 }
 
 // ---- host side --------------------------------------------------------------
-// Converts an operation to its loop form; 0 when the loop does not take it.
-int to_loop_req(const gbx_op &o, LoopReq &r)
+// Tiles of a GEMM-core request of m x n (a lower or upper triangle when tri).
+int loop_tiles(int m, int n, bool tri, int tile)
+{
+    const int tm = (m + tile - 1) / tile, tn = (n + tile - 1) / tile;
+    return tri ? tm * (tm + 1) / 2 : tm * tn;
+}
+
+// Converts an operation to its loop form for a loop of `ctas` CTAs; 0 when
+// the loop does not take it.
+int to_loop_req(const gbx_op &o, LoopReq &r, int ctas)
 {
     r = LoopReq{};
     if (o.kind == GBX_OP_GEMM) {
@@ -281,8 +290,10 @@ int to_loop_req(const gbx_op &o, LoopReq &r)
         g.alpha = o.alpha; g.beta = o.beta;
         g.C = o.C; g.ldc = o.ldc;
         g.c_part = C_FULL;
-        g.tiles_m = (o.m + LOOP_TILE - 1) / LOOP_TILE;
-        g.tiles_n = (o.n + LOOP_TILE - 1) / LOOP_TILE;
+        r.small = loop_tiles(o.m, o.n, false, LOOP_TILE) < 2 * ctas;
+        const int tile = r.small ? LOOP_TILE_SMALL : LOOP_TILE;
+        g.tiles_m = (o.m + tile - 1) / tile;
+        g.tiles_n = (o.n + tile - 1) / tile;
         r.kind = LOOP_GEMM;
         r.nitems = g.tiles_m * g.tiles_n;
         return o.m <= LOOP_MAX_MN && o.n <= LOOP_MAX_MN && o.k <= LOOP_MAX_K;
@@ -298,7 +309,9 @@ int to_loop_req(const gbx_op &o, LoopReq &r)
         g.alpha = o.alpha; g.beta = o.beta;
         g.C = o.C; g.ldc = o.ldc;
         g.c_part = gbx_lsame(o.uplo, 'U') ? C_UPPER : C_LOWER;
-        g.tiles_m = g.tiles_n = (o.n + LOOP_TILE - 1) / LOOP_TILE;
+        r.small = loop_tiles(o.n, o.n, true, LOOP_TILE) < 2 * ctas;
+        const int tile = r.small ? LOOP_TILE_SMALL : LOOP_TILE;
+        g.tiles_m = g.tiles_n = (o.n + tile - 1) / tile;
         r.kind = LOOP_GEMM;
         r.nitems = g.tiles_m * (g.tiles_m + 1) / 2;
         return o.n <= LOOP_MAX_MN && o.k <= LOOP_MAX_K;
@@ -374,7 +387,7 @@ gbx_status loop_ensure_running(gbx_loop *l)
 extern "C" int gbx_loop_accepts(const gbx_op *op)
 {
     LoopReq r;
-    return op && to_loop_req(*op, r);
+    return op && to_loop_req(*op, r, 0);
 }
 
 extern "C" gbx_status gbx_loop_create(int device, int ctas, gbx_loop **out)
@@ -412,7 +425,7 @@ extern "C" gbx_status gbx_loop_create(int device, int ctas, gbx_loop **out)
 extern "C" gbx_status gbx_loop_call(gbx_loop *l, const gbx_op *op)
 {
     LoopReq r;
-    if (!l || !op || !to_loop_req(*op, r)) return GBX_ERR_ARG;
+    if (!l || !op || !to_loop_req(*op, r, l->ctas)) return GBX_ERR_ARG;
     cudaSetDevice(l->device);
     const unsigned long long t = l->head.fetch_add(1);
     RingSlot *rs = &l->ring_h[t % LOOP_RING];
