@@ -452,7 +452,7 @@ def run_ours(args):
             achieved = value / ws
         else:
             achieved = work.units * args.steps / (k_ms / 1e3) if k_ms > 0 else None
-        line["roofline"] = {"bound": "fp64", "kernel": "gemm_simt_kernel<double,8,8,8>",
+        line["roofline"] = {"bound": "fp64", "kernel": "gemm_simt_kernel<double,4,4,8>",
                             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                             "frac": achieved / peak if (achieved and peak) else None,
                             "peak_source": "measured in this run: DFMA throughput loop "

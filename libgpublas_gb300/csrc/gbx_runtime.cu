@@ -540,7 +540,8 @@ static gbx_status aux_ready(gbx_ctx *c)
 
 // Block grid for an m x n product: row blocks of op(A) of >= 2048 rows (at
 // most 8) and column panels of >= 1024 columns (at most 8), reduced until
-// every block holds at least 128 tiles of 128 x 128.  Small first blocks keep
+// every block holds at least 128 * 128^2 outputs (512 of the 64 x 64 FP64
+// tiles, more than two per SM).  Small first blocks keep
 // the exposed copy-in short (the host link runs at a few tens of GB/s on
 // some boxes); the two compute streams keep the SMs busy across blocks.
 // Returns 0 when the call is too small to split.

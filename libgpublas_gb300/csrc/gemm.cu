@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <type_traits>
 
 using namespace gbx_gemm;
 
@@ -75,14 +76,17 @@ gbx_status launch_gemm_tile(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
     return gbx_check_launch(ctx, what);
 }
 
-// Tile choice: the largest block tile that still gives every SM two tiles;
-// 128x128 (8x8 per thread) for large problems, 64x64 and 32x32 for the
+// Tile choice: the largest block tile that still gives every SM two tiles,
+// shrinking to 64x64, 32x32 and then 16x16 (one element per thread) for the
 // skinny and small products that DTRSM's recursion and small calls produce
-// (with few large tiles most SMs would idle), and 16x16 (one element per
-// thread) below that: at 2 FP64 lanes per clock per SM a small product's
-// latency is its FMAs per SM, so spreading it over four times the SMs cuts
-// it almost fourfold.  Complex double uses 64x64 / 32x32 (its 8x8 register
-// tile would not fit).
+// (with few large tiles most SMs would idle): at 2 FP64 lanes per clock per
+// SM a small product's latency is its FMAs per SM, so spreading it over four
+// times the SMs cuts it almost fourfold.  Real double starts at 64x64: two
+// CTAs of 124 registers per SM keep the DFMA pipe fed across each CTA's
+// barriers, and DGEMM 8192^3 takes 881 ms against 901 ms with 128x128 tiles
+// (one CTA of 254 registers per SM).  Complex double uses 64x64 / 32x32 (its
+// 8x8 register tile would not fit); float and complex float start at
+// 128x128, whose operand reuse their faster FMA pipe needs.
 template <typename T>
 gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
 {
@@ -93,7 +97,8 @@ gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
         return p.c_part == C_FULL ? tm * tn : tm * (tm + 1) / 2;
     };
     if constexpr (sizeof(T) <= 8) {
-        if (tiles(128) >= want) return launch_gemm_tile<T, 8>(ctx, p, what);
+        if constexpr (!std::is_same<T, double>::value)
+            if (tiles(128) >= want) return launch_gemm_tile<T, 8>(ctx, p, what);
         if (tiles(64) >= want) return launch_gemm_tile<T, 4>(ctx, p, what);
         if (tiles(32) >= want) return launch_gemm_tile<T, 2>(ctx, p, what);
         return launch_gemm_tile<T, 1>(ctx, p, what);

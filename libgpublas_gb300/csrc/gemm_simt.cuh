@@ -4,10 +4,11 @@
 // Measured on GB300: SIMT DFMA sustains about 1.2 TFLOP/s per GPU, the legacy
 // FP64 tensor path (mma.sync.m8n8k4.f64) about 1.05 TFLOP/s, so the plain
 // FP64 GEMM-class routines run on DFMA.  At 2 DFMA lanes per clock per SM the
-// kernel is compute-bound at any sane tile size: a 128x128 block tile with
-// 8x8 register tiles moves 16 KB of operands per 131k FMAs, so operand
-// staging through shared memory with register prefetch is all the memory
-// pipeline needs.
+// kernel is compute-bound at any sane tile size: a 64x64 block tile with
+// 4x4 register tiles moves 8 KB of operands per 32k FMAs, so operand staging
+// through shared memory with register prefetch is all the memory pipeline
+// needs; what counts is keeping the pipe fed across the barriers of each
+// K step, which two resident CTAs per SM do better than one large one.
 //
 // One kernel template serves xGEMM, xSYRK/xHERK and xSYR2K/xHER2K (triangular
 // tile grid), xSYMM/xHEMM (an operand read from one stored triangle), xTRMM

@@ -2,10 +2,11 @@
 benchmarks time.
 
 The GEMM core picks its block tile from the number of output tiles (the
-largest tile that still gives every SM two of them): the 128 x 128 FP64 tile
-(8 x 8 per thread) needs about 2200 rows and columns, the 64 x 64 complex tile
-about 1100, and the Ozaki product takes its 128 x 256 tile once 152 such tiles
-exist (about 2560 x 2560) with K > 1024.  The small shapes of the other test
+largest tile that still gives every SM two of them): the 64 x 64 FP64 tile
+(4 x 4 per thread, the one the DGEMM benchmark times) and the 64 x 64
+complex tile need about 1100 rows and columns, and the Ozaki product takes
+its 128 x 256 tile once 152 such tiles exist (about 2560 x 2560) with
+K > 1024.  The small shapes of the other test
 files never reach those instantiations, so each case here is sized past the
 threshold, with ragged edges (sizes that are not multiples of the tile), odd
 leading dimensions whose padding rows hold a sentinel, and beta != 0.
@@ -70,10 +71,10 @@ def op(x, t):
     return x if t == "N" else x.T
 
 
-# ------------------------------------------------------------ FP64 DGEMM, 128 x 128 tile
+# ------------------------------------------------------------ FP64 DGEMM, 64 x 64 tile
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
 @pytest.mark.parametrize("m,n,k", [(2311, 2305, 129), (2304, 2304, 512)])
-def test_dgemm_128_tile(orc, dev, ta, tb, m, n, k):
+def test_dgemm_large_tile(orc, dev, ta, tb, m, n, k):
     if (m, n, k) == (2304, 2304, 512) and tb == "T":
         pytest.skip("the square case runs NN and TN (the benchmarked forms)")
     ra, ca = (m, k) if ta == "N" else (k, m)
@@ -98,7 +99,7 @@ def test_dgemm_128_tile(orc, dev, ta, tb, m, n, k):
         assert rel(got[:m], full) <= TOL
 
 
-def test_dgemm_128_tile_through_fortran_symbol(orc, f77):
+def test_dgemm_large_tile_through_fortran_symbol(orc, f77):
     # the drop-in path: host operands with an odd leading dimension, staged
     m, n, k = 2400, 2333, 300
     a, s = padded(orc, m, k, 71)
@@ -113,11 +114,11 @@ def test_dgemm_128_tile_through_fortran_symbol(orc, f77):
     assert rel(got[:m], -0.5 * (a[:m] @ b[:k]) + 0.25 * c[:m]) <= TOL
 
 
-# ------------------------------------------------------------ FP64 DSYRK, 128 x 128 tile
+# ------------------------------------------------------------ FP64 DSYRK, 64 x 64 tile
 @pytest.mark.parametrize("uplo", ["L", "U"])
 @pytest.mark.parametrize("trans", ["N", "T"])
-def test_dsyrk_128_tile(orc, dev, uplo, trans):
-    # 26 x 27 / 2 = 351 triangular tiles of 128 (>= 2 per SM)
+def test_dsyrk_large_tile(orc, dev, uplo, trans):
+    # 51 x 52 / 2 = 1326 triangular tiles of 64 (>= 2 per SM)
     n, k = 3201, 300
     ra, ca = (n, k) if trans == "N" else (k, n)
     a, s = padded(orc, ra, ca, 7100 + ord(uplo) + ord(trans))
@@ -140,9 +141,9 @@ def test_dsyrk_128_tile(orc, dev, uplo, trans):
     assert np.array_equal(got[:n][untouched], c[:n][untouched])
 
 
-# ------------------------------------------------------------ FP64 DTRMM on the 128 tile
+# ------------------------------------------------------------ FP64 DTRMM on the 64 tile
 @pytest.mark.parametrize("side,uplo,ta", [("L", "L", "N"), ("R", "U", "T")])
-def test_dtrmm_128_tile(orc, dev, side, uplo, ta):
+def test_dtrmm_large_tile(orc, dev, side, uplo, ta):
     m, n = 2311, 2305
     na = m if side == "L" else n
     a, s = orc.trsm_matrix(na, 7200 + ord(side))
@@ -263,10 +264,10 @@ def test_dsyrk_ozaki_wide(orc, dev, uplo):
     assert np.array_equal(got[untouched], c[untouched])
 
 
-# ------------------------------------------------------------ DTRSM with 128-tile updates
+# ------------------------------------------------------------ DTRSM with 64-tile updates
 def test_dtrsm_large_left_lower(orc, dev):
     # config-2 distribution (diagonal uniform[1,2], off-diagonal
-    # uniform[-1,1]/m); the recursive updates run on the 128 x 128 tile.
+    # uniform[-1,1]/m); the recursive updates run on the 64 x 64 tile.
     # Backward residual of 16 sampled right-hand sides against the
     # double-double oracle, forward error of the same columns against the
     # oracle's substitution.
