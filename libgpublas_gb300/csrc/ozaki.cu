@@ -46,9 +46,8 @@ using namespace gbx_tc;
 namespace {
 
 // Tile: OZ_BM rows by OZ_BN (256) or 128 columns (oz_gemm_kernel<BN>), K in
-// blocks of OZ_BK digits.  OZ_THREADS is the CTA-pair kernel's block.
+// blocks of OZ_BK digits.
 constexpr int OZ_BM = 128, OZ_BN = 256, OZ_BK = 128;
-constexpr int OZ_THREADS = 192;
 constexpr int OZ_SMAX = 14;
 constexpr int OZ_KEXT_MAX = 65536;   // 2^24 / 16^2
 constexpr int OZ_A_BYTES = OZ_BM * OZ_BK;
@@ -666,6 +665,8 @@ oz_prep_small(OzPrepOp a, OzPrepOp b, int planes, int *status)
 struct OzParams {
     int M, N, Mp, Np, Kp;
     int tiles_m, tiles_n;
+    int t_split, nunits;       // wide-tile kernel: units below t_split are whole tiles, the rest
+                               // half tiles (two per tile t_split + (u - t_split) / 2)
     int *S;                    // slice count (written by the small-K kernel, read by the others)
     const int *row_exp;        // Mp: e_i - 4
     const int *col_exp;        // Np: f_j - 4
@@ -843,7 +844,10 @@ __device__ __forceinline__ void oz_report(const OzParams &p)
 
 // Group enumeration shared by the three roles.  Items are (pair, k chunk);
 // a group is a run of consecutive items of one diagonal whose K extent stays
-// within the exact-accumulation bound.
+// within the exact-accumulation bound.  A diagonal of n items is cut into
+// ceil(n / items_per_group) groups of near-equal size (K = 8192: nine items
+// as 5 + 4, not 8 + 1): the MMAs of a short group cannot hide the drain of
+// the group before it, so the tensor pipe waited on every one-item group.
 struct GroupPlan {
     int S, nkb, kch_blocks, nchunks, items_per_group;
     __device__ void init(int S_, int Kp)
@@ -855,6 +859,10 @@ struct GroupPlan {
         nchunks = (nkb + kch_blocks - 1) / kch_blocks;
         items_per_group = max(1, OZ_KEXT_MAX / (kch_blocks * OZ_BK));
     }
+    __device__ int ngroups(int nitems) const { return (nitems + items_per_group - 1) / items_per_group; }
+    // first item of group g of ng (g = ng gives nitems); every group holds at
+    // most ceil(nitems / ng) <= items_per_group items
+    __device__ int gbegin(int nitems, int ng, int g) const { return g * nitems / ng; }
 };
 
 __device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, int bm = OZ_BM, int bn = OZ_BN)
@@ -864,26 +872,8 @@ __device__ __forceinline__ bool tile_needed(const OzParams &p, int tm, int tn, i
     return p.c_part == 1 ? (r1 >= c0) : (r0 <= c1);
 }
 
-// The exact drain (the CTA-pair kernel; the wide-tile kernel uses the
-// Horner drain oz_drain_row_h below): per output element, the diagonal sums
-// D_q (integers, |D_q| < 2^24 per accumulation group, exact in the FP32 TMEM
-// accumulator) are summed exactly as one signed 128-bit integer in units of
-// the last diagonal's weight,
-//     V = sum_q D_q 2^(5(S-1-q)),     C_ij = V 2^(e_i + f_j - 8 - 5(S-1)),
-// held in W (two 64-bit words per element, column-major Mp x Np) between
-// diagonals.  Each diagonal costs a decode of the FP32 value and a 128-bit
-// shift-and-add on the integer pipe per element; the final conversion and
-// scale are integer work too (oz_i128_ldexp), so the FP64 pipe (the scarce
-// one on GB300) sees one multiply-add per element, for beta, and one
-// multiply when alpha is not a power of two.  |V| < 2^(24 + 65 + 14) for
-// S <= 14 and K <= 2^30.
-//
-// One row (grow) and NCOL columns from gcol0 per call, walked in CH-column
-// chunks and software-pipelined: the global loads of chunk c+1 (running
-// sums, and C on the last pass) are issued before chunk c is converted and
-// stored.  Loads and stores are never interleaved element by element: the
-// compiler cannot prove that W and C do not overlap, and a load/add/store
-// per element serialised one L2 round trip per element.
+// Whether element (grow, gcol) of C is written: inside N and, for DSYRK, in
+// the stored triangle.
 __device__ __forceinline__ bool oz_c_keep(const OzParams &p, int grow, int gcol)
 {
     return gcol < p.N && (p.c_part == 0 || (p.c_part == 1 ? grow >= gcol : grow <= gcol));
@@ -895,22 +885,6 @@ template <>
 __device__ __forceinline__ void tmem_ld_chunk<8>(uint32_t taddr, uint32_t (&r)[8]) { tmem_ld_32x32b_x8(taddr, r); }
 template <>
 __device__ __forceinline__ void tmem_ld_chunk<4>(uint32_t taddr, uint32_t (&r)[4]) { tmem_ld_32x32b_x4(taddr, r); }
-
-// d * 2^sh as a signed 128-bit (lo, hi) pair, 0 <= sh <= 70 (sh is uniform
-// across the warp: every lane drains the same diagonal)
-__device__ __forceinline__ void oz_shift128(long long d, int sh, unsigned long long &lo, long long &hi)
-{
-    if (sh == 0) {
-        lo = (unsigned long long)d;
-        hi = d >> 63;
-    } else if (sh < 64) {
-        lo = (unsigned long long)d << sh;
-        hi = d >> (64 - sh);
-    } else {
-        lo = 0ull;
-        hi = d << (sh - 64);
-    }
-}
 
 // V (128-bit) as a double: the exact integer rounded once to 53 bits when it
 // fits 64 bits, else hi * 2^64 + lo (the low word rounded first, within one
@@ -933,6 +907,18 @@ __device__ __forceinline__ double oz_alpha_pow2(double alpha, int e)
     return ldexp(alpha, e);
 }
 
+// An FP32 accumulator value (an integer, so zero or normal) widened to
+// double by re-biasing its exponent field on the integer pipe: the FP32 to
+// FP64 conversion instruction issues to the FP64 pipe, which the Horner
+// step already keeps half busy.  Exact, like the conversion it replaces.
+__device__ __forceinline__ double oz_f32_to_f64(uint32_t b)
+{
+    const unsigned long long mag = b & 0x7FFFFFFFu;
+    const unsigned long long bits =
+        ((unsigned long long)(b & 0x80000000u) << 32) | (mag ? (mag + (896ull << 23)) << 29 : 0ull);
+    return __longlong_as_double((long long)bits);
+}
+
 // FP32 accumulator values are integers.  Float-to-integer conversion
 // instructions issue to the FP64 pipe, which on this part retires two lanes
 // per clock per SM (one drain of a 128 x 32 tile with ten diagonals spent
@@ -943,19 +929,6 @@ __device__ __forceinline__ double oz_alpha_pow2(double alpha, int e)
 __device__ __forceinline__ int oz_f2i22(float v)
 {
     return __float_as_int(__fadd_rn(v, 12582912.0f)) - 0x4B400000;
-}
-
-//   |v| <= 2^24: v = m * 2^(e - 150) with the 24-bit significand m, so a
-//   right shift by 150 - e (a left shift by one for 2^24 itself); zero has
-//   e = 0 and shifts out.
-__device__ __forceinline__ int oz_f2i24(float v)
-{
-    const int b = __float_as_int(v);
-    const int e = (b >> 23) & 0xFF;
-    const unsigned m = ((unsigned)b & 0x7FFFFFu) | 0x800000u;
-    const unsigned mag = e > 150 ? (m << 1) : (m >> min(150 - e, 31));
-    const int s = b >> 31;
-    return ((int)mag ^ s) - s;
 }
 
 // The signed 128-bit integer (hi:lo) times 2^e as a double, rounded to
@@ -1152,83 +1125,6 @@ __device__ __noinline__ double oz_result_split_slow(long long vh, long long vl, 
     return oz_result_split(vh, vl, lsh, e, alpha, as, beta, cold);
 }
 
-template <int NCOL, int CH>
-__device__ __forceinline__ void oz_drain_row(const OzParams &p, uint32_t taddr, int grow, int gcol0, int q, int S,
-                                             int rexp, bool first, bool last)
-{
-    constexpr int NCH = NCOL / CH;
-    const int sh = 5 * (S - 1 - q);
-    const int erow = rexp - 5 * (S - 1);   // scale of V without the column part
-    const bool row_ok = grow < p.M;
-    const bool need_c = last && row_ok && p.beta != 0.0;
-    const longlong2 *wrow = (const longlong2 *)p.W + (size_t)gcol0 * p.Mp + grow;
-    double *crow = p.C + (size_t)gcol0 * p.ldc + grow;
-    longlong2 wn[CH];
-    double cn[CH];
-#pragma unroll
-    for (int j = 0; j < CH; j++) { wn[j] = make_longlong2(0, 0); cn[j] = 0.0; }
-    if (!first) {
-#pragma unroll
-        for (int j = 0; j < CH; j++) wn[j] = __ldcg(wrow + (size_t)j * p.Mp);
-    }
-    if (need_c) {
-#pragma unroll
-        for (int j = 0; j < CH; j++) cn[j] = oz_c_keep(p, grow, gcol0 + j) ? crow[(size_t)j * p.ldc] : 0.0;
-    }
-#pragma unroll 1
-    for (int c = 0; c < NCH; c++) {
-        longlong2 wc[CH];
-        double cc[CH];
-#pragma unroll
-        for (int j = 0; j < CH; j++) { wc[j] = wn[j]; cc[j] = cn[j]; }
-        const int nc = (c + 1) * CH;
-        if (c + 1 < NCH) {
-            if (!first) {
-#pragma unroll
-                for (int j = 0; j < CH; j++) wn[j] = __ldcg(wrow + (size_t)(nc + j) * p.Mp);
-            }
-            if (need_c) {
-#pragma unroll
-                for (int j = 0; j < CH; j++)
-                    cn[j] = oz_c_keep(p, grow, gcol0 + nc + j) ? crow[(size_t)(nc + j) * p.ldc] : 0.0;
-            }
-        }
-        uint32_t r[CH];
-        tmem_ld_chunk<CH>(taddr + (uint32_t)(c * CH), r);
-        tmem_ld_wait();
-        const int cb = c * CH;
-#pragma unroll
-        for (int j = 0; j < CH; j++) {
-            unsigned long long slo;
-            long long shi;
-            oz_shift128((long long)oz_f2i24(__uint_as_float(r[j])), sh, slo, shi);
-            if (first) {
-                wc[j].x = (long long)slo;
-                wc[j].y = shi;
-            } else {
-                const unsigned long long lo = (unsigned long long)wc[j].x + slo;
-                wc[j].y = wc[j].y + shi + (lo < slo ? 1 : 0);
-                wc[j].x = (long long)lo;
-            }
-        }
-        if (!last) {
-            longlong2 *wdst = (longlong2 *)p.W + (size_t)(gcol0 + cb) * p.Mp + grow;
-#pragma unroll
-            for (int j = 0; j < CH; j++) __stcg(wdst + (size_t)j * p.Mp, wc[j]);
-        } else if (row_ok) {
-            const OzAlpha as = oz_alpha_split(p.alpha, need_c ? p.beta : 0.0);
-            const double beta = p.beta;
-#pragma unroll
-            for (int j = 0; j < CH; j++) {
-                const int gcol = gcol0 + cb + j;
-                if (!oz_c_keep(p, grow, gcol)) continue;
-                crow[(size_t)(cb + j) * p.ldc] = oz_result((unsigned long long)wc[j].x, wc[j].y,
-                                                           erow + __ldg(p.col_exp + gcol), p.alpha, as, beta, cc[j]);
-            }
-        }
-    }
-}
-
 // Tile order of the wide-tile kernel: groups of OZ_GROUP_M row tiles, the
 // row tile fastest within a group, so the 152 tiles resident at once form an
 // 8 x 19 block (at 8192^2) instead of all 64 row tiles of two or three
@@ -1246,6 +1142,30 @@ __device__ __forceinline__ void oz_tile_coords(int t, int tiles_m, int tiles_n, 
     tn = r / rows;
 }
 
+// Work unit u of the wide-tile kernel: whole tiles in the grouped order,
+// then the tiles of the last, partial wave cut into two half-width tiles, so
+// that wave runs on twice the SMs for half the time (2048 tiles of 128 x 256
+// on 152 SMs: 13 full waves and one of 144 half tiles instead of a 14th wave
+// of 72 tiles).  col_off: first column of the unit within its tile.
+__device__ __forceinline__ void oz_unit(const OzParams &p, int u, int bn, int &tm, int &tn, int &col_off,
+                                        bool &narrow)
+{
+    int t = u;
+    narrow = u >= p.t_split;
+    col_off = 0;
+    if (narrow) {
+        const int v = u - p.t_split;
+        t = p.t_split + (v >> 1);
+        col_off = (v & 1) * (bn / 2);
+    }
+    oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+}
+
+__device__ __forceinline__ bool oz_unit_needed(const OzParams &p, int tm, int tn, int col_off, bool narrow, int bn)
+{
+    return narrow ? tile_needed(p, tm, 2 * tn + (col_off ? 1 : 0), OZ_BM, bn / 2) : tile_needed(p, tm, tn, OZ_BM, bn);
+}
+
 // Drain of the wide-tile kernel: diagonals arrive in ascending q (largest
 // weight first) and each element's running value is one double, combined by
 // Horner's rule: v = 32 v + D_q at the first accumulation group of diagonal
@@ -1258,6 +1178,13 @@ __device__ __forceinline__ void oz_tile_coords(int t, int tiles_m, int tiles_n, 
 // Horner step rounds once, relative to the partial value, so the result
 // carries about S units of roundoff of |C| -- far below the target error of
 // the slice truncation.
+//
+// One row (grow) and NCOL columns from gcol0 per call, walked in CH-column
+// chunks and software-pipelined: the global loads of chunk c+1 (running
+// values, and C on the last pass) are issued before chunk c is combined and
+// stored.  Loads and stores are never interleaved element by element: the
+// compiler cannot prove that W and C do not overlap, and a load/add/store
+// per element serialised one L2 round trip per element.
 template <int NCOL, int CH>
 __device__ __forceinline__ void oz_drain_row_h(const OzParams &p, uint32_t taddr, int grow, int gcol0, int S,
                                                int rexp, bool first, bool new_diag, bool last)
@@ -1302,7 +1229,7 @@ __device__ __forceinline__ void oz_drain_row_h(const OzParams &p, uint32_t taddr
         const int cb = c * CH;
 #pragma unroll
         for (int j = 0; j < CH; j++) {
-            const double d = (double)__uint_as_float(r[j]);
+            const double d = oz_f32_to_f64(r[j]);
             wc[j] = first ? d : (new_diag ? fma(wc[j], 32.0, d) : wc[j] + d);
         }
         if (!last) {
@@ -1347,7 +1274,8 @@ struct OzCfg {
 
 template <int BN>
 __global__ void __launch_bounds__(OzCfg<BN>::THREADS, 1)
-oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
+oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               const __grid_constant__ CUtensorMap tmBh, OzParams p)
 {
     if (oz_skip_kernel(p)) {
         oz_report(p);
@@ -1371,6 +1299,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         fence_barrier_init();
         prefetch_tmap(&tmA);
         prefetch_tmap(&tmB);
+        prefetch_tmap(&tmBh);
     }
     if (warp == 1) {
         tmem_alloc(tmem_slot, 512);
@@ -1383,7 +1312,6 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 
     GroupPlan gp;
     gp.init(*p.S, p.Kp);
-    const int ntiles = p.tiles_m * p.tiles_n;
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
@@ -1391,10 +1319,13 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                int tm, tn;
-                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-                if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
+            for (int u = blockIdx.x; u < p.nunits && ok; u += gridDim.x) {
+                int tm, tn, col_off;
+                bool narrow;
+                oz_unit(p, u, BN, tm, tn, col_off, narrow);
+                if (!oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
+                const CUtensorMap *mb = narrow ? &tmBh : &tmB;
+                const uint32_t bytes = narrow ? OZ_A_BYTES + Cfg::B_BYTES / 2 : STAGE_BYTES;
                 for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
@@ -1404,9 +1335,10 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         for (int kb = kb0; kb < kb1; kb++) {
                             if (!mbar_wait(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
                             uint8_t *sa = smem + stage * STAGE_BYTES;
-                            mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
+                            mbar_arrive_expect_tx(&full[stage], bytes);
                             tma_load_2d(sa, &tmA, &full[stage], kb * OZ_BK, s * p.Mp + tm * OZ_BM);
-                            tma_load_2d(sa + OZ_A_BYTES, &tmB, &full[stage], kb * OZ_BK, t2 * p.Np + tn * BN);
+                            tma_load_2d(sa + OZ_A_BYTES, mb, &full[stage], kb * OZ_BK,
+                                        t2 * p.Np + tn * BN + col_off);
                             if (++stage == STAGES) { stage = 0; phase ^= 1u; }
                         }
                     }
@@ -1421,20 +1353,22 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_e4m3_f32(OZ_BM, BN);
             int stage = 0, buf = 0;
             uint32_t phase = 0, tphase = 0;
             bool ok = true;
             const uint32_t smem_base = smem_u32(smem);
-            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-                int tm, tn;
-                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-                if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
+            for (int u = blockIdx.x; u < p.nunits && ok; u += gridDim.x) {
+                int tm, tn, col_off;
+                bool narrow;
+                oz_unit(p, u, BN, tm, tn, col_off, narrow);
+                if (!oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
+                const uint32_t idesc = narrow ? idesc_e4m3_f32(OZ_BM, BN / 2) : idesc_e4m3_f32(OZ_BM, BN);
                 for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
-                    for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
-                        const int g1 = min(nitems, g0 + gp.items_per_group);
+                    const int ng = gp.ngroups(nitems);
+                    for (int g = 0; g < ng && ok; g++) {
+                        const int g0 = gp.gbegin(nitems, ng, g), g1 = gp.gbegin(nitems, ng, g + 1);
                         if (!mbar_wait(&tempty[buf], tphase ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
                         tc_fence_after();
                         const uint32_t d_tmem = tmem_base + (uint32_t)(buf * BN);
@@ -1468,31 +1402,39 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     } else {
         // ---------------- drain (warps 2..9) ----------------
         const int quarter = warp & 3;               // TMEM lane window of this warp
-        const int half = (warp - 2) >> 2;           // which half of the tile's columns
+        const int half = (warp - 2) >> 2;           // which half of the unit's columns
         const int row = quarter * 32 + lane;
         int buf = 0;
         uint32_t tphase = 0;
         bool ok = true;
-        for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-            int tm, tn;
-                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-            if (!tile_needed(p, tm, tn, OZ_BM, BN)) continue;
+        for (int u = blockIdx.x; u < p.nunits && ok; u += gridDim.x) {
+            int tm, tn, col_off;
+            bool narrow;
+            oz_unit(p, u, BN, tm, tn, col_off, narrow);
+            if (!oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
+            const int dcols = narrow ? Cfg::DRAIN_COLS / 2 : Cfg::DRAIN_COLS;
             const int grow = tm * OZ_BM + row;
             const int rexp = p.row_exp[grow];
             bool first = true;
             for (int q = 0; q < gp.S && ok; q++) {
                 const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                 const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
-                for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
-                    const bool last = (q == gp.S - 1) && (g0 + gp.items_per_group >= nitems);
+                const int ng = gp.ngroups(nitems);
+                for (int g = 0; g < ng && ok; g++) {
+                    const bool last = (q == gp.S - 1) && (g == ng - 1);
                     // warp-uniform outcome: tcgen05.ld below is .sync.aligned
                     ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], tphase, status, TC_TIMEOUT_TMEM_FULL));
                     if (!ok) break;
                     tc_fence_after();
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) +
-                                           (uint32_t)(buf * BN + half * Cfg::DRAIN_COLS);
-                    oz_drain_row_h<Cfg::DRAIN_COLS, Cfg::DRAIN_CH>(p, taddr, grow, tn * BN + half * Cfg::DRAIN_COLS,
-                                                                   gp.S, rexp, first, g0 == 0, last);
+                                           (uint32_t)(buf * BN + half * dcols);
+                    const int gcol0 = tn * BN + col_off + half * dcols;
+                    if (narrow)
+                        oz_drain_row_h<Cfg::DRAIN_COLS / 2, Cfg::DRAIN_CH>(p, taddr, grow, gcol0, gp.S, rexp, first,
+                                                                          g == 0, last);
+                    else
+                        oz_drain_row_h<Cfg::DRAIN_COLS, Cfg::DRAIN_CH>(p, taddr, grow, gcol0, gp.S, rexp, first,
+                                                                      g == 0, last);
                     tc_fence_before();
                     mbar_arrive(&tempty[buf]);
                     first = false;
@@ -1885,21 +1827,26 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 // computes a 256x256 tile with M=256 MMAs issued by the even CTA.  Each CTA
 // loads its own 128 rows of the A slice and its own 128 rows of the B slice
 // (half of N), so every SM moves 32 KB per k-block instead of 48 KB for the
-// same tensor work, and six stages fit in shared memory.  Each CTA's TMEM
-// holds its 128 rows x 256 columns of the accumulator; both CTAs drain their
-// own half in the epilogue.
+// same tensor work, and seven stages fit in shared memory.  Each CTA's TMEM
+// holds its 128 rows x 256 columns of the accumulator (two buffers); eight
+// drain warps per CTA take them as the one-CTA kernel does (two warps per
+// TMEM lane quarter, each half of the columns), with the same Horner drain,
+// diagonals in ascending order and the same grouped tile order.
 //   full[s]   (even CTA): both producers arrive + expect 32 KB each; both
 //             CTAs' TMA loads complete on it (cta_group::2 TMA)
 //   empty[s]  (each CTA): arrived by the MMA commit, multicast to both CTAs
 //   tfull[b]  (each CTA): arrived by the MMA commit, multicast to both CTAs
-//   tempty[b] (even CTA): 256 epilogue threads of both CTAs arrive
+//   tempty[b] (even CTA): the 512 drain threads of both CTAs arrive
 // ---------------------------------------------------------------------------
-constexpr int OZ2_BM = 256, OZ2_STAGES = 6;
+constexpr int OZ2_BM = 256, OZ2_STAGES = 7;
 constexpr int OZ2_HALF = 128 * OZ_BK;                // 16 KB: 128 rows x 128 bytes
 constexpr int OZ2_STAGE_BYTES = 2 * OZ2_HALF;        // A half + B half
+constexpr int OZ2_EPI_WARPS = 8;
+constexpr int OZ2_THREADS = 64 + 32 * OZ2_EPI_WARPS;
 constexpr size_t OZ2_SMEM = (size_t)OZ2_STAGES * OZ2_STAGE_BYTES + 1024 + 256;
+static_assert(OZ2_SMEM <= 227 * 1024, "CTA-pair stages must fit the opt-in shared memory");
 
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(OZ_THREADS, 1)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(OZ2_THREADS, 1)
 oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
 {
     if (oz_skip_kernel(p)) {
@@ -1920,7 +1867,7 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < OZ2_STAGES; i++) { mbar_init(&full[i], 2); mbar_init(&empty[i], 1); }
-        for (int i = 0; i < 2; i++) { mbar_init(&tfull[i], 1); mbar_init(&tempty[i], 256); }
+        for (int i = 0; i < 2; i++) { mbar_init(&tfull[i], 1); mbar_init(&tempty[i], 2 * 32 * OZ2_EPI_WARPS); }
         fence_barrier_init();
         prefetch_tmap(&tmA);
         prefetch_tmap(&tmB);
@@ -1948,9 +1895,10 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
             uint32_t phase = 0;
             bool ok = true;
             for (int t = pair; t < ntiles && ok; t += npairs) {
-                const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+                int tm, tn;
+                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
                 if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
-                for (int q = gp.S - 1; q >= 0 && ok; q--) {
+                for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
                     for (int it = 0; it < nitems && ok; it++) {
@@ -1984,13 +1932,15 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
             bool ok = true;
             const uint32_t smem_base = smem_u32(smem);
             for (int t = pair; t < ntiles && ok; t += npairs) {
-                const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+                int tm, tn;
+                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
                 if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
-                for (int q = gp.S - 1; q >= 0 && ok; q--) {
+                for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
-                    for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
-                        const int g1 = min(nitems, g0 + gp.items_per_group);
+                    const int ng = gp.ngroups(nitems);
+                    for (int g = 0; g < ng && ok; g++) {
+                        const int g0 = gp.gbegin(nitems, ng, g), g1 = gp.gbegin(nitems, ng, g + 1);
                         if (!mbar_wait_cl(&tempty[buf], tphase ^ 1u, status, TC_TIMEOUT_TMEM_EMPTY)) { ok = false; break; }
                         tc_fence_after();
                         const uint32_t d_tmem = tmem_base + (uint32_t)(buf * OZ_BN);
@@ -2002,11 +1952,11 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
                                 if (!mbar_wait_cl(&full[stage], phase, status, TC_TIMEOUT_FULL)) { ok = false; break; }
                                 tc_fence_after();
                                 const uint32_t a_addr = smem_base + stage * OZ2_STAGE_BYTES;
-                                const uint32_t b_addr = a_addr + OZ2_HALF;
+                                const uint64_t a_d = smem_desc_k128(a_addr);
+                                const uint64_t b_d = smem_desc_k128(a_addr + OZ2_HALF);
 #pragma unroll
                                 for (int kk = 0; kk < OZ_BK / 32; kk++) {
-                                    mma_f8f6f4_pair(d_tmem, smem_desc_k128(a_addr + kk * 32),
-                                                    smem_desc_k128(b_addr + kk * 32), idesc, acc);
+                                    mma_f8f6f4_pair(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, acc);
                                     acc = 1;
                                 }
                                 mma_commit_pair_mc(&empty[stage], (uint16_t)(3u << leader_rank));
@@ -2020,8 +1970,9 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
             }
         }
     } else {
-        // ---------------- epilogue (warps 2..5, both CTAs) ----------------
-        const int quarter = warp & 3;
+        // ---------------- drain (warps 2..9, both CTAs) ----------------
+        const int quarter = warp & 3;               // TMEM lane window of this warp
+        const int half = (warp - 2) >> 2;           // which half of the tile's columns
         const int row = quarter * 32 + lane;
         int buf = 0;
         uint32_t tphase = 0;
@@ -2029,21 +1980,26 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         const uint32_t tempty_cl0 = mapa_cluster(smem_u32(&tempty[0]), leader_rank);
         const uint32_t tempty_cl1 = mapa_cluster(smem_u32(&tempty[1]), leader_rank);
         for (int t = pair; t < ntiles && ok; t += npairs) {
-            const int tm = t % p.tiles_m, tn = t / p.tiles_m;
+            int tm, tn;
+            oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
             if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
             const int grow = tm * OZ2_BM + (int)(rank & 1u) * 128 + row;
             const int rexp = p.row_exp[grow];
             bool first = true;
-            for (int q = gp.S - 1; q >= 0 && ok; q--) {
+            for (int q = 0; q < gp.S && ok; q++) {
                 const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                 const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
-                for (int g0 = 0; g0 < nitems && ok; g0 += gp.items_per_group) {
-                    const bool last = (q == 0) && (g0 + gp.items_per_group >= nitems);
+                const int ng = gp.ngroups(nitems);
+                for (int g = 0; g < ng && ok; g++) {
+                    const bool last = (q == gp.S - 1) && (g == ng - 1);
+                    // warp-uniform outcome: tcgen05.ld below is .sync.aligned
                     ok = __all_sync(0xffffffffu, mbar_wait_cl(&tfull[buf], tphase, status, TC_TIMEOUT_TMEM_FULL));
                     if (!ok) break;
                     tc_fence_after();
-                    const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * OZ_BN);
-                    oz_drain_row<OZ_BN, 8>(p, taddr, grow, tn * OZ_BN, q, gp.S, rexp, first, last);
+                    const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) +
+                                           (uint32_t)(buf * OZ_BN + half * (OZ_BN / 2));
+                    oz_drain_row_h<OZ_BN / 2, 8>(p, taddr, grow, tn * OZ_BN + half * (OZ_BN / 2), gp.S, rexp, first,
+                                                 g == 0, last);
                     tc_fence_before();
                     mbar_arrive_cluster(buf ? tempty_cl1 : tempty_cl0);
                     first = false;
@@ -2373,16 +2329,25 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     }
     gbx_timer_end(ctx);
 
-    CUtensorMap tmA, tmB;
-    // small K: op(B)^T's planes as a 3-D map, the B stage of a tile in one load
+    CUtensorMap tmA, tmB, tmBh;
+    // small K: op(B)^T's planes as a 3-D map, the B stage of a tile in one load;
+    // wide tiles: also a half-width B box for the half tiles of the last wave
+    const bool wide = !small_k && !pair;
     if (!make_map(&tmA, b.A8, (long long)OZ_SMAX * Mp, Kp, OZ_BM) ||
         !(small_k ? make_map(&tmB, B8, Np, Kp, -(bn * 256 + planes))
-                  : make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : bn)))
+                  : make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : bn)) ||
+        (wide && !make_map(&tmBh, B8, (long long)OZ_SMAX * Np, Kp, bn / 2)))
         return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
 
     OzParams p{};
     p.M = pr.M; p.N = pr.N; p.Mp = Mp; p.Np = Np; p.Kp = Kp;
     p.tiles_m = Mp / (pair ? OZ2_BM : OZ_BM); p.tiles_n = Np / bn;
+    {
+        // wide tiles: a last wave filling at most half the SMs runs as half tiles
+        const int nt = p.tiles_m * p.tiles_n, g = std::min(nt, gbx_ctx_sms(ctx)), r = nt % g;
+        p.t_split = (wide && r > 0 && 2 * r <= g) ? nt - r : nt;
+        p.nunits = p.t_split + 2 * (nt - p.t_split);
+    }
     p.S = b.S;
     p.row_exp = b.rsa;
     p.col_exp = csb;
@@ -2429,7 +2394,7 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
             // how many CTA pairs can be resident at once (clusters must fit in a GPC)
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(2 * (unsigned)std::max(1, gbx_ctx_sms(ctx) / 2));
-            cfg.blockDim = dim3(OZ_THREADS);
+            cfg.blockDim = dim3(OZ2_THREADS);
             cfg.dynamicSmemBytes = OZ2_SMEM;
             int nc = 0;
             if (cudaOccupancyMaxActiveClusters(&nc, oz_gemm2_kernel, &cfg) != cudaSuccess || nc < 1) {
@@ -2444,7 +2409,7 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     gbx_timer_begin(ctx, GBX_TIMER_OZAKI_MMA);
     if (pair) {
         const int npairs = std::max(1, std::min(ntiles, max_pairs));
-        oz_gemm2_kernel<<<2 * npairs, OZ_THREADS, OZ2_SMEM, s>>>(tmA, tmB, p);
+        oz_gemm2_kernel<<<2 * npairs, OZ2_THREADS, OZ2_SMEM, s>>>(tmA, tmB, p);
     } else {
         const int grid = std::min(ntiles, gbx_ctx_sms(ctx));
         if (small_k) {
@@ -2466,9 +2431,9 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
                 return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki gemm: %s", cudaGetErrorString(le));
             }
         } else if (bn == 128)
-            oz_gemm_kernel<128><<<grid, OzCfg<128>::THREADS, OzCfg<128>::SMEM, s>>>(tmA, tmB, p);
+            oz_gemm_kernel<128><<<grid, OzCfg<128>::THREADS, OzCfg<128>::SMEM, s>>>(tmA, tmB, tmBh, p);
         else
-            oz_gemm_kernel<256><<<grid, OzCfg<256>::THREADS, OzCfg<256>::SMEM, s>>>(tmA, tmB, p);
+            oz_gemm_kernel<256><<<grid, OzCfg<256>::THREADS, OzCfg<256>::SMEM, s>>>(tmA, tmB, tmBh, p);
     }
     gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);

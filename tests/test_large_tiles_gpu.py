@@ -225,6 +225,49 @@ def test_dgemm_ozaki_wide_256_tile_ragged(orc, dev, ta, tb):
     assert rel(got[:m], full) <= TOL
 
 
+# ------------------------------------------------------------ Ozaki, half tiles in the last wave
+@pytest.mark.parametrize("m,n,k", [(4000, 2500, 1500), (2048, 1536, 1100)])
+def test_dgemm_ozaki_half_tile_tail(orc, dev, m, n, k):
+    # A last wave that would fill at most half the SMs runs as half-width
+    # tiles: 4000 x 2500 is 32 x 10 = 320 tiles of 128 x 256, the 16 left
+    # after two waves of 152 run as 32 tiles of 128 x 128 (ragged in M and
+    # N); 2048 x 1536 takes 128-wide tiles (16 x 12 = 192), the 40 left run
+    # as 80 tiles of 128 x 64.  Every entry against an FP64 host product,
+    # sampled entries (edges included) against the double-double oracle.
+    a, s = orc.matrix(m, k, 7450 + n)
+    b, s = orc.matrix(k, n, s)
+    c, _ = orc.matrix(m, n, s)
+    C = to_dev(c)
+    dev.dgemm_ozaki("N", "N", m, n, k, 0.75, to_dev(a), m, to_dev(b), k, -0.5, C, m)
+    dev.sync()
+    got = from_dev(C, m, n)
+    assert rel(got, 0.75 * (a @ b) - 0.5 * c) <= TOL
+    rows, cols = samples(m, n, 2048, 7451 + n)
+    ref = orc.dgemm_dd_sample("N", "N", k, 0.75, a, b, -0.5, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL_OZ
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_dsyrk_ozaki_half_tile_tail(orc, dev, uplo):
+    # 18 x 9 = 162 tiles of 128 x 256 over the whole square; the 10 left
+    # after one wave run as half tiles, those outside the triangle skipped
+    n, k = 2304, 1536
+    a, s = orc.matrix(n, k, 7720 + ord(uplo))
+    c, _ = orc.matrix(n, n, s)
+    C = to_dev(c)
+    dev.dsyrk_ozaki(uplo, "N", n, k, -1.0, to_dev(a), n, 1.0, C, n)
+    dev.sync()
+    got = from_dev(C, n, n)
+    lower = uplo == "L"
+    keep = np.tril(np.ones((n, n), bool)) if lower else np.triu(np.ones((n, n), bool))
+    full = -(a @ a.T) + c
+    assert rel(got[keep], full[keep]) <= TOL
+    assert np.array_equal(got[~keep], c[~keep])
+    rows, cols = samples(n, n, 2048, 7721, lower=lower)
+    ref = orc.dgemm_dd_sample("N", "T", k, -1.0, a, a, 1.0, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL_OZ
+
+
 @pytest.mark.parametrize("spread", [0, 8])
 def test_zgemm_ozaki_wide_256_tile(orc, dev, spread):
     # complex K = 1024 is a real product of K = 2048 on the wide tile
