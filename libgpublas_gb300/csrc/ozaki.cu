@@ -27,7 +27,10 @@
 // loads of 128x128-byte (A) and BNx128-byte (B, BN = 256 or 128) slice tiles
 // into a shared-memory ring; warp 1 allocates all 512 TMEM columns and
 // issues the tcgen05.mma.kind::f8f6f4 (M=128, N=BN, K=32) into one of
-// 512/BN accumulators; warps 2-9 drain the others.
+// 512/BN accumulators; warps 2-9 drain the others.  Large full products run
+// in clusters of two CTAs on vertically adjacent tiles that multicast their
+// shared B tile to each other, and the tiles of a last wave that would fill
+// at most half the SMs run as half-width tiles.
 #include "gbx_internal.h"
 #include "gemm_host.h"
 #include "tc_ptx.cuh"
@@ -1146,9 +1149,11 @@ __device__ __forceinline__ void oz_tile_coords(int t, int tiles_m, int tiles_n, 
 // then the tiles of the last, partial wave cut into two half-width tiles, so
 // that wave runs on twice the SMs for half the time (2048 tiles of 128 x 256
 // on 152 SMs: 13 full waves and one of 144 half tiles instead of a 14th wave
-// of 72 tiles).  col_off: first column of the unit within its tile.
-__device__ __forceinline__ void oz_unit(const OzParams &p, int u, int bn, int &tm, int &tn, int &col_off,
-                                        bool &narrow)
+// of 72 tiles).  With B multicast (mrows = 2) a unit is a pair of vertically
+// adjacent tiles and CTA rank r of the cluster takes row tile 2 tm + r.
+// col_off: first column of the unit within its column tile.
+__device__ __forceinline__ void oz_unit(const OzParams &p, int u, int bn, int mrows, int rank, int &tm, int &tn,
+                                        int &col_off, bool &narrow)
 {
     int t = u;
     narrow = u >= p.t_split;
@@ -1158,7 +1163,8 @@ __device__ __forceinline__ void oz_unit(const OzParams &p, int u, int bn, int &t
         t = p.t_split + (v >> 1);
         col_off = (v & 1) * (bn / 2);
     }
-    oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+    oz_tile_coords(t, p.tiles_m / mrows, p.tiles_n, tm, tn);
+    tm = tm * mrows + rank;
 }
 
 __device__ __forceinline__ bool oz_unit_needed(const OzParams &p, int tm, int tn, int col_off, bool narrow, int bn)
@@ -1253,12 +1259,20 @@ __device__ __forceinline__ void oz_drain_row_h(const OzParams &p, uint32_t taddr
     }
 }
 
-// 1-CTA kernel, BM = 128 rows by BN = 256 or 128 columns.  Warp 0 issues the
-// TMA loads, warp 1 the MMAs, warps 2..9 drain: two warps per TMEM lane
-// quarter (a warp may only read the 32 TMEM lanes of its rank within its
-// warpgroup), each taking half of the tile's columns.  TMEM holds 512/BN
-// accumulator buffers, so the MMAs run up to that many diagonal groups ahead
-// of the drain.
+// 1-CTA MMA kernel, BM = 128 rows by BN = 256 or 128 columns.  Warp 0
+// issues the TMA loads, warp 1 the MMAs, warps 2..9 drain: two warps per
+// TMEM lane quarter (a warp may only read the 32 TMEM lanes of its rank
+// within its warpgroup), each taking half of the tile's columns.  TMEM holds
+// 512/BN accumulator buffers, so the MMAs run up to that many diagonal
+// groups ahead of the drain.
+//
+// MC (B multicast): CTAs run in clusters of two on vertically adjacent
+// tiles that share their B slice tile.  Each CTA loads its own A tile and
+// half of the B tile, multicast into both CTAs' shared memory, so an SM
+// pulls 32 KB from L2 per K step instead of 48 KB; the tensor pipe of the
+// one-CTA form waited on its loads about 30 % of the time.  A stage is free
+// again once both CTAs' MMAs have read it (each MMA commit arrives on both
+// CTAs' empty barrier).
 template <int BN>
 struct OzCfg {
     static constexpr int NBUF = 512 / BN;
@@ -1272,7 +1286,7 @@ struct OzCfg {
     static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 };
 
-template <int BN>
+template <int BN, bool MC>
 __global__ void __launch_bounds__(OzCfg<BN>::THREADS, 1)
 oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                const __grid_constant__ CUtensorMap tmBh, OzParams p)
@@ -1283,6 +1297,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     }
     using Cfg = OzCfg<BN>;
     constexpr int STAGES = Cfg::STAGES, NBUF = Cfg::NBUF, STAGE_BYTES = Cfg::STAGE_BYTES;
+    constexpr int MROWS = MC ? 2 : 1;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(smem + STAGES * STAGE_BYTES);
@@ -1291,10 +1306,13 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     uint32_t *tmem_slot = (uint32_t *)(tempty + NBUF);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rank = MC ? (int)(cluster_ctarank() & 1u) : 0;
+    const int unit0 = MC ? (int)blockIdx.x >> 1 : (int)blockIdx.x;
+    const int ustep = MC ? (int)gridDim.x >> 1 : (int)gridDim.x;
     volatile int *status = p.status;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < STAGES; i++) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
+        for (int i = 0; i < STAGES; i++) { mbar_init(&full[i], 1); mbar_init(&empty[i], MROWS); }
         for (int i = 0; i < NBUF; i++) { mbar_init(&tfull[i], 1); mbar_init(&tempty[i], 32 * Cfg::EPI_WARPS); }
         fence_barrier_init();
         prefetch_tmap(&tmA);
@@ -1307,6 +1325,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     }
     tc_fence_before();
     __syncthreads();
+    if (MC) cluster_sync();   // the peer's barriers are initialised before any multicast reaches them
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
 
@@ -1319,13 +1338,15 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
-            for (int u = blockIdx.x; u < p.nunits && ok; u += gridDim.x) {
+            for (int u = unit0; u < p.nunits && ok; u += ustep) {
                 int tm, tn, col_off;
                 bool narrow;
-                oz_unit(p, u, BN, tm, tn, col_off, narrow);
-                if (!oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
+                oz_unit(p, u, BN, MROWS, rank, tm, tn, col_off, narrow);
+                if (!MC && !oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
                 const CUtensorMap *mb = narrow ? &tmBh : &tmB;
-                const uint32_t bytes = narrow ? OZ_A_BYTES + Cfg::B_BYTES / 2 : STAGE_BYTES;
+                const int bytes = OZ_A_BYTES + (narrow ? Cfg::B_BYTES / 2 : Cfg::B_BYTES);
+                // with MC each CTA brings this share of the unit's B rows to both CTAs
+                const int b_rows = (narrow ? BN / 2 : BN) / MROWS;
                 for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
@@ -1335,16 +1356,21 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         for (int kb = kb0; kb < kb1; kb++) {
                             if (!mbar_wait(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
                             uint8_t *sa = smem + stage * STAGE_BYTES;
-                            mbar_arrive_expect_tx(&full[stage], bytes);
+                            mbar_arrive_expect_tx(&full[stage], (uint32_t)bytes);
                             tma_load_2d(sa, &tmA, &full[stage], kb * OZ_BK, s * p.Mp + tm * OZ_BM);
-                            tma_load_2d(sa + OZ_A_BYTES, mb, &full[stage], kb * OZ_BK,
-                                        t2 * p.Np + tn * BN + col_off);
+                            if (MC)
+                                tma_load_2d_mc(sa + OZ_A_BYTES + rank * b_rows * OZ_BK, mb, &full[stage], kb * OZ_BK,
+                                               t2 * p.Np + tn * BN + col_off + rank * b_rows, (uint16_t)3u);
+                            else
+                                tma_load_2d(sa + OZ_A_BYTES, mb, &full[stage], kb * OZ_BK,
+                                            t2 * p.Np + tn * BN + col_off);
                             if (++stage == STAGES) { stage = 0; phase ^= 1u; }
                         }
                     }
                 }
             }
-            // drain: wait (bounded) until every issued load has landed
+            // drain: wait (bounded) until every issued load has landed and, with
+            // MC, both CTAs' MMAs are done with every stage
             for (int i = 0; i < STAGES; i++) {
                 mbar_wait(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY);
                 if (++stage == STAGES) { stage = 0; phase ^= 1u; }
@@ -1357,11 +1383,11 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             uint32_t phase = 0, tphase = 0;
             bool ok = true;
             const uint32_t smem_base = smem_u32(smem);
-            for (int u = blockIdx.x; u < p.nunits && ok; u += gridDim.x) {
+            for (int u = unit0; u < p.nunits && ok; u += ustep) {
                 int tm, tn, col_off;
                 bool narrow;
-                oz_unit(p, u, BN, tm, tn, col_off, narrow);
-                if (!oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
+                oz_unit(p, u, BN, MROWS, rank, tm, tn, col_off, narrow);
+                if (!MC && !oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
                 const uint32_t idesc = narrow ? idesc_e4m3_f32(OZ_BM, BN / 2) : idesc_e4m3_f32(OZ_BM, BN);
                 for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
@@ -1389,7 +1415,8 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                                     mma_f8f6f4(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, acc);
                                     acc = 1;
                                 }
-                                mma_commit(&empty[stage]);
+                                if (MC) mma_commit_mc(&empty[stage], (uint16_t)3u);
+                                else mma_commit(&empty[stage]);
                                 if (++stage == STAGES) { stage = 0; phase ^= 1u; }
                             }
                         }
@@ -1407,11 +1434,11 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         int buf = 0;
         uint32_t tphase = 0;
         bool ok = true;
-        for (int u = blockIdx.x; u < p.nunits && ok; u += gridDim.x) {
+        for (int u = unit0; u < p.nunits && ok; u += ustep) {
             int tm, tn, col_off;
             bool narrow;
-            oz_unit(p, u, BN, tm, tn, col_off, narrow);
-            if (!oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
+            oz_unit(p, u, BN, MROWS, rank, tm, tn, col_off, narrow);
+            if (!MC && !oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
             const int dcols = narrow ? Cfg::DRAIN_COLS / 2 : Cfg::DRAIN_COLS;
             const int grow = tm * OZ_BM + row;
             const int rexp = p.row_exp[grow];
@@ -1446,6 +1473,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 
     tc_fence_before();
     __syncthreads();
+    if (MC) cluster_sync();   // no CTA leaves while its peer may still write to it
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem_base, 512);
@@ -2126,6 +2154,53 @@ bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int bo
     return true;
 }
 
+// B multicast between cluster pairs of the wide-tile kernel is the default;
+// GBX_OZAKI_MC=0 turns it off.
+bool oz_use_mc()
+{
+    static int env = [] {
+        const char *s = getenv("GBX_OZAKI_MC");
+        return s ? atoi(s) : 1;
+    }();
+    return env != 0;
+}
+
+// Clusters of two of the wide-tile kernel resident at once on the context's
+// device (clusters must fit in a GPC), once per device and tile width; the
+// shared-memory attribute of the cluster instantiations is set then too.
+int oz_mc_clusters(gbx_ctx *ctx, int bn)
+{
+    static std::mutex mu;
+    static int cached[64][2] = {};
+    const int dev = gbx_ctx_device(ctx), w = bn == 128 ? 0 : 1;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && cached[dev][w]) return cached[dev][w];
+    const void *fn = bn == 128 ? (const void *)oz_gemm_kernel<128, true> : (const void *)oz_gemm_kernel<256, true>;
+    const int smem = (int)(bn == 128 ? OzCfg<128>::SMEM : OzCfg<256>::SMEM);
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * (unsigned)std::max(1, gbx_ctx_sms(ctx) / 2));
+    cfg.blockDim = dim3(bn == 128 ? OzCfg<128>::THREADS : OzCfg<256>::THREADS);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, fn, &cfg) != cudaSuccess || nc < 1) {
+        cudaGetLastError();
+        nc = gbx_ctx_sms(ctx) / 2;
+    }
+    if (dev >= 0 && dev < 64) cached[dev][w] = nc;
+    return nc;
+}
+
 // The CTA-pair kernel is selected with GBX_OZAKI_PAIR=1 for problems with
 // more than one 128-row tile of op(A).  It is correct but measured slower
 // than the one-CTA kernel at n = 8192 (43 ms vs 30 ms of MMA time), so the
@@ -2271,6 +2346,10 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
                            : oz_tile_n(pr.M, pr.N, gbx_ctx_sms(ctx), pair);
     const int Mp = (int)rup(pr.M, pair ? OZ2_BM : OZ_BM), Np = (int)rup(pr.N, bn);
     const int Kp = (int)rup(std::max(pr.K, 1), OZ_BK);
+    // wide tiles in clusters of two sharing (multicasting) their B tile: full
+    // products whose row tiles pair up and that fill every SM at least twice
+    const bool mc = !small_k && !pair && pr.c_part == 0 && (Mp / OZ_BM) % 2 == 0 && oz_use_mc() &&
+                    (long long)(Mp / OZ_BM) * (Np / bn) >= 2LL * gbx_ctx_sms(ctx);
     if (tol <= 0.0) tol = 1e-14;
     // small K: the digit planes to prepare, the largest S the tolerance can
     // call for (gamma <= 2 sqrt(K) per operand in the slice-count model)
@@ -2335,16 +2414,21 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     const bool wide = !small_k && !pair;
     if (!make_map(&tmA, b.A8, (long long)OZ_SMAX * Mp, Kp, OZ_BM) ||
         !(small_k ? make_map(&tmB, B8, Np, Kp, -(bn * 256 + planes))
-                  : make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : bn)) ||
-        (wide && !make_map(&tmBh, B8, (long long)OZ_SMAX * Np, Kp, bn / 2)))
+                  : make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : (mc ? bn / 2 : bn))) ||
+        (wide && !make_map(&tmBh, B8, (long long)OZ_SMAX * Np, Kp, mc ? bn / 4 : bn / 2)))
         return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
 
     OzParams p{};
     p.M = pr.M; p.N = pr.N; p.Mp = Mp; p.Np = Np; p.Kp = Kp;
     p.tiles_m = Mp / (pair ? OZ2_BM : OZ_BM); p.tiles_n = Np / bn;
+    int mc_clusters = 0;
     {
-        // wide tiles: a last wave filling at most half the SMs runs as half tiles
-        const int nt = p.tiles_m * p.tiles_n, g = std::min(nt, gbx_ctx_sms(ctx)), r = nt % g;
+        // wide tiles: a last wave filling at most half the SMs (cluster pairs
+        // with B multicast) runs as half tiles
+        const int per = mc ? 2 : 1;
+        if (mc && (mc_clusters = oz_mc_clusters(ctx, bn)) < 1) return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: clusters");
+        const int nt = p.tiles_m / per * p.tiles_n;
+        const int g = std::min(nt, mc ? mc_clusters : gbx_ctx_sms(ctx)), r = nt % g;
         p.t_split = (wide && r > 0 && 2 * r <= g) ? nt - r : nt;
         p.nunits = p.t_split + 2 * (nt - p.t_split);
     }
@@ -2384,9 +2468,9 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
                                      (int)OZS_SMEM) != cudaSuccess ||
                 cudaFuncSetAttribute(oz_gemm_sk_kernel<OZS_BN / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OZS_SMEM) != cudaSuccess ||
-                cudaFuncSetAttribute(oz_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                cudaFuncSetAttribute(oz_gemm_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OzCfg<256>::SMEM) != cudaSuccess ||
-                cudaFuncSetAttribute(oz_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                cudaFuncSetAttribute(oz_gemm_kernel<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OzCfg<128>::SMEM) != cudaSuccess ||
                 cudaFuncSetAttribute(oz_gemm2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)OZ2_SMEM) != cudaSuccess)
@@ -2430,10 +2514,29 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
                 cudaGetLastError();
                 return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki gemm: %s", cudaGetErrorString(le));
             }
+        } else if (mc) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(2 * (unsigned)std::min(p.nunits, mc_clusters));
+            cfg.blockDim = dim3(bn == 128 ? OzCfg<128>::THREADS : OzCfg<256>::THREADS);
+            cfg.dynamicSmemBytes = bn == 128 ? OzCfg<128>::SMEM : OzCfg<256>::SMEM;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = 2;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            const cudaError_t le = bn == 128 ? cudaLaunchKernelEx(&cfg, oz_gemm_kernel<128, true>, tmA, tmB, tmBh, p)
+                                             : cudaLaunchKernelEx(&cfg, oz_gemm_kernel<256, true>, tmA, tmB, tmBh, p);
+            if (le != cudaSuccess) {
+                cudaGetLastError();
+                return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki gemm: %s", cudaGetErrorString(le));
+            }
         } else if (bn == 128)
-            oz_gemm_kernel<128><<<grid, OzCfg<128>::THREADS, OzCfg<128>::SMEM, s>>>(tmA, tmB, tmBh, p);
+            oz_gemm_kernel<128, false><<<grid, OzCfg<128>::THREADS, OzCfg<128>::SMEM, s>>>(tmA, tmB, tmBh, p);
         else
-            oz_gemm_kernel<256><<<grid, OzCfg<256>::THREADS, OzCfg<256>::SMEM, s>>>(tmA, tmB, tmBh, p);
+            oz_gemm_kernel<256, false><<<grid, OzCfg<256>::THREADS, OzCfg<256>::SMEM, s>>>(tmA, tmB, tmBh, p);
     }
     gbx_timer_end(ctx);
     gbx_count_launch(ctx, 1);

@@ -155,6 +155,30 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar)
                  : "memory");
 }
 
+// Arrive (once) on the mbarrier at the same offset in every CTA of cta_mask
+// (a cluster) when all previously issued tcgen05 ops of this thread complete.
+__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t cta_mask)
+{
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(bar)),
+        "h"(cta_mask)
+        : "memory");
+}
+
+// 2-D TMA tile load multicast to the same shared-memory offset in every CTA
+// of cta_mask; each destination's mbarrier at the offset of bar receives
+// the bytes it got.
+__device__ __forceinline__ void tma_load_2d_mc(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y,
+                                               uint16_t cta_mask)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster "
+        "[%0], [%1, {%3, %4}], [%2], %5;" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "h"(cta_mask)
+        : "memory");
+}
+
 // 32 lanes x 32 consecutive 32-bit columns: thread i of the warp gets row
 // (lane base + i), columns [col, col+32).
 __device__ __forceinline__ void tmem_ld_32x32b_x32(uint32_t taddr, uint32_t (&r)[32])

@@ -247,6 +247,56 @@ def test_dgemm_ozaki_half_tile_tail(orc, dev, m, n, k):
     assert rel(got[rows, cols], ref) <= TOL_OZ
 
 
+# ------------------------------------------------------------ Ozaki, B tiles multicast in cluster pairs
+@pytest.mark.parametrize("m,n,k,ta,tb", [(4050, 2600, 2100, "T", "N"), (4096, 4096, 2048, "N", "T")])
+def test_dgemm_ozaki_multicast_pairs(orc, dev, m, n, k, ta, tb):
+    # Products with an even number of 128-row tiles and at least two tiles
+    # per SM run in clusters of two CTAs on vertically adjacent tiles, each
+    # loading half of the shared B tile for both: 4050 x 2600 is 16 x 11
+    # tile pairs (ragged in every dimension, the 24 pairs of the last wave
+    # as half tiles), 4096 x 4096 is 16 x 16 pairs (28 left as half tiles).
+    ra, ca = (m, k) if ta == "N" else (k, m)
+    rb, cb = (k, n) if tb == "N" else (n, k)
+    a, s = padded(orc, ra, ca, 7460 + m)
+    b, s = padded(orc, rb, cb, s)
+    c, _ = padded(orc, m, n, s)
+    C = to_dev(c)
+    dev.dgemm_ozaki(ta, tb, m, n, k, -0.75, to_dev(a), a.shape[0], to_dev(b), b.shape[0], 1.5, C, c.shape[0])
+    dev.sync()
+    got = from_dev(C, c.shape[0], n)
+    assert np.all(got[m:] == SENT)
+    full = -0.75 * (op(a[:ra], ta) @ op(b[:rb], tb)) + 1.5 * c[:m]
+    assert rel(got[:m], full) <= TOL
+    rows, cols = samples(m, n, 2048, 7461 + m)
+    ref = orc.dgemm_dd_sample(ta, tb, k, -0.75, a, b, 1.5, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL_OZ
+
+
+def test_zgemm_ozaki_multicast_pairs(orc, dev):
+    # complex K = 600 is a real product of K = 1200 on the wide tile, in
+    # cluster pairs (4000 x 2500: 16 x 10 tile pairs)
+    m, n, k = 4000, 2500, 600
+    ar, s = orc.matrix(m, k, 7620)
+    ai, s = orc.matrix(m, k, s)
+    br, s = orc.matrix(k, n, s)
+    bi, s = orc.matrix(k, n, s)
+    cr, s = orc.matrix(m, n, s)
+    a = np.asfortranarray(ar + 1j * ai)
+    b = np.asfortranarray(br + 1j * bi)
+    c = np.asfortranarray(cr + 0.5j * cr)
+    alpha, beta = 0.75 + 0.5j, -0.5 + 0.25j
+    A = to_dev(a.ravel(order="F").view(np.float64))
+    B = to_dev(b.ravel(order="F").view(np.float64))
+    C = to_dev(c.ravel(order="F").view(np.float64))
+    dev.zgemm_ozaki("N", "N", m, n, k, alpha, A, m, B, k, beta, C, m)
+    dev.sync()
+    got = C.cpu().numpy().view(np.complex128).reshape(m, n, order="F")
+    assert rel(got, alpha * (a @ b) + beta * c) <= TOL
+    rows, cols = samples(m, n, 1024, 7621)
+    ref = orc.zgemm_dd_sample("N", "N", k, alpha, a, b, beta, c, rows, cols)
+    assert rel(got[rows, cols], ref) <= TOL_OZ
+
+
 @pytest.mark.parametrize("uplo", ["L", "U"])
 def test_dsyrk_ozaki_half_tile_tail(orc, dev, uplo):
     # 18 x 9 = 162 tiles of 128 x 256 over the whole square; the 10 left
