@@ -853,14 +853,14 @@ __device__ __forceinline__ void oz_report(const OzParams &p)
 // the group before it, so the tensor pipe waited on every one-item group.
 struct GroupPlan {
     int S, nkb, kch_blocks, nchunks, items_per_group;
-    __device__ void init(int S_, int Kp)
+    __device__ void init(int S_, int Kp, int bk = OZ_BK)
     {
         S = S_;
-        nkb = Kp / OZ_BK;
+        nkb = Kp / bk;
         const int kch = min(Kp, OZ_KEXT_MAX);
-        kch_blocks = kch / OZ_BK;
+        kch_blocks = kch / bk;
         nchunks = (nkb + kch_blocks - 1) / kch_blocks;
-        items_per_group = max(1, OZ_KEXT_MAX / (kch_blocks * OZ_BK));
+        items_per_group = max(1, OZ_KEXT_MAX / (kch_blocks * bk));
     }
     __device__ int ngroups(int nitems) const { return (nitems + items_per_group - 1) / items_per_group; }
     // first item of group g of ng (g = ng gives nitems); every group holds at
@@ -1273,17 +1273,25 @@ __device__ __forceinline__ void oz_drain_row_h(const OzParams &p, uint32_t taddr
 // one-CTA form waited on its loads about 30 % of the time.  A stage is free
 // again once both CTAs' MMAs have read it (each MMA commit arrives on both
 // CTAs' empty barrier).
+constexpr int OZ_WBK = 128;   // K block of the wide-tile kernel, in digits (bytes per tile row)
 template <int BN>
 struct OzCfg {
     static constexpr int NBUF = 512 / BN;
-    static constexpr int B_BYTES = BN * OZ_BK;
-    static constexpr int STAGE_BYTES = OZ_A_BYTES + B_BYTES;
-    static constexpr int STAGES = (BN == 256) ? 4 : 6;
+    static constexpr int BK = OZ_WBK;
+    static constexpr int A_BYTES = OZ_BM * BK;
+    static constexpr int B_BYTES = BN * BK;
+    static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+    // as many stages as the opt-in shared memory holds (the loads in flight
+    // are what hide the L2/DRAM latency: three stages ran 10 % slower than four)
+    static constexpr int STAGES = (227 * 1024 - 1024 - 512) / STAGE_BYTES < 16
+                                      ? (227 * 1024 - 1024 - 512) / STAGE_BYTES : 16;
     static constexpr int EPI_WARPS = 8;
     static constexpr int THREADS = 64 + 32 * EPI_WARPS;
     static constexpr int DRAIN_COLS = BN / 2;
     static constexpr int DRAIN_CH = 8;
-    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 /*align*/ + 512 /*barriers*/;
+    static_assert((2 * STAGES + 2 * NBUF) * 8 + 4 <= 512, "barriers and the TMEM slot fit their region");
+    static_assert(SMEM <= 227 * 1024, "opt-in shared memory");
 };
 
 template <int BN, bool MC>
@@ -1330,7 +1338,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     const uint32_t tmem_base = *tmem_slot;
 
     GroupPlan gp;
-    gp.init(*p.S, p.Kp);
+    gp.init(*p.S, p.Kp, Cfg::BK);
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
@@ -1344,7 +1352,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 oz_unit(p, u, BN, MROWS, rank, tm, tn, col_off, narrow);
                 if (!MC && !oz_unit_needed(p, tm, tn, col_off, narrow, BN)) continue;
                 const CUtensorMap *mb = narrow ? &tmBh : &tmB;
-                const int bytes = OZ_A_BYTES + (narrow ? Cfg::B_BYTES / 2 : Cfg::B_BYTES);
+                const int bytes = Cfg::A_BYTES + (narrow ? Cfg::B_BYTES / 2 : Cfg::B_BYTES);
                 // with MC each CTA brings this share of the unit's B rows to both CTAs
                 const int b_rows = (narrow ? BN / 2 : BN) / MROWS;
                 for (int q = 0; q < gp.S && ok; q++) {
@@ -1357,12 +1365,13 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                             if (!mbar_wait(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
                             uint8_t *sa = smem + stage * STAGE_BYTES;
                             mbar_arrive_expect_tx(&full[stage], (uint32_t)bytes);
-                            tma_load_2d(sa, &tmA, &full[stage], kb * OZ_BK, s * p.Mp + tm * OZ_BM);
+                            tma_load_2d(sa, &tmA, &full[stage], kb * Cfg::BK, s * p.Mp + tm * OZ_BM);
                             if (MC)
-                                tma_load_2d_mc(sa + OZ_A_BYTES + rank * b_rows * OZ_BK, mb, &full[stage], kb * OZ_BK,
-                                               t2 * p.Np + tn * BN + col_off + rank * b_rows, (uint16_t)3u);
+                                tma_load_2d_mc(sa + Cfg::A_BYTES + rank * b_rows * Cfg::BK, mb, &full[stage],
+                                               kb * Cfg::BK, t2 * p.Np + tn * BN + col_off + rank * b_rows,
+                                               (uint16_t)3u);
                             else
-                                tma_load_2d(sa + OZ_A_BYTES, mb, &full[stage], kb * OZ_BK,
+                                tma_load_2d(sa + Cfg::A_BYTES, mb, &full[stage], kb * Cfg::BK,
                                             t2 * p.Np + tn * BN + col_off);
                             if (++stage == STAGES) { stage = 0; phase ^= 1u; }
                         }
@@ -1408,10 +1417,10 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                                 const uint32_t a_addr = smem_base + stage * STAGE_BYTES;
                                 // descriptors built once per stage, advanced by 32 bytes
                                 // (2 in the address field) per k step
-                                const uint64_t a_d = smem_desc_k128(a_addr);
-                                const uint64_t b_d = smem_desc_k128(a_addr + OZ_A_BYTES);
+                                const uint64_t a_d = smem_desc_kmaj<Cfg::BK>(a_addr);
+                                const uint64_t b_d = smem_desc_kmaj<Cfg::BK>(a_addr + Cfg::A_BYTES);
 #pragma unroll
-                                for (int kk = 0; kk < OZ_BK / 32; kk++) {
+                                for (int kk = 0; kk < Cfg::BK / 32; kk++) {
                                     mma_f8f6f4(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, acc);
                                     acc = 1;
                                 }
@@ -2091,17 +2100,17 @@ EncodeTiledFn get_encode()
 }
 
 // 2-D byte tensor [rows][Kp] with a (box_rows x 128-byte) box, 128B swizzle.
-bool make_map_uncached(CUtensorMap *map, void *base, long long rows, long long Kp, int box_rows)
+bool make_map_uncached(CUtensorMap *map, void *base, long long rows, long long Kp, int box_rows, int inner)
 {
     EncodeTiledFn enc = get_encode();
     if (!enc) return false;
     cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)Kp};
-    cuuint32_t box[2] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows};
+    cuuint32_t box[2] = {(cuuint32_t)inner, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               inner == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // The digit planes as a 3-D tensor (k, row, plane): one load brings a
@@ -2124,25 +2133,25 @@ bool make_map3_uncached(CUtensorMap *map, void *base, long long rows, long long 
 // calling thread sees the same few (base, rows, K, box) over and over: the
 // encoded maps are kept per thread (8 entries, round robin) instead of
 // re-encoding two per call on the host.
-bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int box_rows)
+bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int box_rows, int inner = OZ_BK)
 {
     struct Entry {
         void *base;
         long long rows, Kp;
-        int box;
+        int box, inner;
         CUtensorMap map;
     };
     thread_local Entry cache[8] = {};
     thread_local int next = 0;
     for (auto &e : cache)
-        if (e.base == base && e.rows == rows && e.Kp == Kp && e.box == box_rows) {
+        if (e.base == base && e.rows == rows && e.Kp == Kp && e.box == box_rows && e.inner == inner) {
             *map = e.map;
             return true;
         }
     // box_rows < 0 asks for the 3-D form: -box_rows = rows x 256 + planes
     const bool three = box_rows < 0;
     if (three ? !make_map3_uncached(map, base, rows, Kp, (-box_rows) >> 8, (-box_rows) & 255)
-              : !make_map_uncached(map, base, rows, Kp, box_rows))
+              : !make_map_uncached(map, base, rows, Kp, box_rows, inner))
         return false;
     Entry &e = cache[next];
     next = (next + 1) & 7;
@@ -2150,6 +2159,7 @@ bool make_map(CUtensorMap *map, void *base, long long rows, long long Kp, int bo
     e.rows = rows;
     e.Kp = Kp;
     e.box = box_rows;
+    e.inner = inner;
     e.map = *map;
     return true;
 }
@@ -2412,10 +2422,11 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     // small K: op(B)^T's planes as a 3-D map, the B stage of a tile in one load;
     // wide tiles: also a half-width B box for the half tiles of the last wave
     const bool wide = !small_k && !pair;
-    if (!make_map(&tmA, b.A8, (long long)OZ_SMAX * Mp, Kp, OZ_BM) ||
+    const int inner = wide ? OZ_WBK : OZ_BK;
+    if (!make_map(&tmA, b.A8, (long long)OZ_SMAX * Mp, Kp, OZ_BM, inner) ||
         !(small_k ? make_map(&tmB, B8, Np, Kp, -(bn * 256 + planes))
-                  : make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : (mc ? bn / 2 : bn))) ||
-        (wide && !make_map(&tmBh, B8, (long long)OZ_SMAX * Np, Kp, mc ? bn / 4 : bn / 2)))
+                  : make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : (mc ? bn / 2 : bn), inner)) ||
+        (wide && !make_map(&tmBh, B8, (long long)OZ_SMAX * Np, Kp, mc ? bn / 4 : bn / 2, inner)))
         return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
 
     OzParams p{};

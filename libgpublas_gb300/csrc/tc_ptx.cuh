@@ -359,6 +359,23 @@ __device__ __forceinline__ uint64_t smem_desc_k128(uint32_t smem_addr)
     return d;
 }
 
+
+// The same descriptor for K-major tiles of BK-byte rows: 128 (128-byte
+// swizzle, 8-row groups 1024 bytes apart) or 64 (64-byte swizzle, layout
+// type 4, groups 512 bytes apart).
+template <int BK>
+__device__ __forceinline__ uint64_t smem_desc_kmaj(uint32_t smem_addr)
+{
+    static_assert(BK == 128 || BK == 64, "K-major rows of 128 or 64 bytes");
+    uint64_t d = 0;
+    d |= (uint64_t)((smem_addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1u << 16;
+    d |= (uint64_t)((8u * BK) >> 4) << 32;
+    d |= (uint64_t)1u << 46;
+    d |= (uint64_t)(BK == 128 ? 2u : 4u) << 61;
+    return d;
+}
+
 // Instruction descriptor, kind::f8f6f4, dense: D = F32, A = B = E4M3, both
 // K-major, shape M x N.
 __host__ __device__ constexpr uint32_t idesc_e4m3_f32(int M, int N)
