@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cmath>
 #include <type_traits>
 
 using namespace gbx_gemm;
@@ -76,17 +77,22 @@ gbx_status launch_gemm_tile(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
     return gbx_check_launch(ctx, what);
 }
 
-// Tile choice: the largest block tile that still gives every SM two tiles,
-// shrinking to 64x64, 32x32 and then 16x16 (one element per thread) for the
-// skinny and small products that DTRSM's recursion and small calls produce
-// (with few large tiles most SMs would idle): at 2 FP64 lanes per clock per
-// SM a small product's latency is its FMAs per SM, so spreading it over four
-// times the SMs cuts it almost fourfold.  Real double starts at 64x64: two
+// Tile choice.  Real double: the tile (64x64, 32x32 or 16x16 with one
+// element per thread) with the best product of its kernel's efficiency and
+// the fill of its last wave.  At 2 FP64 lanes per clock per SM each SM works
+// through its share of tiles one after another, so a launch takes
+// ceil(tiles / SMs) tile times: 512 tiles of 64x64 (DGEMM 2048x1024x2048, a
+// DTRSM update) take four tile times on 152 SMs for 3.37 tiles' work (0.84),
+// the same product as 8192 tiles of 16x16 runs at 0.98.  Measured DGEMM
+// rates with the other shapes equal: 64x64 1.249, 32x32 1.247, 16x16 1.23
+// TFLOP/s; 2048x1024x2048 takes 8.25 / 7.17 / 6.96 ms on the three tiles,
+// 1024^3 2.11 / 1.80 / 1.75 ms, 4096x1024x4096 28.7 / 27.6 / 27.8 ms.  Two
 // CTAs of 124 registers per SM keep the DFMA pipe fed across each CTA's
-// barriers, and DGEMM 8192^3 takes 881 ms against 901 ms with 128x128 tiles
-// (one CTA of 254 registers per SM).  Complex double uses 64x64 / 32x32 (its
-// 8x8 register tile would not fit); float and complex float start at
-// 128x128, whose operand reuse their faster FMA pipe needs.
+// barriers, so 64x64 beats 128x128 (DGEMM 8192^3 881 against 901 ms).
+// Other types: the largest tile that still gives every SM two tiles,
+// 128x128 for float and complex float (their faster FMA pipe needs the
+// operand reuse), 64x64 and 32x32 for complex double (its 8x8 register tile
+// would not fit), then smaller for the skinny and small products.
 template <typename T>
 gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
 {
@@ -96,9 +102,18 @@ gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
         const long long tm = (p.m + bm - 1) / bm, tn = (p.n + bm - 1) / bm;
         return p.c_part == C_FULL ? tm * tn : tm * (tm + 1) / 2;
     };
-    if constexpr (sizeof(T) <= 8) {
-        if constexpr (!std::is_same<T, double>::value)
-            if (tiles(128) >= want) return launch_gemm_tile<T, 8>(ctx, p, what);
+    if constexpr (std::is_same<T, double>::value) {
+        const double sms = (double)gbx_ctx_sms(ctx);
+        auto score = [&](int bm, double eff) {
+            const double w = (double)tiles(bm) / sms;
+            return eff * w / std::ceil(w);
+        };
+        const double s64 = score(64, 1.0), s32 = score(32, 0.998), s16 = score(16, 0.985);
+        if (s64 >= s32 && s64 >= s16) return launch_gemm_tile<T, 4>(ctx, p, what);
+        if (s32 >= s16) return launch_gemm_tile<T, 2>(ctx, p, what);
+        return launch_gemm_tile<T, 1>(ctx, p, what);
+    } else if constexpr (sizeof(T) <= 8) {
+        if (tiles(128) >= want) return launch_gemm_tile<T, 8>(ctx, p, what);
         if (tiles(64) >= want) return launch_gemm_tile<T, 4>(ctx, p, what);
         if (tiles(32) >= want) return launch_gemm_tile<T, 2>(ctx, p, what);
         return launch_gemm_tile<T, 1>(ctx, p, what);

@@ -1,15 +1,16 @@
 """Parity at the shapes that select the large tiles, i.e. the kernels the
 benchmarks time.
 
-The GEMM core picks its block tile from the number of output tiles (the
-largest tile that still gives every SM two of them): the 64 x 64 FP64 tile
-(4 x 4 per thread, the one the DGEMM benchmark times) and the 64 x 64
-complex tile need about 1100 rows and columns, and the Ozaki product takes
-its 128 x 256 tile once 152 such tiles exist (about 2560 x 2560) with
-K > 1024.  The small shapes of the other test
-files never reach those instantiations, so each case here is sized past the
-threshold, with ragged edges (sizes that are not multiples of the tile), odd
-leading dimensions whose padding rows hold a sentinel, and beta != 0.
+The GEMM core picks its FP64 block tile (64 x 64, 32 x 32 or 16 x 16) by
+how well the last wave of tiles fills the SMs, and the 64 x 64 complex tile
+once every SM gets two tiles; the Ozaki product takes its 128 x 256 tile
+once 152 such tiles exist (about 2560 x 2560) with K > 1024.  The cases
+here are sized to select the tiles the benchmarks time: 64 x 64 for DGEMM
+(2040 x 1210 and 1287 x 1287, as at 8192), 32 x 32 for DSYRK (n = 3201, as
+at 8192 / 2048), 16 x 16 for large ragged products (2311 x 2305, as in the
+DTRSM updates), with ragged edges (sizes that are not multiples of the
+tile), odd leading dimensions whose padding rows hold a sentinel, and
+beta != 0.
 
 Checks, each with the tolerance stated:
   * sampled entries (random plus the last rows and columns, where the edge
@@ -71,11 +72,13 @@ def op(x, t):
     return x if t == "N" else x.T
 
 
-# ------------------------------------------------------------ FP64 DGEMM, 64 x 64 tile
+# ------------------------------------------------------------ FP64 DGEMM, 64 x 64 and 16 x 16 tiles
 @pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
-@pytest.mark.parametrize("m,n,k", [(2311, 2305, 129), (2304, 2304, 512)])
+@pytest.mark.parametrize("m,n,k", [(2040, 1210, 129), (1287, 1287, 512), (2311, 2305, 129)])
 def test_dgemm_large_tile(orc, dev, ta, tb, m, n, k):
-    if (m, n, k) == (2304, 2304, 512) and tb == "T":
+    # 2040 x 1210: 32 x 19 = 608 tiles of 64 (four per SM); 1287^2: 21 x 21
+    # tiles of 64; 2311 x 2305: 145 x 145 tiles of 16
+    if (m, n, k) == (1287, 1287, 512) and tb == "T":
         pytest.skip("the square case runs NN and TN (the benchmarked forms)")
     ra, ca = (m, k) if ta == "N" else (k, m)
     rb, cb = (k, n) if tb == "N" else (n, k)
@@ -114,11 +117,11 @@ def test_dgemm_large_tile_through_fortran_symbol(orc, f77):
     assert rel(got[:m], -0.5 * (a[:m] @ b[:k]) + 0.25 * c[:m]) <= TOL
 
 
-# ------------------------------------------------------------ FP64 DSYRK, 64 x 64 tile
+# ------------------------------------------------------------ FP64 DSYRK, 32 x 32 tile
 @pytest.mark.parametrize("uplo", ["L", "U"])
 @pytest.mark.parametrize("trans", ["N", "T"])
 def test_dsyrk_large_tile(orc, dev, uplo, trans):
-    # 51 x 52 / 2 = 1326 triangular tiles of 64 (>= 2 per SM)
+    # 101 x 102 / 2 = 5151 triangular tiles of 32 (34 per SM)
     n, k = 3201, 300
     ra, ca = (n, k) if trans == "N" else (k, n)
     a, s = padded(orc, ra, ca, 7100 + ord(uplo) + ord(trans))
@@ -141,7 +144,7 @@ def test_dsyrk_large_tile(orc, dev, uplo, trans):
     assert np.array_equal(got[:n][untouched], c[:n][untouched])
 
 
-# ------------------------------------------------------------ FP64 DTRMM on the 64 tile
+# ------------------------------------------------------------ FP64 DTRMM, 16 x 16 tile
 @pytest.mark.parametrize("side,uplo,ta", [("L", "L", "N"), ("R", "U", "T")])
 def test_dtrmm_large_tile(orc, dev, side, uplo, ta):
     m, n = 2311, 2305
@@ -357,10 +360,11 @@ def test_dsyrk_ozaki_wide(orc, dev, uplo):
     assert np.array_equal(got[untouched], c[untouched])
 
 
-# ------------------------------------------------------------ DTRSM with 64-tile updates
+# ------------------------------------------------------------ DTRSM with 32 / 16-tile updates
 def test_dtrsm_large_left_lower(orc, dev):
     # config-2 distribution (diagonal uniform[1,2], off-diagonal
-    # uniform[-1,1]/m); the recursive updates run on the 64 x 64 tile.
+    # uniform[-1,1]/m); the recursive updates run on 32 x 32 and 16 x 16
+    # tiles.
     # Backward residual of 16 sampled right-hand sides against the
     # double-double oracle, forward error of the same columns against the
     # oracle's substitution.
