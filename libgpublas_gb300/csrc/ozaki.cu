@@ -1869,13 +1869,21 @@ oz_gemm_sk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
 // drain warps per CTA take them as the one-CTA kernel does (two warps per
 // TMEM lane quarter, each half of the columns), with the same Horner drain,
 // diagonals in ascending order and the same grouped tile order.
-//   full[s]   (even CTA): both producers arrive + expect 32 KB each; both
-//             CTAs' TMA loads complete on it (cta_group::2 TMA)
+//   full[s]   (even CTA): its producer arrives expecting both CTAs' 64 KB;
+//             both CTAs' TMA loads complete on it (cta_group::2 TMA)
 //   empty[s]  (each CTA): arrived by the MMA commit, multicast to both CTAs
 //   tfull[b]  (each CTA): arrived by the MMA commit, multicast to both CTAs
 //   tempty[b] (even CTA): the 512 drain threads of both CTAs arrive
 // ---------------------------------------------------------------------------
 constexpr int OZ2_BM = 256, OZ2_STAGES = 7;
+
+// Whether a unit of the CTA-pair kernel (a 256-row tile or half of one) has
+// any element in the written part of C.
+__device__ __forceinline__ bool oz_pair_unit_needed(const OzParams &p, int tm, int tn, int col_off, bool narrow)
+{
+    return narrow ? tile_needed(p, tm, 2 * tn + (col_off ? 1 : 0), OZ2_BM, OZ_BN / 2)
+                  : tile_needed(p, tm, tn, OZ2_BM, OZ_BN);
+}
 constexpr int OZ2_HALF = 128 * OZ_BK;                // 16 KB: 128 rows x 128 bytes
 constexpr int OZ2_STAGE_BYTES = 2 * OZ2_HALF;        // A half + B half
 constexpr int OZ2_EPI_WARPS = 8;
@@ -1884,7 +1892,8 @@ constexpr size_t OZ2_SMEM = (size_t)OZ2_STAGES * OZ2_STAGE_BYTES + 1024 + 256;
 static_assert(OZ2_SMEM <= 227 * 1024, "CTA-pair stages must fit the opt-in shared memory");
 
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(OZ2_THREADS, 1)
-oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, OzParams p)
+oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                const __grid_constant__ CUtensorMap tmBh, OzParams p)
 {
     if (oz_skip_kernel(p)) {
         oz_report(p);
@@ -1903,11 +1912,12 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     volatile int *status = p.status;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < OZ2_STAGES; i++) { mbar_init(&full[i], 2); mbar_init(&empty[i], 1); }
+        for (int i = 0; i < OZ2_STAGES; i++) { mbar_init(&full[i], 1); mbar_init(&empty[i], 1); }
         for (int i = 0; i < 2; i++) { mbar_init(&tfull[i], 1); mbar_init(&tempty[i], 2 * 32 * OZ2_EPI_WARPS); }
         fence_barrier_init();
         prefetch_tmap(&tmA);
         prefetch_tmap(&tmB);
+        prefetch_tmap(&tmBh);
     }
     if (warp == 1) {
         tmem_alloc_pair(tmem_slot, 512);
@@ -1922,7 +1932,6 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
 
     GroupPlan gp;
     gp.init(*p.S, p.Kp);
-    const int ntiles = p.tiles_m * p.tiles_n;
     const int pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
 
     if (warp == 0) {
@@ -1931,10 +1940,14 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
-            for (int t = pair; t < ntiles && ok; t += npairs) {
-                int tm, tn;
-                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-                if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
+            for (int u = pair; u < p.nunits && ok; u += npairs) {
+                int tm, tn, col_off;
+                bool narrow;
+                oz_unit(p, u, OZ_BN, 1, 0, tm, tn, col_off, narrow);
+                if (!oz_pair_unit_needed(p, tm, tn, col_off, narrow)) continue;
+                const CUtensorMap *mb = narrow ? &tmBh : &tmB;
+                const int b_rows = narrow ? OZ_BN / 4 : OZ_BN / 2;     // this CTA's share of the unit's B
+                const uint32_t bytes = (uint32_t)(OZ2_HALF + b_rows * OZ_BK);
                 for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
@@ -1945,11 +1958,14 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
                             if (!mbar_wait_cl(&empty[stage], phase ^ 1u, status, TC_TIMEOUT_EMPTY)) { ok = false; break; }
                             uint8_t *sa = smem + stage * OZ2_STAGE_BYTES;
                             const uint32_t fbar = mapa_cluster(smem_u32(&full[stage]), leader_rank);
-                            mbar_arrive_expect_tx_cluster(fbar, OZ2_STAGE_BYTES);
+                            // only the even CTA arrives, expecting both CTAs' bytes: a
+                            // remote arrive from the odd CTA per stage cut the load
+                            // rate to a third
+                            if (leader) mbar_arrive_expect_tx(&full[stage], 2u * bytes);
                             tma_load_2d_pair(sa, &tmA, fbar, kb * OZ_BK,
                                              s * p.Mp + tm * OZ2_BM + (int)(rank & 1u) * 128);
-                            tma_load_2d_pair(sa + OZ2_HALF, &tmB, fbar, kb * OZ_BK,
-                                             t2 * p.Np + tn * OZ_BN + (int)(rank & 1u) * 128);
+                            tma_load_2d_pair(sa + OZ2_HALF, mb, fbar, kb * OZ_BK,
+                                             t2 * p.Np + tn * OZ_BN + col_off + (int)(rank & 1u) * b_rows);
                             if (++stage == OZ2_STAGES) { stage = 0; phase ^= 1u; }
                         }
                     }
@@ -1963,15 +1979,16 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     } else if (warp == 1) {
         // ---------------- MMA issuer (even CTA only) ----------------
         if (leader && lane == 0) {
-            constexpr uint32_t idesc = idesc_e4m3_f32(OZ2_BM, OZ_BN);
             int stage = 0, buf = 0;
             uint32_t phase = 0, tphase = 0;
             bool ok = true;
             const uint32_t smem_base = smem_u32(smem);
-            for (int t = pair; t < ntiles && ok; t += npairs) {
-                int tm, tn;
-                oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-                if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
+            for (int u = pair; u < p.nunits && ok; u += npairs) {
+                int tm, tn, col_off;
+                bool narrow;
+                oz_unit(p, u, OZ_BN, 1, 0, tm, tn, col_off, narrow);
+                if (!oz_pair_unit_needed(p, tm, tn, col_off, narrow)) continue;
+                const uint32_t idesc = narrow ? idesc_e4m3_f32(OZ2_BM, OZ_BN / 2) : idesc_e4m3_f32(OZ2_BM, OZ_BN);
                 for (int q = 0; q < gp.S && ok; q++) {
                     const int s_lo = max(0, q - (gp.S - 1)), s_hi = min(q, gp.S - 1);
                     const int nitems = (s_hi - s_lo + 1) * gp.nchunks;
@@ -2016,10 +2033,12 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         bool ok = true;
         const uint32_t tempty_cl0 = mapa_cluster(smem_u32(&tempty[0]), leader_rank);
         const uint32_t tempty_cl1 = mapa_cluster(smem_u32(&tempty[1]), leader_rank);
-        for (int t = pair; t < ntiles && ok; t += npairs) {
-            int tm, tn;
-            oz_tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-            if (!tile_needed(p, tm, tn, OZ2_BM)) continue;
+        for (int u = pair; u < p.nunits && ok; u += npairs) {
+            int tm, tn, col_off;
+            bool narrow;
+            oz_unit(p, u, OZ_BN, 1, 0, tm, tn, col_off, narrow);
+            if (!oz_pair_unit_needed(p, tm, tn, col_off, narrow)) continue;
+            const int dcols = narrow ? OZ_BN / 4 : OZ_BN / 2;
             const int grow = tm * OZ2_BM + (int)(rank & 1u) * 128 + row;
             const int rexp = p.row_exp[grow];
             bool first = true;
@@ -2034,9 +2053,12 @@ oz_gemm2_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
                     if (!ok) break;
                     tc_fence_after();
                     const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) +
-                                           (uint32_t)(buf * OZ_BN + half * (OZ_BN / 2));
-                    oz_drain_row_h<OZ_BN / 2, 8>(p, taddr, grow, tn * OZ_BN + half * (OZ_BN / 2), gp.S, rexp, first,
-                                                 g == 0, last);
+                                           (uint32_t)(buf * OZ_BN + half * dcols);
+                    const int gcol0 = tn * OZ_BN + col_off + half * dcols;
+                    if (narrow)
+                        oz_drain_row_h<OZ_BN / 4, 8>(p, taddr, grow, gcol0, gp.S, rexp, first, g == 0, last);
+                    else
+                        oz_drain_row_h<OZ_BN / 2, 8>(p, taddr, grow, gcol0, gp.S, rexp, first, g == 0, last);
                     tc_fence_before();
                     mbar_arrive_cluster(buf ? tempty_cl1 : tempty_cl0);
                     first = false;
@@ -2426,7 +2448,8 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     if (!make_map(&tmA, b.A8, (long long)OZ_SMAX * Mp, Kp, OZ_BM, inner) ||
         !(small_k ? make_map(&tmB, B8, Np, Kp, -(bn * 256 + planes))
                   : make_map(&tmB, B8, (long long)OZ_SMAX * Np, Kp, pair ? 128 : (mc ? bn / 2 : bn), inner)) ||
-        (wide && !make_map(&tmBh, B8, (long long)OZ_SMAX * Np, Kp, mc ? bn / 4 : bn / 2, inner)))
+        (wide && !make_map(&tmBh, B8, (long long)OZ_SMAX * Np, Kp, mc ? bn / 4 : bn / 2, inner)) ||
+        (pair && !make_map(&tmBh, B8, (long long)OZ_SMAX * Np, Kp, OZ_BN / 4)))
         return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
 
     OzParams p{};
@@ -2439,8 +2462,9 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
         const int per = mc ? 2 : 1;
         if (mc && (mc_clusters = oz_mc_clusters(ctx, bn)) < 1) return gbx_fail(ctx, GBX_ERR_CUDA, "ozaki: clusters");
         const int nt = p.tiles_m / per * p.tiles_n;
-        const int g = std::min(nt, mc ? mc_clusters : gbx_ctx_sms(ctx)), r = nt % g;
-        p.t_split = (wide && r > 0 && 2 * r <= g) ? nt - r : nt;
+        const int slots = mc ? mc_clusters : (pair ? std::max(1, gbx_ctx_sms(ctx) / 2) : gbx_ctx_sms(ctx));
+        const int g = std::min(nt, slots), r = nt % g;
+        p.t_split = ((wide || pair) && r > 0 && 2 * r <= g) ? nt - r : nt;
         p.nunits = p.t_split + 2 * (nt - p.t_split);
     }
     p.S = b.S;
@@ -2504,7 +2528,7 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
     gbx_timer_begin(ctx, GBX_TIMER_OZAKI_MMA);
     if (pair) {
         const int npairs = std::max(1, std::min(ntiles, max_pairs));
-        oz_gemm2_kernel<<<2 * npairs, OZ2_THREADS, OZ2_SMEM, s>>>(tmA, tmB, p);
+        oz_gemm2_kernel<<<2 * npairs, OZ2_THREADS, OZ2_SMEM, s>>>(tmA, tmB, tmBh, p);
     } else {
         const int grid = std::min(ntiles, gbx_ctx_sms(ctx));
         if (small_k) {

@@ -248,13 +248,6 @@ __device__ __forceinline__ uint32_t mapa_cluster(uint32_t smem_addr, uint32_t ra
     return r;
 }
 
-__device__ __forceinline__ void mbar_arrive_expect_tx_cluster(uint32_t cl_addr, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.release.cluster.shared::cluster.b64 _, [%0], %1;" ::"r"(cl_addr),
-                 "r"(bytes)
-                 : "memory");
-}
-
 __device__ __forceinline__ void mbar_arrive_cluster(uint32_t cl_addr)
 {
     asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cl_addr) : "memory");
