@@ -2233,17 +2233,36 @@ int oz_mc_clusters(gbx_ctx *ctx, int bn)
     return nc;
 }
 
-// The CTA-pair kernel is selected with GBX_OZAKI_PAIR=1 for problems with
-// more than one 128-row tile of op(A).  It is correct but measured slower
-// than the one-CTA kernel at n = 8192 (43 ms vs 30 ms of MMA time), so the
-// one-CTA kernel is the default; the tests cover both.
-bool oz_use_pair(int M)
+// Small-K products (the rank-nb updates of blocked factorizations) take the
+// kernel with every diagonal in TMEM; GBX_OZAKI_SMALLK=0 turns it off.
+bool oz_small_k(int K)
+{
+    static int env = [] {
+        const char *s = getenv("GBX_OZAKI_SMALLK");
+        return s ? atoi(s) : 1;
+    }();
+    return env != 0 && K <= 1024;
+}
+
+// The CTA-pair kernel takes the products (K > 1024) of at most four waves of
+// its 256 x 256 tiles: measured one after another on one GB300 it ran 2048^3
+// in 0.50 ms against 0.70 ms and 4096^3 in 2.90 against 3.07 ms of the
+// one-CTA kernel; from 8192 on (calls of 20 ms and more under the power
+// cap) it draws more power, the SM clock falls further, and it ties (8192)
+// or loses (16384: 185-194 against 163 ms).  GBX_OZAKI_PAIR=1 selects it
+// for every product with more than one 128-row tile (small K included),
+// GBX_OZAKI_PAIR=0 never.
+bool oz_use_pair(int M, int N, int K, int sms)
 {
     static int env = [] {
         const char *s = getenv("GBX_OZAKI_PAIR");
-        return s ? atoi(s) : 0;
+        return s ? atoi(s) : -1;
     }();
-    return env != 0 && M > OZ_BM;
+    if (env == 0 || M <= OZ_BM) return false;
+    if (env > 0) return true;
+    if (rup(std::max(K, 1), OZ_BK) <= OZS_KMAX && oz_small_k(K)) return false;
+    const long long tiles = (long long)((M + OZ2_BM - 1) / OZ2_BM) * ((N + OZ_BN - 1) / OZ_BN);
+    return tiles <= 4LL * std::max(1, sms / 2);
 }
 
 // Column tile: 128 when N fits in it (the rank-nb updates of blocked
@@ -2256,17 +2275,6 @@ int oz_tile_n(int M, int N, int sms, bool pair)
     if (N <= 128) return 128;
     const long long tiles256 = ((M + OZ_BM - 1) / OZ_BM) * (long long)((N + OZ_BN - 1) / OZ_BN);
     return tiles256 < sms ? 128 : OZ_BN;
-}
-
-// Small-K products (the rank-nb updates of blocked factorizations) take the
-// kernel with every diagonal in TMEM; GBX_OZAKI_SMALLK=0 turns it off.
-bool oz_small_k(int K)
-{
-    static int env = [] {
-        const char *s = getenv("GBX_OZAKI_SMALLK");
-        return s ? atoi(s) : 1;
-    }();
-    return env != 0 && K <= 1024;
 }
 
 // Workspace layout for one Ozaki product.
@@ -2371,7 +2379,7 @@ gbx_status run_ozaki(gbx_ctx *ctx, const OzProblem &pr, double tol, int forced, 
                      OzBuffers *keep = nullptr, int nW = 1, int w_index = 0)
 {
     if (pr.K > 0x3fffffff) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: K too large");
-    const bool pair = oz_use_pair(pr.M);
+    const bool pair = oz_use_pair(pr.M, pr.N, pr.K, gbx_ctx_sms(ctx));
     const bool small_k = !pair && rup(std::max(pr.K, 1), OZ_BK) <= OZS_KMAX && oz_small_k(pr.K);
     const long long sk_tiles = ((long long)pr.M + OZ_BM - 1) / OZ_BM * (((long long)pr.N + OZS_BN - 1) / OZS_BN);
     const int bn = small_k ? (2 * sk_tiles <= gbx_ctx_sms(ctx) ? OZS_BN / 2 : OZS_BN)
@@ -2790,7 +2798,7 @@ extern "C" gbx_status gbx_zgemm_ozaki(gbx_ctx *ctx, char ta, char tb, int m, int
     }
     if (2LL * k > 0x3fffffffLL) return gbx_fail(ctx, GBX_ERR_UNSUPPORTED, "ozaki: K too large");
     const int K2 = 2 * k;
-    const int Mp = (int)rup(m, oz_use_pair(m) ? OZ2_BM : OZ_BM), Np = (int)rup(n, OZ_BN);
+    const int Mp = (int)rup(m, oz_use_pair(m, n, K2, gbx_ctx_sms(ctx)) ? OZ2_BM : OZ_BM), Np = (int)rup(n, OZ_BN);
     const int Kp = (int)rup(K2, OZ_BK);
     OzBuffers b;
     gbx_status st = oz_buffers(ctx, Mp, Np, Kp, 2, b);

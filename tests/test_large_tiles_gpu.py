@@ -418,3 +418,21 @@ def test_fortran_dgemm_pipelined_copies_match_device_path(orc, f77, dev, ta, tb,
     rows, cols = samples(m, n, 1024, 7901)
     ref = orc.dgemm_dd_sample(ta, tb, k, 1.25, a, b, beta, c, rows, cols)
     assert rel(got[rows, cols], ref) <= TOL
+
+
+@pytest.mark.skipif(__import__("os").environ.get("GBX_OZAKI_PAIR") == "0",
+                    reason="already running with the one-CTA kernel")
+def test_one_cta_ozaki_kernel_variant():
+    # Products of at most four waves of 256 x 256 tiles take the CTA-pair
+    # kernel by default, so the Ozaki cases above run on it; rerun them in a
+    # child process with GBX_OZAKI_PAIR=0, on the one-CTA kernel that the
+    # larger products (the 8192 benchmark) use, with and without B multicast.
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, GBX_OZAKI_PAIR="0", PYTHONPATH=root)
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider", "-m", "gpu",
+                        os.path.abspath(__file__), "-k", "ozaki and not variant"],
+                       capture_output=True, text=True, env=env, cwd=root, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]

@@ -266,8 +266,10 @@ def test_wide_tile_kernel_for_small_k():
 @pytest.mark.skipif(__import__("os").environ.get("GBX_OZAKI_PAIR") == "1",
                     reason="already running with the CTA-pair kernel")
 def test_cta_pair_kernel_variant():
-    # The one-CTA kernel is the default; rerun the kernel tests in a child
-    # process with the CTA-pair (tcgen05 cta_group::2) kernel selected.
+    # The CTA-pair (tcgen05 cta_group::2) kernel is chosen by size (mid-size
+    # products with K > 1024); rerun the kernel tests in a child process with
+    # it forced for every product with more than one 128-row tile, small K
+    # included.
     import os
     import subprocess
     import sys
