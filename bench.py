@@ -1032,11 +1032,11 @@ MODES = {
     # name: (through the serving layer, Ozaki forms of dtrsm/dsyrk/dgemm,
     # device-side request loop on)
     "plain": (False, False, False),         # FP64, plain per-call dispatch
-    "served": (True, False, True),          # FP64, serving layer with its device-side loop
-    "served_all": (True, False, "all"),     # FP64, the same with the loop on every SM
-    "served_host": (True, False, False),    # FP64, serving layer on host worker threads only
+    "served": (True, False, False),         # FP64, serving layer as created by default
+    "served_loop": (True, False, True),     # FP64, serving layer with its device-side loop (opt-in)
+    "served_loop_all": (True, False, "all"),  # FP64, the same with the loop on every SM
     "ozaki_plain": (False, True, False),    # Ozaki, plain per-call dispatch
-    "ozaki": (True, True, True),            # Ozaki, serving layer
+    "ozaki": (True, True, False),           # Ozaki, serving layer
 }
 
 
@@ -1063,7 +1063,7 @@ def make_server(g, slots, loop):
                 os.environ[k] = v
 
 
-def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=("plain", "served", "served_host", "ozaki_plain", "ozaki"),
+def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=("plain", "served", "served_loop", "ozaki_plain", "ozaki"),
                   chains=True):
     """Closed-loop Cholesky trace: nthreads native caller threads, thread t
     factorising A = G G^T + n I (G uniform[-1,1], n log-uniform in
@@ -1160,13 +1160,13 @@ def serving_trace(g, nthreads, nmin, nmax, seed=5, modes=("plain", "served", "se
     return sizes, nbs, results
 
 
-def small_call_trace(g, nthreads, ncalls, size=64, modes=("plain", "served", "served_all", "served_host")):
+def small_call_trace(g, nthreads, ncalls, size=64, modes=("plain", "served", "served_loop", "served_loop_all")):
     """Latency-bound calls: nthreads native threads each issue ncalls FP64
     DGEMMs of size^3 (C += A B on the thread's own operands), one at a time,
-    per mode: plain per-call dispatch, the serving layer with its device-side
-    loop (on a quarter of the SMs, and on every SM), and the serving layer on
-    host worker threads.  Returns calls/s, p50/p99 per mode and the loop's
-    gain over plain dispatch."""
+    per mode: plain per-call dispatch, the serving layer as created by
+    default, and with its device-side loop (on a quarter of the SMs, and on
+    every SM).  Returns calls/s, p50/p99 per mode and the gains over plain
+    dispatch."""
     import torch
     n = size
     bufs = []
@@ -1194,10 +1194,9 @@ def small_call_trace(g, nthreads, ncalls, size=64, modes=("plain", "served", "se
         err = float((got - want).norm() / want.norm())
         out[mode] = {"calls": r["calls"], "calls_per_s": r["calls"] / r["wall_s"], "p50_us": r["p50_us"],
                      "p99_us": r["p99_us"], "rel_err_thread0": err, "first_error": r["first_error"]}
-    if "plain" in out and "served" in out:
-        out["loop_vs_plain"] = out["served"]["calls_per_s"] / out["plain"]["calls_per_s"]
-    if "plain" in out and "served_all" in out:
-        out["loop_all_sms_vs_plain"] = out["served_all"]["calls_per_s"] / out["plain"]["calls_per_s"]
+    for mode in ("served", "served_loop", "served_loop_all"):
+        if "plain" in out and mode in out:
+            out[f"{mode}_vs_plain"] = out[mode]["calls_per_s"] / out["plain"]["calls_per_s"]
     return out
 
 
@@ -1207,8 +1206,7 @@ def serving_ratios(results, fp64_peak_tflops=None):
     def ratio(a, b):
         return results[a]["calls_per_s"] / results[b]["calls_per_s"] if a in results and b in results else None
     out = {"served_vs_plain_fp64": ratio("served", "plain"),
-           "served_all_sms_vs_plain_fp64": ratio("served_all", "plain"),
-           "served_loop_vs_host_workers_fp64": ratio("served", "served_host"),
+           "served_loop_vs_plain_fp64": ratio("served_loop", "plain"),
            "served_vs_plain_ozaki": ratio("ozaki", "ozaki_plain"),
            "ozaki_plain_vs_fp64_plain": ratio("ozaki_plain", "plain"),
            "ozaki_served_vs_fp64_plain": ratio("ozaki", "plain")}
@@ -1244,7 +1242,7 @@ def run_serving(args):
                        "matrix": "A = G G^T + n I, G uniform[-1,1] (device generator, seed 5)",
                        "driver": "16 native host threads (gbx_diag_cholesky_trace), one call at a time each",
                        "calls": "dpotrf(diag) dtrsm dsyrk dgemm + ddot residual checks",
-                       "headline_mode": "ozaki: serving loop, dgemm/dsyrk/dtrsm through the Ozaki path "
+                       "headline_mode": "ozaki: serving layer, dgemm/dsyrk/dtrsm through the Ozaki path "
                                         "(tolerance 1e-14, FP64 results), dpotrf in FP64"},
             "modes": results,
             "ratios": serving_ratios(results, g.Device(0).fp64_peak()),

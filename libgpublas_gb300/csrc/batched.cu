@@ -105,7 +105,10 @@ __device__ void gemm_tile(const DevOp &o, int tm, int tn, double *smem)
             const int row = m0 + ty + 16 * i;
             if (row >= o.m) continue;
             double *cp = o.C + (long long)col * o.ldc + row;
-            *cp = (o.beta == 0.0) ? o.alpha * acc[i][j] : fma(o.alpha, acc[i][j], o.beta * *cp);
+            // the GEMM core's epilogue, rounding for rounding: a request gives
+            // the same bits here as through gbx_dgemm
+            *cp = (o.beta == 0.0) ? __dmul_rn(o.alpha, acc[i][j])
+                                  : __fma_rn(o.beta, *cp, __dmul_rn(o.alpha, acc[i][j]));
         }
     }
 }

@@ -13,9 +13,11 @@
 // of enqueueing (argument checks, tensor-map encoding, launches) is spread
 // over the workers instead of one dispatcher thread.
 
-// Routing depends only on the operation (small GEMM: m, n <= 512 and
-// k <= 4096; small TRSM: order <= 256; everything else runs alone), so a
-// result is bit-identical whether the call was served alone or in a mix.
+// A result is bit-identical whether the call was served alone or in a mix:
+// a small DGEMM (m, n <= 512, k <= 4096) runs inline on a free slot when
+// nothing is queued to group it with, else grouped, and both routes compute
+// each element with the same FMA chain and epilogue; a small DTRSM (order
+// <= 256) always runs grouped; everything else runs alone.
 // Critical-path requests (DPOTRF of a diagonal block, DTRSM of a panel) run
 // on a high-priority stream of their slot.
 //
@@ -346,18 +348,33 @@ extern "C" gbx_status gbx_server_call(gbx_server *s, const gbx_op *op, double *l
         if (latency_us) *latency_us = std::chrono::duration<double, std::micro>(t1 - t0).count();
         return st;
     }
-    if (!is_small(*op)) {
+    // Large requests, and small DGEMMs that would find nothing queued to
+    // group with, run inline on a free slot: a hand-off to a worker and back
+    // cost a small call about 85 us.  A small DGEMM gives the same bits
+    // either way (the grouped tile uses the GEMM core's arithmetic); small
+    // DTRSMs always take the grouped route, whose substitution differs from
+    // the stream path's inverted blocks, so their bits never depend on load.
+    const bool small = is_small(*op);
+    if (!small || op->kind == GBX_OP_GEMM) {
         Slot *sl = nullptr;
         const auto t0 = clk::now();
         {
             std::lock_guard<std::mutex> lk(s->mu);
             if (s->stop) return GBX_ERR_ARG;
-            for (auto &q : s->slots)
-                if (!q.busy) {
-                    sl = &q;
-                    q.busy = true;
-                    break;
-                }
+            bool group = false;
+            if (small)
+                for (auto *r : s->queue)
+                    if (is_small(r->op)) {
+                        group = true;
+                        break;
+                    }
+            if (!group)
+                for (auto &q : s->slots)
+                    if (!q.busy) {
+                        sl = &q;
+                        q.busy = true;
+                        break;
+                    }
         }
         if (sl) {
             cudaSetDevice(s->device);
