@@ -17,7 +17,8 @@
 // a small DGEMM (m, n <= 512, k <= 4096) runs inline on a free slot when
 // nothing is queued to group it with, else grouped, and both routes compute
 // each element with the same FMA chain and epilogue; a small DTRSM (order
-// <= 256) always runs grouped; everything else runs alone.
+// <= 256) always runs in the grouped kernel, inline as a group of one or
+// with others; everything else runs alone.
 // Critical-path requests (DPOTRF of a diagonal block, DTRSM of a panel) run
 // on a high-priority stream of their slot.
 //
@@ -149,6 +150,18 @@ gbx_status run_on_slot(Slot *sl, const gbx_op &o)
     if (hi) gbx_ctx_set_stream(sl->ctx, sl->hi);
     gbx_status st = run_request(sl->ctx, o);
     const gbx_status sync = gbx_ctx_sync(sl->ctx);   // also collects bounded-wait status words
+    if (hi) gbx_ctx_set_stream(sl->ctx, nullptr);
+    return st == GBX_OK ? sync : st;
+}
+
+// A small DTRSM run inline by its caller: the grouped kernel on its own, so
+// that its bits are those of the grouped route it takes under load.
+gbx_status run_grouped_on_slot(Slot *sl, const gbx_op &o)
+{
+    const bool hi = sl->hi && is_critical(o);
+    if (hi) gbx_ctx_set_stream(sl->ctx, sl->hi);
+    gbx_status st = gbx_grouped_launch_inline(sl->ctx, &o, 1);
+    const gbx_status sync = gbx_ctx_sync(sl->ctx);
     if (hi) gbx_ctx_set_stream(sl->ctx, nullptr);
     return st == GBX_OK ? sync : st;
 }
@@ -348,14 +361,14 @@ extern "C" gbx_status gbx_server_call(gbx_server *s, const gbx_op *op, double *l
         if (latency_us) *latency_us = std::chrono::duration<double, std::micro>(t1 - t0).count();
         return st;
     }
-    // Large requests, and small DGEMMs that would find nothing queued to
+    // Large requests, and small ones that would find nothing queued to
     // group with, run inline on a free slot: a hand-off to a worker and back
     // cost a small call about 85 us.  A small DGEMM gives the same bits
-    // either way (the grouped tile uses the GEMM core's arithmetic); small
-    // DTRSMs always take the grouped route, whose substitution differs from
-    // the stream path's inverted blocks, so their bits never depend on load.
+    // either way (the grouped tile uses the GEMM core's arithmetic); a small
+    // DTRSM runs inline as a grouped launch of its own, so its bits are
+    // those of the grouped route whatever the load.
     const bool small = is_small(*op);
-    if (!small || op->kind == GBX_OP_GEMM) {
+    {
         Slot *sl = nullptr;
         const auto t0 = clk::now();
         {
@@ -378,7 +391,8 @@ extern "C" gbx_status gbx_server_call(gbx_server *s, const gbx_op *op, double *l
         }
         if (sl) {
             cudaSetDevice(s->device);
-            const gbx_status st = run_on_slot(sl, *op);
+            const gbx_status st = (small && op->kind == GBX_OP_TRSM) ? run_grouped_on_slot(sl, *op)
+                                                                      : run_on_slot(sl, *op);
             const auto t1 = clk::now();
             bool waiting;
             {
