@@ -317,20 +317,23 @@ gbx_status gbx_ops_run(gbx_ctx *ctx, const gbx_op *ops, int count);
 /* ---- serving loop (no reference counterpart: the reference serves one call
  * at a time on one cuBLAS handle, runtime-blas.c:14-23) -------------------
  * Continuous batching of calls from many host threads on device-resident
- * operands.  With GBX_SERVE_LOOP=1 at creation, gbx_server_call hands the
- * small FP64 requests (DGEMM and DSYRK with m, n <= 512 and k <= 4096; DTRSM
- * of order <= 256 with at most 256 right-hand sides) to a device-side request
- * loop: a resident kernel on a quarter of the SMs that takes them from a
- * ring in pinned host memory and shares its CTAs among them tile by tile,
- * with no launch or synchronisation per call.  Larger calls from the calling
- * thread run on a free slot's stream with the whole GPU.  Other requests (and
- * gbx_server_submit) go to worker threads that group the small DGEMM
- * (m, n <= 512, k <= 4096) and DTRSM (order <= 256) requests queued at that
- * moment into one grouped kernel and run the others with the regular
- * routines, each batch on the stream of a free slot, so new requests overlap
- * with work already on the GPU.  Routing depends only on the operation, so results are identical
- * served alone or in a mix.  gbx_server_admit / gbx_server_release reserve
- * staging memory against a budget (mem_budget, or 80% of the HBM free at
+ * operands.  gbx_server_call runs a request on the calling thread, on a free
+ * slot's stream with the whole GPU, unless the slots are all busy or, for a
+ * small request (DGEMM with m, n <= 512 and k <= 4096, DTRSM of order
+ * <= 256), other small requests are already queued; queued requests (and
+ * those of gbx_server_submit) go to worker threads that take every small
+ * request queued at that moment as one grouped kernel and the others one by
+ * one, each batch on the stream of a free slot, so new requests overlap with
+ * work already on the GPU.  A small DGEMM computes the same bits on either
+ * route and a small DTRSM always runs in the grouped kernel (a group of one
+ * when run inline), so results are identical served alone or in a mix.
+ * With GBX_SERVE_LOOP=1 at creation, the small FP64 requests (DGEMM and
+ * DSYRK with m, n <= 512 and k <= 4096; DTRSM of order <= 256 with at most
+ * 256 right-hand sides) go instead to a device-side request loop: a
+ * resident kernel on a quarter of the SMs that takes them from a ring in
+ * pinned host memory and shares its CTAs among them tile by tile, with no
+ * launch or synchronisation per call.  gbx_server_admit / gbx_server_release
+ * reserve staging memory against a budget (mem_budget, or 80% of the HBM free at
  * creation when 0) and block while it is exhausted. */
 typedef struct gbx_server gbx_server;
 gbx_status gbx_server_create(int device, int slots, size_t mem_budget, gbx_server **srv);
