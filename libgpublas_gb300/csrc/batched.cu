@@ -3,9 +3,10 @@
 // cuBLAS call at a time on one handle, runtime-blas.c:14-23).
 //
 // A plan is built once from a list of operations:
-//   * every DGEMM is cut into C tiles of 32x32 or 64x64 (the variant is chosen
-//     per size bucket by the autotuner below); every DTRSM (order <= 256) is
-//     one work item solved by one CTA;
+//   * every DGEMM is cut into C tiles of 32x32 or 64x64 computed by the GEMM
+//     core of the stream path (so a grouped DGEMM gives the bits of
+//     gbx_dgemm; the variant is chosen per size bucket by the autotuner
+//     below); every DTRSM (order <= 256) is one work item solved by one CTA;
 //   * work items are ordered by decreasing cost (longest first) and handed
 //     out dynamically: each CTA of a persistent grid (2 CTAs per SM) takes
 //     the next item with one atomicAdd on a counter that the launch resets;
@@ -18,6 +19,7 @@
 // $HOME/.cache/gbxblas/autotune.json), so later plans skip the timing.
 #include "gbx_internal.h"
 #include "gemm_host.h"
+#include "gemm_simt.cuh"
 #include "grouped_dev.cuh"
 
 #include <cuda_runtime.h>
@@ -38,7 +40,6 @@ using gbx_grouped::DevOp;
 using gbx_grouped::trsm_item;
 
 constexpr int BT_THREADS = 256;
-constexpr int BT_BK = 16;
 constexpr int TRSM_MAX_ORDER = 256;
 constexpr int TRSM_SYS = 16;      // right-hand sides solved together
 constexpr int NBUCKET = 6;        // max(M,N) <= 32, 64, 128, 256, 512, larger
@@ -49,75 +50,29 @@ struct Item {
     int tm, tn;
 };
 
-// ---------------------------------------------------------------- GEMM tile
-template <int TS>
-__device__ void gemm_tile(const DevOp &o, int tm, int tn, double *smem)
+// One tile of a DGEMM on the GEMM core (double-buffered shared-memory
+// stages with register prefetch), the arithmetic of gbx_dgemm element for
+// element.
+__device__ __forceinline__ void core_tile(const DevOp &o, const Item &w)
 {
-    constexpr int TPR = TS / 16;               // outputs per thread per dim (2 or 4)
-    double (*As)[TS] = (double (*)[TS])smem;             // [BT_BK][TS]
-    double (*Bs)[TS] = (double (*)[TS])(smem + BT_BK * TS);
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int m0 = tm * TS, n0 = tn * TS;
-    double acc[TPR][TPR];
-#pragma unroll
-    for (int i = 0; i < TPR; i++)
-#pragma unroll
-        for (int j = 0; j < TPR; j++) acc[i][j] = 0.0;
-    for (int k0 = 0; k0 < o.k; k0 += BT_BK) {
-        for (int t = threadIdx.x; t < TS * BT_BK; t += BT_THREADS) {
-            int mn, kk;
-            // A tile: op(A)(m0+mn, k0+kk)
-            if (!o.ta) { mn = t % TS; kk = t / TS; } else { kk = t % BT_BK; mn = t / BT_BK; }
-            int gm = m0 + mn, gk = k0 + kk;
-            As[kk][mn] = (gm < o.m && gk < o.k)
-                             ? (o.ta ? o.A[(long long)gm * o.lda + gk] : o.A[(long long)gk * o.lda + gm])
-                             : 0.0;
-            // B tile: op(B)(k0+kk, n0+mn)
-            if (o.tb) { mn = t % TS; kk = t / TS; } else { kk = t % BT_BK; mn = t / BT_BK; }
-            const int gn = n0 + mn;
-            gk = k0 + kk;
-            Bs[kk][mn] = (gn < o.n && gk < o.k)
-                             ? (o.tb ? o.B[(long long)gk * o.ldb + gn] : o.B[(long long)gn * o.ldb + gk])
-                             : 0.0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < BT_BK; kk++) {
-            double a[TPR], b[TPR];
-#pragma unroll
-            for (int i = 0; i < TPR; i++) {
-                a[i] = As[kk][ty + 16 * i];
-                b[i] = Bs[kk][tx + 16 * i];
-            }
-#pragma unroll
-            for (int i = 0; i < TPR; i++)
-#pragma unroll
-                for (int j = 0; j < TPR; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int j = 0; j < TPR; j++) {
-        const int col = n0 + tx + 16 * j;
-        if (col >= o.n) continue;
-#pragma unroll
-        for (int i = 0; i < TPR; i++) {
-            const int row = m0 + ty + 16 * i;
-            if (row >= o.m) continue;
-            double *cp = o.C + (long long)col * o.ldc + row;
-            // the GEMM core's epilogue, rounding for rounding: a request gives
-            // the same bits here as through gbx_dgemm
-            *cp = (o.beta == 0.0) ? __dmul_rn(o.alpha, acc[i][j])
-                                  : __fma_rn(o.beta, *cp, __dmul_rn(o.alpha, acc[i][j]));
-        }
-    }
+    gbx_gemm::GemmArgs<double> g{};
+    g.m = o.m; g.n = o.n; g.k = o.k;
+    g.A = o.A; g.lda = o.lda; g.ta = o.ta;
+    g.B = o.B; g.ldb = o.ldb; g.tb = o.tb;
+    g.alpha = o.alpha; g.beta = o.beta;
+    g.C = o.C; g.ldc = o.ldc;
+    g.c_part = gbx_gemm::C_FULL;
+    const int ts = w.variant ? 64 : 32;
+    g.tiles_m = (o.m + ts - 1) / ts;
+    g.tiles_n = (o.n + ts - 1) / ts;
+    if (w.variant) gbx_gemm::gemm_simt_tile<double, 4, 4, 8>(g, w.tm + w.tn * g.tiles_m);
+    else gbx_gemm::gemm_simt_tile<double, 2, 2, 8>(g, w.tm + w.tn * g.tiles_m);
 }
 
 __global__ void __launch_bounds__(BT_THREADS, 2)
 grouped_kernel(const DevOp *__restrict__ ops, const Item *__restrict__ items, int nitems, int *counter)
 {
-    __shared__ __align__(16) double smem[2 * BT_BK * 64 > TRSM_MAX_ORDER * TRSM_SYS ? 2 * BT_BK * 64
-                                                                                   : TRSM_MAX_ORDER * TRSM_SYS];
+    __shared__ __align__(16) double smem[TRSM_MAX_ORDER * TRSM_SYS];
     __shared__ int s_item;
     while (true) {
         if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
@@ -128,8 +83,7 @@ grouped_kernel(const DevOp *__restrict__ ops, const Item *__restrict__ items, in
         const Item w = items[it];
         const DevOp o = ops[w.op];
         if (o.kind == GBX_OP_TRSM) trsm_item<TRSM_SYS, BT_THREADS>(o, w.variant * TRSM_SYS, smem);
-        else if (w.variant == 0) gemm_tile<32>(o, w.tm, w.tn, smem);
-        else gemm_tile<64>(o, w.tm, w.tn, smem);
+        else core_tile(o, w);
         __syncthreads();
     }
 }
@@ -155,8 +109,10 @@ std::string tune_path()
     return std::string(h ? h : "/tmp") + "/.cache/gbxblas/autotune.json";
 }
 
-// The cache file is a small JSON object {"<device name>": [v0, ..., v5]}; it
-// is written by this library only, so a fixed-format parser suffices.
+// The cache file is a small JSON object {"<device name> core tiles": [v0,
+// ..., v5]} (the key names the tile code, so choices timed on an earlier one
+// are timed again); it is written by this library only, so a fixed-format
+// parser suffices.
 void tune_load_locked(int dev, const char *devname)
 {
     for (int d = 0; d < 64; d++)
@@ -168,7 +124,7 @@ void tune_load_locked(int dev, const char *devname)
     size_t len = fread(buf, 1, sizeof buf - 1, f);
     fclose(f);
     buf[len] = '\0';
-    std::string key = std::string("\"") + devname + "\": [";
+    std::string key = std::string("\"") + devname + " core tiles\": [";
     const char *p = strstr(buf, key.c_str());
     if (!p) return;
     p += key.size();
@@ -195,7 +151,7 @@ void tune_save_locked(int dev, const char *devname)
     }
     FILE *f = fopen(path.c_str(), "w");
     if (!f) return;
-    fprintf(f, "{\"%s\": [", devname);
+    fprintf(f, "{\"%s core tiles\": [", devname);
     for (int b = 0; b < NBUCKET; b++) fprintf(f, "%d%s", g_tune[dev][b] < 0 ? 1 : g_tune[dev][b], b + 1 < NBUCKET ? ", " : "");
     fprintf(f, "]}\n");
     fclose(f);
