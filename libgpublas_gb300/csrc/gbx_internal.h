@@ -159,6 +159,9 @@ void gbx_f77_report(const char *name, gbx_ctx *ctx, gbx_status st);
 /* netlib argument checks (INFO numbering); 0 when the call is valid */
 enum { GBX_TR_N = 1, GBX_TR_T = 2, GBX_TR_C = 4 };   /* transposition letters a routine takes */
 int gbx_check_gemm_args(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc);
+// FP64 GEMM core block tile (64, 32 or 16) for an m x n output (a triangle
+// when triangular) on `sms` SMs
+int gbx_dgemm_tile_choice(int m, int n, int triangular, int sms);
 int gbx_check_syrk_args(char uplo, char trans, int n, int k, int lda, int ldc);
 int gbx_check_trxm_args(char side, char uplo, char ta, char diag, int m, int n, int lda, int ldb);
 int gbx_check_rank_k_args(char uplo, char trans, int allowed, int n, int k, int lda, int ldc);

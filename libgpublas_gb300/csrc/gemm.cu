@@ -103,14 +103,9 @@ gbx_status launch_gemm(gbx_ctx *ctx, GemmArgs<T> p, const char *what)
         return p.c_part == C_FULL ? tm * tn : tm * (tm + 1) / 2;
     };
     if constexpr (std::is_same<T, double>::value) {
-        const double sms = (double)gbx_ctx_sms(ctx);
-        auto score = [&](int bm, double eff) {
-            const double w = (double)tiles(bm) / sms;
-            return eff * w / std::ceil(w);
-        };
-        const double s64 = score(64, 1.0), s32 = score(32, 0.998), s16 = score(16, 0.985);
-        if (s64 >= s32 && s64 >= s16) return launch_gemm_tile<T, 4>(ctx, p, what);
-        if (s32 >= s16) return launch_gemm_tile<T, 2>(ctx, p, what);
+        const int bm = gbx_dgemm_tile_choice(p.m, p.n, p.c_part != C_FULL, gbx_ctx_sms(ctx));
+        if (bm == 64) return launch_gemm_tile<T, 4>(ctx, p, what);
+        if (bm == 32) return launch_gemm_tile<T, 2>(ctx, p, what);
         return launch_gemm_tile<T, 1>(ctx, p, what);
     } else if constexpr (sizeof(T) <= 8) {
         if (tiles(128) >= want) return launch_gemm_tile<T, 8>(ctx, p, what);
@@ -128,6 +123,22 @@ template gbx_status launch_gemm<fcplx>(gbx_ctx *, GemmArgs<fcplx>, const char *)
 template gbx_status launch_gemm<dcplx>(gbx_ctx *, GemmArgs<dcplx>, const char *);
 
 }  // namespace gbx_gemm
+
+// The FP64 block tile (64, 32 or 16) for an m x n output (its lower or upper
+// triangle when triangular) on `sms` SMs: the best product of the kernel's
+// own efficiency and the fill of its last wave (see launch_gemm).
+extern "C" int gbx_dgemm_tile_choice(int m, int n, int triangular, int sms)
+{
+    if (m <= 0 || n <= 0 || sms <= 0) return 16;
+    auto score = [&](int bm, double eff) {
+        const long long tm = (m + bm - 1) / bm, tn = (n + bm - 1) / bm;
+        const double w = (double)(triangular ? tm * (tm + 1) / 2 : tm * tn) / sms;
+        return eff * w / std::ceil(w);
+    };
+    const double s64 = score(64, 1.0), s32 = score(32, 0.998), s16 = score(16, 0.985);
+    if (s64 >= s32 && s64 >= s16) return 64;
+    return s32 >= s16 ? 32 : 16;
+}
 
 // ------------------------------------------------------------------ checks
 extern "C" int gbx_check_gemm_args(char ta, char tb, int m, int n, int k, int lda, int ldb, int ldc)

@@ -141,3 +141,26 @@ def test_options_parsing(lib):
     assert r.returncode == 0, r.stderr
     assert r.stdout.split() == ["1", "1e-12", "0", "0", "1"]
     assert "gbxblas options" in r.stderr and "unknown option 'bogus'" in r.stderr
+
+
+@pytest.mark.parametrize("m,n,tri,tile", [
+    (8192, 8192, 0, 64),    # the DGEMM headline: 16384 tiles of 64, 107.8 per SM
+    (2040, 1210, 0, 64),    # 608 tiles of 64: exactly four per SM
+    (1287, 1287, 0, 64),
+    (4096, 1024, 0, 32),    # a DTRSM update: 1024 tiles of 64 would leave 0.74 of a wave
+    (2048, 1024, 0, 16),    # 512 tiles of 64: four tile times for 3.37 tiles of work
+    (1024, 1024, 0, 16),
+    (2311, 2305, 0, 16),
+    (64, 64, 0, 16),        # a small product: the most SMs
+    (8192, 8192, 1, 32),    # DSYRK 8192: 32896 triangular tiles of 32
+    (3201, 3201, 1, 32),
+])
+def test_fp64_tile_choice(lib, m, n, tri, tile):
+    # The FP64 GEMM core's block tile for a 152-SM part: the best product
+    # of the kernel's efficiency (64: 1.0, 32: 0.998, 16: 0.985, measured)
+    # and the fill of the last wave of tiles.
+    import ctypes as C
+    f = lib.gbx_dgemm_tile_choice
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
+    assert f(m, n, tri, 152) == tile
