@@ -2811,14 +2811,16 @@ extern "C" gbx_status gbx_zgemm_ozaki(gbx_ctx *ctx, char ta, char tb, int m, int
     pr.b.X = B; pr.b.ld = ldb; pr.b.row_k = gbx_lsame(tb, 'N'); pr.b.cplx = 1;
     pr.b.conj = gbx_lsame(tb, 'C'); pr.b.part0 = 0; pr.b.part1 = 2; pr.b.Ksplit = k;   // [Br ; -Bi]
     pr.alpha = 1.0; pr.beta = 0.0; pr.c_part = 0;
-    double *Wre = (double *)(b.W + 2 * (size_t)Mp * Np);   // second plane holds the real part result
+    // W holds two planes of 16 bytes per element: the first takes each
+    // product's running values, the second keeps Re (Mp x n doubles) while
+    // the imaginary product runs
+    double *Wre = (double *)(b.W + 2 * (size_t)Mp * Np);
     pr.C = Wre; pr.ldc = Mp;
     int used_re = 0, used_im = 0;
-    // W plane 0 is the running-sum workspace of each product; plane 1 keeps Re.
+    // real part: Re = Ar Br - Ai Bi, one real product of [Ar Ai] and [Br ; -Bi]
     if ((st = run_ozaki(ctx, pr, tol, slices, slices_used ? &used_re : nullptr, &b, 2, 0)) != GBX_OK) return st;
-    // imaginary part: [Bi ; Br]; Im result goes to C's workspace via a third
-    // buffer: reuse the running-sum plane after the real product is done by
-    // writing Im into plane 0 with its own running sums in... (see below)
+    // imaginary part: Im = Ar Bi + Ai Br, [Ar Ai] times [Bi ; Br], into its
+    // own workspace slot; its running values reuse W's first plane
     double *Wim;
     void *p;
     if ((st = gbx_ws(ctx, GBX_WS_TMP1, sizeof(double) * (size_t)Mp * n, &p)) != GBX_OK) return st;
